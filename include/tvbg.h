@@ -1,0 +1,243 @@
+/*
+ * tvbg.h -- C ABI of the GB300 brain-network step engine.
+ *
+ * The engine runs the per-instance network time step of tvb-hpc: each node
+ * gathers delayed neighbour observables from a circular history ring, applies
+ * the coupling function and the neural-mass drift, takes an Euler or
+ * Euler-Maruyama step with counter-based Philox noise, and optionally feeds a
+ * Balloon-Windkessel BOLD monitor.  A Pearson functional-connectivity (FC)
+ * kernel and a Philox normal generator complete the path.
+ *
+ * Conventions shared by every entry point:
+ *   - return 0 on success, a negative TVBG_E* code on failure; the message of
+ *     the last failure on the calling thread is returned by tvbg_last_error();
+ *   - pointers named d_* are device pointers owned by the caller; no entry
+ *     point allocates device memory (scratch words such as queue counters and
+ *     status words are caller-provided);
+ *   - `stream` is a cudaStream_t passed as void* (NULL = legacy default);
+ *     every call is asynchronous with respect to the host unless stated.
+ *
+ * Reference interfaces replaced (paths inside the tvb-hpc project):
+ *   tvbg_sweep         <- the fused loopy kernel of
+ *                         tvb_hpc/transforms.py:23-49 (network_time_step,
+ *                         called as knl(nstep, nnode, ntime, state, ...),
+ *                         tvb_hpc/examples/hackathon.py:48-54) and the CUDA
+ *                         DSL step kernel
+ *                         dsl/dsl_cuda/CUDAmodels/kuramoto.c:29-146 launched
+ *                         by dsl/dsl_cuda/example/cuda_run.py:124-142
+ *   tvbg_batch_run     <- the OpenMP subject batch of examples/hcp100.py:65-118
+ *                         (lp.to_batched over i_subj), as one persistent launch
+ *   tvbg_fc            <- tvb_hpc/metric.py:18-139 (Covar, CovToCorr) and
+ *                         dsl/dsl_cuda/CUDAmodels/refs/covar.c:9-109
+ *   tvbg_philox_normal <- tvb_hpc/rng.py:30-96 (RNG.fill, tvb_rng)
+ *   tvbg_pack_edges    <- tvb_hpc/network.py:66-78 (Connectivity.from_dense)
+ *                         plus the delay rule of hackathon.py:44 / kuramoto.c:105
+ */
+#ifndef TVBG_H
+#define TVBG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TVBG_ABI_VERSION 1
+
+/* ---- status codes ------------------------------------------------------ */
+#define TVBG_OK 0
+#define TVBG_EINVAL (-1)       /* bad argument (size, pointer, combination) */
+#define TVBG_ECUDA (-2)        /* a CUDA runtime call failed */
+#define TVBG_ETIMEOUT (-3)     /* a bounded device wait gave up */
+#define TVBG_EUNSUPPORTED (-4) /* model / coupling pair not built */
+#define TVBG_EDEVICE (-5)      /* device-side check failed (status word) */
+
+/* ---- neural-mass models (tvb_hpc/model.py) ------------------------------ */
+#define TVBG_MODEL_KURAMOTO 0 /* model.py:169-182  state theta, param omega  */
+#define TVBG_MODEL_G2DO 1     /* model.py:262-276  state W V, param a        */
+#define TVBG_MODEL_MPR 2      /* Montbrio-Pazo-Roxin 2015, state r V, param eta */
+#define TVBG_MODEL_LINEAR 3   /* model.py:250-259  state x, param lam        */
+
+/* ---- coupling functions (tvb_hpc/coupling.py) --------------------------- */
+#define TVBG_CFUN_LINEAR 0    /* pre = x_j,                  post = a*sum + b */
+#define TVBG_CFUN_DIFF 1      /* pre = x_j - x_i,            post = a*sum + b */
+#define TVBG_CFUN_KURAMOTO 2  /* pre = sin(x_j - x_i),       post = a*mean    */
+#define TVBG_CFUN_SIGMOIDAL 3 /* pre = cmax/(1+exp(r(mid-x_j))), post = a*sum */
+
+/* ---- per-instance flags ------------------------------------------------- */
+#define TVBG_F_NOISE 1u      /* Euler-Maruyama with Philox normals          */
+#define TVBG_F_BOLD 2u       /* integrate the Balloon-Windkessel monitor    */
+#define TVBG_F_TRACE 4u      /* write observables every trace_every steps   */
+#define TVBG_F_WRAP_FMOD 8u  /* Kuramoto wrap by fmod (CUDA DSL) not shift  */
+#define TVBG_F_SMEM_RING 16u /* ring staged in shared memory (planner sets)  */
+#define TVBG_F_NO_WRAP 32u   /* disable the model's limit/wrap rule          */
+/* Track-A step order (tvb_hpc/transforms.py:30-42, fused loopy kernel): the
+ * gather of step t reads ring slot t before the model writes obs(x_t) into
+ * it, so post and zero-delay reads see the slot's old content. */
+#define TVBG_F_TRACKA 64u
+#define TVBG_F_MIDSYNC 128u  /* block barrier between gather and update      */
+
+/*
+ * Packed connectivity edge, one per CSR non-zero, rows = target node i:
+ *   pk = (col << lognh) | ((col - delay) & (nh - 1)),  w = weight bits.
+ * The ring of an instance is node-major and skewed:
+ *   value of node j at time slot s lives at  j*nh + ((s + j) & (nh-1)),
+ * so the delayed read of edge e at slot tm is
+ *   ((tm + pk) & (nh-1)) | (pk & ~(nh-1)).
+ * nh = 1 << lognh must exceed max(delay) + sync_every.
+ */
+typedef struct tvbg_edge {
+    uint32_t pk;
+    float w;
+} tvbg_edge;
+
+/*
+ * One simulation instance (one parameter point of a sweep).  An array of
+ * these lives in device memory; tvbg_instance_size() must equal
+ * sizeof(tvbg_instance) on both sides of the FFI.
+ */
+typedef struct tvbg_instance {
+    const tvbg_edge *edges;  /* [nnz] packed edges for this instance's delays */
+    const int32_t *row;      /* [N+1] CSR row offsets (in-edges of node i)   */
+    float *ring;             /* [N << lognh] history ring backing store      */
+    float *state;            /* [N][nsvar] state at t0, updated in place      */
+    const float *nparam;     /* [N][npar] per-node model parameter            */
+    float *bold;             /* [4][N] balloon s, f-1, v-1, q-1 (rest = 0)    */
+    float *bold_out;         /* [bold_len][N] BOLD samples                    */
+    float *trace;            /* trace rows, see trace_* (TVBG_F_TRACE)        */
+    int64_t t0;              /* absolute step index of the first step         */
+    int64_t trace_stride;    /* floats between consecutive trace rows          */
+    int32_t nsteps;          /* steps to take in this launch                  */
+    int32_t N;               /* nodes (<= 1024)                               */
+    int32_t nnz;             /* edges                                         */
+    int32_t lognh;           /* ring length nh = 1 << lognh                   */
+    int32_t model;           /* TVBG_MODEL_* (must equal the launch's)        */
+    int32_t cfun;            /* TVBG_CFUN_* (must equal the launch's)         */
+    uint32_t flags;          /* TVBG_F_*                                      */
+    int32_t sync_every;      /* steps between block barriers (1..d_min+1)     */
+    int32_t trace_every;     /* sample trace when t % trace_every == 0        */
+    int32_t trace_len;       /* trace row = (t / trace_every) % trace_len     */
+    int32_t trace_nobs;      /* observables per node written to the trace     */
+    int32_t bold_period;     /* BOLD sample when (t + 1) % bold_period == 0   */
+    int32_t bold_len;        /* rows available in bold_out                    */
+    int32_t bold_obs;        /* observable index feeding the BOLD monitor     */
+    uint32_t seed_lo;        /* Philox key word 0                             */
+    uint32_t seed_hi;        /* Philox counter word 2                         */
+    uint32_t inst_id;        /* Philox key word 1 (request-local instance id) */
+    int32_t reserved0;
+    float dt;                /* integration step (ms)                         */
+    float sqrt_dt;           /* sqrtf(dt)                                     */
+    float dt_bold;           /* balloon step (s) = dt / 1000                  */
+    float cf_a;              /* coupling a (global coupling G)                */
+    float cf_b;              /* coupling b                                    */
+    float cf_p[3];           /* sigmoidal: cmax, midpoint, r                  */
+    float sigma[4];          /* noise amplitude per state variable            */
+    float consts[16];        /* model constants, order fixed per model        */
+} tvbg_instance;
+
+/* Launch-wide configuration. */
+typedef struct tvbg_launch {
+    int32_t model;         /* TVBG_MODEL_* shared by every instance of the call */
+    int32_t cfun;          /* TVBG_CFUN_* shared by every instance of the call  */
+    int32_t threads;       /* CTA size, multiple of 32, >= max N rounded up     */
+    int32_t tpn;           /* lanes per node in the gather: 1, 2, 4 or 8        */
+    int32_t smem_ring;     /* shared-memory bytes reserved for the ring (0 ok)  */
+    int32_t ctas;          /* persistent CTAs (tvbg_batch_run); 0 = 1 per SM    */
+    int32_t reserved0;
+    int32_t *d_status;     /* optional device int: first device error code      */
+    int32_t *d_counter;    /* tvbg_batch_run work counter (zeroed by the call)  */
+    const int32_t *d_order;/* tvbg_batch_run instance order (cost-descending)   */
+} tvbg_launch;
+
+/* ---- entry points ------------------------------------------------------ */
+
+/* ABI version (TVBG_ABI_VERSION) and struct sizes, for FFI checks. */
+int tvbg_abi_version(void);
+size_t tvbg_instance_size(void);
+size_t tvbg_launch_size(void);
+
+/* Message for the last failing call on this thread ("" if none). */
+const char *tvbg_last_error(void);
+
+/* Largest dynamic shared memory a CTA may use on the current device. */
+int tvbg_max_smem(int32_t *bytes);
+
+/*
+ * Host helper: pack CSR connectivity and integer delays into tvbg_edge.
+ * row[N+1], col[nnz] (int32), weights[nnz] (float), delays[nnz] (int32 >= 0).
+ * Fails if a delay >= nh or N << lognh overflows 32 bits.
+ * Replaces the CSR build of tvb_hpc/network.py:66-78 for the kernel layout.
+ */
+int tvbg_pack_edges(int32_t N, int32_t nnz, const int32_t *row,
+                    const int32_t *col, const float *weights,
+                    const int32_t *delays, int32_t lognh, tvbg_edge *out);
+
+/*
+ * Host helper: integer delays d = op(f32(f32(len / speed) / dt)),
+ * op = ceil (rounding = 1) or trunc (rounding = 0): the float32 arithmetic of
+ * tvb_hpc/examples/hackathon.py:44 under numpy 1.15 casting.  rounding = 2
+ * uses the CUDA DSL rule trunc(len * f32(f32(1/speed)/dt)) of
+ * dsl/dsl_cuda/CUDAmodels/kuramoto.c:65,105.
+ */
+int tvbg_delays(int32_t nnz, const float *lengths, float speed, float dt,
+                int32_t rounding, int32_t *out);
+
+/*
+ * Run every instance of d_inst[0..n_inst) for its nsteps, one CTA per
+ * instance, all instances sharing the (model, cfun) pair of cfg.  This is the plain
+ * one-sweep-per-launch path (the fused network step of
+ * tvb_hpc/transforms.py:23-49 batched over instances).
+ */
+int tvbg_sweep(const tvbg_instance *d_inst, int32_t n_inst,
+               const tvbg_launch *cfg, void *stream);
+
+/*
+ * Persistent batched run: cfg->ctas CTAs pull instances (in d_order order)
+ * from the device counter cfg->d_counter until all n_inst are done.
+ * Instances may differ in N, nnz, ring length and nsteps; they share the
+ * (model, cfun) pair of cfg.  The counter is reset on `stream` before the
+ * launch, so the call may be captured into a CUDA graph.
+ */
+int tvbg_batch_run(const tvbg_instance *d_inst, int32_t n_inst,
+                   const tvbg_launch *cfg, void *stream);
+
+/*
+ * Pearson FC per instance over T samples of N nodes, FP64 reduction.
+ * d_x: float [n_inst][T][N] (inst_stride floats between instances).
+ * d_fc: float [n_inst][N][N].  If d_target ([N][N]) and d_err ([n_inst])
+ * are given, d_err[b] = sum_{i<j} (fc_ij - target_ij)^2 in FP64.
+ * Replaces tvb_hpc/metric.py:18-139 and refs/covar.c:9-109.
+ */
+int tvbg_fc(const float *d_x, int32_t n_inst, int32_t T, int32_t N,
+            int64_t inst_stride, float *d_fc, const float *d_target,
+            double *d_err, void *stream);
+
+/*
+ * tvbg_fc with caller scratch: N > 126 needs d_scratch of
+ * tvbg_fc_scratch_bytes(n_inst, N) bytes (FP64 means and Gram); smaller N
+ * needs none (d_scratch may be NULL).
+ */
+int tvbg_fc_scratch_bytes(int32_t n_inst, int32_t N, int64_t *bytes);
+int tvbg_fc_ex(const float *d_x, int32_t n_inst, int32_t T, int32_t N,
+               int64_t inst_stride, float *d_fc, const float *d_target,
+               double *d_err, double *d_scratch, void *stream);
+
+/*
+ * Fill d_out[0..n) with standard normals from Philox4x32-10 (Salmon et al.
+ * 2011) + Box-Muller: key = (seed_lo, stream_id), counter = (i/4, 0,
+ * seed_hi, 0) for output i.  Replaces tvb_hpc/rng.py:30-96 (RNG.fill).
+ */
+int tvbg_philox_normal(uint64_t seed, uint32_t stream_id, float *d_out,
+                       int64_t n, void *stream);
+
+/* Raw Philox4x32-10 words: d_out[4*i + k] = philox(ctr=(i, c1, c2, c3), key)[k]. */
+int tvbg_philox_u32(uint32_t k0, uint32_t k1, uint32_t c1, uint32_t c2,
+                    uint32_t c3, uint32_t *d_out, int64_t n_blocks,
+                    void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TVBG_H */

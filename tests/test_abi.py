@@ -1,0 +1,137 @@
+"""
+The C-ABI library (no GPU needed): it loads, exports every entry point that
+include/tvbg.h declares, agrees with the ctypes struct layouts, and its host
+helpers (delay rule, edge packing) give the specified integers.
+"""
+
+import ctypes
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+from tvb_hpc import _native as nat
+from tvb_hpc import engine, network
+
+HEADER = os.path.join(ROOT, 'include', 'tvbg.h')
+
+
+def declared_symbols():
+    text = open(HEADER).read()
+    text = re.sub(r'/\*.*?\*/', '', text, flags=re.S)
+    return sorted(set(re.findall(r'\b(tvbg_[a-z0-9_]+)\s*\(', text)))
+
+
+def test_library_exports_every_declared_symbol():
+    lib = nat.load()
+    syms = declared_symbols()
+    assert len(syms) >= 12
+    out = subprocess.run(['nm', '-D', '--defined-only', nat.LIB_PATH], capture_output=True,
+                         text=True, check=True).stdout
+    exported = set(line.split()[-1] for line in out.splitlines() if ' T ' in line)
+    missing = [s for s in syms if s not in exported]
+    assert not missing, missing
+    for s in syms:
+        assert hasattr(lib, s)
+    assert set(nat.SIGNATURES) <= set(syms)
+
+
+def test_struct_layouts_match():
+    lib = nat.load()
+    assert lib.tvbg_abi_version() == nat.ABI_VERSION
+    assert lib.tvbg_instance_size() == ctypes.sizeof(nat.tvbg_instance) == nat.INSTANCE_DTYPE.itemsize
+    assert lib.tvbg_launch_size() == ctypes.sizeof(nat.tvbg_launch)
+
+
+@pytest.mark.parametrize('rounding', ['trunc', 'ceil', 'dsl'])
+def test_delay_rule_host_helper_matches_numpy(rounding):
+    lib = nat.load()
+    rng = np.random.default_rng(0)
+    lengths = rng.uniform(0, 250, 5000).astype(np.float32)
+    # include exact multiples, where trunc and ceil agree and rounding bites
+    lengths[:100] = (np.arange(100) * 0.4).astype(np.float32)
+    for speed, dt in [(4.0, 0.1), (1.0, 0.1), (3.7, 0.1), (10 ** 0.5, 1.0), (100.0, 1.0)]:
+        out = np.zeros(lengths.size, np.int32)
+        nat.check(lib.tvbg_delays(lengths.size, lengths.ctypes.data, speed, dt,
+                                  network.ROUNDING[rounding], out.ctypes.data))
+        np.testing.assert_array_equal(out, network.delays_f32(lengths, speed, dt, rounding))
+
+
+def test_delay_rule_is_the_float32_reference_rule():
+    "hackathon.py:44 under numpy 1.15 casting: f32(f32(len / speed) / dt)."
+    ln = np.array([10.0, 200.0, 123.4567, 0.4, 0.30000001], np.float32)
+    speed, dt = np.float64(4.0), 0.1
+    q = (ln / np.float32(speed)).astype(np.float32) / np.float32(dt)
+    np.testing.assert_array_equal(network.delays_f32(ln, speed, dt, 'trunc'),
+                                  np.trunc(q.astype(np.float32)).astype(np.int32))
+    np.testing.assert_array_equal(network.delays_f32(ln, speed, dt, 'ceil'),
+                                  np.ceil(q.astype(np.float32)).astype(np.int32))
+    # ceil(len/speed/dt) of the benchmark configurations
+    assert network.delays_f32(np.float32([10.0]), 4.0, 0.1, 'ceil')[0] == 25
+    assert network.delays_f32(np.float32([200.0]), 4.0, 0.1, 'ceil')[0] == 500
+
+
+def test_pack_edges_ring_addressing_is_bit_exact():
+    """pk = (col << lognh) | ((col - d) & mask) reproduces the reference ring
+    address (t - d + nh) % nh (kuramoto.c:108) in the skewed layout."""
+    rng = np.random.default_rng(3)
+    N, lognh = 37, 7
+    nh = 1 << lognh
+    nnz = 300
+    row = np.sort(rng.integers(0, nnz + 1, N - 1))
+    row = np.concatenate([[0], row, [nnz]]).astype(np.int32)
+    col = rng.integers(0, N, nnz).astype(np.int32)
+    d = rng.integers(0, nh - 1, nnz).astype(np.int32)
+    w = rng.random(nnz).astype(np.float32)
+    pk = engine.pack_edges(row, col, w, d, lognh)['pk'].astype(np.int64)
+    mask = nh - 1
+    for t in [0, 1, 5, nh - 1, nh, 3 * nh + 17, 123456789]:
+        tm = t & mask
+        idx = ((tm + pk) & mask) | (pk & ~mask)
+        slot = (t - d.astype(np.int64) + nh) % nh
+        np.testing.assert_array_equal(idx, engine.ring_index(N, lognh, col, slot))
+    # unskew(ring_index) is the identity layout
+    ring = np.zeros(N * nh, np.float32)
+    slots = np.arange(nh)
+    for j in range(N):
+        ring[engine.ring_index(N, lognh, j, slots)] = j * 1000 + slots
+    plain = engine.unskew_ring(ring, N, lognh)
+    assert np.array_equal(plain, (np.arange(N)[None, :] * 1000 + slots[:, None]).astype(np.float32))
+
+
+def test_pack_edges_rejects_bad_input():
+    lib = nat.load()
+    row = np.array([0, 1], np.int32)
+    col = np.array([0], np.int32)
+    w = np.array([1.0], np.float32)
+    out = np.zeros(1, np.dtype([('pk', '<u4'), ('w', '<f4')]))
+    for d, lognh in [(4, 2), (-1, 4), (0, 1), (0, 25)]:
+        dd = np.array([d], np.int32)
+        rc = lib.tvbg_pack_edges(1, 1, row.ctypes.data, col.ctypes.data, w.ctypes.data,
+                                 dd.ctypes.data, lognh, out.ctypes.data)
+        assert rc == nat.TVBG_EINVAL
+        assert lib.tvbg_last_error()
+    bad_col = np.array([3], np.int32)
+    dd = np.array([0], np.int32)
+    assert lib.tvbg_pack_edges(1, 1, row.ctypes.data, bad_col.ctypes.data, w.ctypes.data,
+                               dd.ctypes.data, 4, out.ctypes.data) == nat.TVBG_EINVAL
+
+
+def test_plan_ring_constraints():
+    for order in ('cuda', 'tracka'):
+        for dmin, dmax in [(0, 0), (0, 5), (1, 1), (25, 500), (100, 2000), (5, 6), (3, 250)]:
+            lognh, sync, fl = engine.plan_ring(dmin, dmax, order=order)
+            nh = 1 << lognh
+            assert nh >= dmax + 2
+            if order == 'cuda':
+                assert 1 <= sync <= max(1, dmin + 1) and sync <= nh - dmax - 1
+            else:
+                assert fl & nat.F_TRACKA
+                if dmin == 0:
+                    assert sync == 1 and fl & nat.F_MIDSYNC
+                else:
+                    assert 1 <= sync <= dmin and sync <= nh - dmax

@@ -1,0 +1,233 @@
+// C ABI of the engine: argument checks, kernel dispatch, host helpers and
+// the Philox generator kernels.  Declarations and reference citations are in
+// include/tvbg.h.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+
+#include "tvbg_abi_internal.h"
+#include "tvbg_device.cuh"
+
+namespace tvbg {
+
+static thread_local char g_last_error[512] = "";
+
+int set_error(int code, const char* msg) {
+    std::snprintf(g_last_error, sizeof(g_last_error), "%s", msg);
+    return code;
+}
+
+int set_cuda_error(cudaError_t e, const char* where) {
+    std::snprintf(g_last_error, sizeof(g_last_error), "%s: %s (%s)", where, cudaGetErrorName(e),
+                  cudaGetErrorString(e));
+    return TVBG_ECUDA;
+}
+
+static StepKernel lookup(int model, int cfun, int tpn) {
+    switch (model) {
+        case TVBG_MODEL_KURAMOTO: return step_kernel_kuramoto(cfun, tpn);
+        case TVBG_MODEL_G2DO: return step_kernel_g2do(cfun, tpn);
+        case TVBG_MODEL_MPR: return step_kernel_mpr(cfun, tpn);
+        case TVBG_MODEL_LINEAR: return step_kernel_linear(cfun, tpn);
+        default: return nullptr;
+    }
+}
+
+// Dynamic shared memory of a step launch: ring capacity + per-warp sums + mbarrier.
+static size_t step_smem_bytes(int threads, int smem_ring) {
+    return static_cast<size_t>(smem_ring) + 4u * static_cast<size_t>(threads) + 16u;
+}
+
+static int check_launch(const tvbg_launch* cfg, const tvbg_instance* d_inst, int32_t n_inst) {
+    if (!cfg || !d_inst || n_inst < 0) return set_error(TVBG_EINVAL, "null launch config or instances");
+    if (cfg->threads < 32 || cfg->threads > 1024 || (cfg->threads & 31))
+        return set_error(TVBG_EINVAL, "threads must be a multiple of 32 in [32, 1024]");
+    if (cfg->tpn != 1 && cfg->tpn != 2 && cfg->tpn != 4 && cfg->tpn != 8)
+        return set_error(TVBG_EINVAL, "tpn must be 1, 2, 4 or 8");
+    if (cfg->smem_ring < 0 || (cfg->smem_ring & 15))
+        return set_error(TVBG_EINVAL, "smem_ring must be a non-negative multiple of 16");
+    return TVBG_OK;
+}
+
+static int launch_step(int model, int cfun, const tvbg_instance* d_inst, int32_t n_inst,
+                       const tvbg_launch* cfg, bool persistent, void* stream) {
+    StepKernel k = lookup(model, cfun, cfg->tpn);
+    if (!k) return set_error(TVBG_EUNSUPPORTED, "model/coupling pair not built into the library");
+    const size_t smem = step_smem_bytes(cfg->threads, cfg->smem_ring);
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return set_cuda_error(e, "cudaGetDevice");
+    int optin = 0;
+    e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (e != cudaSuccess) return set_cuda_error(e, "cudaDeviceGetAttribute");
+    // the static __shared__ int of the kernel needs a few bytes too
+    if (smem + 64 > static_cast<size_t>(optin))
+        return set_error(TVBG_EINVAL, "ring capacity exceeds the shared memory of one CTA");
+    e = cudaFuncSetAttribute(reinterpret_cast<const void*>(k),
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+    if (e != cudaSuccess) return set_cuda_error(e, "cudaFuncSetAttribute(smem)");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    int grid = n_inst;
+    if (persistent) {
+        if (!cfg->d_counter) return set_error(TVBG_EINVAL, "tvbg_batch_run needs d_counter");
+        int sms = 0;
+        e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (e != cudaSuccess) return set_cuda_error(e, "cudaDeviceGetAttribute(SMs)");
+        grid = cfg->ctas > 0 ? cfg->ctas : sms;
+        if (grid > n_inst) grid = n_inst;
+        e = cudaMemsetAsync(cfg->d_counter, 0, sizeof(int32_t), st);
+        if (e != cudaSuccess) return set_cuda_error(e, "cudaMemsetAsync(counter)");
+    }
+    if (grid == 0) return TVBG_OK;
+    k<<<grid, cfg->threads, smem, st>>>(d_inst, n_inst, persistent ? cfg->d_order : nullptr,
+                                        persistent ? cfg->d_counter : nullptr, cfg->d_status,
+                                        static_cast<uint32_t>(cfg->smem_ring));
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return set_cuda_error(e, "step kernel launch");
+    return TVBG_OK;
+}
+
+// ---- Philox fill kernels ---------------------------------------------------
+__global__ void philox_normal_kernel(uint32_t k0, uint32_t k1, uint32_t c2, float* __restrict__ out,
+                                     long long n) {
+    const long long nb = (n + 3) / 4;
+    for (long long b = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; b < nb;
+         b += static_cast<long long>(gridDim.x) * blockDim.x) {
+        float z[4];
+        philox_normals4(static_cast<uint32_t>(b), static_cast<uint32_t>(b >> 32), c2, k0, k1, z);
+        const long long i = 4 * b;
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+            if (i + q < n) out[i + q] = z[q];
+    }
+}
+
+__global__ void philox_u32_kernel(uint32_t k0, uint32_t k1, uint32_t c1, uint32_t c2, uint32_t c3,
+                                  uint32_t* __restrict__ out, long long nb) {
+    for (long long b = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; b < nb;
+         b += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const u32x4 w = philox4x32_10(static_cast<uint32_t>(b), c1, c2, c3, k0, k1);
+        reinterpret_cast<uint4*>(out)[b] = make_uint4(w.v[0], w.v[1], w.v[2], w.v[3]);
+    }
+}
+
+}  // namespace tvbg
+
+using namespace tvbg;
+
+extern "C" {
+
+int tvbg_abi_version(void) { return TVBG_ABI_VERSION; }
+size_t tvbg_instance_size(void) { return sizeof(tvbg_instance); }
+size_t tvbg_launch_size(void) { return sizeof(tvbg_launch); }
+const char* tvbg_last_error(void) { return g_last_error; }
+
+int tvbg_max_smem(int32_t* bytes) {
+    if (!bytes) return set_error(TVBG_EINVAL, "tvbg_max_smem: null");
+    int dev = 0, optin = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return set_cuda_error(e, "cudaGetDevice");
+    e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (e != cudaSuccess) return set_cuda_error(e, "cudaDeviceGetAttribute");
+    *bytes = optin;
+    return TVBG_OK;
+}
+
+int tvbg_pack_edges(int32_t N, int32_t nnz, const int32_t* row, const int32_t* col,
+                    const float* weights, const int32_t* delays, int32_t lognh, tvbg_edge* out) {
+    if (N <= 0 || nnz < 0 || !row || (nnz > 0 && (!col || !weights || !delays || !out)))
+        return set_error(TVBG_EINVAL, "tvbg_pack_edges: bad arguments");
+    if (lognh < 2 || lognh > 24) return set_error(TVBG_EINVAL, "tvbg_pack_edges: lognh out of [2, 24]");
+    const uint64_t nh = 1ull << lognh;
+    if (static_cast<uint64_t>(N) * nh > (1ull << 32))
+        return set_error(TVBG_EINVAL, "tvbg_pack_edges: N * nh overflows 32-bit ring indices");
+    if (row[0] != 0 || row[N] != nnz) return set_error(TVBG_EINVAL, "tvbg_pack_edges: row[0] != 0 or row[N] != nnz");
+    for (int32_t i = 0; i < N; ++i)
+        if (row[i + 1] < row[i]) return set_error(TVBG_EINVAL, "tvbg_pack_edges: row not monotone");
+    const uint32_t mask = static_cast<uint32_t>(nh - 1);
+    for (int32_t e = 0; e < nnz; ++e) {
+        const int32_t c = col[e];
+        const int32_t d = delays[e];
+        if (c < 0 || c >= N) return set_error(TVBG_EINVAL, "tvbg_pack_edges: column out of range");
+        if (d < 0 || static_cast<uint64_t>(d) >= nh)
+            return set_error(TVBG_EINVAL, "tvbg_pack_edges: delay out of [0, nh)");
+        const uint32_t uc = static_cast<uint32_t>(c);
+        out[e].pk = (uc << lognh) | ((uc - static_cast<uint32_t>(d)) & mask);
+        out[e].w = weights[e];
+    }
+    return TVBG_OK;
+}
+
+int tvbg_delays(int32_t nnz, const float* lengths, float speed, float dt, int32_t rounding,
+                int32_t* out) {
+    if (nnz < 0 || (nnz > 0 && (!lengths || !out)) || !(speed > 0.0f) || !(dt > 0.0f) || rounding < 0 ||
+        rounding > 2)
+        return set_error(TVBG_EINVAL, "tvbg_delays: bad arguments");
+    // volatile keeps each float32 rounding explicit (no contraction / excess precision)
+    const volatile float vs = speed, vdt = dt;
+    const volatile float rec = (1.0f / vs) / vdt;
+    for (int32_t e = 0; e < nnz; ++e) {
+        const float len = lengths[e];
+        if (!(len >= 0.0f)) return set_error(TVBG_EINVAL, "tvbg_delays: negative or NaN length");
+        float q;
+        if (rounding == 2) {
+            volatile float m = len * rec;
+            q = std::trunc(static_cast<float>(m));
+        } else {
+            volatile float a = len / vs;
+            volatile float b = a / vdt;
+            q = rounding == 1 ? std::ceil(static_cast<float>(b)) : std::trunc(static_cast<float>(b));
+        }
+        if (q > 2147483647.0f) return set_error(TVBG_EINVAL, "tvbg_delays: delay overflows int32");
+        out[e] = static_cast<int32_t>(q);
+    }
+    return TVBG_OK;
+}
+
+int tvbg_sweep(const tvbg_instance* d_inst, int32_t n_inst, const tvbg_launch* cfg, void* stream) {
+    int rc = check_launch(cfg, d_inst, n_inst);
+    if (rc) return rc;
+    if (n_inst == 0) return TVBG_OK;
+    return launch_step(cfg->model, cfg->cfun, d_inst, n_inst, cfg, false, stream);
+}
+
+int tvbg_batch_run(const tvbg_instance* d_inst, int32_t n_inst, const tvbg_launch* cfg, void* stream) {
+    int rc = check_launch(cfg, d_inst, n_inst);
+    if (rc) return rc;
+    if (n_inst == 0) return TVBG_OK;
+    return launch_step(cfg->model, cfg->cfun, d_inst, n_inst, cfg, true, stream);
+}
+
+int tvbg_philox_normal(uint64_t seed, uint32_t stream_id, float* d_out, int64_t n, void* stream) {
+    if (!d_out || n < 0) return set_error(TVBG_EINVAL, "tvbg_philox_normal: bad arguments");
+    if (n == 0) return TVBG_OK;
+    const long long nb = (n + 3) / 4;
+    int grid = static_cast<int>((nb + 255) / 256);
+    if (grid > 152 * 32) grid = 152 * 32;
+    philox_normal_kernel<<<grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        static_cast<uint32_t>(seed), stream_id, static_cast<uint32_t>(seed >> 32), d_out, n);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return set_cuda_error(e, "philox_normal launch");
+    return TVBG_OK;
+}
+
+int tvbg_philox_u32(uint32_t k0, uint32_t k1, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t* d_out,
+                    int64_t n_blocks, void* stream) {
+    if (!d_out || n_blocks < 0 || n_blocks > 0xffffffffLL)
+        return set_error(TVBG_EINVAL, "tvbg_philox_u32: bad arguments");
+    if ((reinterpret_cast<uintptr_t>(d_out) & 15u) != 0)
+        return set_error(TVBG_EINVAL, "tvbg_philox_u32: d_out must be 16-byte aligned");
+    if (n_blocks == 0) return TVBG_OK;
+    int grid = static_cast<int>((n_blocks + 255) / 256);
+    if (grid > 152 * 32) grid = 152 * 32;
+    philox_u32_kernel<<<grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(k0, k1, c1, c2, c3, d_out,
+                                                                           n_blocks);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return set_cuda_error(e, "philox_u32 launch");
+    return TVBG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,278 @@
+// Device building blocks of the network step: Philox4x32-10, Box-Muller,
+// neural-mass drifts, coupling functions and the Balloon-Windkessel monitor.
+//
+// Every formula here restates the tvb-hpc definition cited beside it; the
+// oracle (oracle/tvbg_oracle.c) restates the same definitions on the CPU.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/tvbg.h"
+
+namespace tvbg {
+
+// ---------------------------------------------------------------------------
+// Philox4x32-10, from Salmon, Moraes, Dror, Shaw, "Parallel random numbers:
+// as easy as 1, 2, 3" (SC'11): a 4x32-bit counter and a 2x32-bit key, ten
+// rounds of two 32x32->64 multiplies; the key is bumped by the Weyl
+// constants between rounds.  tvb-hpc calls Random123's philox4x32 from
+// tvb_hpc/rng.py:30-60 with an uninitialised key; here the key is
+// (seed_lo, instance) so streams are reproducible per request.
+// ---------------------------------------------------------------------------
+constexpr uint32_t kPhiloxM0 = 0xD2511F53u;
+constexpr uint32_t kPhiloxM1 = 0xCD9E8D57u;
+constexpr uint32_t kPhiloxW0 = 0x9E3779B9u;
+constexpr uint32_t kPhiloxW1 = 0xBB67AE85u;
+
+struct u32x4 {
+    uint32_t v[4];
+};
+
+__device__ __forceinline__ u32x4 philox4x32_10(uint32_t c0, uint32_t c1, uint32_t c2,
+                                               uint32_t c3, uint32_t k0, uint32_t k1) {
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        const uint32_t lo0 = kPhiloxM0 * c0;
+        const uint32_t hi0 = __umulhi(kPhiloxM0, c0);
+        const uint32_t lo1 = kPhiloxM1 * c2;
+        const uint32_t hi1 = __umulhi(kPhiloxM1, c2);
+        const uint32_t n0 = hi1 ^ c1 ^ k0;
+        const uint32_t n2 = hi0 ^ c3 ^ k1;
+        c0 = n0;
+        c1 = lo1;
+        c2 = n2;
+        c3 = lo0;
+        k0 += kPhiloxW0;
+        k1 += kPhiloxW1;
+    }
+    u32x4 o;
+    o.v[0] = c0;
+    o.v[1] = c1;
+    o.v[2] = c2;
+    o.v[3] = c3;
+    return o;
+}
+
+// Box-Muller (Box & Muller 1958) on two 32-bit words.  u1 in (0,1) from the
+// top 24 bits plus one half, u2 in [0,1) from the top 24 bits; the angle is
+// evaluated with sincospif so 2*pi*u2 is never rounded.
+__device__ __forceinline__ void box_muller(uint32_t a, uint32_t b, float& z0, float& z1) {
+    const float u1 = (static_cast<float>(a >> 8) + 0.5f) * 5.9604644775390625e-8f;  // 2^-24
+    const float u2 = static_cast<float>(b >> 8) * 5.9604644775390625e-8f;
+    const float r = sqrtf(-2.0f * logf(u1));
+    float s, c;
+    sincospif(2.0f * u2, &s, &c);
+    z0 = r * c;
+    z1 = r * s;
+}
+
+__device__ __forceinline__ void philox_normals4(uint32_t c0, uint32_t c1, uint32_t c2,
+                                               uint32_t k0, uint32_t k1, float z[4]) {
+    const u32x4 w = philox4x32_10(c0, c1, c2, 0u, k0, k1);
+    box_muller(w.v[0], w.v[1], z[0], z[1]);
+    box_muller(w.v[2], w.v[3], z[2], z[3]);
+}
+
+// ---------------------------------------------------------------------------
+// Neural-mass models.  Each provides NS state variables, NP per-node
+// parameters, its drift f(x, c, p), the observable obs_k(x) and the limit
+// rule applied after the step.
+// ---------------------------------------------------------------------------
+constexpr float kTwoPi = 6.28318530717958647692f;
+
+// tvb_hpc/model.py:169-182: theta' = omega + I; obsrv = theta, sin(theta);
+// wrap into [0, 2pi] by one branchless shift (_wrap_limit, model.py:142-155).
+struct Kuramoto {
+    static constexpr int ID = TVBG_MODEL_KURAMOTO;
+    static constexpr int NS = 1;
+    static constexpr int NP = 1;
+    static constexpr int NOBS = 2;
+    __device__ static __forceinline__ void drift(const float* x, float c, const float* p,
+                                                 const float* /*K*/, float* f) {
+        f[0] = p[0] + c;
+    }
+    __device__ static __forceinline__ float obs(const float* x, int k) {
+        return k == 0 ? x[0] : sinf(x[0]);
+    }
+    __device__ static __forceinline__ void limit(float* x, uint32_t flags) {
+        if (flags & TVBG_F_NO_WRAP) return;
+        const float v = x[0];
+        if (flags & TVBG_F_WRAP_FMOD) {
+            // dsl/dsl_cuda/CUDAmodels/kuramoto.c:19-27 (wrap_it_PI)
+            const bool neg = v < 0.0f;
+            const float pos_val = fmodf(v, kTwoPi);
+            const float neg_val = kTwoPi - fmodf(-v, kTwoPi);
+            x[0] = neg ? neg_val : pos_val;
+        } else {
+            // model.py:142-155 with x0 = 0, x1 = 2 pi, dx = 2 pi
+            const float lo = (v < 0.0f) ? (v + kTwoPi) : 0.0f;
+            const float hi = (v > kTwoPi) ? (v - kTwoPi) : 0.0f;
+            const float in = (v >= 0.0f && v <= kTwoPi) ? v : 0.0f;
+            x[0] = lo + hi + in;
+        }
+    }
+};
+
+// tvb_hpc/model.py:262-276 (G2DO), state (W, V), param a, constants in
+// K = [tau, I, b, c, d, e, f, g, alpha, beta, gamma]; obsrv = W, V.
+struct G2DO {
+    static constexpr int ID = TVBG_MODEL_G2DO;
+    static constexpr int NS = 2;
+    static constexpr int NP = 1;
+    static constexpr int NOBS = 2;
+    __device__ static __forceinline__ void drift(const float* x, float c0, const float* p,
+                                                 const float* K, float* fo) {
+        const float W = x[0], V = x[1];
+        const float a = p[0];
+        const float tau = K[0], I = K[1], b = K[2], c = K[3], d = K[4], e = K[5];
+        const float f = K[6], g = K[7], alpha = K[8], beta = K[9], gamma = K[10];
+        const float V2 = V * V;
+        const float V3 = V2 * V;
+        fo[0] = d * tau * (alpha * W - f * V3 + e * V2 + g * V + gamma * I + gamma * c0);
+        fo[1] = d * (a + b * V + c * V2 - beta * W) / tau;
+    }
+    __device__ static __forceinline__ float obs(const float* x, int k) { return k == 0 ? x[0] : x[1]; }
+    __device__ static __forceinline__ void limit(float*, uint32_t) {}
+};
+
+// Montbrio, Pazo, Roxin (2015) firing-rate model, state (r, V), per-node eta,
+// K = [Delta, J, tau, I]:
+//   r' = (Delta / (pi tau) + 2 r V) / tau
+//   V' = (V^2 + eta + J tau r + I + c - (pi tau r)^2) / tau
+// obsrv = r, V; the rate is kept non-negative after each step.
+struct MPR {
+    static constexpr int ID = TVBG_MODEL_MPR;
+    static constexpr int NS = 2;
+    static constexpr int NP = 1;
+    static constexpr int NOBS = 2;
+    __device__ static __forceinline__ void drift(const float* x, float c, const float* p,
+                                                 const float* K, float* f) {
+        const float r = x[0], V = x[1];
+        const float Delta = K[0], J = K[1], tau = K[2], I = K[3];
+        const float pi = 3.14159265358979323846f;
+        const float ptr = pi * tau * r;
+        f[0] = (Delta / (pi * tau) + 2.0f * r * V) / tau;
+        f[1] = (V * V + p[0] + J * tau * r + I + c - ptr * ptr) / tau;
+    }
+    __device__ static __forceinline__ float obs(const float* x, int k) { return k == 0 ? x[0] : x[1]; }
+    __device__ static __forceinline__ void limit(float* x, uint32_t flags) {
+        if (flags & TVBG_F_NO_WRAP) return;
+        x[0] = x[0] < 0.0f ? 0.0f : x[0];
+    }
+};
+
+// tvb_hpc/model.py:250-259: x' = lam x + c; obsrv = x.
+struct Linear {
+    static constexpr int ID = TVBG_MODEL_LINEAR;
+    static constexpr int NS = 1;
+    static constexpr int NP = 1;
+    static constexpr int NOBS = 1;
+    __device__ static __forceinline__ void drift(const float* x, float c, const float* p,
+                                                 const float*, float* f) {
+        f[0] = p[0] * x[0] + c;
+    }
+    __device__ static __forceinline__ float obs(const float* x, int) { return x[0]; }
+    __device__ static __forceinline__ void limit(float*, uint32_t) {}
+};
+
+// ---------------------------------------------------------------------------
+// Coupling functions, tvb_hpc/coupling.py:103-121 and network.py:115-136:
+//   input_i = post( sum_e w_e * pre(obsrv_j(t - d_e), obsrv_i(t)) ),
+// with `mean` = sum / nnode.
+// ---------------------------------------------------------------------------
+template <int CF>
+struct Cfun;
+
+template <>
+struct Cfun<TVBG_CFUN_LINEAR> {
+    static constexpr bool kNeedsPost = false;
+    __device__ static __forceinline__ float pre(float xj, float, const tvbg_instance&) { return xj; }
+    __device__ static __forceinline__ float post(float s, const tvbg_instance& d) {
+        return d.cf_a * s + d.cf_b;
+    }
+};
+
+template <>
+struct Cfun<TVBG_CFUN_DIFF> {
+    static constexpr bool kNeedsPost = true;
+    __device__ static __forceinline__ float pre(float xj, float xi, const tvbg_instance&) {
+        return xj - xi;
+    }
+    __device__ static __forceinline__ float post(float s, const tvbg_instance& d) {
+        return d.cf_a * s + d.cf_b;
+    }
+};
+
+template <>
+struct Cfun<TVBG_CFUN_KURAMOTO> {
+    static constexpr bool kNeedsPost = true;
+    __device__ static __forceinline__ float pre(float xj, float xi, const tvbg_instance&) {
+        return sinf(xj - xi);
+    }
+    __device__ static __forceinline__ float post(float s, const tvbg_instance& d) {
+        return d.cf_a * (s / static_cast<float>(d.N));
+    }
+};
+
+template <>
+struct Cfun<TVBG_CFUN_SIGMOIDAL> {
+    static constexpr bool kNeedsPost = false;
+    __device__ static __forceinline__ float pre(float xj, float, const tvbg_instance& d) {
+        return d.cf_p[0] / (1.0f + expf(d.cf_p[2] * (d.cf_p[1] - xj)));
+    }
+    __device__ static __forceinline__ float post(float s, const tvbg_instance& d) {
+        return d.cf_a * s;
+    }
+};
+
+// ---------------------------------------------------------------------------
+// Balloon-Windkessel monitor, tvb_hpc/bold.py:24-74 and
+// dsl/dsl_cuda/CUDAmodels/refs/balloon.c:24-67 (Stephan et al. 2007
+// constants): one explicit Euler step of (s, f, v, q) with input x, all
+// derivatives taken from the old values; BOLD = V0 (k1 (1-q) + k2 (1-q/v)
+// + k3 (1-v)).
+//
+// The state is held as deviations from rest (s, F = f-1, V = v-1, Q = q-1)
+// and the powers are evaluated with log1pf/expm1f:
+//   v^(1/alpha) - 1            = expm1(log1p(V) / alpha)
+//   f (1 - a^(1/f)) / E0 - 1   = F - (1+F) a expm1(-ln(a) F/(1+F)) / E0,  a = 1-E0
+//   v^(1/alpha) q / v - 1      = expm1((1/alpha - 1) log1p(V)) (1+Q) + Q
+//   BOLD = V0 (-k1 Q + k2 (V - Q)/(1+V) - k3 V)
+// which is the same system, algebraically, without the cancellation of the
+// float32 form (increments of f, v, q ~ 1 fall below float resolution at the
+// 1e-4 s balloon step of a 0.1 ms simulation).
+// ---------------------------------------------------------------------------
+struct Balloon {
+    static constexpr float TAU_S = 0.65f, TAU_F = 0.41f, TAU_O = 0.98f, ALPHA = 0.32f;
+    static constexpr float TE = 0.04f, V0 = 4.0f, E0 = 0.4f, EPSILON = 0.5f;
+    static constexpr float NU_0 = 40.3f, R_0 = 25.0f;
+    __device__ static __forceinline__ void step(float& s, float& F, float& V, float& Q, float x,
+                                                float dt) {
+        const float rts = 1.0f / TAU_S, rtf = 1.0f / TAU_F, rto = 1.0f / TAU_O;
+        const float ra = 1.0f / ALPHA;
+        const float a = 1.0f - E0;
+        const float neg_ln_a = 0.51082562376599068f;  // -ln(0.6)
+        const float lv = log1pf(V);
+        const float vpow_m1 = expm1f(ra * lv);
+        const float em = expm1f(neg_ln_a * F / (1.0f + F));
+        const float t1 = F - (1.0f + F) * a * em * (1.0f / E0);
+        const float t2 = expm1f((ra - 1.0f) * lv) * (1.0f + Q) + Q;
+        const float ds = x - rts * s - rtf * F;
+        const float dF = s;
+        const float dV = rto * (F - vpow_m1);
+        const float dQ = rto * (t1 - t2);
+        s = fmaf(dt, ds, s);
+        F = fmaf(dt, dF, F);
+        V = fmaf(dt, dV, V);
+        Q = fmaf(dt, dQ, Q);
+    }
+    __device__ static __forceinline__ float signal(float V, float Q) {
+        const float k1 = 4.3f * NU_0 * E0 * TE;
+        const float k2 = EPSILON * R_0 * E0 * TE;
+        const float k3 = 1.0f - EPSILON;
+        return V0 * (-k1 * Q + k2 * (V - Q) / (1.0f + V) - k3 * V);
+    }
+};
+
+}  // namespace tvbg

@@ -1,0 +1,187 @@
+"""
+ctypes binding of the engine's C ABI (include/tvbg.h).
+
+The shared library ``_lib/libtvbg.so`` is built in-tree by
+``__graft_entry__.build()`` (nvcc, sm_103a).  There is no fallback: every
+compute call goes through this library, and loading fails loudly when it is
+missing.  The binding style mirrors tvb_hpc/compiler.py:140-225
+(CompiledKernel: ctypes pointers for arrays, scalars by value), with int
+status returns turned into exceptions.
+"""
+
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_DIR = os.path.join(HERE, '_lib')
+LIB_PATH = os.path.join(LIB_DIR, 'libtvbg.so')
+
+ABI_VERSION = 1
+
+TVBG_OK = 0
+TVBG_EINVAL = -1
+TVBG_ECUDA = -2
+TVBG_ETIMEOUT = -3
+TVBG_EUNSUPPORTED = -4
+TVBG_EDEVICE = -5
+
+MODEL_KURAMOTO, MODEL_G2DO, MODEL_MPR, MODEL_LINEAR = 0, 1, 2, 3
+CFUN_LINEAR, CFUN_DIFF, CFUN_KURAMOTO, CFUN_SIGMOIDAL = 0, 1, 2, 3
+
+F_NOISE = 1
+F_BOLD = 2
+F_TRACE = 4
+F_WRAP_FMOD = 8
+F_SMEM_RING = 16
+F_NO_WRAP = 32
+F_TRACKA = 64
+F_MIDSYNC = 128
+
+
+class tvbg_edge(ctypes.Structure):
+    _fields_ = [('pk', ctypes.c_uint32), ('w', ctypes.c_float)]
+
+
+class tvbg_instance(ctypes.Structure):
+    _fields_ = [
+        ('edges', ctypes.c_void_p),
+        ('row', ctypes.c_void_p),
+        ('ring', ctypes.c_void_p),
+        ('state', ctypes.c_void_p),
+        ('nparam', ctypes.c_void_p),
+        ('bold', ctypes.c_void_p),
+        ('bold_out', ctypes.c_void_p),
+        ('trace', ctypes.c_void_p),
+        ('t0', ctypes.c_int64),
+        ('trace_stride', ctypes.c_int64),
+        ('nsteps', ctypes.c_int32),
+        ('N', ctypes.c_int32),
+        ('nnz', ctypes.c_int32),
+        ('lognh', ctypes.c_int32),
+        ('model', ctypes.c_int32),
+        ('cfun', ctypes.c_int32),
+        ('flags', ctypes.c_uint32),
+        ('sync_every', ctypes.c_int32),
+        ('trace_every', ctypes.c_int32),
+        ('trace_len', ctypes.c_int32),
+        ('trace_nobs', ctypes.c_int32),
+        ('bold_period', ctypes.c_int32),
+        ('bold_len', ctypes.c_int32),
+        ('bold_obs', ctypes.c_int32),
+        ('seed_lo', ctypes.c_uint32),
+        ('seed_hi', ctypes.c_uint32),
+        ('inst_id', ctypes.c_uint32),
+        ('reserved0', ctypes.c_int32),
+        ('dt', ctypes.c_float),
+        ('sqrt_dt', ctypes.c_float),
+        ('dt_bold', ctypes.c_float),
+        ('cf_a', ctypes.c_float),
+        ('cf_b', ctypes.c_float),
+        ('cf_p', ctypes.c_float * 3),
+        ('sigma', ctypes.c_float * 4),
+        ('consts', ctypes.c_float * 16),
+    ]
+
+
+class tvbg_launch(ctypes.Structure):
+    _fields_ = [
+        ('model', ctypes.c_int32),
+        ('cfun', ctypes.c_int32),
+        ('threads', ctypes.c_int32),
+        ('tpn', ctypes.c_int32),
+        ('smem_ring', ctypes.c_int32),
+        ('ctas', ctypes.c_int32),
+        ('reserved0', ctypes.c_int32),
+        ('d_status', ctypes.c_void_p),
+        ('d_counter', ctypes.c_void_p),
+        ('d_order', ctypes.c_void_p),
+    ]
+
+
+#: numpy view of tvbg_instance (used to build instance tables in bulk)
+INSTANCE_DTYPE = np.dtype(tvbg_instance)
+
+_i32, _i64, _u32, _u64 = ctypes.c_int32, ctypes.c_int64, ctypes.c_uint32, ctypes.c_uint64
+_vp, _sz = ctypes.c_void_p, ctypes.c_size_t
+_fp = ctypes.POINTER(ctypes.c_float)
+_ip = ctypes.POINTER(ctypes.c_int32)
+
+# name -> (restype, argtypes); every entry point declared in include/tvbg.h
+SIGNATURES = {
+    'tvbg_abi_version': (ctypes.c_int, []),
+    'tvbg_instance_size': (_sz, []),
+    'tvbg_launch_size': (_sz, []),
+    'tvbg_last_error': (ctypes.c_char_p, []),
+    'tvbg_max_smem': (ctypes.c_int, [_ip]),
+    'tvbg_pack_edges': (ctypes.c_int, [_i32, _i32, _vp, _vp, _vp, _vp, _i32, _vp]),
+    'tvbg_delays': (ctypes.c_int, [_i32, _vp, ctypes.c_float, ctypes.c_float, _i32, _vp]),
+    'tvbg_sweep': (ctypes.c_int, [_vp, _i32, ctypes.POINTER(tvbg_launch), _vp]),
+    'tvbg_batch_run': (ctypes.c_int, [_vp, _i32, ctypes.POINTER(tvbg_launch), _vp]),
+    'tvbg_fc': (ctypes.c_int, [_vp, _i32, _i32, _i32, _i64, _vp, _vp, _vp, _vp]),
+    'tvbg_fc_ex': (ctypes.c_int, [_vp, _i32, _i32, _i32, _i64, _vp, _vp, _vp, _vp, _vp]),
+    'tvbg_fc_scratch_bytes': (ctypes.c_int, [_i32, _i32, ctypes.POINTER(_i64)]),
+    'tvbg_philox_normal': (ctypes.c_int, [_u64, _u32, _vp, _i64, _vp]),
+    'tvbg_philox_u32': (ctypes.c_int, [_u32, _u32, _u32, _u32, _u32, _vp, _i64, _vp]),
+}
+
+
+class TvbgError(RuntimeError):
+    "A C-ABI call returned a negative status."
+
+    def __init__(self, code, msg):
+        super().__init__('%s (status %d)' % (msg, code))
+        self.code = code
+
+
+_lib = None
+
+
+def load():
+    "Load and type the library once; raise if it has not been built."
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(
+            'tvb-hpc GB300 engine library missing at %s; build it with '
+            '`python -c "import __graft_entry__ as g; g.build()"`' % LIB_PATH)
+    lib = ctypes.CDLL(LIB_PATH)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if lib.tvbg_abi_version() != ABI_VERSION:
+        raise RuntimeError('libtvbg ABI version mismatch')
+    if lib.tvbg_instance_size() != ctypes.sizeof(tvbg_instance):
+        raise RuntimeError('tvbg_instance layout mismatch: C %d vs ctypes %d' % (
+            lib.tvbg_instance_size(), ctypes.sizeof(tvbg_instance)))
+    if lib.tvbg_launch_size() != ctypes.sizeof(tvbg_launch):
+        raise RuntimeError('tvbg_launch layout mismatch')
+    _lib = lib
+    return lib
+
+
+def check(rc):
+    "Turn a status code into an exception carrying tvbg_last_error()."
+    if rc != TVBG_OK:
+        msg = _lib.tvbg_last_error().decode(errors='replace') if _lib else 'libtvbg'
+        raise TvbgError(rc, msg)
+    return rc
+
+
+def ptr(t):
+    "Device (or host) address of a torch tensor / numpy array, or None."
+    if t is None:
+        return None
+    if hasattr(t, 'data_ptr'):
+        return t.data_ptr()
+    return t.ctypes.data
+
+
+def stream_handle(stream=None):
+    "cudaStream_t of a torch stream (current stream by default) as int."
+    import torch
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return s.cuda_stream

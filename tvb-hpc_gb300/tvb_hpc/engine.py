@@ -1,0 +1,438 @@
+"""
+The GB300 network-step engine: instance tables, ring planning and launches.
+
+An *instance* is one parameter point of a sweep (one (G, speed, per-node
+parameters, seed) tuple) on one connectome.  The engine keeps for every
+instance, resident in device memory:
+  - its history ring (node-major, skewed, length nh = 2^k > max delay + 1),
+  - its state [N][nsvar], per-node parameters, balloon state and outputs,
+and describes it to the kernels with one ``tvbg_instance`` record
+(include/tvbg.h).  Instances that share a speed share one packed edge table.
+
+Launch planning:
+  - a ring of N * nh * 4 bytes that fits the shared memory of one CTA is
+    staged there by TMA bulk copies (flag F_SMEM_RING); otherwise the kernel
+    works on the ring in global memory (L2-resident when it fits);
+  - instances are grouped by (ring placement, nh) so each launch reserves
+    only the shared memory its rings need;
+  - sync_every = min(d_min + 1, nh - d_max - 1) block barriers (see
+    tvbg_step.cuh) and the gather width tpn come from the planner/autotuner.
+
+Reference behaviour mirrored: the per-instance time loop of
+dsl/dsl_cuda/example/cuda_run.py:124-142 (one launch per chunk of steps,
+state and history resident on the device between launches) and the
+subject batch of examples/hcp100.py:65-118.
+"""
+
+import ctypes
+import math
+
+import numpy as np
+
+from . import _native as nat
+from .network import delays_f32
+from .utils import getLogger, next_pow2
+
+LOG = getLogger(__name__)
+
+_SMEM_RESERVE = 1024  # static shared memory of the step kernel + slack
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def _device_ok():
+    torch = _torch()
+    if not torch.cuda.is_available():
+        raise RuntimeError('the GB300 engine needs a CUDA device; there is no CPU fallback')
+
+
+def ring_index(N, lognh, node, slot):
+    "Physical index of (node, time slot) in a skewed node-major ring."
+    nh = 1 << lognh
+    node = np.asarray(node, np.int64)
+    slot = np.asarray(slot, np.int64)
+    return node * nh + ((slot + node) & (nh - 1))
+
+
+def unskew_ring(ring_flat, N, lognh):
+    "Skewed node-major ring (N*nh,) -> plain slot-major [nh, N] (numpy)."
+    nh = 1 << lognh
+    r = np.asarray(ring_flat).reshape(N, nh)
+    out = np.empty((nh, N), r.dtype)
+    s = np.arange(nh)
+    for j in range(N):
+        out[:, j] = r[j, (s + j) & (nh - 1)]
+    return out
+
+
+def pack_edges(row, col, weights, delays, lognh):
+    "tvbg_pack_edges through the C ABI (host helper) -> structured numpy array."
+    lib = nat.load()
+    row = np.ascontiguousarray(row, np.int32)
+    col = np.ascontiguousarray(col, np.int32)
+    w = np.ascontiguousarray(weights, np.float32)
+    d = np.ascontiguousarray(delays, np.int32)
+    N = row.size - 1
+    out = np.zeros(col.size, dtype=np.dtype([('pk', '<u4'), ('w', '<f4')]))
+    nat.check(lib.tvbg_pack_edges(N, col.size, row.ctypes.data, col.ctypes.data, w.ctypes.data,
+                                  d.ctypes.data, int(lognh), out.ctypes.data if col.size else None))
+    return out
+
+
+def plan_ring(dmin, dmax, extra=0, order='cuda'):
+    """
+    (lognh, sync_every, extra_flags) for delays in [dmin, dmax]: the smallest
+    power-of-two ring with nh >= dmax + 2 (+ extra), then the largest barrier
+    interval that keeps the read-after-write and overwrite constraints:
+      CUDA order  : value of step t written to slot t+1, first read at
+                    t + 1 + dmin  ->  sync <= dmin + 1, sync <= nh - dmax - 1;
+      Track-A order: value of step t written to slot t after the gather,
+                    first read at t + dmin -> sync <= dmin, sync <= nh - dmax;
+                    with zero delays every step needs a barrier between the
+                    gather and the update as well (F_MIDSYNC).
+    """
+    nh = max(4, next_pow2(int(dmax) + 2 + int(extra)))
+    dmin, dmax = int(dmin), int(dmax)
+    if order == 'cuda':
+        return int(math.log2(nh)), max(1, min(dmin + 1, nh - dmax - 1)), 0
+    if order != 'tracka':
+        raise ValueError("order must be 'cuda' or 'tracka'")
+    if dmin == 0:
+        return int(math.log2(nh)), 1, nat.F_TRACKA | nat.F_MIDSYNC
+    return int(math.log2(nh)), max(1, min(dmin, nh - dmax)), nat.F_TRACKA
+
+
+def max_smem():
+    lib = nat.load()
+    v = ctypes.c_int32(0)
+    nat.check(lib.tvbg_max_smem(ctypes.byref(v)))
+    return int(v.value)
+
+
+class DeviceStatus:
+    "A device int the kernels set to their first error code."
+
+    def __init__(self):
+        torch = _torch()
+        self.t = torch.zeros(1, dtype=torch.int32, device='cuda')
+
+    def reset(self):
+        self.t.zero_()
+
+    def check(self):
+        v = int(self.t.item())
+        if v != 0:
+            raise nat.TvbgError(v, 'device-side check failed in a step kernel')
+
+
+class InstanceSet:
+    """
+    Device-resident instances sharing (model, coupling, scheme) and one
+    connectome; the building block of Sweep, batch and serving.
+
+    Parameters
+    ----------
+    model, cfun, scheme : tvb_hpc model / coupling / scheme objects
+    conn : Connectivity (CSR, float32 weights and lengths)
+    dt : float, ms
+    speeds : (I,) conduction speeds (mm/ms), or None with ``delays`` given
+    couplings : (I,) coupling `a` per instance (global coupling G)
+    state0 : (I, N, nsvar) initial state, or (N, nsvar) shared
+    nparam : (I, N, npar) or (N, npar) per-node parameters (default: const)
+    delays : optional (nnz,) int delays shared by all instances
+    rounding : 'ceil' | 'trunc' | 'dsl' delay rule (see network.delays_f32)
+    seed : uint64 Philox seed; inst_ids : (I,) request-local ids (key word 1)
+    history : 'zero' (zero history before t0) or 'fill' (state0 everywhere)
+    order : 'cuda' (gather, drift, update, write slot t+1: the CUDA DSL
+            kernels, dsl/dsl_cuda/CUDAmodels/kuramoto.c:85-139) or 'tracka'
+            (the fused loopy kernel: gather reads slot t before the model
+            writes obs(x_t) into it, tvb_hpc/transforms.py:30-42)
+    bold_period, bold_len : BOLD sampling (steps) and rows to keep
+    trace_every, trace_len, trace_nobs : observable trace sampling
+    flags : extra TVBG_F_* bits (e.g. F_WRAP_FMOD)
+    cf_b : coupling offset b (default from cfun.param)
+    """
+
+    def __init__(self, model, cfun, scheme, conn, dt, couplings, speeds=None, state0=None,
+                 nparam=None, delays=None, rounding='ceil', seed=0, inst_ids=None,
+                 history='zero', bold_period=0, bold_len=0, trace_every=0, trace_len=0,
+                 trace_nobs=None, flags=0, cf_b=None, nh_extra=0, t0=0, order='cuda'):
+        _device_ok()
+        torch = _torch()
+        self.torch = torch
+        self.model, self.cfun, self.scheme = model, cfun, scheme
+        self.model_id, self.consts, self.sigma = model.engine_spec()
+        self.cfun_id, cf_a0, cf_b0, self.cf_p = cfun.engine_spec()
+        self.N = N = int(conn.nnode)
+        self.ns = model.nsvar
+        self.nobs = model.nobs
+        if N > 1024:
+            raise ValueError('the step kernel holds one node per lane: N <= 1024')
+        couplings = np.atleast_1d(np.asarray(couplings, np.float32))
+        I = self.n = couplings.size
+        self.dt = float(dt)
+        row = np.asarray(conn.row, np.int64).astype(np.int32)
+        col = np.asarray(conn.col, np.int64).astype(np.int32)
+        w = np.asarray(conn.wnz, np.float32)
+        self.row_np, self.col_np, self.w_np = row, col, w
+        self.nnz = int(col.size)
+        # delay tables: one per distinct speed
+        if delays is not None:
+            tables = [np.asarray(delays, np.int64).astype(np.int32)]
+            tab_of = np.zeros(I, np.int64)
+            self.speeds = None
+        else:
+            speeds = np.broadcast_to(np.asarray(speeds, np.float32), (I, )).copy()
+            self.speeds = speeds
+            uniq, tab_of = np.unique(speeds, return_inverse=True)
+            tables = [delays_f32(conn.lnz, s, dt, rounding) for s in uniq]
+        self.delay_tables = tables
+        self.tab_of = tab_of
+        # ring plan per table
+        plans = []
+        for d in tables:
+            dmin = int(d.min()) if d.size else 0
+            dmax = int(d.max()) if d.size else 0
+            plans.append(plan_ring(dmin, dmax, nh_extra, order))
+        self.order = order
+        self.lognh = np.array([plans[t][0] for t in tab_of], np.int32)
+        self.sync_every = np.array([plans[t][1] for t in tab_of], np.int32)
+        self.order_flags = np.array([plans[t][2] for t in tab_of], np.uint32)
+        # packed edges per (table), device
+        ebufs, eoff = [], []
+        off = 0
+        for t, d in enumerate(tables):
+            e = pack_edges(row, col, w, d, plans[t][0])
+            ebufs.append(e)
+            eoff.append(off)
+            off += max(1, e.size)
+        edges = np.zeros(off, dtype=np.dtype([('pk', '<u4'), ('w', '<f4')]))
+        for t, e in enumerate(ebufs):
+            edges[eoff[t]:eoff[t] + e.size] = e
+        self.edges = torch.from_numpy(edges.view(np.uint8).copy()).cuda()
+        self.edge_off = eoff
+        self.row = torch.from_numpy(row).cuda()
+        # rings (16-byte aligned: N * nh floats, nh >= 4)
+        ring_len = (N << self.lognh.astype(np.int64))
+        self.ring_off = np.concatenate([[0], np.cumsum(ring_len)[:-1]]).astype(np.int64)
+        self.ring = torch.zeros(int(ring_len.sum()), dtype=torch.float32, device='cuda')
+        # state and parameters
+        if state0 is None:
+            st = np.zeros((I, N, self.ns), np.float32)
+        else:
+            st = np.broadcast_to(np.asarray(state0, np.float32), (I, N, self.ns)).copy()
+        self.state = torch.from_numpy(st).cuda()
+        npar = len(model.param_sym)
+        if nparam is None:
+            npm = np.broadcast_to(model.node_params(N), (I, N, npar)).copy()
+        else:
+            npm = np.asarray(nparam, np.float32)
+            if npm.ndim == 1:
+                npm = npm.reshape(N, 1)
+            if npm.ndim == 2 and npm.shape == (I, N) and npar == 1 and I != N:
+                npm = npm[:, :, None]
+            npm = np.broadcast_to(npm, (I, N, npar)).copy()
+        self.nparam = torch.from_numpy(np.ascontiguousarray(npm, np.float32)).cuda()
+        if history == 'fill':
+            self.fill_history(st)
+        elif history != 'zero':
+            raise ValueError("history must be 'zero' or 'fill'")
+        # monitors
+        self.bold_period = int(bold_period)
+        self.bold_len = int(bold_len)
+        self.bold = None
+        self.bold_out = None
+        fl = int(flags)
+        if self.bold_period > 0:
+            # deviation state (s, f-1, v-1, q-1); rest is zero
+            self.bold = torch.zeros((I, 4, N), dtype=torch.float32, device='cuda')
+            self.bold_out = torch.full((I, max(1, self.bold_len), N), float('nan'),
+                                       dtype=torch.float32, device='cuda')
+            fl |= nat.F_BOLD
+        self.trace_every = int(trace_every)
+        self.trace_len = int(trace_len)
+        self.trace_nobs = int(trace_nobs if trace_nobs is not None else self.nobs)
+        self.trace = None
+        if self.trace_every > 0:
+            self.trace = torch.zeros((I, max(1, self.trace_len), N, self.trace_nobs),
+                                     dtype=torch.float32, device='cuda')
+            fl |= nat.F_TRACE
+        if getattr(scheme, 'noise', False):
+            fl |= nat.F_NOISE
+        self.flags = fl
+        self.seed = int(seed) & ((1 << 64) - 1)
+        self.inst_ids = (np.arange(I, dtype=np.uint32) if inst_ids is None
+                         else np.asarray(inst_ids, np.uint32))
+        self.cf_a = couplings
+        self.cf_b = np.float32(cf_b if cf_b is not None else
+                               (cf_b0 if isinstance(cf_b0, (int, float, np.number)) else 0.0))
+        self.t = np.full(I, int(t0), np.int64)
+        # smem placement
+        cap = max_smem()
+        self.ring_bytes = (N << self.lognh.astype(np.int64)) * 4
+        self.smem_cap = cap
+        self.table = None
+        self.table_dev = None
+
+    # -- helpers ---------------------------------------------------------------
+    def fill_history(self, st):
+        "Fill every ring slot with obs0 of the initial state (history='fill')."
+        torch = self.torch
+        N = self.N
+        obs0 = st[:, :, 0]
+        for b in range(self.n):
+            nh = 1 << int(self.lognh[b])
+            o = int(self.ring_off[b])
+            self.ring[o:o + N * nh] = torch.from_numpy(
+                np.repeat(obs0[b], nh).astype(np.float32)).cuda()
+
+    def threads(self):
+        return 32 * ((self.N + 31) // 32)
+
+    def smem_ring_limit(self, threads):
+        return self.smem_cap - 4 * threads - 16 - _SMEM_RESERVE
+
+    def build_table(self, nsteps, smem_allowed=True):
+        "Fill the numpy instance table for the next `nsteps` steps (vectorised)."
+        I, N = self.n, self.N
+        tab = np.zeros(I, dtype=nat.INSTANCE_DTYPE)
+        bidx = np.arange(I, dtype=np.int64)
+        eoff = np.asarray(self.edge_off, np.int64)[self.tab_of]
+        tab['edges'] = self.edges.data_ptr() + 8 * eoff
+        tab['row'] = self.row.data_ptr()
+        tab['ring'] = self.ring.data_ptr() + 4 * self.ring_off
+        tab['state'] = self.state.data_ptr() + 4 * bidx * N * self.ns
+        tab['nparam'] = self.nparam.data_ptr() + 4 * bidx * N * self.nparam.shape[2]
+        if self.bold is not None:
+            tab['bold'] = self.bold.data_ptr() + 4 * bidx * 4 * N
+            tab['bold_out'] = self.bold_out.data_ptr() + 4 * bidx * self.bold_out.shape[1] * N
+        if self.trace is not None:
+            tab['trace'] = (self.trace.data_ptr()
+                            + 4 * bidx * self.trace.shape[1] * N * self.trace_nobs)
+        tab['t0'] = self.t
+        tab['trace_stride'] = N * self.trace_nobs
+        tab['nsteps'] = np.broadcast_to(np.asarray(nsteps, np.int64), (I, )).astype(np.int32)
+        tab['N'] = N
+        tab['nnz'] = self.nnz
+        tab['lognh'] = self.lognh
+        tab['model'] = self.model_id
+        tab['cfun'] = self.cfun_id
+        limit = self.smem_ring_limit(self.threads())
+        fits = (self.ring_bytes <= limit) if smem_allowed else np.zeros(I, bool)
+        fl = (self.flags | self.order_flags).astype(np.uint32)
+        tab['flags'] = np.where(fits, fl | nat.F_SMEM_RING, fl).astype(np.uint32)
+        tab['sync_every'] = self.sync_every
+        tab['trace_every'] = max(1, self.trace_every)
+        tab['trace_len'] = max(1, self.trace_len)
+        tab['trace_nobs'] = self.trace_nobs
+        tab['bold_period'] = max(1, self.bold_period)
+        tab['bold_len'] = self.bold_len
+        tab['bold_obs'] = self.bold_obs()
+        tab['seed_lo'] = self.seed & 0xffffffff
+        tab['seed_hi'] = (self.seed >> 32) & 0xffffffff
+        tab['inst_id'] = self.inst_ids
+        tab['dt'] = np.float32(self.dt)
+        tab['sqrt_dt'] = np.sqrt(np.float32(self.dt)).astype(np.float32)
+        tab['dt_bold'] = np.float32(self.dt / 1000.0)
+        tab['cf_a'] = self.cf_a
+        tab['cf_b'] = self.cf_b
+        tab['cf_p'] = np.asarray(self.cf_p, np.float32)
+        tab['sigma'] = self.sigma
+        tab['consts'] = self.consts
+        return tab
+
+    def bold_obs(self):
+        "Observable feeding the balloon: sin(theta) for Kuramoto, V for G2DO, r for MPR."
+        if self.model_id == nat.MODEL_KURAMOTO:
+            return 1
+        if self.model_id == nat.MODEL_G2DO:
+            return 1
+        return 0
+
+    def groups(self, tab):
+        """
+        Launch groups: (indices, smem_ring) with indices sharing a ring
+        placement and size, so each launch reserves only what it needs.
+        """
+        smem = (tab['flags'] & nat.F_SMEM_RING) != 0
+        keys = {}
+        for b in range(self.n):
+            k = (bool(smem[b]), int(tab['lognh'][b]) if smem[b] else -1)
+            keys.setdefault(k, []).append(b)
+        out = []
+        for (sm, lognh), idx in sorted(keys.items(), key=lambda kv: -len(kv[1])):
+            ring = int(self.ring_bytes[idx[0]]) if sm else 0
+            out.append((np.array(idx, np.int64), ring))
+        return out
+
+
+class Sweep(InstanceSet):
+    """
+    The plain path: ``run(nsteps)`` advances every instance by nsteps with
+    one tvbg_sweep launch per ring group (one CTA per instance).
+    """
+
+    def __init__(self, *args, tpn=None, **kwargs):
+        super().__init__(*args, **kwargs)
+        self.tpn = tpn
+        self.status = DeviceStatus()
+        self._uploaded = None
+
+    def _launch_cfg(self, smem_ring, tpn):
+        cfg = nat.tvbg_launch()
+        cfg.model = self.model_id
+        cfg.cfun = self.cfun_id
+        cfg.threads = self.threads()
+        cfg.tpn = int(tpn)
+        cfg.smem_ring = int((smem_ring + 15) // 16 * 16)
+        cfg.ctas = 0
+        cfg.d_status = self.status.t.data_ptr()
+        return cfg
+
+    def prepare(self, nsteps):
+        "Build and upload the instance tables of every launch group."
+        torch = self.torch
+        tab = self.build_table(nsteps)
+        launches = []
+        for idx, smem in self.groups(tab):
+            sub = np.ascontiguousarray(tab[idx])
+            dev = torch.from_numpy(sub.view(np.uint8).copy()).cuda()
+            launches.append((dev, len(idx), smem))
+        self._uploaded = launches
+        return launches
+
+    def pick_tpn(self):
+        if self.tpn is None:
+            from .autotune import tune_tpn
+            self.tpn = tune_tpn(self)
+        return self.tpn
+
+    def launch(self, launches=None, tpn=None, stream=None):
+        "Enqueue the prepared launches on `stream` (no host sync)."
+        lib = nat.load()
+        launches = launches if launches is not None else self._uploaded
+        tpn = tpn if tpn is not None else (self.tpn or 2)
+        sh = nat.stream_handle(stream)
+        for dev, n, smem in launches:
+            cfg = self._launch_cfg(smem, tpn)
+            nat.check(lib.tvbg_sweep(dev.data_ptr(), n, ctypes.byref(cfg), sh))
+
+    def run(self, nsteps, stream=None, check=True):
+        "Advance all instances by nsteps (chunk boundaries are exact)."
+        tpn = self.pick_tpn()
+        launches = self.prepare(nsteps)
+        self.launch(launches, tpn, stream)
+        self.t += int(nsteps)
+        if check:
+            self.torch.cuda.synchronize()
+            self.status.check()
+
+    # -- results ----------------------------------------------------------------
+    def ring_plain(self, b):
+        "Ring of instance b as numpy [nh, N] slot-major (the oracle's layout)."
+        nh = 1 << int(self.lognh[b])
+        o = int(self.ring_off[b])
+        return unskew_ring(self.ring[o:o + self.N * nh].cpu().numpy(), self.N, int(self.lognh[b]))
