@@ -1,0 +1,423 @@
+"""
+Benchmark of the GB300 brain-network step engine.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload NAME]
+    python bench.py --impl reference ...      (the CPU arm, host cores)
+
+One bench "step" is one full pass of the workload: every instance of the
+sweep is reset to its seeded initial state (device-resident copy) and run
+for all of its time steps, then the per-instance FC is computed.  The
+workload sizes are those of the benchmark configurations (seeded synthetic
+connectomes; there is no dataset):
+
+  grid   (default) dense parameter grid: generic 2-D oscillator (G2DO) with
+         linear difference coupling and Euler-Maruyama noise (sigma 1e-3,
+         Philox keyed by seed/instance/node/step), N = 84, 30% density,
+         64 x 64 grid of G in logspace(-3, 0) x speed in linspace(1, 20)
+         mm/ms = 4096 instances, dt 0.1 ms, 100k steps, Balloon-Windkessel
+         BOLD sampled every 720 ms, 84 x 84 Pearson FC per instance against a
+         seeded target FC.
+  kuramoto  plain Kuramoto sweep, N = 68, 32 instances, 1000 steps (the
+         CPU-runnable parity case).
+
+Metric: node-steps/s (one node x one instance x one time step).  `value`
+is device-resident throughput (CUDA events on the launching stream, max
+over ranks); `e2e` repeats the step through the public API with the
+initial state uploaded from pinned host memory and the FC matrices read
+back every step.  Multi-GPU runs (torchrun) are replicas: every rank runs
+the whole workload on its GPU (weak scaling, no collective on the data
+path).
+"""
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, 'tvb-hpc_gb300'))
+
+METRIC = 'node-steps/s on 1 GB300: batched/served vs plain, same tol; p50/p99 sweep latency'
+UNIT = 'node-steps/s'
+
+
+# ---------------------------------------------------------------------------
+# workloads
+# ---------------------------------------------------------------------------
+def grid_workload(n_g=64, n_s=64, nsteps=100_000, N=84, seed=0):
+    from tvb_hpc import network
+    w, ln = network.synthetic_connectome(N, 0.3, seed=seed)
+    conn = network.Connectivity.from_dense(w, ln)
+    G = np.logspace(-3, 0, n_g).astype(np.float32)
+    S = np.linspace(1, 20, n_s).astype(np.float32)
+    gg, ss = np.meshgrid(G, S, indexing='ij')
+    rng = np.random.default_rng(seed + 1)
+    I = gg.size
+    x0 = rng.uniform(-0.5, 0.5, (I, N, 2)).astype(np.float32)
+    target = np.corrcoef(rng.normal(size=(N, 200))).astype(np.float32)
+    bold_period = 7200  # 720 ms at dt 0.1 ms
+    return dict(name='grid', conn=conn, couplings=gg.ravel(), speeds=ss.ravel(), x0=x0,
+                nsteps=nsteps, dt=0.1, bold_period=bold_period,
+                bold_len=nsteps // bold_period, target=target, model='G2DO', cfun='Diff',
+                noise=True, seed=12345)
+
+
+def kuramoto_workload(I=32, N=68, nsteps=1000, seed=0):
+    from tvb_hpc import network
+    w, ln = network.synthetic_connectome(N, 0.3, seed=seed)
+    conn = network.Connectivity.from_dense(w, ln)
+    rng = np.random.default_rng(seed + 1)
+    x0 = rng.uniform(0, 2 * np.pi, (I, N, 1)).astype(np.float32)
+    omega = rng.normal(2 * np.pi * 0.01, 0.001, (I, N, 1)).astype(np.float32)
+    return dict(name='kuramoto', conn=conn, couplings=np.logspace(-2, 1, I).astype(np.float32),
+                speeds=np.full(I, 4.0, np.float32), x0=x0, nparam=omega, nsteps=nsteps, dt=0.1,
+                bold_period=0, bold_len=0, target=None, model='Kuramoto', cfun='Kuramoto',
+                noise=False, seed=0)
+
+
+WORKLOADS = {'grid': grid_workload, 'kuramoto': kuramoto_workload}
+
+
+def workload_config(wl):
+    c = wl['conn']
+    return {'workload': wl['name'], 'model': wl['model'], 'coupling': wl['cfun'],
+            'nodes': int(c.nnode), 'edges': int(c.nnz), 'instances': int(wl['couplings'].size),
+            'time_steps': int(wl['nsteps']), 'dt_ms': wl['dt'],
+            'noise': 'philox-em' if wl['noise'] else 'off',
+            'bold_period_steps': int(wl['bold_period']), 'fc': wl['target'] is not None,
+            'l2': 'inputs larger than L2 (rings+state)', 'parallelism': 'replicas'}
+
+
+def node_steps(wl):
+    return float(wl['couplings'].size) * wl['conn'].nnode * wl['nsteps']
+
+
+def algorithmic_bytes_per_node_step(wl, nsvar):
+    """Data touched per node-step (SURVEY 8(d) accounting): 4 B per delayed
+    read of the coupled variable, 8 B per state variable (read + write),
+    32 B for the balloon state when BOLD is on."""
+    E = wl['conn'].nnz / wl['conn'].nnode
+    return 4.0 * E + 8.0 * nsvar + (32.0 if wl['bold_period'] else 0.0)
+
+
+# ---------------------------------------------------------------------------
+# clocks sampled during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    QUERY = ('clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,'
+             'clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,'
+             'clocks_event_reasons.sw_power_cap')
+
+    def __init__(self, index=0):
+        self.index = index
+        self.samples = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ['nvidia-smi', '-i', str(self.index), '--query-gpu=' + self.QUERY,
+                 '--format=csv,noheader,nounits', '-lms', '200'],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.samples.append([x.strip() for x in line.split(',')])
+
+    def stop(self):
+        if self.proc is None:
+            return {'sm_mhz': None, 'sm_max_mhz': None, 'reasons': ['nvidia-smi unavailable']}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+        for s in self.samples:
+            try:
+                sm.append(float(s[0]))
+                mx.append(float(s[1]))
+            except (ValueError, IndexError):
+                continue
+            for name, v in zip(names, s[3:7]):
+                if v.lower() == 'active':
+                    reasons.add(name)
+        return {'sm_mhz': float(np.median(sm)) if sm else None,
+                'sm_max_mhz': float(max(mx)) if mx else None,
+                'reasons': sorted(reasons), 'samples': len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+def build_sweep(wl, tpn=None):
+    from tvb_hpc import model, coupling, scheme, engine
+    m = getattr(model, wl['model'])()
+    cf = getattr(coupling, wl['cfun'])(m)
+    scm = scheme.EulerMaryuyamaStep(wl['dt']) if wl['noise'] else scheme.EulerStep(wl['dt'])
+    return engine.Sweep(m, cf, scm, wl['conn'], dt=wl['dt'], couplings=wl['couplings'],
+                        speeds=wl['speeds'], state0=wl['x0'], nparam=wl.get('nparam'),
+                        seed=wl['seed'], bold_period=wl['bold_period'], bold_len=wl['bold_len'],
+                        tpn=tpn)
+
+
+class GpuStep:
+    """One bench step on the device: reset state/ring/balloon from resident
+    copies, run every instance for all steps, compute FC."""
+
+    def __init__(self, wl, torch):
+        self.torch = torch
+        self.wl = wl
+        self.sw = build_sweep(wl)
+        self.sw.pick_tpn()
+        self.x0 = self.sw.state.clone()
+        self.target = (torch.from_numpy(wl['target']).cuda() if wl['target'] is not None
+                       else None)
+        self.launches = self.sw.prepare(wl['nsteps'])
+        self.n_launch = len(self.launches)
+        self.kernel_ms = []
+
+    def reset(self, x0=None):
+        sw = self.sw
+        sw.state.copy_(self.x0 if x0 is None else x0)
+        sw.ring.zero_()
+        if sw.bold is not None:
+            sw.bold.zero_()
+
+    def run(self, time_kernels=False):
+        from tvb_hpc import metric
+        torch = self.torch
+        sw = self.sw
+        evs = []
+        if time_kernels:
+            for dev, n, smem in self.launches:
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record()
+                sw.launch([(dev, n, smem)], sw.tpn)
+                e1.record()
+                evs.append((e0, e1))
+        else:
+            sw.launch(self.launches, sw.tpn)
+        fc = None
+        if sw.bold is not None and self.target is not None:
+            fc = metric.fc(sw.bold_out, self.target)
+        return evs, fc
+
+    def launches_per_step(self):
+        fc_launches = 1 if (self.sw.bold is not None and self.target is not None) else 0
+        return self.n_launch + fc_launches
+
+
+def roofline_entry(wl, gs, kernel_ms_total, n_launches):
+    peaks = {}
+    p = os.path.join(ROOT, 'MEASURED_PEAKS.json')
+    if os.path.exists(p):
+        peaks = json.load(open(p))
+    hbm = peaks.get('hbm_gbs')
+    src = 'measured' if hbm else 'fallback'
+    hbm = hbm or 6800.0
+    bpn = algorithmic_bytes_per_node_step(wl, gs.sw.ns)
+    bytes_per_launch = bpn * node_steps(wl) / max(1, gs.n_launch)
+    avg_launch_s = (kernel_ms_total / max(1, n_launches)) / 1e3
+    achieved = bytes_per_launch / avg_launch_s / 1e9
+    traffic = None
+    tp = os.path.join(ROOT, 'profiles', 'traffic.json')
+    if os.path.exists(tp):
+        t = json.load(open(tp)).get(wl['name'])
+        if t:
+            traffic = t.get('dram_bytes_per_launch')
+    return {'bound': 'hbm', 'achieved': round(achieved, 1), 'peak': hbm, 'unit': 'GB/s',
+            'frac': round(achieved / hbm, 4), 'traffic': traffic, 'peak_source': src,
+            'algorithmic_bytes_per_node_step': round(bpn, 2),
+            'note': 'rings staged in shared memory move no HBM bytes; frac > 1 means '
+                    'on-chip reuse beyond an HBM-streaming step'}
+
+
+def cpu_baseline(wl, budget_s=12.0):
+    "The oracle (C restatement, OpenMP over instances) on a bounded sample."
+    sys.path.insert(0, os.path.join(ROOT, 'oracle'))
+    import pyoracle as orc
+    from tvb_hpc import network, model as mdl
+    m = getattr(mdl, wl['model'])()
+    kid, consts, sigma = m.engine_spec()
+    cf_id = {'Diff': 1, 'Kuramoto': 2, 'Linear': 0}[wl['cfun']]
+    cores = os.cpu_count() or 1
+    c = wl['conn']
+    I_all = wl['couplings'].size
+    # sample: instances spread over the grid (all speeds present)
+    n_inst = min(I_all, max(cores * 2, 16))
+    idx = np.linspace(0, I_all - 1, n_inst).astype(int)
+
+    def run(nsteps):
+        speeds = wl['speeds'][idx]
+        delays = np.stack([c.delays(s, wl['dt'], 'ceil') for s in speeds])
+        nh = int(2 ** np.ceil(np.log2(delays.max() + 2)))
+        nparam = (np.asarray(wl['nparam'])[idx, :, 0] if wl.get('nparam') is not None
+                  else np.broadcast_to(m.node_params(c.nnode)[:, 0], (n_inst, c.nnode)))
+        t = time.perf_counter()
+        orc.run(kid, cf_id, c.row, c.col, c.wnz, nh, nsteps, wl['dt'], delays,
+                wl['couplings'][idx], nparam, wl['x0'][idx],
+                flags=(orc.F_NOISE if wl['noise'] else 0) | orc.F_BOLD_DEV, sigma=sigma,
+                consts=consts, seed=wl['seed'], bold_period=wl['bold_period'] or 0,
+                bold_len=max(1, nsteps // max(1, wl['bold_period'] or 1)), bold_obs=1,
+                nthreads=cores)
+        return time.perf_counter() - t
+
+    probe = 50
+    dt_probe = run(probe)
+    nsteps = int(np.clip(probe * budget_s / max(dt_probe, 1e-6), probe, wl['nsteps']))
+    el = run(nsteps)
+    v = n_inst * c.nnode * nsteps / el
+    return {'value': round(v, 1), 'unit': UNIT, 'cores': cores, 'kind': 'port',
+            'sample': '%d of %d instances x %d steps (%.1f s), oracle C + OpenMP, -O3' % (
+                n_inst, I_all, nsteps, el)}
+
+
+def gpu_arm(args):
+    import torch
+    import torch.distributed as dist
+    world = int(os.environ.get('WORLD_SIZE', '1'))
+    rank = int(os.environ.get('RANK', '0'))
+    local = int(os.environ.get('LOCAL_RANK', '0'))
+    if world > 1:
+        dist.init_process_group('nccl')
+    torch.cuda.set_device(local)
+    from tvb_hpc import _native
+    _native.load()
+    wl = WORKLOADS[args.workload]()
+    gs = GpuStep(wl, torch)
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    # warm-up
+    for _ in range(args.warmup):
+        gs.reset()
+        gs.run()
+    torch.cuda.synchronize()
+    # device-resident timed region
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier()
+    e_start = torch.cuda.Event(enable_timing=True)
+    e_stop = torch.cuda.Event(enable_timing=True)
+    kern_ms, n_kern = 0.0, 0
+    all_evs = []
+    e_start.record()
+    for _ in range(args.steps):
+        gs.reset()
+        evs, fc = gs.run(time_kernels=True)
+        all_evs.extend(evs)
+    e_stop.record()
+    barrier()
+    clk = clocks.stop()
+    total_ms = e_start.elapsed_time(e_stop)
+    for a, b in all_evs:
+        kern_ms += a.elapsed_time(b)
+        n_kern += 1
+    t = torch.tensor([total_ms], device='cuda')
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    total_ms = float(t.item())
+    ms_per_step = total_ms / args.steps
+    value = world * node_steps(wl) * args.steps / (total_ms / 1e3)
+    gs.sw.status.check()
+
+    # end-to-end through the public API: pinned host state in, FC out
+    host_x0 = gs.x0.cpu().pin_memory()
+    host_fc = torch.empty((wl['couplings'].size, wl['conn'].nnode, wl['conn'].nnode),
+                          dtype=torch.float32).pin_memory() if wl['target'] is not None else None
+    host_state = torch.empty_like(gs.sw.state, device='cpu').pin_memory()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        x0_dev = host_x0.cuda(non_blocking=True)
+        gs.reset(x0_dev)
+        _, fc = gs.run()
+        if fc is not None:
+            host_fc.copy_(fc[0], non_blocking=True)
+        else:
+            host_state.copy_(gs.sw.state, non_blocking=True)
+        torch.cuda.synchronize()
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    te = torch.tensor([e2e_s], device='cuda')
+    if world > 1:
+        dist.all_reduce(te, op=dist.ReduceOp.MAX)
+    e2e_s = float(te.item())
+    h2d = host_x0.numel() * 4
+    d2h = (host_fc.numel() if host_fc is not None else host_state.numel()) * 4
+    e2e = {'value': round(world * node_steps(wl) * args.steps / e2e_s, 1), 'unit': UNIT,
+           'h2d_bytes_per_step': int(h2d), 'd2h_bytes_per_step': int(d2h)}
+
+    line = {'metric': METRIC, 'value': round(value, 1), 'unit': UNIT, 'n_gpus': world,
+            'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': round(ms_per_step, 3),
+            'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32',
+            'data': 'synthetic (seeded connectomes, config recipe)',
+            'config': workload_config(wl), 'e2e': e2e,
+            'gpu_launches': gs.launches_per_step() * args.steps,
+            'roofline': roofline_entry(wl, gs, kern_ms, n_kern),
+            'clocks': clk, 'tpn': gs.sw.tpn}
+    if rank == 0 and world == 1 and not args.no_cpu:
+        line['cpu_baseline'] = cpu_baseline(wl)
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def reference_arm(args):
+    "The reference path's CPU implementation (the oracle port) on host cores."
+    rank = int(os.environ.get('RANK', '0'))
+    if rank != 0:
+        return
+    wl = WORKLOADS[args.workload]()
+    vals = []
+    for i in range(args.warmup + args.steps):
+        cb = cpu_baseline(wl, budget_s=args.ref_seconds)
+        if i >= args.warmup:
+            vals.append(cb['value'])
+    v = float(np.median(vals))
+    cb['value'] = round(v, 1)
+    line = {'metric': METRIC, 'value': round(v, 1), 'unit': UNIT, 'n_gpus': 0,
+            'steps': args.steps, 'warmup': args.warmup, 'higher_is_better': True,
+            'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32',
+            'data': 'synthetic (seeded connectomes, config recipe)', 'impl': 'reference',
+            'config': workload_config(wl), 'cpu_baseline': cb,
+            'e2e': {'value': round(v, 1), 'unit': UNIT, 'h2d_bytes_per_step': 0,
+                    'd2h_bytes_per_step': 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.split('\n')[1])
+    ap.add_argument('--gpus', type=int, default=1)
+    ap.add_argument('--steps', type=int, default=3)
+    ap.add_argument('--warmup', type=int, default=3)
+    ap.add_argument('--workload', default='grid', choices=sorted(WORKLOADS))
+    ap.add_argument('--impl', default='engine', choices=['engine', 'reference'])
+    ap.add_argument('--no-cpu', action='store_true', help='skip the cpu_baseline leg')
+    ap.add_argument('--ref-seconds', type=float, default=8.0)
+    args = ap.parse_args()
+    if args.impl == 'reference':
+        reference_arm(args)
+    else:
+        gpu_arm(args)
+
+
+if __name__ == '__main__':
+    main()

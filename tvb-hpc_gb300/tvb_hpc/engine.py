@@ -159,7 +159,8 @@ class InstanceSet:
     def __init__(self, model, cfun, scheme, conn, dt, couplings, speeds=None, state0=None,
                  nparam=None, delays=None, rounding='ceil', seed=0, inst_ids=None,
                  history='zero', bold_period=0, bold_len=0, trace_every=0, trace_len=0,
-                 trace_nobs=None, flags=0, cf_b=None, nh_extra=0, t0=0, order='cuda'):
+                 trace_nobs=None, flags=0, cf_b=None, nh_extra=0, t0=0, order='cuda',
+                 sync_every=None):
         _device_ok()
         torch = _torch()
         self.torch = torch
@@ -201,6 +202,8 @@ class InstanceSet:
         self.lognh = np.array([plans[t][0] for t in tab_of], np.int32)
         self.sync_every = np.array([plans[t][1] for t in tab_of], np.int32)
         self.order_flags = np.array([plans[t][2] for t in tab_of], np.uint32)
+        if sync_every is not None:  # tighter barrier interval (never looser than planned)
+            self.sync_every = np.minimum(self.sync_every, int(sync_every)).astype(np.int32)
         # packed edges per (table), device
         ebufs, eoff = [], []
         off = 0
