@@ -16,7 +16,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, '_build', 'liboracle.so')
 REF_LIB = os.path.join(HERE, '_ref', 'libtvbref.so')
 
-F_NOISE, F_BOLD, F_TRACE, F_WRAP_FMOD, F_NO_WRAP, F_BOLD_DEV, F_TRACKA = 1, 2, 4, 8, 32, 64, 128
+# the same bit values as include/tvbg.h's TVBG_F_*; F_BOLD_DEV is oracle-only
+F_NOISE, F_BOLD, F_TRACE, F_WRAP_FMOD, F_NO_WRAP, F_TRACKA = 1, 2, 4, 8, 32, 64
+F_BOLD_DEV = 256
+_SEMANTIC = F_NOISE | F_WRAP_FMOD | F_NO_WRAP | F_TRACKA
 
 
 class OrcCfg(ctypes.Structure):
@@ -131,11 +134,11 @@ def run_sweep_like(sw, state0, nsteps, real='f32', t0=0, rings=None, bold=None, 
     I = sw.n
     state0 = np.broadcast_to(np.asarray(state0), (I, sw.N, sw.ns))
     nparam = sw.nparam.cpu().numpy()[:, :, 0]
-    flags = (sw.flags & ~(F_BOLD | F_TRACE)) | F_BOLD_DEV
+    flags = (int(sw.flags) & _SEMANTIC) | F_BOLD_DEV
     res = dict(state=None, rings=[None] * I, bold=None, bold_out=None, trace=None)
     for lognh in sorted(set(int(x) for x in sw.lognh)):
         idx = np.nonzero(sw.lognh == lognh)[0]
-        fl = flags | int(sw.order_flags[idx[0]]) & F_TRACKA
+        fl = flags | (int(sw.order_flags[idx[0]]) & F_TRACKA)
         delays = np.stack([sw.delay_tables[int(sw.tab_of[b])] for b in idx])
         ring = None if rings is None else np.stack([rings[b] for b in idx])
         bo = None if bold is None else np.asarray(bold)[idx]

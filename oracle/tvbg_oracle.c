@@ -47,16 +47,17 @@
 #define ORC_CFUN_KURAMOTO 2
 #define ORC_CFUN_SIGMOIDAL 3
 
+/* flag values shared with include/tvbg.h (TVBG_F_*), plus oracle-only bits */
 #define ORC_F_NOISE 1u
 #define ORC_F_BOLD 2u
 #define ORC_F_TRACE 4u
 #define ORC_F_WRAP_FMOD 8u
 #define ORC_F_NO_WRAP 32u
-#define ORC_F_BOLD_DEV 64u /* balloon on deviations from rest (the engine's form) */
+#define ORC_F_BOLD_DEV 256u /* balloon on deviations from rest (the engine's form) */
 /* Track-A order (tvb_hpc/transforms.py:30-42): the network gather of step t
  * runs before the model writes obsrv[t], so slot t is read as it was (post
  * and zero delays see the old row) and is then overwritten with obs(x_t). */
-#define ORC_F_TRACKA 128u
+#define ORC_F_TRACKA 64u
 
 /* Launch-wide configuration (host memory). */
 typedef struct orc_cfg {

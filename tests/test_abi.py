@@ -135,3 +135,17 @@ def test_plan_ring_constraints():
                     assert sync == 1 and fl & nat.F_MIDSYNC
                 else:
                     assert 1 <= sync <= dmin and sync <= nh - dmax
+
+
+def test_oracle_flag_values_match_the_abi():
+    "The oracle reads engine flags directly: the bit values must agree with tvbg.h."
+    import pyoracle as orc
+    text = open(HEADER).read()
+    for name in ('NOISE', 'BOLD', 'TRACE', 'WRAP_FMOD', 'NO_WRAP', 'TRACKA'):
+        m = re.search(r'#define TVBG_F_%s (\d+)u' % name, text)
+        assert m, name
+        assert int(m.group(1)) == getattr(orc, 'F_' + name) == getattr(nat, 'F_' + name)
+    src = open(os.path.join(ROOT, 'oracle', 'tvbg_oracle.c')).read()
+    for name in ('NOISE', 'BOLD', 'TRACE', 'WRAP_FMOD', 'NO_WRAP', 'TRACKA'):
+        m = re.search(r'#define ORC_F_%s (\d+)u' % name, src)
+        assert int(m.group(1)) == getattr(nat, 'F_' + name)
