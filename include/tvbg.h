@@ -224,6 +224,28 @@ int tvbg_fc_ex(const float *d_x, int32_t n_inst, int32_t T, int32_t N,
                double *d_err, double *d_scratch, void *stream);
 
 /*
+ * Allocation-free variant of tvbg_fc_ex, for callers that cannot call
+ * cudaMalloc: code whose device memory is owned by a host framework's pool
+ * or budget (a serving runtime, a plugin inside another runtime) and loops
+ * that may not take cudaMalloc's implicit device synchronisation.  It has no
+ * counterpart in the reference.
+ *
+ * The FP64 scratch of the N > 126 path lives in a file-scope device array of
+ * TVBG_FC_NOALLOC_MAX_DOUBLES doubles (8 MiB), which every GPU that loads the
+ * library holds until the process exits; a call needs n_inst * N * (N + 1)
+ * doubles and is rejected with TVBG_EINVAL beyond that.  The first call on a
+ * device looks up the array's device address (cudaGetSymbolAddress) with
+ * that device current; make that first call before any stream capture.  All
+ * calls share the one array: every scratch entry a call reads it has written
+ * first, but calls that overlap on the GPU (different streams, no ordering)
+ * race on it and must be serialised by the caller.
+ */
+#define TVBG_FC_NOALLOC_MAX_DOUBLES 1048576
+int tvbg_fc_noalloc(const float *d_x, int32_t n_inst, int32_t T, int32_t N,
+                    int64_t inst_stride, float *d_fc, const float *d_target,
+                    double *d_err, void *stream);
+
+/*
  * Fill d_out[0..n) with standard normals from Philox4x32-10 (Salmon et al.
  * 2011) + Box-Muller: key = (seed_lo, stream_id), counter = (i/4, 0,
  * seed_hi, 0) for output i.  Replaces tvb_hpc/rng.py:30-96 (RNG.fill).

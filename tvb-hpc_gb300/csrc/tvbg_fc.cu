@@ -10,6 +10,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <mutex>
 
 #include "tvbg_abi_internal.h"
 
@@ -231,4 +232,57 @@ extern "C" int tvbg_fc_ex(const float* d_x, int32_t n_inst, int32_t T, int32_t N
 extern "C" int tvbg_fc(const float* d_x, int32_t n_inst, int32_t T, int32_t N, int64_t inst_stride,
                        float* d_fc, const float* d_target, double* d_err, void* stream) {
     return tvbg_fc_ex(d_x, n_inst, T, N, inst_stride, d_fc, d_target, d_err, nullptr, stream);
+}
+
+// ---- allocation-free variant (tvbg_fc_noalloc) ------------------------------
+// Scratch for callers that cannot allocate device memory: a file-scope device
+// array, one instance per device that loads this library.  Host code must not
+// pass `g_fc_noalloc_scratch` itself to a kernel (in host code the name is a
+// host-side stand-in); its device address comes from cudaGetSymbolAddress.
+static __device__ __align__(256) double g_fc_noalloc_scratch[TVBG_FC_NOALLOC_MAX_DOUBLES];
+
+namespace {
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+double* g_noalloc_addr[kMaxDevices] = {};
+
+// Device address of the scratch array on `dev` (the current device), looked
+// up once per device on first use.
+int noalloc_scratch(int dev, double** out) {
+    if (dev < 0 || dev >= kMaxDevices) return set_error(TVBG_EINVAL, "tvbg_fc_noalloc: device index out of range");
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_addr[dev]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_fc_noalloc_scratch);
+        if (e != cudaSuccess) return set_cuda_error(e, "tvbg_fc_noalloc: cudaGetSymbolAddress");
+        g_noalloc_addr[dev] = static_cast<double*>(p);
+    }
+    *out = g_noalloc_addr[dev];
+    return TVBG_OK;
+}
+}  // namespace
+
+extern "C" int tvbg_fc_noalloc(const float* d_x, int32_t n_inst, int32_t T, int32_t N,
+                               int64_t inst_stride, float* d_fc, const float* d_target,
+                               double* d_err, void* stream) {
+    if (n_inst <= 0 || N <= 0) return set_error(TVBG_EINVAL, "tvbg_fc_noalloc: bad arguments");
+    int64_t need = 0;
+    int rc = tvbg_fc_scratch_bytes(n_inst, N, &need);
+    if (rc) return rc;
+    need /= static_cast<int64_t>(sizeof(double));
+    if (need > TVBG_FC_NOALLOC_MAX_DOUBLES)
+        return set_error(TVBG_EINVAL,
+                         "tvbg_fc_noalloc: n_inst * N * (N + 1) exceeds TVBG_FC_NOALLOC_MAX_DOUBLES; "
+                         "split the instances over several calls or use tvbg_fc_ex");
+    double* scratch = nullptr;
+    if (need > 0) {
+        int dev = 0;
+        cudaError_t e = cudaGetDevice(&dev);
+        if (e != cudaSuccess) return set_cuda_error(e, "tvbg_fc_noalloc: cudaGetDevice");
+        rc = noalloc_scratch(dev, &scratch);
+        if (rc) return rc;
+    }
+    // the mean and Gram kernels write every scratch entry they later read,
+    // so the previous call's contents need no clearing
+    return tvbg_fc_ex(d_x, n_inst, T, N, inst_stride, d_fc, d_target, d_err, scratch, stream);
 }

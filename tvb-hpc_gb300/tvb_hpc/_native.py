@@ -27,6 +27,8 @@ TVBG_ETIMEOUT = -3
 TVBG_EUNSUPPORTED = -4
 TVBG_EDEVICE = -5
 
+FC_NOALLOC_MAX_DOUBLES = 1048576
+
 MODEL_KURAMOTO, MODEL_G2DO, MODEL_MPR, MODEL_LINEAR = 0, 1, 2, 3
 CFUN_LINEAR, CFUN_DIFF, CFUN_KURAMOTO, CFUN_SIGMOIDAL = 0, 1, 2, 3
 
@@ -122,6 +124,7 @@ SIGNATURES = {
     'tvbg_fc': (ctypes.c_int, [_vp, _i32, _i32, _i32, _i64, _vp, _vp, _vp, _vp]),
     'tvbg_fc_ex': (ctypes.c_int, [_vp, _i32, _i32, _i32, _i64, _vp, _vp, _vp, _vp, _vp]),
     'tvbg_fc_scratch_bytes': (ctypes.c_int, [_i32, _i32, ctypes.POINTER(_i64)]),
+    'tvbg_fc_noalloc': (ctypes.c_int, [_vp, _i32, _i32, _i32, _i64, _vp, _vp, _vp, _vp]),
     'tvbg_philox_normal': (ctypes.c_int, [_u64, _u32, _vp, _i64, _vp]),
     'tvbg_philox_u32': (ctypes.c_int, [_u32, _u32, _u32, _u32, _u32, _vp, _i64, _vp]),
 }
