@@ -200,11 +200,11 @@ class GpuStep:
         sw = self.sw
         evs = []
         if time_kernels:
-            for dev, n, smem in self.launches:
+            for launch in self.launches:
                 e0 = torch.cuda.Event(enable_timing=True)
                 e1 = torch.cuda.Event(enable_timing=True)
                 e0.record()
-                sw.launch([(dev, n, smem)], sw.tpn)
+                sw.launch([launch], sw.tpn)
                 e1.record()
                 evs.append((e0, e1))
         else:

@@ -144,6 +144,9 @@ typedef struct tvbg_launch {
     int32_t tpn;           /* lanes per node in the gather: 1, 2, 4 or 8        */
     int32_t smem_ring;     /* shared-memory bytes reserved for the ring (0 ok)  */
     int32_t ctas;          /* persistent CTAs (tvbg_batch_run); 0 = 1 per SM    */
+    int32_t block_k;       /* 0 or 1: per-step kernel; 4 or 8: time-blocked     */
+                           /* kernel (K steps per block, padded ring layout)    */
+    int32_t nmax;          /* largest N of the call (blocked kernel); 0 = threads */
     int32_t reserved0;
     int32_t *d_status;     /* optional device int: first device error code      */
     int32_t *d_counter;    /* tvbg_batch_run work counter (zeroed by the call)  */
@@ -174,6 +177,17 @@ int tvbg_pack_edges(int32_t N, int32_t nnz, const int32_t *row,
                     const int32_t *delays, int32_t lognh, tvbg_edge *out);
 
 /*
+ * Host helper for the time-blocked kernel (tvbg_launch.block_k = 4 or 8),
+ * whose ring rows carry 8 ghost slots: node j, slot s lives at
+ * j*(nh+8) + ((s + j) & (nh-1)), and positions < 8 are mirrored at +nh.
+ * pk = (col << 16) | ((col - delay) & (nh - 1)); needs N, nh <= 65536.
+ */
+int tvbg_pack_edges_blocked(int32_t N, int32_t nnz, const int32_t *row,
+                            const int32_t *col, const float *weights,
+                            const int32_t *delays, int32_t lognh,
+                            tvbg_edge *out);
+
+/*
  * Host helper: integer delays d = op(f32(f32(len / speed) / dt)),
  * op = ceil (rounding = 1) or trunc (rounding = 0): the float32 arithmetic of
  * tvb_hpc/examples/hackathon.py:44 under numpy 1.15 casting.  rounding = 2
@@ -191,6 +205,14 @@ int tvbg_delays(int32_t nnz, const float *lengths, float speed, float dt,
  */
 int tvbg_sweep(const tvbg_instance *d_inst, int32_t n_inst,
                const tvbg_launch *cfg, void *stream);
+
+/*
+ * With cfg->block_k = 4 or 8, tvbg_sweep and tvbg_batch_run use the
+ * time-blocked kernel: CUDA step order, couplings whose pre-summation term
+ * depends on the source only (LINEAR, DIFF, SIGMOIDAL), every delay >=
+ * block_k - 1, rings in the padded layout of tvbg_pack_edges_blocked.  It
+ * computes the same step (same Philox stream) as the per-step kernel.
+ */
 
 /*
  * Persistent batched run: cfg->ctas CTAs pull instances (in d_order order)

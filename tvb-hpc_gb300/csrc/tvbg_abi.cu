@@ -36,6 +36,20 @@ static StepKernel lookup(int model, int cfun, int tpn) {
     }
 }
 
+static BlockedKernel lookup_blocked(int model, int cfun, int tpn, int k) {
+    switch (model) {
+        case TVBG_MODEL_G2DO: return blocked_kernel_g2do(cfun, tpn, k);
+        case TVBG_MODEL_MPR: return blocked_kernel_mpr(cfun, tpn, k);
+        case TVBG_MODEL_LINEAR: return blocked_kernel_linear(cfun, tpn, k);
+        default: return nullptr;
+    }
+}
+
+uint32_t blocked_aux_bytes(int model, int k, int nmax) {
+    const int ns = (model == TVBG_MODEL_G2DO || model == TVBG_MODEL_MPR) ? 2 : 1;
+    return 4u * static_cast<uint32_t>(k * nmax * (2 + ns) + 4 * nmax) + 32u;
+}
+
 // Dynamic shared memory of a step launch: ring capacity + per-warp sums + mbarrier.
 static size_t step_smem_bytes(int threads, int smem_ring) {
     return static_cast<size_t>(smem_ring) + 4u * static_cast<size_t>(threads) + 16u;
@@ -49,25 +63,44 @@ static int check_launch(const tvbg_launch* cfg, const tvbg_instance* d_inst, int
         return set_error(TVBG_EINVAL, "tpn must be 1, 2, 4 or 8");
     if (cfg->smem_ring < 0 || (cfg->smem_ring & 15))
         return set_error(TVBG_EINVAL, "smem_ring must be a non-negative multiple of 16");
+    if (cfg->block_k != 0 && cfg->block_k != 1 && cfg->block_k != 4 && cfg->block_k != 8)
+        return set_error(TVBG_EINVAL, "block_k must be 0, 1, 4 or 8");
+    if (cfg->nmax < 0 || cfg->nmax > cfg->threads)
+        return set_error(TVBG_EINVAL, "nmax must be in [0, threads]");
     return TVBG_OK;
 }
 
 static int launch_step(int model, int cfun, const tvbg_instance* d_inst, int32_t n_inst,
                        const tvbg_launch* cfg, bool persistent, void* stream) {
-    StepKernel k = lookup(model, cfun, cfg->tpn);
-    if (!k) return set_error(TVBG_EUNSUPPORTED, "model/coupling pair not built into the library");
-    const size_t smem = step_smem_bytes(cfg->threads, cfg->smem_ring);
+    const bool blocked = cfg->block_k > 1;
+    const int nmax = cfg->nmax > 0 ? cfg->nmax : cfg->threads;
+    const void* kfn = nullptr;
+    StepKernel k1 = nullptr;
+    BlockedKernel kb = nullptr;
+    size_t smem = 0;
+    if (blocked) {
+        kb = lookup_blocked(model, cfun, cfg->tpn, cfg->block_k);
+        if (!kb)
+            return set_error(TVBG_EUNSUPPORTED,
+                             "time-blocked kernel not built for this model/coupling/tpn/block_k");
+        kfn = reinterpret_cast<const void*>(kb);
+        smem = static_cast<size_t>(cfg->smem_ring) + blocked_aux_bytes(model, cfg->block_k, nmax);
+    } else {
+        k1 = lookup(model, cfun, cfg->tpn);
+        if (!k1) return set_error(TVBG_EUNSUPPORTED, "model/coupling pair not built into the library");
+        kfn = reinterpret_cast<const void*>(k1);
+        smem = step_smem_bytes(cfg->threads, cfg->smem_ring);
+    }
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return set_cuda_error(e, "cudaGetDevice");
     int optin = 0;
     e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     if (e != cudaSuccess) return set_cuda_error(e, "cudaDeviceGetAttribute");
-    // the static __shared__ int of the kernel needs a few bytes too
-    if (smem + 64 > static_cast<size_t>(optin))
+    // the kernel's static shared memory (instance descriptor, counter) needs ~300 bytes
+    if (smem + 512 > static_cast<size_t>(optin))
         return set_error(TVBG_EINVAL, "ring capacity exceeds the shared memory of one CTA");
-    e = cudaFuncSetAttribute(reinterpret_cast<const void*>(k),
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+    e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
     if (e != cudaSuccess) return set_cuda_error(e, "cudaFuncSetAttribute(smem)");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     int grid = n_inst;
@@ -82,9 +115,14 @@ static int launch_step(int model, int cfun, const tvbg_instance* d_inst, int32_t
         if (e != cudaSuccess) return set_cuda_error(e, "cudaMemsetAsync(counter)");
     }
     if (grid == 0) return TVBG_OK;
-    k<<<grid, cfg->threads, smem, st>>>(d_inst, n_inst, persistent ? cfg->d_order : nullptr,
-                                        persistent ? cfg->d_counter : nullptr, cfg->d_status,
-                                        static_cast<uint32_t>(cfg->smem_ring));
+    const int32_t* order = persistent ? cfg->d_order : nullptr;
+    int32_t* counter = persistent ? cfg->d_counter : nullptr;
+    if (blocked)
+        kb<<<grid, cfg->threads, smem, st>>>(d_inst, n_inst, order, counter, cfg->d_status,
+                                             static_cast<uint32_t>(cfg->smem_ring), nmax);
+    else
+        k1<<<grid, cfg->threads, smem, st>>>(d_inst, n_inst, order, counter, cfg->d_status,
+                                             static_cast<uint32_t>(cfg->smem_ring));
     e = cudaGetLastError();
     if (e != cudaSuccess) return set_cuda_error(e, "step kernel launch");
     return TVBG_OK;
@@ -156,6 +194,33 @@ int tvbg_pack_edges(int32_t N, int32_t nnz, const int32_t* row, const int32_t* c
             return set_error(TVBG_EINVAL, "tvbg_pack_edges: delay out of [0, nh)");
         const uint32_t uc = static_cast<uint32_t>(c);
         out[e].pk = (uc << lognh) | ((uc - static_cast<uint32_t>(d)) & mask);
+        out[e].w = weights[e];
+    }
+    return TVBG_OK;
+}
+
+int tvbg_pack_edges_blocked(int32_t N, int32_t nnz, const int32_t* row, const int32_t* col,
+                            const float* weights, const int32_t* delays, int32_t lognh,
+                            tvbg_edge* out) {
+    if (N <= 0 || N > 65536 || nnz < 0 || !row || (nnz > 0 && (!col || !weights || !delays || !out)))
+        return set_error(TVBG_EINVAL, "tvbg_pack_edges_blocked: bad arguments");
+    if (lognh < 3 || lognh > 16) return set_error(TVBG_EINVAL, "tvbg_pack_edges_blocked: lognh out of [3, 16]");
+    const uint64_t nh = 1ull << lognh;
+    if (static_cast<uint64_t>(N) * (nh + 8) > (1ull << 32))
+        return set_error(TVBG_EINVAL, "tvbg_pack_edges_blocked: ring indices overflow 32 bits");
+    if (row[0] != 0 || row[N] != nnz)
+        return set_error(TVBG_EINVAL, "tvbg_pack_edges_blocked: row[0] != 0 or row[N] != nnz");
+    for (int32_t i = 0; i < N; ++i)
+        if (row[i + 1] < row[i]) return set_error(TVBG_EINVAL, "tvbg_pack_edges_blocked: row not monotone");
+    const uint32_t mask = static_cast<uint32_t>(nh - 1);
+    for (int32_t e = 0; e < nnz; ++e) {
+        const int32_t c = col[e];
+        const int32_t d = delays[e];
+        if (c < 0 || c >= N) return set_error(TVBG_EINVAL, "tvbg_pack_edges_blocked: column out of range");
+        if (d < 0 || static_cast<uint64_t>(d) >= nh)
+            return set_error(TVBG_EINVAL, "tvbg_pack_edges_blocked: delay out of [0, nh)");
+        const uint32_t uc = static_cast<uint32_t>(c);
+        out[e].pk = (uc << 16) | ((uc - static_cast<uint32_t>(d)) & mask);
         out[e].w = weights[e];
     }
     return TVBG_OK;

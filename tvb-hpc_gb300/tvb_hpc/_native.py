@@ -41,6 +41,8 @@ F_NO_WRAP = 32
 F_TRACKA = 64
 F_MIDSYNC = 128
 
+GHOST = 8  # ghost slots per ring row of the time-blocked kernel
+
 
 class tvbg_edge(ctypes.Structure):
     _fields_ = [('pk', ctypes.c_uint32), ('w', ctypes.c_float)]
@@ -95,6 +97,8 @@ class tvbg_launch(ctypes.Structure):
         ('tpn', ctypes.c_int32),
         ('smem_ring', ctypes.c_int32),
         ('ctas', ctypes.c_int32),
+        ('block_k', ctypes.c_int32),
+        ('nmax', ctypes.c_int32),
         ('reserved0', ctypes.c_int32),
         ('d_status', ctypes.c_void_p),
         ('d_counter', ctypes.c_void_p),
@@ -119,6 +123,7 @@ SIGNATURES = {
     'tvbg_max_smem': (ctypes.c_int, [_ip]),
     'tvbg_pack_edges': (ctypes.c_int, [_i32, _i32, _vp, _vp, _vp, _vp, _i32, _vp]),
     'tvbg_delays': (ctypes.c_int, [_i32, _vp, ctypes.c_float, ctypes.c_float, _i32, _vp]),
+    'tvbg_pack_edges_blocked': (ctypes.c_int, [_i32, _i32, _vp, _vp, _vp, _vp, _i32, _vp]),
     'tvbg_sweep': (ctypes.c_int, [_vp, _i32, ctypes.POINTER(tvbg_launch), _vp]),
     'tvbg_batch_run': (ctypes.c_int, [_vp, _i32, ctypes.POINTER(tvbg_launch), _vp]),
     'tvbg_fc': (ctypes.c_int, [_vp, _i32, _i32, _i32, _i64, _vp, _vp, _vp, _vp]),

@@ -20,7 +20,8 @@ TPN_CHOICES = (1, 2, 4, 8)
 
 def _key(iset):
     return (iset.model_id, iset.cfun_id, iset.N, iset.nnz,
-            tuple(sorted(set(int(x) for x in iset.lognh))), bool(iset.bold is not None))
+            tuple(sorted(set(int(x) for x in iset.lognh))), bool(iset.bold is not None),
+            tuple(sorted(set(int(k) for k in iset.block_k))), iset.warps)
 
 
 def tune_tpn(iset, trial_steps=None, choices=TPN_CHOICES):
@@ -33,6 +34,8 @@ def tune_tpn(iset, trial_steps=None, choices=TPN_CHOICES):
         trial_steps = int(np.clip(20000 // max(1, iset.n), 50, 400))
     snap = [t.clone() if t is not None else None
             for t in (iset.ring, iset.state, iset.bold, iset.bold_out, iset.trace)]
+    if np.all(iset.block_k > 0):
+        choices = tuple(c for c in choices if c >= 2)
     best, best_ms = choices[0], None
     launches = iset.prepare(trial_steps)
     for tpn in choices:

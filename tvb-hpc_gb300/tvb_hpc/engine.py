@@ -82,6 +82,21 @@ def pack_edges(row, col, weights, delays, lognh):
     return out
 
 
+def pack_edges_blocked(row, col, weights, delays, lognh):
+    "tvbg_pack_edges_blocked (padded ring layout of the time-blocked kernel)."
+    lib = nat.load()
+    row = np.ascontiguousarray(row, np.int32)
+    col = np.ascontiguousarray(col, np.int32)
+    w = np.ascontiguousarray(weights, np.float32)
+    d = np.ascontiguousarray(delays, np.int32)
+    N = row.size - 1
+    out = np.zeros(col.size, dtype=np.dtype([('pk', '<u4'), ('w', '<f4')]))
+    nat.check(lib.tvbg_pack_edges_blocked(N, col.size, row.ctypes.data, col.ctypes.data,
+                                          w.ctypes.data, d.ctypes.data, int(lognh),
+                                          out.ctypes.data if col.size else None))
+    return out
+
+
 def plan_ring(dmin, dmax, extra=0, order='cuda'):
     """
     (lognh, sync_every, extra_flags) for delays in [dmin, dmax]: the smallest
@@ -154,13 +169,17 @@ class InstanceSet:
     trace_every, trace_len, trace_nobs : observable trace sampling
     flags : extra TVBG_F_* bits (e.g. F_WRAP_FMOD)
     cf_b : coupling offset b (default from cfun.param)
+    blocked : 'auto' | True | False -- use the time-blocked kernel (K steps
+              per block, padded ring rows) where the coupling is separable,
+              the order is 'cuda' and d_min + 1 >= 4
+    warps : CTA width of the blocked kernel in warps (default: autotuned)
     """
 
     def __init__(self, model, cfun, scheme, conn, dt, couplings, speeds=None, state0=None,
                  nparam=None, delays=None, rounding='ceil', seed=0, inst_ids=None,
                  history='zero', bold_period=0, bold_len=0, trace_every=0, trace_len=0,
                  trace_nobs=None, flags=0, cf_b=None, nh_extra=0, t0=0, order='cuda',
-                 sync_every=None):
+                 sync_every=None, blocked='auto', warps=None):
         _device_ok()
         torch = _torch()
         self.torch = torch
@@ -204,11 +223,28 @@ class InstanceSet:
         self.order_flags = np.array([plans[t][2] for t in tab_of], np.uint32)
         if sync_every is not None:  # tighter barrier interval (never looser than planned)
             self.sync_every = np.minimum(self.sync_every, int(sync_every)).astype(np.int32)
+        # time-blocked kernel where it applies (K steps per block)
+        separable = self.cfun_id in (nat.CFUN_LINEAR, nat.CFUN_DIFF, nat.CFUN_SIGMOIDAL)
+        can_block = separable and order == 'cuda' and self.model_id != nat.MODEL_KURAMOTO
+        tab_k = []
+        for t, d in enumerate(tables):
+            dmin = int(d.min()) if d.size else 0
+            k = 8 if dmin + 1 >= 8 else (4 if dmin + 1 >= 4 else 0)
+            if blocked is False or not can_block or plans[t][0] > 16:
+                k = 0
+            elif blocked is True and k == 0:
+                raise ValueError('blocked kernel needs d_min + 1 >= 4 (d_min = %d)' % dmin)
+            tab_k.append(k)
+        self.block_k = np.array([tab_k[t] for t in tab_of], np.int32)
+        self.warps = warps
         # packed edges per (table), device
         ebufs, eoff = [], []
         off = 0
         for t, d in enumerate(tables):
-            e = pack_edges(row, col, w, d, plans[t][0])
+            if tab_k[t]:
+                e = pack_edges_blocked(row, col, w, d, plans[t][0])
+            else:
+                e = pack_edges(row, col, w, d, plans[t][0])
             ebufs.append(e)
             eoff.append(off)
             off += max(1, e.size)
@@ -218,8 +254,11 @@ class InstanceSet:
         self.edges = torch.from_numpy(edges.view(np.uint8).copy()).cuda()
         self.edge_off = eoff
         self.row = torch.from_numpy(row).cuda()
-        # rings (16-byte aligned: N * nh floats, nh >= 4)
-        ring_len = (N << self.lognh.astype(np.int64))
+        # rings (16-byte aligned): N * stride floats, stride = nh (per-step
+        # kernel) or nh + GHOST (time-blocked kernel)
+        self.stride = ((1 << self.lognh.astype(np.int64))
+                       + np.where(self.block_k > 0, nat.GHOST, 0)).astype(np.int64)
+        ring_len = N * self.stride
         self.ring_off = np.concatenate([[0], np.cumsum(ring_len)[:-1]]).astype(np.int64)
         self.ring = torch.zeros(int(ring_len.sum()), dtype=torch.float32, device='cuda')
         # state and parameters
@@ -275,7 +314,7 @@ class InstanceSet:
         self.t = np.full(I, int(t0), np.int64)
         # smem placement
         cap = max_smem()
-        self.ring_bytes = (N << self.lognh.astype(np.int64)) * 4
+        self.ring_bytes = N * self.stride * 4
         self.smem_cap = cap
         self.table = None
         self.table_dev = None
@@ -287,15 +326,24 @@ class InstanceSet:
         N = self.N
         obs0 = st[:, :, 0]
         for b in range(self.n):
-            nh = 1 << int(self.lognh[b])
+            R = int(self.stride[b])
             o = int(self.ring_off[b])
-            self.ring[o:o + N * nh] = torch.from_numpy(
-                np.repeat(obs0[b], nh).astype(np.float32)).cuda()
+            self.ring[o:o + N * R] = torch.from_numpy(
+                np.repeat(obs0[b], R).astype(np.float32)).cuda()
 
-    def threads(self):
-        return 32 * ((self.N + 31) // 32)
+    def threads(self, blocked_k=0):
+        own = 32 * ((self.N + 31) // 32)
+        if blocked_k and self.warps:
+            return max(own, 32 * int(self.warps))
+        if blocked_k:
+            return max(own, 256)
+        return own
 
-    def smem_ring_limit(self, threads):
+    def smem_ring_limit(self, threads, blocked_k=0):
+        if blocked_k:
+            ns = self.ns
+            aux = 4 * (blocked_k * self.N * (2 + ns) + 4 * self.N) + 32
+            return self.smem_cap - aux - _SMEM_RESERVE
         return self.smem_cap - 4 * threads - 16 - _SMEM_RESERVE
 
     def build_table(self, nsteps, smem_allowed=True):
@@ -323,7 +371,7 @@ class InstanceSet:
         tab['lognh'] = self.lognh
         tab['model'] = self.model_id
         tab['cfun'] = self.cfun_id
-        limit = self.smem_ring_limit(self.threads())
+        limit = np.array([self.smem_ring_limit(self.threads(k), k) for k in self.block_k])
         fits = (self.ring_bytes <= limit) if smem_allowed else np.zeros(I, bool)
         fl = (self.flags | self.order_flags).astype(np.uint32)
         tab['flags'] = np.where(fits, fl | nat.F_SMEM_RING, fl).astype(np.uint32)
@@ -363,12 +411,12 @@ class InstanceSet:
         smem = (tab['flags'] & nat.F_SMEM_RING) != 0
         keys = {}
         for b in range(self.n):
-            k = (bool(smem[b]), int(tab['lognh'][b]) if smem[b] else -1)
+            k = (int(self.block_k[b]), bool(smem[b]), int(tab['lognh'][b]) if smem[b] else -1)
             keys.setdefault(k, []).append(b)
         out = []
-        for (sm, lognh), idx in sorted(keys.items(), key=lambda kv: -len(kv[1])):
+        for (bk, sm, lognh), idx in sorted(keys.items(), key=lambda kv: -len(kv[1])):
             ring = int(self.ring_bytes[idx[0]]) if sm else 0
-            out.append((np.array(idx, np.int64), ring))
+            out.append((np.array(idx, np.int64), ring, bk))
         return out
 
 
@@ -384,14 +432,18 @@ class Sweep(InstanceSet):
         self.status = DeviceStatus()
         self._uploaded = None
 
-    def _launch_cfg(self, smem_ring, tpn):
+    def _launch_cfg(self, smem_ring, tpn, block_k=0):
         cfg = nat.tvbg_launch()
         cfg.model = self.model_id
         cfg.cfun = self.cfun_id
-        cfg.threads = self.threads()
+        cfg.threads = self.threads(block_k)
         cfg.tpn = int(tpn)
+        if block_k and cfg.tpn < 2:
+            cfg.tpn = 2
         cfg.smem_ring = int((smem_ring + 15) // 16 * 16)
         cfg.ctas = 0
+        cfg.block_k = int(block_k)
+        cfg.nmax = self.N if block_k else 0
         cfg.d_status = self.status.t.data_ptr()
         return cfg
 
@@ -400,10 +452,10 @@ class Sweep(InstanceSet):
         torch = self.torch
         tab = self.build_table(nsteps)
         launches = []
-        for idx, smem in self.groups(tab):
+        for idx, smem, bk in self.groups(tab):
             sub = np.ascontiguousarray(tab[idx])
             dev = torch.from_numpy(sub.view(np.uint8).copy()).cuda()
-            launches.append((dev, len(idx), smem))
+            launches.append((dev, len(idx), smem, bk))
         self._uploaded = launches
         return launches
 
@@ -419,8 +471,8 @@ class Sweep(InstanceSet):
         launches = launches if launches is not None else self._uploaded
         tpn = tpn if tpn is not None else (self.tpn or 2)
         sh = nat.stream_handle(stream)
-        for dev, n, smem in launches:
-            cfg = self._launch_cfg(smem, tpn)
+        for dev, n, smem, bk in launches:
+            cfg = self._launch_cfg(smem, tpn, bk)
             nat.check(lib.tvbg_sweep(dev.data_ptr(), n, ctypes.byref(cfg), sh))
 
     def run(self, nsteps, stream=None, check=True):
@@ -436,6 +488,8 @@ class Sweep(InstanceSet):
     # -- results ----------------------------------------------------------------
     def ring_plain(self, b):
         "Ring of instance b as numpy [nh, N] slot-major (the oracle's layout)."
-        nh = 1 << int(self.lognh[b])
+        R = int(self.stride[b])
         o = int(self.ring_off[b])
-        return unskew_ring(self.ring[o:o + self.N * nh].cpu().numpy(), self.N, int(self.lognh[b]))
+        rows = self.ring[o:o + self.N * R].cpu().numpy().reshape(self.N, R)
+        nh = 1 << int(self.lognh[b])
+        return unskew_ring(rows[:, :nh].reshape(-1), self.N, int(self.lognh[b]))
