@@ -67,6 +67,19 @@ def grid_workload(n_g=64, n_s=64, nsteps=100_000, N=84, seed=0):
                 noise=True, seed=12345)
 
 
+def grid_small_workload():
+    """Profiling case of the grid kernel: the 64 G values x 24 speeds in
+    [8, 20] mm/ms (every ring in shared memory), 2000 steps; 1536 instances,
+    ring backing store + state > L2 is not needed for the smem-ring kernel."""
+    wl = grid_workload(n_g=64, n_s=24, nsteps=2000)
+    S = np.linspace(8, 20, 24).astype(np.float32)
+    G = np.logspace(-3, 0, 64).astype(np.float32)
+    gg, ss = np.meshgrid(G, S, indexing='ij')
+    wl.update(name='grid_small', couplings=gg.ravel(), speeds=ss.ravel(), bold_period=200,
+              bold_len=10)
+    return wl
+
+
 def kuramoto_workload(I=32, N=68, nsteps=1000, seed=0):
     from tvb_hpc import network
     w, ln = network.synthetic_connectome(N, 0.3, seed=seed)
@@ -80,10 +93,47 @@ def kuramoto_workload(I=32, N=68, nsteps=1000, seed=0):
                 noise=False, seed=0)
 
 
-WORKLOADS = {'grid': grid_workload, 'kuramoto': kuramoto_workload}
+MIXED_SPEC = [(68, 0.30, 1024), (84, 0.30, 1024), (192, 0.15, 256), (400, 0.08, 64),
+              (998, 0.03, 16)]
+
+
+def mixed_workload(seed=0, scale=1.0, steps_lo=5000, steps_hi=50000):
+    """Uneven batch: connectomes of N in {68, 84, 192, 400, 998} at densities
+    30/30/15/8/3%, 1024/1024/256/64/16 instances, step counts uniform in
+    [5k, 50k], Montbrio-Pazo-Roxin (Delta 1, J 15, eta ~ U(-6, -4), noise
+    sigma 1e-2) with linear coupling, speed 4 mm/ms so the longest delay is
+    500 steps at dt 0.1 ms."""
+    from tvb_hpc import network
+    parts = []
+    for k, (N, dens, I) in enumerate(MIXED_SPEC):
+        I = max(1, int(round(I * scale)))
+        w, ln = network.synthetic_connectome(N, dens, seed=seed + k)
+        conn = network.Connectivity.from_dense(w, ln)
+        rng = np.random.default_rng(seed + 100 + k)
+        x0 = np.stack([rng.uniform(0.05, 0.3, (I, N)), rng.uniform(-1.5, -0.5, (I, N))], -1)
+        eta = rng.uniform(-6, -4, (I, N, 1)).astype(np.float32)
+        steps = rng.integers(steps_lo, steps_hi + 1, I)
+        parts.append(dict(conn=conn, couplings=np.logspace(-2, -0.5, I).astype(np.float32),
+                          speeds=np.full(I, 4.0, np.float32), x0=x0.astype(np.float32),
+                          nparam=eta, steps=steps, seed=seed + 1000 + k))
+    return dict(name='mixed', parts=parts, model='MPR', cfun='Linear', noise=True, dt=0.1,
+                bold_period=0, bold_len=0, target=None, seed=seed)
+
+
+WORKLOADS = {'grid': grid_workload, 'grid_small': grid_small_workload,
+             'kuramoto': kuramoto_workload, 'mixed': mixed_workload}
 
 
 def workload_config(wl):
+    if wl['name'] == 'mixed':
+        return {'workload': 'mixed', 'model': wl['model'], 'coupling': wl['cfun'],
+                'nodes': [int(p['conn'].nnode) for p in wl['parts']],
+                'edges': [int(p['conn'].nnz) for p in wl['parts']],
+                'instances': [int(p['couplings'].size) for p in wl['parts']],
+                'time_steps': 'uniform 5k-50k per instance', 'dt_ms': wl['dt'],
+                'noise': 'philox-em', 'max_delay_steps': 500,
+                'l2': 'inputs larger than L2 (rings+state)', 'parallelism': 'replicas',
+                'path': 'persistent batch, one CUDA graph'}
     c = wl['conn']
     return {'workload': wl['name'], 'model': wl['model'], 'coupling': wl['cfun'],
             'nodes': int(c.nnode), 'edges': int(c.nnz), 'instances': int(wl['couplings'].size),
@@ -94,6 +144,8 @@ def workload_config(wl):
 
 
 def node_steps(wl):
+    if wl['name'] == 'mixed':
+        return float(sum(p['conn'].nnode * p['steps'].sum() for p in wl['parts']))
     return float(wl['couplings'].size) * wl['conn'].nnode * wl['nsteps']
 
 
@@ -101,6 +153,10 @@ def algorithmic_bytes_per_node_step(wl, nsvar):
     """Data touched per node-step (SURVEY 8(d) accounting): 4 B per delayed
     read of the coupled variable, 8 B per state variable (read + write),
     32 B for the balloon state when BOLD is on."""
+    if wl['name'] == 'mixed':
+        tot = sum(p['conn'].nnode * p['steps'].sum() for p in wl['parts'])
+        E = sum(p['conn'].nnz * p['steps'].sum() for p in wl['parts']) / tot
+        return 4.0 * E + 8.0 * nsvar
     E = wl['conn'].nnz / wl['conn'].nnode
     return 4.0 * E + 8.0 * nsvar + (32.0 if wl['bold_period'] else 0.0)
 
@@ -171,6 +227,67 @@ def build_sweep(wl, tpn=None):
                         tpn=tpn)
 
 
+class MixedStep:
+    """One bench step of the uneven batch: reset every instance from resident
+    copies and run the whole batch as one CUDA-graph launch (persistent
+    kernels on forked streams).  `run_plain` runs the same work as one
+    tvbg_sweep per connectome, sequentially (the plain path)."""
+
+    def __init__(self, wl, torch):
+        from tvb_hpc import model, coupling, scheme, engine
+        self.torch = torch
+        self.wl = wl
+        m = getattr(model, wl['model'])()
+        cf = getattr(coupling, wl['cfun'])(m)
+        scm = scheme.EulerMaryuyamaStep(wl['dt'])
+        self.sets = []
+        for p in wl['parts']:
+            self.sets.append(engine.InstanceSet(
+                m, cf, scm, p['conn'], dt=wl['dt'], couplings=p['couplings'], speeds=p['speeds'],
+                state0=p['x0'], nparam=p['nparam'], seed=p['seed']))
+        self.x0 = [s.state.clone() for s in self.sets]
+        self.batch = engine.Batch(self.sets, [p['steps'] for p in wl['parts']])
+        self.batch.capture()
+        self.sw = self.sets[0]
+        self.sw.tpn = self.batch.launches[0]['cfg'].tpn
+        self.n_launch = len(self.batch.launches)
+        # plain path: one sweep launch per connectome
+        self.plain = []
+        for s, p in zip(self.sets, wl['parts']):
+            sw = engine.Sweep.__new__(engine.Sweep)
+            sw.__dict__.update(s.__dict__)
+            sw.tpn = 4
+            sw.status = self.batch.status
+            sw._uploaded = None
+            self.plain.append((sw, sw.prepare(p['steps'])))
+
+    def reset(self, x0=None):
+        for s, x in zip(self.sets, self.x0 if x0 is None else x0):
+            s.state.copy_(x)
+            s.ring.zero_()
+
+    def run(self, time_kernels=False):
+        evs = []
+        torch = self.torch
+        if time_kernels:
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            self.batch.replay()
+            e1.record()
+            evs.append((e0, e1))
+        else:
+            self.batch.replay()
+        return evs, None
+
+    def run_plain(self):
+        for sw, launches in self.plain:
+            sw.launch(launches, 4)
+
+    def launches_per_step(self):
+        return self.n_launch
+
+
 class GpuStep:
     """One bench step on the device: reset state/ring/balloon from resident
     copies, run every instance for all steps, compute FC."""
@@ -195,7 +312,7 @@ class GpuStep:
             sw.bold.zero_()
 
     def run(self, time_kernels=False):
-        from tvb_hpc import metric
+        from tvb_hpc import metric  # noqa: F401
         torch = self.torch
         sw = self.sw
         evs = []
@@ -219,7 +336,10 @@ class GpuStep:
         return self.n_launch + fc_launches
 
 
-def roofline_entry(wl, gs, kernel_ms_total, n_launches):
+def roofline_entry(wl, nsvar, kernel_ms_total, steps):
+    """Roofline of the step kernel: algorithmic bytes of the timed steps over
+    the step kernels' event-timed duration (for the uneven batch, the graph
+    of concurrent persistent kernels), against the measured HBM copy rate."""
     peaks = {}
     p = os.path.join(ROOT, 'MEASURED_PEAKS.json')
     if os.path.exists(p):
@@ -227,10 +347,8 @@ def roofline_entry(wl, gs, kernel_ms_total, n_launches):
     hbm = peaks.get('hbm_gbs')
     src = 'measured' if hbm else 'fallback'
     hbm = hbm or 6800.0
-    bpn = algorithmic_bytes_per_node_step(wl, gs.sw.ns)
-    bytes_per_launch = bpn * node_steps(wl) / max(1, gs.n_launch)
-    avg_launch_s = (kernel_ms_total / max(1, n_launches)) / 1e3
-    achieved = bytes_per_launch / avg_launch_s / 1e9
+    bpn = algorithmic_bytes_per_node_step(wl, nsvar)
+    achieved = bpn * node_steps(wl) * steps / (kernel_ms_total / 1e3) / 1e9
     traffic = None
     tp = os.path.join(ROOT, 'profiles', 'traffic.json')
     if os.path.exists(tp):
@@ -296,7 +414,7 @@ def gpu_arm(args):
     from tvb_hpc import _native
     _native.load()
     wl = WORKLOADS[args.workload]()
-    gs = GpuStep(wl, torch)
+    gs = MixedStep(wl, torch) if wl['name'] == 'mixed' else GpuStep(wl, torch)
 
     def barrier():
         if world > 1:
@@ -336,6 +454,26 @@ def gpu_arm(args):
     value = world * node_steps(wl) * args.steps / (total_ms / 1e3)
     gs.sw.status.check()
 
+    plain = None
+    if wl['name'] == 'mixed':
+        # the plain path on the same work: one sweep launch per connectome
+        gs.reset()
+        gs.run_plain()
+        torch.cuda.synchronize()
+        gs.reset()
+        p0 = torch.cuda.Event(enable_timing=True)
+        p1 = torch.cuda.Event(enable_timing=True)
+        p0.record()
+        gs.run_plain()
+        p1.record()
+        torch.cuda.synchronize()
+        pms = p0.elapsed_time(p1)
+        plain = {'value': round(node_steps(wl) / (pms / 1e3), 1), 'unit': UNIT,
+                 'ms_per_step': round(pms, 3),
+                 'path': 'one tvbg_sweep launch per connectome, sequential'}
+        return finish_mixed(args, wl, gs, world, rank, value, ms_per_step, clk, kern_ms, n_kern,
+                            plain, torch, dist, barrier)
+
     # end-to-end through the public API: pinned host state in, FC out
     host_x0 = gs.x0.cpu().pin_memory()
     host_fc = torch.empty((wl['couplings'].size, wl['conn'].nnode, wl['conn'].nnode),
@@ -369,7 +507,7 @@ def gpu_arm(args):
             'data': 'synthetic (seeded connectomes, config recipe)',
             'config': workload_config(wl), 'e2e': e2e,
             'gpu_launches': gs.launches_per_step() * args.steps,
-            'roofline': roofline_entry(wl, gs, kern_ms, n_kern),
+            'roofline': roofline_entry(wl, gs.sw.ns, kern_ms, args.steps),
             'clocks': clk, 'tpn': gs.sw.tpn}
     if rank == 0 and world == 1 and not args.no_cpu:
         line['cpu_baseline'] = cpu_baseline(wl)
@@ -378,6 +516,74 @@ def gpu_arm(args):
         dist.destroy_process_group()
     if rank == 0:
         print(json.dumps(line), flush=True)
+
+
+def finish_mixed(args, wl, gs, world, rank, value, ms_per_step, clk, kern_ms, n_kern, plain,
+                 torch, dist, barrier):
+    "e2e and the JSON line of the uneven-batch workload."
+    host_x0 = [x.cpu().pin_memory() for x in gs.x0]
+    host_st = [torch.empty_like(s.state, device='cpu').pin_memory() for s in gs.sets]
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        gs.reset([h.cuda(non_blocking=True) for h in host_x0])
+        gs.run()
+        for h, s in zip(host_st, gs.sets):
+            h.copy_(s.state, non_blocking=True)
+        torch.cuda.synchronize()
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    te = torch.tensor([e2e_s], device='cuda')
+    if world > 1:
+        dist.all_reduce(te, op=dist.ReduceOp.MAX)
+    e2e_s = float(te.item())
+    nbytes = sum(h.numel() * 4 for h in host_x0)
+    e2e = {'value': round(world * node_steps(wl) * args.steps / e2e_s, 1), 'unit': UNIT,
+           'h2d_bytes_per_step': int(nbytes), 'd2h_bytes_per_step': int(nbytes)}
+    line = {'metric': METRIC, 'value': round(value, 1), 'unit': UNIT, 'n_gpus': world,
+            'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': round(ms_per_step, 3),
+            'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32',
+            'data': 'synthetic (seeded connectomes, config recipe)',
+            'config': workload_config(wl), 'e2e': e2e,
+            'gpu_launches': gs.launches_per_step() * args.steps,
+            'roofline': roofline_entry(wl, gs.sw.ns, kern_ms, args.steps),
+            'clocks': clk, 'plain': plain,
+            'batched_vs_plain': round(value / plain['value'], 3) if plain else None}
+    if rank == 0 and world == 1 and not args.no_cpu:
+        line['cpu_baseline'] = cpu_baseline_mixed(wl)
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def cpu_baseline_mixed(wl, budget_s=12.0):
+    "The oracle on a bounded sample of the uneven batch (instances of every connectome)."
+    sys.path.insert(0, os.path.join(ROOT, 'oracle'))
+    import pyoracle as orc
+    from tvb_hpc import model as mdl
+    m = getattr(mdl, wl['model'])()
+    kid, consts, sigma = m.engine_spec()
+    cores = os.cpu_count() or 1
+    done_ns, el_tot, desc = 0.0, 0.0, []
+    for p in wl['parts']:
+        c = p['conn']
+        n_inst = min(p['couplings'].size, cores)
+        delays = np.stack([c.delays(s, wl['dt'], 'ceil') for s in p['speeds'][:n_inst]])
+        nh = int(2 ** np.ceil(np.log2(delays.max() + 2)))
+        nsteps = int(max(50, budget_s / len(wl['parts']) * 2e7 / (c.nnz * n_inst / cores + 1)))
+        nsteps = min(nsteps, 5000)
+        t = time.perf_counter()
+        orc.run(kid, 0, c.row, c.col, c.wnz, nh, nsteps, wl['dt'], delays,
+                p['couplings'][:n_inst], p['nparam'][:n_inst, :, 0], p['x0'][:n_inst],
+                flags=orc.F_NOISE, sigma=sigma, consts=consts, seed=p['seed'], nthreads=cores)
+        el = time.perf_counter() - t
+        done_ns += n_inst * c.nnode * nsteps
+        el_tot += el
+        desc.append('N=%d: %d inst x %d steps' % (c.nnode, n_inst, nsteps))
+    return {'value': round(done_ns / el_tot, 1), 'unit': UNIT, 'cores': cores, 'kind': 'port',
+            'sample': '; '.join(desc) + ' (%.1f s), oracle C + OpenMP, -O3' % el_tot}
 
 
 def reference_arm(args):

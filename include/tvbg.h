@@ -167,6 +167,13 @@ const char *tvbg_last_error(void);
 int tvbg_max_smem(int32_t *bytes);
 
 /*
+ * Resident CTAs per SM of the step kernel a launch with `cfg` would use
+ * (cudaOccupancyMaxActiveBlocksPerMultiprocessor), and the SM count; used by
+ * the batch planner to size persistent grids.
+ */
+int tvbg_occupancy(const tvbg_launch *cfg, int32_t *ctas_per_sm, int32_t *sms);
+
+/*
  * Host helper: pack CSR connectivity and integer delays into tvbg_edge.
  * row[N+1], col[nnz] (int32), weights[nnz] (float), delays[nnz] (int32 >= 0).
  * Fails if a delay >= nh or N << lognh overflows 32 bits.

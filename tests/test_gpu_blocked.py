@@ -28,6 +28,9 @@ def make(model_name='G2DO', cfun_name='Diff', I=8, N=84, speeds=(5.0, 20.0), noi
     if model_name == 'MPR':
         x0 = np.stack([rng.uniform(0.05, 0.3, (I, N)), rng.uniform(-1.5, -0.5, (I, N))], -1)
         nparam = rng.uniform(-6, -4, (I, N, 1)).astype(np.float32)
+    elif model_name == 'Linear':
+        x0 = rng.uniform(-0.5, 0.5, (I, N, m.nsvar))
+        nparam = np.float32(-0.3)
     else:
         x0 = rng.uniform(-0.5, 0.5, (I, N, m.nsvar))
         nparam = None
@@ -55,7 +58,7 @@ def check(sw, x0, nsteps):
 @pytest.mark.parametrize('warps', [3, 8])
 def test_blocked_g2do_diff_noise(cuda, tpn, warps):
     sw, x0 = make(tpn=tpn, warps=warps)
-    assert set(sw.block_k) == {8}
+    assert set(sw.block_k) == {4, 8}      # speed 20: d_min = 5 -> K = 4
     check(sw, x0, 603)
 
 
@@ -71,8 +74,7 @@ def test_blocked_k4_and_global_ring(cuda):
 @pytest.mark.parametrize('model_name,cfun_name', [('MPR', 'Linear'), ('Linear', 'Diff'),
                                                   ('G2DO', 'Sigmoidal'), ('Linear', 'Linear')])
 def test_blocked_other_pairs(cuda, model_name, cfun_name):
-    sw, x0 = make(model_name, cfun_name, I=4, tpn=4,
-                  **({'nparam': np.float32(-0.3)} if model_name == 'Linear' else {}))
+    sw, x0 = make(model_name, cfun_name, I=4, tpn=4)
     check(sw, x0, 400)
 
 

@@ -174,6 +174,41 @@ int tvbg_max_smem(int32_t* bytes) {
     return TVBG_OK;
 }
 
+int tvbg_occupancy(const tvbg_launch* cfg, int32_t* ctas_per_sm, int32_t* sms) {
+    if (!cfg || !ctas_per_sm || !sms) return set_error(TVBG_EINVAL, "tvbg_occupancy: null");
+    const tvbg_instance dummy{};
+    int rc = check_launch(cfg, &dummy, 0);
+    if (rc) return rc;
+    const bool blocked = cfg->block_k > 1;
+    const int nmax = cfg->nmax > 0 ? cfg->nmax : cfg->threads;
+    const void* kfn = nullptr;
+    size_t smem = 0;
+    if (blocked) {
+        BlockedKernel kb = lookup_blocked(cfg->model, cfg->cfun, cfg->tpn, cfg->block_k);
+        if (!kb) return set_error(TVBG_EUNSUPPORTED, "time-blocked kernel not built");
+        kfn = reinterpret_cast<const void*>(kb);
+        smem = static_cast<size_t>(cfg->smem_ring) + blocked_aux_bytes(cfg->model, cfg->block_k, nmax);
+    } else {
+        StepKernel k1 = lookup(cfg->model, cfg->cfun, cfg->tpn);
+        if (!k1) return set_error(TVBG_EUNSUPPORTED, "model/coupling pair not built");
+        kfn = reinterpret_cast<const void*>(k1);
+        smem = step_smem_bytes(cfg->threads, cfg->smem_ring);
+    }
+    cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(smem));
+    if (e != cudaSuccess) return set_cuda_error(e, "tvbg_occupancy: smem attribute");
+    int n = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kfn, cfg->threads, smem);
+    if (e != cudaSuccess) return set_cuda_error(e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
+    int dev = 0, nsm = 0;
+    e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return set_cuda_error(e, "tvbg_occupancy: SM count");
+    *ctas_per_sm = n;
+    *sms = nsm;
+    return TVBG_OK;
+}
+
 int tvbg_pack_edges(int32_t N, int32_t nnz, const int32_t* row, const int32_t* col,
                     const float* weights, const int32_t* delays, int32_t lognh, tvbg_edge* out) {
     if (N <= 0 || nnz < 0 || !row || (nnz > 0 && (!col || !weights || !delays || !out)))

@@ -121,6 +121,7 @@ SIGNATURES = {
     'tvbg_launch_size': (_sz, []),
     'tvbg_last_error': (ctypes.c_char_p, []),
     'tvbg_max_smem': (ctypes.c_int, [_ip]),
+    'tvbg_occupancy': (ctypes.c_int, [ctypes.c_void_p, _ip, _ip]),
     'tvbg_pack_edges': (ctypes.c_int, [_i32, _i32, _vp, _vp, _vp, _vp, _i32, _vp]),
     'tvbg_delays': (ctypes.c_int, [_i32, _vp, ctypes.c_float, ctypes.c_float, _i32, _vp]),
     'tvbg_pack_edges_blocked': (ctypes.c_int, [_i32, _i32, _vp, _vp, _vp, _vp, _i32, _vp]),

@@ -25,7 +25,9 @@ def _key(iset):
 
 
 def tune_tpn(iset, trial_steps=None, choices=TPN_CHOICES):
-    "Pick tpn for a Sweep by timing `trial_steps` steps of each choice."
+    """Pick the launch shape of a Sweep by timing `trial_steps` steps of each
+    choice: the gather width tpn and, for the time-blocked kernel, the CTA
+    width in warps (unless the caller fixed it)."""
     import torch
     key = _key(iset)
     if key in _CACHE:
@@ -34,22 +36,29 @@ def tune_tpn(iset, trial_steps=None, choices=TPN_CHOICES):
         trial_steps = int(np.clip(20000 // max(1, iset.n), 50, 400))
     snap = [t.clone() if t is not None else None
             for t in (iset.ring, iset.state, iset.bold, iset.bold_out, iset.trace)]
+    blocked = bool(np.any(iset.block_k > 0))
     if np.all(iset.block_k > 0):
         choices = tuple(c for c in choices if c >= 2)
-    best, best_ms = choices[0], None
-    launches = iset.prepare(trial_steps)
-    for tpn in choices:
-        iset.launch(launches, tpn)  # warm-up (also loads the module)
-        torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
-        iset.launch(launches, tpn)
-        e1.record()
-        torch.cuda.synchronize()
-        ms = e0.elapsed_time(e1)
-        LOG.debug('tpn=%d: %.3f ms for %d steps', tpn, ms, trial_steps)
-        if best_ms is None or ms < best_ms:
-            best, best_ms = tpn, ms
+    fixed_warps = iset.warps
+    warp_choices = ((fixed_warps, ) if fixed_warps or not blocked else
+                    tuple(w for w in (4, 8, 16, 32) if 32 * w >= iset.N and 32 * w <= 1024))
+    best, best_ms, best_w = choices[0], None, fixed_warps
+    for wv in warp_choices:
+        iset.warps = wv
+        launches = iset.prepare(trial_steps)
+        for tpn in choices:
+            iset.launch(launches, tpn)  # warm-up (also loads the module)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            iset.launch(launches, tpn)
+            e1.record()
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1)
+            LOG.debug('warps=%s tpn=%d: %.3f ms for %d steps', wv, tpn, ms, trial_steps)
+            if best_ms is None or ms < best_ms:
+                best, best_ms, best_w = tpn, ms, wv
+    iset.warps = best_w
     for dst, src in zip((iset.ring, iset.state, iset.bold, iset.bold_out, iset.trace), snap):
         if dst is not None:
             dst.copy_(src)

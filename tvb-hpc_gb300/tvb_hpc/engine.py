@@ -493,3 +493,122 @@ class Sweep(InstanceSet):
         rows = self.ring[o:o + self.N * R].cpu().numpy().reshape(self.N, R)
         nh = 1 << int(self.lognh[b])
         return unskew_ring(rows[:, :nh].reshape(-1), self.N, int(self.lognh[b]))
+
+
+def occupancy(cfg):
+    "Resident CTAs per SM and SM count for a launch configuration."
+    lib = nat.load()
+    per, sms = ctypes.c_int32(0), ctypes.c_int32(0)
+    nat.check(lib.tvbg_occupancy(ctypes.byref(cfg), ctypes.byref(per), ctypes.byref(sms)))
+    return int(per.value), int(sms.value)
+
+
+class Batch:
+    """
+    Uneven batch: instances of several connectomes (different N, ring
+    lengths and step counts) that share the model, coupling and scheme, run
+    by persistent kernels (tvbg_batch_run).
+
+    Instances are grouped by the CTA width they need; every group is one
+    persistent launch whose CTAs pull instances from a device counter in
+    longest-first order (cost = N x steps), and the groups run concurrently
+    on forked streams with CTA counts proportional to their cost.  The whole
+    batch can be captured into one CUDA graph (``capture()``), so a sweep of
+    uneven instances is a single graph launch.
+
+    This is the persistent counterpart of the subject batch of
+    examples/hcp100.py:65-118 (OpenMP over subjects).
+    """
+
+    def __init__(self, sets, nsteps, tpn=None):
+        import torch
+        self.torch = torch
+        self.sets = list(sets)
+        m0 = self.sets[0]
+        for s in self.sets:
+            if (s.model_id, s.cfun_id) != (m0.model_id, m0.cfun_id):
+                raise ValueError('a batch shares one model and coupling')
+        self.nsteps = [np.broadcast_to(np.asarray(n, np.int64), (s.n, )).astype(np.int64)
+                       for s, n in zip(self.sets, nsteps)]
+        self.tpn = tpn
+        self.status = DeviceStatus()
+        self.graph = None
+        self._build()
+
+    @property
+    def node_steps(self):
+        return float(sum((s.N * n).sum() for s, n in zip(self.sets, self.nsteps)))
+
+    def _build(self):
+        torch = self.torch
+        rows = []   # (threads, block_k, table record, cost, smem ring bytes or 0)
+        for s, ns in zip(self.sets, self.nsteps):
+            tab = s.build_table(ns)
+            for b in range(s.n):
+                bk = int(s.block_k[b])
+                thr = s.threads(bk)
+                smem = int(s.ring_bytes[b]) if tab['flags'][b] & nat.F_SMEM_RING else 0
+                rows.append((thr, bk, tab[b], float(s.N * ns[b]), smem, s.N))
+        groups = {}
+        for r in rows:
+            groups.setdefault((r[0], r[1]), []).append(r)
+        total = sum(r[3] for r in rows)
+        self.launches = []
+        m0 = self.sets[0]
+        for (thr, bk), rs in sorted(groups.items(), key=lambda kv: -sum(r[3] for r in kv[1])):
+            rs.sort(key=lambda r: -r[3])               # longest first
+            tab = np.array([r[2] for r in rs], dtype=nat.INSTANCE_DTYPE)
+            dev = torch.from_numpy(tab.view(np.uint8).copy()).cuda()
+            cfg = nat.tvbg_launch()
+            cfg.model, cfg.cfun, cfg.threads = m0.model_id, m0.cfun_id, thr
+            cfg.tpn = int(self.tpn or (4 if bk else 2))
+            cfg.smem_ring = int((max(r[4] for r in rs) + 15) // 16 * 16)
+            cfg.block_k = bk
+            cfg.nmax = max(r[5] for r in rs) if bk else 0
+            counter = torch.zeros(1, dtype=torch.int32, device='cuda')
+            cfg.d_counter = counter.data_ptr()
+            cfg.d_status = self.status.t.data_ptr()
+            per_sm, sms = occupancy(cfg)
+            cost = sum(r[3] for r in rs)
+            cfg.ctas = int(max(1, min(len(rs), round(max(1, per_sm) * sms * cost / total))))
+            self.launches.append(dict(dev=dev, n=len(rs), cfg=cfg, counter=counter, cost=cost,
+                                      threads=thr, block_k=bk, per_sm=per_sm))
+        self.streams = [torch.cuda.Stream() for _ in self.launches]
+
+    def launch(self, stream=None):
+        "Enqueue every group on forked streams joined back into `stream`."
+        torch = self.torch
+        lib = nat.load()
+        main = stream or torch.cuda.current_stream()
+        for L, s in zip(self.launches, self.streams):
+            s.wait_stream(main)
+            with torch.cuda.stream(s):
+                nat.check(lib.tvbg_batch_run(L['dev'].data_ptr(), L['n'], ctypes.byref(L['cfg']),
+                                             s.cuda_stream))
+        for s in self.streams:
+            main.wait_stream(s)
+
+    def capture(self):
+        """Capture the batch launch into one CUDA graph (replay with replay()).
+        Nothing runs during capture; kernels were loaded by the planner."""
+        torch = self.torch
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        cap = torch.cuda.Stream()
+        with torch.cuda.stream(cap):
+            with torch.cuda.graph(g, stream=cap):
+                self.launch(cap)
+        self.graph = g
+        return g
+
+    def replay(self):
+        self.graph.replay()
+
+    def run(self, check=True):
+        if self.graph is not None:
+            self.replay()
+        else:
+            self.launch()
+        if check:
+            self.torch.cuda.synchronize()
+            self.status.check()
