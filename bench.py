@@ -216,7 +216,7 @@ class ClockSampler:
 # ---------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------
-def build_sweep(wl, tpn=None):
+def build_sweep(wl, tpn=None, warps=None):
     from tvb_hpc import model, coupling, scheme, engine
     m = getattr(model, wl['model'])()
     cf = getattr(coupling, wl['cfun'])(m)
@@ -224,7 +224,7 @@ def build_sweep(wl, tpn=None):
     return engine.Sweep(m, cf, scm, wl['conn'], dt=wl['dt'], couplings=wl['couplings'],
                         speeds=wl['speeds'], state0=wl['x0'], nparam=wl.get('nparam'),
                         seed=wl['seed'], bold_period=wl['bold_period'], bold_len=wl['bold_len'],
-                        tpn=tpn)
+                        tpn=tpn, warps=warps)
 
 
 class MixedStep:
@@ -292,10 +292,10 @@ class GpuStep:
     """One bench step on the device: reset state/ring/balloon from resident
     copies, run every instance for all steps, compute FC."""
 
-    def __init__(self, wl, torch):
+    def __init__(self, wl, torch, tpn=None, warps=None):
         self.torch = torch
         self.wl = wl
-        self.sw = build_sweep(wl)
+        self.sw = build_sweep(wl, tpn, warps)
         self.sw.pick_tpn()
         self.x0 = self.sw.state.clone()
         self.target = (torch.from_numpy(wl['target']).cuda() if wl['target'] is not None
@@ -414,7 +414,8 @@ def gpu_arm(args):
     from tvb_hpc import _native
     _native.load()
     wl = WORKLOADS[args.workload]()
-    gs = MixedStep(wl, torch) if wl['name'] == 'mixed' else GpuStep(wl, torch)
+    gs = (MixedStep(wl, torch) if wl['name'] == 'mixed'
+          else GpuStep(wl, torch, args.tpn, args.warps))
 
     def barrier():
         if world > 1:
@@ -618,6 +619,8 @@ def main():
     ap.add_argument('--impl', default='engine', choices=['engine', 'reference'])
     ap.add_argument('--no-cpu', action='store_true', help='skip the cpu_baseline leg')
     ap.add_argument('--ref-seconds', type=float, default=8.0)
+    ap.add_argument('--tpn', type=int, default=None, help='fix the gather width (skip autotune)')
+    ap.add_argument('--warps', type=int, default=None, help='fix the CTA width of the blocked kernel')
     args = ap.parse_args()
     if args.impl == 'reference':
         reference_arm(args)
