@@ -77,6 +77,9 @@ extern "C" {
  * it, so post and zero-delay reads see the slot's old content. */
 #define TVBG_F_TRACKA 64u
 #define TVBG_F_MIDSYNC 128u  /* block barrier between gather and update      */
+/* the trace carries one more column per node: the raw coupling sum S of the
+ * step (written during the step; used by the adjoint's recomputation) */
+#define TVBG_F_TRACE_CSUM 256u
 
 /*
  * Packed connectivity edge, one per CSR non-zero, rows = target node i:
@@ -230,6 +233,38 @@ int tvbg_sweep(const tvbg_instance *d_inst, int32_t n_inst,
  */
 int tvbg_batch_run(const tvbg_instance *d_inst, int32_t n_inst,
                    const tvbg_launch *cfg, void *stream);
+
+/*
+ * Reverse-time adjoint of the delayed Euler scheme for one segment of steps
+ * [t0, t0 + len), Montbrio-Pazo-Roxin with linear coupling, CUDA step order,
+ * deterministic.  With mu(t+1) = lambda(t+1) (r component masked where the
+ * rate was clamped):
+ *   lambda(t)     = mu + dt J(x(t))^T mu + dL/dr(t) e_r
+ *   lambda_r,j(t) += dt G / tau * sum_{edges i <- j, delay d} w mu_V,i(t + d + 1)
+ *   deta_j += dt / tau * mu_V,j(t+1);   dG_j += dt / tau * mu_V,j(t+1) S_j(t)
+ * (FP64 accumulators).  mu_V is kept in an adjoint ring (skewed node-major
+ * layout of tvbg.h, zero before the last segment) gathered over the
+ * transposed CSR, pk = (i << lognh) | ((i + d + 1) & (nh - 1)).
+ * No counterpart kernel exists in the reference (tvb_hpc builds symbolic
+ * partials only, model.py:61-65, scheme.py:42-48).
+ */
+typedef struct tvbg_adjoint {
+    const tvbg_edge *edges_t; /* [nnz] transposed edges (out-edges of node j) */
+    const int32_t *row_t;     /* [N+1] out-edge offsets                       */
+    const float *seg;         /* [len][N][3]: r, V, S at the start of each step */
+    const float *dr;          /* [len][N]: direct dL/dr(t), row t - t0        */
+    float *lam;               /* [N][2]: lambda(t0 + len) in, lambda(t0) out  */
+    float *ring;              /* [N << lognh] adjoint ring of mu_V            */
+    double *deta;             /* [N] accumulated dL/deta                      */
+    double *dG;               /* [N] accumulated per-node part of dL/dG       */
+    int64_t t0;
+    int32_t len, N, lognh, reserved0;
+    float dt, G;
+    float consts[4];          /* MPR: Delta, J, tau, I                        */
+} tvbg_adjoint;
+
+int tvbg_adjoint_mpr(const tvbg_adjoint *d_adj, int32_t n_inst, int32_t threads,
+                     void *stream);
 
 /*
  * Pearson FC per instance over T samples of N nodes, FP64 reduction.

@@ -57,6 +57,11 @@ def load():
         lib.orc_philox_normal.argtypes = [ctypes.c_uint64, ctypes.c_uint32, vp, ctypes.c_int64]
         lib.orc_fc.argtypes = [vp, ctypes.c_int32, ctypes.c_int32, vp]
         lib.orc_fc_onepass_f32.argtypes = [vp, ctypes.c_int32, ctypes.c_int32, vp]
+        i32, f64 = ctypes.c_int32, ctypes.c_double
+        lib.orc_mpr_adjoint_f64.argtypes = [i32, vp, vp, vp, i32, i32, vp, vp, vp, vp, i32, f64,
+                                            vp, vp, vp, vp, vp, i32]
+        lib.orc_mpr_loss_f64.argtypes = [i32, vp, vp, vp, i32, vp, f64, vp, vp, i32, f64, vp, vp,
+                                         vp]
         _lib = lib
     return _lib
 
@@ -192,6 +197,54 @@ def fc_onepass_f32(x):
     out = np.zeros((N, N), np.float32)
     lib.orc_fc_onepass_f32(x.ctypes.data, T, N, out.ctypes.data)
     return out
+
+
+def mpr_adjoint(row, col, w, delays, G, eta, x0, T, dt, consts, target, nthreads=1):
+    """FP64 loss and gradients (dL/dG [I], dL/deta [I, N]) of the FC-fit loss
+    of deterministic MPR + linear coupling (see orc_mpr_adjoint_f64)."""
+    lib = load()
+    row = np.ascontiguousarray(row, np.int32)
+    col = np.ascontiguousarray(col, np.int32)
+    w = np.ascontiguousarray(w, np.float32)
+    N = row.size - 1
+    G = np.ascontiguousarray(np.atleast_1d(G), np.float64)
+    I = G.size
+    delays = np.ascontiguousarray(np.broadcast_to(np.asarray(delays, np.int32), (I, col.size)))
+    eta = np.ascontiguousarray(np.broadcast_to(np.asarray(eta, np.float64), (I, N)))
+    x0 = np.ascontiguousarray(np.broadcast_to(np.asarray(x0, np.float64), (I, N, 2)))
+    consts = np.ascontiguousarray(consts, np.float32)
+    target = np.ascontiguousarray(target, np.float64)
+    loss = np.zeros(I)
+    dG = np.zeros(I)
+    deta = np.zeros((I, N))
+    rc = lib.orc_mpr_adjoint_f64(N, row.ctypes.data, col.ctypes.data, w.ctypes.data, col.size, I,
+                                 delays.ctypes.data, G.ctypes.data, eta.ctypes.data,
+                                 x0.ctypes.data, T, dt, consts.ctypes.data, target.ctypes.data,
+                                 loss.ctypes.data, dG.ctypes.data, deta.ctypes.data, nthreads)
+    if rc:
+        raise RuntimeError('oracle adjoint failed')
+    return loss, dG, deta
+
+
+def mpr_loss(row, col, w, delays, G, eta, x0, T, dt, consts, target):
+    "FP64 FC-fit loss of one instance (forward only)."
+    lib = load()
+    row = np.ascontiguousarray(row, np.int32)
+    col = np.ascontiguousarray(col, np.int32)
+    w = np.ascontiguousarray(w, np.float32)
+    N = row.size - 1
+    delays = np.ascontiguousarray(delays, np.int32)
+    eta = np.ascontiguousarray(eta, np.float64)
+    x0 = np.ascontiguousarray(x0, np.float64)
+    consts = np.ascontiguousarray(consts, np.float32)
+    target = np.ascontiguousarray(target, np.float64)
+    out = ctypes.c_double(0.0)
+    rc = lib.orc_mpr_loss_f64(N, row.ctypes.data, col.ctypes.data, w.ctypes.data, col.size,
+                              delays.ctypes.data, float(G), eta.ctypes.data, x0.ctypes.data, T,
+                              dt, consts.ctypes.data, target.ctypes.data, ctypes.byref(out))
+    if rc:
+        raise RuntimeError('oracle loss failed')
+    return out.value
 
 
 # ---- the reference's own kernels compiled for the host (oracle/_ref) --------

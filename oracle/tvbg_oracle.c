@@ -230,3 +230,195 @@ void orc_fc_onepass_f32(const float *x, int32_t T, int32_t N, float *corr) {
 }
 
 int orc_abi_version(void) { return 1; }
+
+/* ---- FC-fit adjoint of the delayed Euler scheme, FP64 (reference gradient) ----
+ *
+ * TEST INFRASTRUCTURE ONLY.  Deterministic MPR with linear coupling
+ * c_i(t) = G sum_e w_e r_{j_e}(t - d_e) (CUDA step order, zero history,
+ * r clamped at 0), T steps from x(0).  The observed series is X[s] = r(s+1),
+ * s = 0..T-1; FC = Pearson(X) (FP64); loss = mean_{i<j} (FC_ij - F*_ij)^2.
+ * Gradients w.r.t. G and eta_i by the adjoint recursion
+ *   mu(t+1)    = lambda(t+1) * [r_pre(t+1) >= 0 for the r component]
+ *   lambda(t)  = mu + dt J(x(t))^T mu + dL/dx(t)|direct
+ *   lambda_r,j(t) += dt G/tau sum_{e: j -> i} w_e mu_V,i(t + d_e + 1)
+ *   dL/deta_i += dt/tau mu_V,i(t+1);  dL/dG += dt/tau mu_V,i(t+1) S_i(t)
+ * consts K = [Delta, J, tau, I].
+ */
+static double mpr_fwd(int N, const int32_t *row, const int32_t *col, const float *w,
+                      const int32_t *delays, double G, const double *eta, const double *x0,
+                      int T, double dt, const float *Kf, double *X /* (T+1)*N*2 */,
+                      double *S /* T*N */) {
+    const double Delta = Kf[0], J = Kf[1], tau = Kf[2], I = Kf[3];
+    const double pi = 3.14159265358979323846;
+    int t, i, e;
+    memcpy(X, x0, sizeof(double) * 2 * N);
+    for (t = 0; t < T; ++t) {
+        const double *x = X + (int64_t)t * N * 2;
+        double *xn = X + (int64_t)(t + 1) * N * 2;
+        for (i = 0; i < N; ++i) {
+            double acc = 0.0;
+            for (e = row[i]; e < row[i + 1]; ++e) {
+                const int ts = t - delays[e];
+                if (ts >= 0) acc += (double)w[e] * X[((int64_t)ts * N + col[e]) * 2];
+            }
+            S[(int64_t)t * N + i] = acc;
+        }
+        for (i = 0; i < N; ++i) {
+            const double r = x[2 * i], V = x[2 * i + 1];
+            const double c = G * S[(int64_t)t * N + i];
+            const double ptr = pi * tau * r;
+            const double fr = (Delta / (pi * tau) + 2.0 * r * V) / tau;
+            const double fV = (V * V + eta[i] + J * tau * r + I + c - ptr * ptr) / tau;
+            double rn = r + dt * fr;
+            xn[2 * i] = rn < 0.0 ? 0.0 : rn;
+            xn[2 * i + 1] = V + dt * fV;
+        }
+    }
+    return 0.0;
+}
+
+/* FC of X[s] = r(s+1), loss and dL/dX (FP64); returns the loss. */
+static double fc_loss_grad(int N, int T, const double *X, const double *target, double *dX) {
+    double *mu = (double *)calloc((size_t)N, sizeof(double));
+    double *nrm = (double *)calloc((size_t)N, sizeof(double));
+    double *Z = (double *)calloc((size_t)T * N, sizeof(double));
+    double *A = (double *)calloc((size_t)N * N, sizeof(double));
+    double *gZ = (double *)calloc((size_t)T * N, sizeof(double));
+    const double P = (double)N * (N - 1) / 2.0;
+    double loss = 0.0;
+    int s, i, j;
+    for (s = 0; s < T; ++s)
+        for (i = 0; i < N; ++i) mu[i] += X[((int64_t)(s + 1) * N + i) * 2];
+    for (i = 0; i < N; ++i) mu[i] /= T;
+    for (s = 0; s < T; ++s)
+        for (i = 0; i < N; ++i) {
+            const double v = X[((int64_t)(s + 1) * N + i) * 2] - mu[i];
+            Z[(int64_t)s * N + i] = v;
+            nrm[i] += v * v;
+        }
+    for (i = 0; i < N; ++i) nrm[i] = sqrt(nrm[i]);
+    for (s = 0; s < T; ++s)
+        for (i = 0; i < N; ++i) Z[(int64_t)s * N + i] /= nrm[i];
+    for (i = 0; i < N; ++i)
+        for (j = i + 1; j < N; ++j) {
+            double fc = 0.0;
+            for (s = 0; s < T; ++s) fc += Z[(int64_t)s * N + i] * Z[(int64_t)s * N + j];
+            const double dd = fc - (double)target[(int64_t)i * N + j];
+            loss += dd * dd / P;
+            A[(int64_t)i * N + j] = A[(int64_t)j * N + i] = 2.0 * dd / P;
+        }
+    for (s = 0; s < T; ++s)
+        for (i = 0; i < N; ++i) {
+            double g = 0.0;
+            for (j = 0; j < N; ++j) g += A[(int64_t)i * N + j] * Z[(int64_t)s * N + j];
+            gZ[(int64_t)s * N + i] = g;
+        }
+    for (i = 0; i < N; ++i) {
+        double zg = 0.0, m = 0.0;
+        for (s = 0; s < T; ++s) zg += Z[(int64_t)s * N + i] * gZ[(int64_t)s * N + i];
+        for (s = 0; s < T; ++s) {
+            const double v = (gZ[(int64_t)s * N + i] - Z[(int64_t)s * N + i] * zg) / nrm[i];
+            dX[(int64_t)s * N + i] = v;
+            m += v;
+        }
+        m /= T;
+        for (s = 0; s < T; ++s) dX[(int64_t)s * N + i] -= m;
+    }
+    free(mu); free(nrm); free(Z); free(A); free(gZ);
+    return loss;
+}
+
+static int mpr_adjoint_one(int N, const int32_t *row, const int32_t *col, const float *w,
+                           const int32_t *delays, int nnz, double G, const double *eta,
+                           const double *x0, int T, double dt, const float *Kf,
+                           const double *target, double *loss, double *dG, double *deta) {
+    const double J = Kf[1], tau = Kf[2];
+    const double pi = 3.14159265358979323846;
+    double *X = (double *)malloc(sizeof(double) * (size_t)(T + 1) * N * 2);
+    double *S = (double *)malloc(sizeof(double) * (size_t)T * N);
+    double *dX = (double *)calloc((size_t)T * N, sizeof(double));
+    double *lam = (double *)calloc((size_t)2 * N, sizeof(double));
+    double *muV = (double *)calloc((size_t)(T + 2) * N, sizeof(double)); /* mu_V(t), t = 0..T+1 */
+    int t, i, e;
+    if (!X || !S || !dX || !lam || !muV) return -1;
+    mpr_fwd(N, row, col, w, delays, G, eta, x0, T, dt, Kf, X, S);
+    *loss = fc_loss_grad(N, T, X, target, dX);
+    *dG = 0.0;
+    for (i = 0; i < N; ++i) deta[i] = 0.0;
+    /* lambda(T) = direct gradient on r(T) = X[T-1] */
+    for (i = 0; i < N; ++i) {
+        lam[2 * i] = dX[(int64_t)(T - 1) * N + i];
+        lam[2 * i + 1] = 0.0;
+    }
+    for (t = T - 1; t >= 0; --t) {
+        const double *x = X + (int64_t)t * N * 2;
+        double *mu = (double *)malloc(sizeof(double) * 2 * N);
+        double *coup = (double *)calloc((size_t)N, sizeof(double));
+        for (i = 0; i < N; ++i) {
+            const double r = x[2 * i], V = x[2 * i + 1];
+            const double fr = (Kf[0] / (pi * tau) + 2.0 * r * V) / tau;
+            const double rpre = r + dt * fr;
+            mu[2 * i] = rpre >= 0.0 ? lam[2 * i] : 0.0;
+            mu[2 * i + 1] = lam[2 * i + 1];
+            muV[(int64_t)(t + 1) * N + i] = mu[2 * i + 1];
+        }
+        /* coupling: r_j(t) feeds c_i(t + d) for every edge i <- j */
+        for (i = 0; i < N; ++i)
+            for (e = row[i]; e < row[i + 1]; ++e) {
+                const int tt = t + delays[e];
+                if (tt < T) coup[col[e]] += (double)w[e] * muV[(int64_t)(tt + 1) * N + i];
+            }
+        for (i = 0; i < N; ++i) {
+            const double r = x[2 * i], V = x[2 * i + 1];
+            const double mr = mu[2 * i], mv = mu[2 * i + 1];
+            const double dfr_dr = 2.0 * V / tau, dfr_dV = 2.0 * r / tau;
+            const double dfV_dr = (J * tau - 2.0 * pi * pi * tau * tau * r) / tau;
+            const double dfV_dV = 2.0 * V / tau;
+            double lr = mr + dt * (mr * dfr_dr + mv * dfV_dr) + dt * G / tau * coup[i];
+            double lv = mv + dt * (mr * dfr_dV + mv * dfV_dV);
+            if (t >= 1) lr += dX[(int64_t)(t - 1) * N + i];
+            deta[i] += dt / tau * mv;
+            *dG += dt / tau * mv * S[(int64_t)t * N + i];
+            lam[2 * i] = lr;
+            lam[2 * i + 1] = lv;
+        }
+        free(mu);
+        free(coup);
+    }
+    (void)nnz;
+    free(X); free(S); free(dX); free(lam); free(muV);
+    return 0;
+}
+
+/* n_inst instances: G [I], eta [I][N], x0 [I][N][2], delays [I][nnz]. */
+int orc_mpr_adjoint_f64(int32_t N, const int32_t *row, const int32_t *col, const float *w,
+                        int32_t nnz, int32_t n_inst, const int32_t *delays, const double *G,
+                        const double *eta, const double *x0, int32_t T, double dt,
+                        const float *consts, const double *target, double *loss, double *dG,
+                        double *deta, int32_t nthreads) {
+    int b, bad = 0;
+    if (nthreads < 1) nthreads = 1;
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads) reduction(| : bad)
+    for (b = 0; b < n_inst; ++b)
+        if (mpr_adjoint_one(N, row, col, w, delays + (int64_t)b * nnz, nnz, G[b], eta + (int64_t)b * N,
+                            x0 + (int64_t)b * N * 2, T, dt, consts, target, loss + b, dG + b,
+                            deta + (int64_t)b * N))
+            bad = 1;
+    return bad ? -1 : 0;
+}
+
+/* Forward + loss only (FP64), for finite differences. */
+int orc_mpr_loss_f64(int32_t N, const int32_t *row, const int32_t *col, const float *w,
+                     int32_t nnz, const int32_t *delays, double G, const double *eta,
+                     const double *x0, int32_t T, double dt, const float *consts,
+                     const double *target, double *loss) {
+    double *X = (double *)malloc(sizeof(double) * (size_t)(T + 1) * N * 2);
+    double *S = (double *)malloc(sizeof(double) * (size_t)T * N);
+    double *dX = (double *)calloc((size_t)T * N, sizeof(double));
+    (void)nnz;
+    if (!X || !S || !dX) return -1;
+    mpr_fwd(N, row, col, w, delays, G, eta, x0, T, dt, consts, X, S);
+    *loss = fc_loss_grad(N, T, X, target, dX);
+    free(X); free(S); free(dX);
+    return 0;
+}

@@ -1,0 +1,92 @@
+// Reverse-time adjoint of the delayed Euler scheme (Montbrio-Pazo-Roxin,
+// linear coupling), one CTA per instance, one thread per node.  The
+// recursion and its terms are documented at tvbg_adjoint_mpr in tvbg.h.
+#include <cuda_runtime.h>
+
+#include "tvbg_abi_internal.h"
+#include "tvbg_device.cuh"
+
+namespace tvbg {
+
+__global__ void __launch_bounds__(1024, 1)
+    adjoint_mpr_kernel(const tvbg_adjoint* __restrict__ adj, int32_t n_inst) {
+    if (static_cast<int>(blockIdx.x) >= n_inst) return;
+    const tvbg_adjoint a = adj[blockIdx.x];
+    const int j = threadIdx.x;
+    const int N = a.N;
+    const bool own = j < N;
+    const uint32_t lognh = static_cast<uint32_t>(a.lognh);
+    const uint32_t mask = (1u << lognh) - 1u;
+    const float Delta = a.consts[0], J = a.consts[1], tau = a.consts[2];
+    const float pi = 3.14159265358979323846f;
+    const float dt = a.dt;
+    const float cG = dt * a.G / tau;
+    float lr = 0.f, lv = 0.f;
+    double deta = 0.0, dG = 0.0;
+    int lo = 0, hi = 0;
+    if (own) {
+        lr = a.lam[2 * j];
+        lv = a.lam[2 * j + 1];
+        lo = __ldg(a.row_t + j);
+        hi = __ldg(a.row_t + j + 1);
+    }
+    const uint32_t my_row = static_cast<uint32_t>(j) << lognh;
+    for (int k = a.len - 1; k >= 0; --k) {
+        const long long t = a.t0 + k;
+        const uint32_t tm = static_cast<uint32_t>(t) & mask;
+        float r = 0.f, V = 0.f, S = 0.f, mr = 0.f, mv = 0.f;
+        if (own) {
+            const float* x = a.seg + (static_cast<long long>(k) * N + j) * 3;
+            r = x[0];
+            V = x[1];
+            S = x[2];
+            // the rate update of step t was clamped at 0 where it went negative
+            const float fr = (Delta / (pi * tau) + 2.0f * r * V) / tau;
+            const float rpre = fmaf(dt, fr, r);
+            mr = rpre >= 0.0f ? lr : 0.0f;
+            mv = lv;
+            a.ring[my_row | ((tm + 1u + static_cast<uint32_t>(j)) & mask)] = mv;
+        }
+        __syncthreads();
+        if (own) {
+            float coup = 0.0f;
+            for (int e = lo; e < hi; ++e) {
+                const uint2 ew = __ldg(reinterpret_cast<const uint2*>(a.edges_t) + e);
+                const uint32_t idx = ((tm + ew.x) & mask) | (ew.x & ~mask);
+                coup = fmaf(__uint_as_float(ew.y), a.ring[idx], coup);
+            }
+            const float dfr_dr = 2.0f * V / tau, dfr_dV = 2.0f * r / tau;
+            const float dfV_dr = (J * tau - 2.0f * pi * pi * tau * tau * r) / tau;
+            const float dfV_dV = 2.0f * V / tau;
+            float nlr = mr + dt * (mr * dfr_dr + mv * dfV_dr) + cG * coup;
+            const float nlv = mv + dt * (mr * dfr_dV + mv * dfV_dV);
+            nlr += a.dr[static_cast<long long>(k) * N + j];
+            deta += static_cast<double>(dt / tau) * static_cast<double>(mv);
+            dG += static_cast<double>(dt / tau) * static_cast<double>(mv) * static_cast<double>(S);
+            lr = nlr;
+            lv = nlv;
+        }
+        __syncthreads();
+    }
+    if (own) {
+        a.lam[2 * j] = lr;
+        a.lam[2 * j + 1] = lv;
+        a.deta[j] += deta;
+        a.dG[j] += dG;
+    }
+}
+
+}  // namespace tvbg
+
+using namespace tvbg;
+
+extern "C" int tvbg_adjoint_mpr(const tvbg_adjoint* d_adj, int32_t n_inst, int32_t threads,
+                                void* stream) {
+    if (!d_adj || n_inst < 0 || threads < 32 || threads > 1024 || (threads & 31))
+        return set_error(TVBG_EINVAL, "tvbg_adjoint_mpr: bad arguments");
+    if (n_inst == 0) return TVBG_OK;
+    adjoint_mpr_kernel<<<n_inst, threads, 0, static_cast<cudaStream_t>(stream)>>>(d_adj, n_inst);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return set_cuda_error(e, "tvbg_adjoint_mpr launch");
+    return TVBG_OK;
+}

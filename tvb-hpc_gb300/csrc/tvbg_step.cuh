@@ -183,6 +183,8 @@ __device__ __forceinline__ void run_steps(const tvbg_instance& d, const Ring<SME
     const bool trace = (flags & TVBG_F_TRACE) != 0 && d.trace != nullptr;
     const bool tracka = (flags & TVBG_F_TRACKA) != 0;
     const bool midsync = (flags & TVBG_F_MIDSYNC) != 0;
+    const bool trace_csum = trace && (flags & TVBG_F_TRACE_CSUM) != 0;
+    const int trace_cols = d.trace_nobs + (trace_csum ? 1 : 0);
     const tvbg_edge* __restrict__ edges = d.edges;
     const float dt = d.dt, sqrt_dt = d.sqrt_dt;
     const int g = lane / TPN, lig = lane % TPN;
@@ -224,7 +226,7 @@ __device__ __forceinline__ void run_steps(const tvbg_instance& d, const Ring<SME
                 if (own) {
                     const long long row = (t / d.trace_every) % d.trace_len;
                     float* dst = d.trace + row * d.trace_stride +
-                                 static_cast<long long>(my) * d.trace_nobs;
+                                 static_cast<long long>(my) * trace_cols;
                     for (int o = 0; o < d.trace_nobs; ++o) dst[o] = M::obs(x, o);
                 }
                 trace_cd = d.trace_every;
@@ -267,6 +269,11 @@ __device__ __forceinline__ void run_steps(const tvbg_instance& d, const Ring<SME
             if (own) {
                 const float S = lds(csum_base + 4u * static_cast<uint32_t>(lane));
                 const float c = C::post(S, d);
+                if (trace_csum && t % d.trace_every == 0) {
+                    const long long row = (t / d.trace_every) % d.trace_len;
+                    d.trace[row * d.trace_stride + static_cast<long long>(my) * trace_cols +
+                            d.trace_nobs] = S;
+                }
                 if (tracka)  // the model writes obsrv[t] after the gather read it
                     ring.st(my_ring_row | ((tm + static_cast<uint32_t>(my)) & mask), obs0);
                 if (bold) {

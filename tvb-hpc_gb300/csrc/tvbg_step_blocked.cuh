@@ -52,31 +52,31 @@ __device__ __forceinline__ float post_sep(float S, float xi, float wsum, const t
 }
 
 struct BlockedSmem {
-    uint32_t ring;  // N * R floats (shared-memory ring) -- 0 bytes if global
-    uint32_t csum;  // K * N floats
-    uint32_t z;     // K * NS * N floats
-    uint32_t xb;    // K * N floats (BOLD inputs of the block)
-    uint32_t bs;    // 4 * N floats (balloon state)
-    uint32_t mbar;  // 8 bytes
+    uint32_t ring;   // shared address of the ring (TMA copies)
+    uint32_t mbar;   // 8-byte mbarrier
+    float* sring;    // N * R floats (shared-memory ring) -- 0 bytes if global
+    float* csum;     // K * N floats
+    float* z;        // K * NS * N floats
+    float* xb;       // K * N floats (BOLD inputs of the block)
+    float* bs;       // 4 * N floats (balloon state)
 };
 
 // Integrate the balloon of node n over `cnt` stored inputs starting at step tb.
 __device__ __forceinline__ void bold_steps(const tvbg_instance& d, int n, int N, long long tb,
-                                           int cnt, uint32_t xb, uint32_t bsm) {
-    float s = lds(bsm + 4u * (0 * N + n)), F = lds(bsm + 4u * (1 * N + n));
-    float V = lds(bsm + 4u * (2 * N + n)), Q = lds(bsm + 4u * (3 * N + n));
+                                           int cnt, const float* xb, float* bsm) {
+    float s = bsm[0 * N + n], F = bsm[1 * N + n], V = bsm[2 * N + n], Q = bsm[3 * N + n];
     for (int k = 0; k < cnt; ++k) {
         const long long t = tb + k;
-        Balloon::step(s, F, V, Q, lds(xb + 4u * (k * N + n)), d.dt_bold);
+        Balloon::step(s, F, V, Q, xb[k * N + n], d.dt_bold);
         if ((t + 1) % d.bold_period == 0) {
             const long long row = (t + 1) / d.bold_period - 1;
             if (row >= 0 && row < d.bold_len) d.bold_out[row * N + n] = Balloon::signal(V, Q);
         }
     }
-    sts(bsm + 4u * (0 * N + n), s);
-    sts(bsm + 4u * (1 * N + n), F);
-    sts(bsm + 4u * (2 * N + n), V);
-    sts(bsm + 4u * (3 * N + n), Q);
+    bsm[0 * N + n] = s;
+    bsm[1 * N + n] = F;
+    bsm[2 * N + n] = V;
+    bsm[3 * N + n] = Q;
 }
 
 template <class M, int CF, int TPN, int K, bool SMEM>
@@ -124,16 +124,28 @@ __device__ __forceinline__ void run_blocked(const tvbg_instance& d, const Blocke
                 for (int k = 0; k < K; ++k) acc[k] = 0.0f;
                 const int lo = valid ? __ldg(d.row + n) : 0;
                 const int hi = valid ? __ldg(d.row + n + 1) : 0;
-                for (int e = lo + lig; e < hi; e += TPN) {
-                    const uint2 ew = __ldg(reinterpret_cast<const uint2*>(edges) + e);
-                    const uint32_t col = ew.x >> 16, c = ew.x & 0xffffu;
-                    const uint32_t idx = col * R + ((tm + c) & mask);
-                    const float w = __uint_as_float(ew.y);
+                const float* __restrict__ rsrc = SMEM ? sm.sring : gring;
+                int e = lo + lig;
+                // two edges per iteration: independent loads in flight
+                for (; e + TPN < hi; e += 2 * TPN) {
+                    const uint2 e0 = __ldg(reinterpret_cast<const uint2*>(edges) + e);
+                    const uint2 e1 = __ldg(reinterpret_cast<const uint2*>(edges) + e + TPN);
+                    const uint32_t i0 = (e0.x >> 16) * R + ((tm + (e0.x & 0xffffu)) & mask);
+                    const uint32_t i1 = (e1.x >> 16) * R + ((tm + (e1.x & 0xffffu)) & mask);
+                    const float w0 = __uint_as_float(e0.y), w1 = __uint_as_float(e1.y);
 #pragma unroll
                     for (int k = 0; k < K; ++k) {
-                        const float v = SMEM ? lds(sm.ring + 4u * (idx + k)) : gring[idx + k];
-                        acc[k] = fmaf(w, pre_src<CF>(v, d), acc[k]);
+                        const float v0 = rsrc[i0 + k], v1 = rsrc[i1 + k];
+                        acc[k] = fmaf(w0, pre_src<CF>(v0, d), acc[k]);
+                        acc[k] = fmaf(w1, pre_src<CF>(v1, d), acc[k]);
                     }
+                }
+                if (e < hi) {
+                    const uint2 e0 = __ldg(reinterpret_cast<const uint2*>(edges) + e);
+                    const uint32_t i0 = (e0.x >> 16) * R + ((tm + (e0.x & 0xffffu)) & mask);
+                    const float w0 = __uint_as_float(e0.y);
+#pragma unroll
+                    for (int k = 0; k < K; ++k) acc[k] = fmaf(w0, pre_src<CF>(rsrc[i0 + k], d), acc[k]);
                 }
 #pragma unroll
                 for (int k = 0; k < K; ++k) {
@@ -144,7 +156,7 @@ __device__ __forceinline__ void run_blocked(const tvbg_instance& d, const Blocke
                 if (valid && lig == 0) {
 #pragma unroll
                     for (int k = 0; k < K; ++k)
-                        if (k < cnt) sts(sm.csum + 4u * (k * N + n), acc[k]);
+                        if (k < cnt) sm.csum[k * N + n] = acc[k];
                 }
             }
             if (noise) {
@@ -162,7 +174,7 @@ __device__ __forceinline__ void run_blocked(const tvbg_instance& d, const Blocke
                         const long long ts = tc * SPC + r / NS;
                         const int v = r % NS;
                         if (ts >= t0b && ts < t0b + cnt)
-                            sts(sm.z + 4u * ((static_cast<int>(ts - t0b) * NS + v) * N + n), zz[r]);
+                            sm.z[(static_cast<int>(ts - t0b) * NS + v) * N + n] = zz[r];
                     }
                 }
             }
@@ -177,35 +189,36 @@ __device__ __forceinline__ void run_blocked(const tvbg_instance& d, const Blocke
         if (cnt == 0) break;
         // ---------------- phase B: node updates ----------------
         if (own) {
-            for (int k = 0; k < cnt; ++k) {
-                const long long t = t0b + k;
-                if (trace && t % d.trace_every == 0) {
-                    const long long row = (t / d.trace_every) % d.trace_len;
-                    float* dst = d.trace + row * d.trace_stride + static_cast<long long>(tid) * d.trace_nobs;
-                    for (int o = 0; o < d.trace_nobs; ++o) dst[o] = M::obs(x, o);
-                }
-                if (bold) sts(sm.xb + 4u * (k * N + tid), M::obs(x, d.bold_obs));
-                const float S = lds(sm.csum + 4u * (k * N + tid));
-                const float c = post_sep<CF>(S, obs0, wsum, d);
-                float f[NS];
-                M::drift(x, c, p, K_, f);
 #pragma unroll
-                for (int v = 0; v < NS; ++v) x[v] = fmaf(dt, f[v], x[v]);
-                if (noise) {
+            for (int k = 0; k < K; ++k) {
+                if (k < cnt) {
+                    const long long t = t0b + k;
+                    if (trace && t % d.trace_every == 0) {
+                        const long long row = (t / d.trace_every) % d.trace_len;
+                        float* dst = d.trace + row * d.trace_stride +
+                                     static_cast<long long>(tid) * d.trace_nobs;
+                        for (int o = 0; o < d.trace_nobs; ++o) dst[o] = M::obs(x, o);
+                    }
+                    if (bold) sm.xb[k * N + tid] = M::obs(x, d.bold_obs);
+                    const float S = sm.csum[k * N + tid];
+                    const float c = post_sep<CF>(S, obs0, wsum, d);
+                    float f[NS];
+                    M::drift(x, c, p, K_, f);
 #pragma unroll
-                    for (int v = 0; v < NS; ++v)
-                        x[v] = fmaf(sqrt_dt * lds(sm.z + 4u * ((k * NS + v) * N + tid)), d.sigma[v], x[v]);
-                }
-                M::limit(x, flags);
-                obs0 = M::obs(x, 0);
-                const uint32_t pos = (static_cast<uint32_t>(t) + 1u + static_cast<uint32_t>(tid)) & mask;
-                const uint32_t idx = static_cast<uint32_t>(tid) * R + pos;
-                if (SMEM) {
-                    sts(sm.ring + 4u * idx, obs0);
-                    if (pos < kGhost) sts(sm.ring + 4u * (idx + nh), obs0);
-                } else {
-                    gring[idx] = obs0;
-                    if (pos < kGhost) gring[idx + nh] = obs0;
+                    for (int v = 0; v < NS; ++v) x[v] = fmaf(dt, f[v], x[v]);
+                    if (noise) {
+#pragma unroll
+                        for (int v = 0; v < NS; ++v)
+                            x[v] = fmaf(sqrt_dt * sm.z[(k * NS + v) * N + tid], d.sigma[v], x[v]);
+                    }
+                    M::limit(x, flags);
+                    obs0 = M::obs(x, 0);
+                    const uint32_t pos =
+                        (static_cast<uint32_t>(t) + 1u + static_cast<uint32_t>(tid)) & mask;
+                    const uint32_t idx = static_cast<uint32_t>(tid) * R + pos;
+                    float* rdst = SMEM ? sm.sring : gring;
+                    rdst[idx] = obs0;
+                    if (pos < kGhost) rdst[idx + nh] = obs0;
                 }
             }
         }
@@ -245,7 +258,7 @@ __device__ __forceinline__ void run_instance_blocked(const tvbg_instance& d, con
         for (int e = lo; e < hi; ++e) wsum += __uint_as_float(__ldg(&d.edges[e].pk + 1));
     }
     const bool bold = (d.flags & TVBG_F_BOLD) && d.bold;
-    for (int q = tid; q < 4 * N; q += blockDim.x) sts(sp.bs + 4u * q, bold ? d.bold[q] : 0.0f);
+    for (int q = tid; q < 4 * N; q += blockDim.x) sp.bs[q] = bold ? d.bold[q] : 0.0f;
     const uint32_t mask = nh - 1u;
     const uint32_t pos0 = (static_cast<uint32_t>(d.t0) + static_cast<uint32_t>(tid)) & mask;
     const uint32_t seed_idx = static_cast<uint32_t>(tid) * R + pos0;
@@ -257,8 +270,8 @@ __device__ __forceinline__ void run_instance_blocked(const tvbg_instance& d, con
             return;
         }
         if (own) {
-            sts(sp.ring + 4u * seed_idx, M::obs(x, 0));
-            if (pos0 < kGhost) sts(sp.ring + 4u * (seed_idx + nh), M::obs(x, 0));
+            sp.sring[seed_idx] = M::obs(x, 0);
+            if (pos0 < kGhost) sp.sring[seed_idx + nh] = M::obs(x, 0);
         }
         __syncthreads();
         run_blocked<M, CF, TPN, K, true>(d, sp, x, p, wsum);
@@ -277,7 +290,7 @@ __device__ __forceinline__ void run_instance_blocked(const tvbg_instance& d, con
         for (int v = 0; v < M::NS; ++v) d.state[tid * M::NS + v] = x[v];
     }
     if (bold)
-        for (int q = tid; q < 4 * N; q += blockDim.x) d.bold[q] = lds(sp.bs + 4u * q);
+        for (int q = tid; q < 4 * N; q += blockDim.x) d.bold[q] = sp.bs[q];
     __syncthreads();
 }
 
@@ -296,11 +309,12 @@ __global__ void __launch_bounds__(1024, 1)
     __shared__ tvbg_instance s_inst;
     BlockedSmem sp;
     sp.ring = smem_addr(smem);
-    sp.csum = sp.ring + smem_ring_cap;
-    sp.z = sp.csum + 4u * K * nmax;
-    sp.xb = sp.z + 4u * K * M::NS * nmax;
-    sp.bs = sp.xb + 4u * K * nmax;
-    sp.mbar = (sp.bs + 4u * 4 * nmax + 15u) & ~15u;
+    sp.sring = reinterpret_cast<float*>(smem);
+    sp.csum = reinterpret_cast<float*>(smem + smem_ring_cap);
+    sp.z = sp.csum + K * nmax;
+    sp.xb = sp.z + K * M::NS * nmax;
+    sp.bs = sp.xb + K * nmax;
+    sp.mbar = (smem_addr(sp.bs + 4 * nmax) + 15u) & ~15u;
     uint32_t phase = 0;
     if (threadIdx.x == 0) {
         mbar_init(sp.mbar, 1);

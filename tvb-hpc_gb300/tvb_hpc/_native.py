@@ -40,6 +40,7 @@ F_SMEM_RING = 16
 F_NO_WRAP = 32
 F_TRACKA = 64
 F_MIDSYNC = 128
+F_TRACE_CSUM = 256
 
 GHOST = 8  # ghost slots per ring row of the time-blocked kernel
 
@@ -106,6 +107,19 @@ class tvbg_launch(ctypes.Structure):
     ]
 
 
+class tvbg_adjoint(ctypes.Structure):
+    _fields_ = [
+        ('edges_t', ctypes.c_void_p), ('row_t', ctypes.c_void_p), ('seg', ctypes.c_void_p),
+        ('dr', ctypes.c_void_p), ('lam', ctypes.c_void_p), ('ring', ctypes.c_void_p),
+        ('deta', ctypes.c_void_p), ('dG', ctypes.c_void_p), ('t0', ctypes.c_int64),
+        ('len', ctypes.c_int32), ('N', ctypes.c_int32), ('lognh', ctypes.c_int32),
+        ('reserved0', ctypes.c_int32), ('dt', ctypes.c_float), ('G', ctypes.c_float),
+        ('consts', ctypes.c_float * 4),
+    ]
+
+
+ADJOINT_DTYPE = np.dtype(tvbg_adjoint)
+
 #: numpy view of tvbg_instance (used to build instance tables in bulk)
 INSTANCE_DTYPE = np.dtype(tvbg_instance)
 
@@ -132,6 +146,7 @@ SIGNATURES = {
     'tvbg_fc_scratch_bytes': (ctypes.c_int, [_i32, _i32, ctypes.POINTER(_i64)]),
     'tvbg_fc_noalloc': (ctypes.c_int, [_vp, _i32, _i32, _i32, _i64, _vp, _vp, _vp, _vp]),
     'tvbg_philox_normal': (ctypes.c_int, [_u64, _u32, _vp, _i64, _vp]),
+    'tvbg_adjoint_mpr': (ctypes.c_int, [_vp, _i32, _i32, _vp]),
     'tvbg_philox_u32': (ctypes.c_int, [_u32, _u32, _u32, _u32, _u32, _vp, _i64, _vp]),
 }
 

@@ -1,0 +1,222 @@
+"""
+Gradients of an FC-fit loss through the delayed network step (MPR with
+linear coupling), by a hand-written adjoint.
+
+Problem (one connectome, I instances, T steps, deterministic):
+  x(t+1) = x(t) + dt f(x(t), G_b S(t), eta_b)   (Montbrio-Pazo-Roxin, r >= 0)
+  S_i(t) = sum_e w_e r_{j_e}(t - d_e)           (zero history)
+  X_b[s] = r_b(s + 1),  FC_b = Pearson(X_b),  loss_b = mean_{i<j}(FC_b,ij - F*_ij)^2
+
+``FCFit.forward`` runs the step kernel in chunks of `checkpoint_every`
+steps, keeping the state and the history ring at every chunk start
+(checkpoints) and the rate series for the FC.  ``FCFit.backward`` takes the
+FC gradient in FP64 (torch, batched GEMMs), then walks the chunks backwards:
+each chunk is recomputed from its checkpoint (bit-identical to the forward)
+with the state and coupling sums traced, and tvbg_adjoint_mpr runs the
+reverse-time recursion over it, carrying the adjoint state and an adjoint
+ring of mu_V between chunks; dL/dG and dL/deta accumulate in FP64.
+
+``FCFitLoss`` wraps it as a torch.autograd.Function of (G [I], eta [I, N]).
+The reference builds only symbolic partials (tvb_hpc/model.py:61-65) and an
+EM log-density (scheme.py:42-48); it has no gradient kernel.
+"""
+
+import ctypes
+
+import numpy as np
+
+from . import _native as nat
+from . import model as mdl, coupling as cpl, scheme as sch
+from .engine import InstanceSet, plan_ring
+from .utils import getLogger
+
+LOG = getLogger(__name__)
+
+
+def transpose_edges(row, col, w, delays, lognh):
+    """Out-edges of every source node j: (target i, delay d, weight), packed
+    for the adjoint ring read of mu_V,i(t + d + 1): pk = (i << lognh) |
+    ((i + d + 1) & mask).  Returns (row_t [N+1], packed [nnz])."""
+    row = np.asarray(row, np.int64)
+    col = np.asarray(col, np.int64)
+    N = row.size - 1
+    tgt = np.repeat(np.arange(N), np.diff(row))
+    order = np.lexsort((tgt, col))              # by source j, then target i
+    src_sorted = col[order]
+    row_t = np.zeros(N + 1, np.int64)
+    np.add.at(row_t, src_sorted + 1, 1)
+    row_t = np.cumsum(row_t).astype(np.int32)
+    mask = (1 << lognh) - 1
+    i = tgt[order].astype(np.uint64)
+    d = np.asarray(delays, np.int64)[order].astype(np.uint64)
+    out = np.zeros(col.size, dtype=np.dtype([('pk', '<u4'), ('w', '<f4')]))
+    out['pk'] = ((i << np.uint64(lognh)) | ((i + d + np.uint64(1)) & np.uint64(mask))).astype(np.uint32)
+    out['w'] = np.asarray(w, np.float32)[order]
+    return row_t, out
+
+
+class FCFit:
+    """
+    FC-fit problem for I instances of deterministic MPR + linear coupling.
+
+    conn : Connectivity;  dt : ms;  speed : mm/ms (delays ceil(len/speed/dt))
+    x0 : [I, N, 2] initial (r, V);  target : [N, N] target FC;  T : steps
+    """
+
+    def __init__(self, conn, dt, speed, x0, target, T, checkpoint_every=100, rounding='ceil',
+                 model=None):
+        import torch
+        self.torch = torch
+        self.conn = conn
+        self.dt = float(dt)
+        self.speed = float(speed)
+        self.x0 = np.asarray(x0, np.float32)
+        self.I, self.N = self.x0.shape[0], conn.nnode
+        self.T = int(T)
+        self.C = int(checkpoint_every)
+        self.model = model or mdl.MPR()
+        self.cfun = cpl.Linear(self.model)
+        self.cfun.param['b'] = 0.0
+        self.scheme = sch.EulerStep(self.dt)
+        self.target = torch.as_tensor(np.asarray(target), dtype=torch.float64, device='cuda')
+        self.rounding = rounding
+        d = conn.delays(speed, dt, rounding)
+        self.lognh = plan_ring(int(d.min()), int(d.max()))[0]
+        row_t, e_t = transpose_edges(conn.row, conn.col, conn.wnz, d, self.lognh)
+        self.row_t = torch.from_numpy(row_t).cuda()
+        self.edges_t = torch.from_numpy(e_t.view(np.uint8).copy()).cuda()
+        _, consts, _ = self.model.engine_spec()
+        self.consts = consts
+
+    def _set(self, G, eta, trace_len, trace_nobs, trace_csum):
+        return InstanceSet(self.model, self.cfun, self.scheme, self.conn, dt=self.dt,
+                           couplings=np.asarray(G, np.float32), speeds=self.speed,
+                           state0=self.x0, nparam=np.asarray(eta, np.float32).reshape(self.I, self.N, 1),
+                           rounding=self.rounding, blocked=False, trace_every=1,
+                           trace_len=trace_len, trace_nobs=trace_nobs, trace_csum=trace_csum)
+
+    @staticmethod
+    def _run(iset, nsteps, tpn=2):
+        from .engine import Sweep
+        sw = Sweep.__new__(Sweep)
+        sw.__dict__.update(iset.__dict__)
+        sw.tpn = tpn
+        from .engine import DeviceStatus
+        sw.status = DeviceStatus()
+        sw._uploaded = None
+        sw.run(nsteps)
+        iset.t = sw.t
+
+    def forward(self, G, eta):
+        "Loss [I] (FP64); keeps checkpoints and the rate series for backward."
+        torch = self.torch
+        G = np.asarray(G, np.float32).reshape(self.I)
+        eta = np.asarray(eta, np.float32).reshape(self.I, self.N)
+        self.G, self.eta = G, eta
+        fw = self._set(G, eta, self.T, 1, False)
+        self.ckpt = []
+        t = 0
+        while t < self.T:
+            n = min(self.C, self.T - t)
+            self.ckpt.append((t, n, fw.state.clone(), fw.ring.clone()))
+            self._run(fw, n)
+            t += n
+        r_tr = fw.trace[:, :, :, 0]                     # r(t), t = 0..T-1
+        X = torch.cat([r_tr[:, 1:], fw.state[:, None, :, 0]], 1).double()   # X[s] = r(s+1)
+        self.fw = fw
+        loss, dX = self._fc_loss_grad(X)
+        self.dX = dX
+        return loss
+
+    def _fc_loss_grad(self, X):
+        "FP64 loss and dL/dX of the Pearson FC fit (batched GEMMs)."
+        I, T, N = X.shape
+        P = N * (N - 1) / 2.0
+        Xc = X - X.mean(1, keepdim=True)
+        nrm = Xc.norm(dim=1, keepdim=True)
+        Z = Xc / nrm
+        FC = Z.transpose(1, 2) @ Z
+        iu = self.torch.triu_indices(N, N, 1, device=X.device)
+        D = FC - self.target
+        loss = (D[:, iu[0], iu[1]] ** 2).sum(1) / P
+        A = 2.0 * D / P
+        A = A - self.torch.diag_embed(self.torch.diagonal(A, dim1=1, dim2=2))
+        gZ = Z @ A
+        zg = (Z * gZ).sum(1, keepdim=True)
+        dXc = (gZ - Z * zg) / nrm
+        dX = dXc - dXc.mean(1, keepdim=True)
+        self.fc = FC
+        return loss, dX
+
+    def backward(self):
+        "(dL/dG [I], dL/deta [I, N]) in FP64, by the adjoint over the checkpoints."
+        torch = self.torch
+        lib = nat.load()
+        I, N, T = self.I, self.N, self.T
+        nh = 1 << self.lognh
+        dr = torch.zeros((I, T + 1, N), dtype=torch.float32, device='cuda')
+        dr[:, 1:] = self.dX.float()                    # dL/dr(t) = dX[t-1]
+        lam = torch.zeros((I, N, 2), dtype=torch.float32, device='cuda')
+        lam[:, :, 0] = dr[:, T]
+        ring = torch.zeros((I, N * nh), dtype=torch.float32, device='cuda')
+        deta = torch.zeros((I, N), dtype=torch.float64, device='cuda')
+        dGn = torch.zeros((I, N), dtype=torch.float64, device='cuda')
+        rec = self._set(self.G, self.eta, self.C, 2, True)
+        threads = 32 * ((N + 31) // 32)
+        for (t0, n, st, rg) in reversed(self.ckpt):
+            rec.state.copy_(st)
+            rec.ring.copy_(rg)
+            rec.t[:] = t0
+            self._run(rec, n)
+            seg = rec.trace                              # [I, C, N, 3]: r, V, S of steps t0..
+            tab = np.zeros(I, dtype=nat.ADJOINT_DTYPE)
+            b = np.arange(I, dtype=np.int64)
+            tab['edges_t'] = self.edges_t.data_ptr()
+            tab['row_t'] = self.row_t.data_ptr()
+            tab['seg'] = seg.data_ptr() + 4 * b * seg.shape[1] * N * 3
+            tab['dr'] = dr.data_ptr() + 4 * (b * (T + 1) * N + t0 * N)
+            tab['lam'] = lam.data_ptr() + 4 * b * N * 2
+            tab['ring'] = ring.data_ptr() + 4 * b * N * nh
+            tab['deta'] = deta.data_ptr() + 8 * b * N
+            tab['dG'] = dGn.data_ptr() + 8 * b * N
+            tab['t0'] = t0
+            tab['len'] = n
+            tab['N'] = N
+            tab['lognh'] = self.lognh
+            tab['dt'] = np.float32(self.dt)
+            tab['G'] = self.G
+            tab['consts'] = self.consts[:4]
+            dev = torch.from_numpy(tab.view(np.uint8).copy()).cuda()
+            nat.check(lib.tvbg_adjoint_mpr(dev.data_ptr(), I, threads, nat.stream_handle()))
+        torch.cuda.synchronize()
+        return dGn.sum(1), deta
+
+
+class FCFitLoss:
+    """torch.autograd.Function: loss [I] = FCFitLoss.apply(G [I], eta [I, N], problem)."""
+
+    _fn = None
+
+    @classmethod
+    def apply(cls, G, eta, problem):
+        import torch
+
+        if cls._fn is None:
+            class _F(torch.autograd.Function):
+                @staticmethod
+                def forward(ctx, G_, eta_, prob):
+                    ctx.prob = prob
+                    return prob.forward(G_.detach().cpu().numpy(),
+                                        eta_.detach().cpu().numpy()).to(G_.dtype)
+
+                @staticmethod
+                def backward(ctx, gl):
+                    dG, deta = ctx.prob.backward()
+                    gl = gl.to(torch.float64)
+                    return ((gl * dG).to(torch.float32).to(gl.device),
+                            (gl[:, None] * deta).to(torch.float32).to(gl.device), None)
+            cls._fn = _F
+        return cls._fn.apply(G, eta, problem)
+
+
+_ = ctypes

@@ -179,7 +179,7 @@ class InstanceSet:
                  nparam=None, delays=None, rounding='ceil', seed=0, inst_ids=None,
                  history='zero', bold_period=0, bold_len=0, trace_every=0, trace_len=0,
                  trace_nobs=None, flags=0, cf_b=None, nh_extra=0, t0=0, order='cuda',
-                 sync_every=None, blocked='auto', warps=None):
+                 sync_every=None, blocked='auto', warps=None, trace_csum=False):
         _device_ok()
         torch = _torch()
         self.torch = torch
@@ -297,11 +297,15 @@ class InstanceSet:
         self.trace_every = int(trace_every)
         self.trace_len = int(trace_len)
         self.trace_nobs = int(trace_nobs if trace_nobs is not None else self.nobs)
+        # with trace_csum each trace row also carries the step's raw coupling sum
+        self.trace_cols = self.trace_nobs + (1 if trace_csum else 0)
         self.trace = None
         if self.trace_every > 0:
-            self.trace = torch.zeros((I, max(1, self.trace_len), N, self.trace_nobs),
+            self.trace = torch.zeros((I, max(1, self.trace_len), N, self.trace_cols),
                                      dtype=torch.float32, device='cuda')
             fl |= nat.F_TRACE
+            if trace_csum:
+                fl |= nat.F_TRACE_CSUM
         if getattr(scheme, 'noise', False):
             fl |= nat.F_NOISE
         self.flags = fl
@@ -362,9 +366,9 @@ class InstanceSet:
             tab['bold_out'] = self.bold_out.data_ptr() + 4 * bidx * self.bold_out.shape[1] * N
         if self.trace is not None:
             tab['trace'] = (self.trace.data_ptr()
-                            + 4 * bidx * self.trace.shape[1] * N * self.trace_nobs)
+                            + 4 * bidx * self.trace.shape[1] * N * self.trace_cols)
         tab['t0'] = self.t
-        tab['trace_stride'] = N * self.trace_nobs
+        tab['trace_stride'] = N * self.trace_cols
         tab['nsteps'] = np.broadcast_to(np.asarray(nsteps, np.int64), (I, )).astype(np.int32)
         tab['N'] = N
         tab['nnz'] = self.nnz
