@@ -250,6 +250,7 @@ class MixedStep:
         self.batch.capture()
         self.sw = self.sets[0]
         self.sw.tpn = self.batch.launches[0]['cfg'].tpn
+        self.status = self.batch.status
         self.n_launch = len(self.batch.launches)
         # plain path: one sweep launch per connectome
         self.plain = []
@@ -453,7 +454,7 @@ def gpu_arm(args):
     total_ms = float(t.item())
     ms_per_step = total_ms / args.steps
     value = world * node_steps(wl) * args.steps / (total_ms / 1e3)
-    gs.sw.status.check()
+    (gs.status if hasattr(gs, 'status') else gs.sw.status).check()
 
     plain = None
     if wl['name'] == 'mixed':

@@ -1,0 +1,236 @@
+"""
+Serving loop with continuous batching for sweep requests.
+
+A request is a parameter sweep: a model (Kuramoto, G2DO or MPR) on a
+connectome, a number of instances, a number of steps, seeds -- optionally
+with FC-fit gradients (MPR, through tvb_hpc.adjoint).  The server keeps every
+admitted request's state, parameters and history rings resident in device
+memory and advances all of them together:
+
+  tick:
+    1. admit queued requests (arrival time <= now) while their device
+       footprint fits the HBM budget;
+    2. advance every active request by min(chunk, steps left): one
+       persistent batch launch per model (tvbg_batch_run, forked streams),
+       instances of all requests interleaved longest-first;
+    3. retire requests that reached their step count: copy the final state
+       (and gradients) to the host, free the device memory, record latency.
+
+Requests that arrive while a tick runs join at the next tick, as slots and
+memory free up; their work overlaps on the device with the requests already
+running.  Chunk boundaries are exact (the step kernels resume bit-for-bit
+from the resident state and ring), and every request keeps its own Philox
+key (request seed, request-local instance id) and launch shape, so a
+request's result is the same alone and in any mix.
+
+The reference has no serving layer; its CUDA launcher runs one sweep per
+call and copies results back after every chunk
+(dsl/dsl_cuda/example/cuda_run.py:124-142).
+"""
+
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import model as mdl, coupling as cpl, scheme as sch
+from .engine import InstanceSet, Batch
+from .utils import getLogger
+
+LOG = getLogger(__name__)
+
+MODELS = {
+    'Kuramoto': (mdl.Kuramoto, cpl.Kuramoto, False),
+    'G2DO': (mdl.G2DO, cpl.Diff, True),
+    'MPR': (mdl.MPR, cpl.Linear, True),
+}
+
+
+@dataclass
+class Request:
+    rid: int
+    model: str
+    conn: object
+    couplings: np.ndarray
+    speeds: np.ndarray
+    x0: np.ndarray
+    nsteps: int
+    nparam: object = None
+    seed: int = 0
+    dt: float = 0.1
+    want_grad: bool = False
+    target: object = None
+    arrival: float = 0.0
+    # filled by the server
+    admitted: float = None
+    finished: float = None
+    state: np.ndarray = None
+    grad: tuple = None
+    steps_done: int = 0
+    iset: object = field(default=None, repr=False)
+    nbytes: int = 0
+
+    @property
+    def node_steps(self):
+        return float(self.couplings.size) * self.conn.nnode * self.nsteps
+
+    @property
+    def latency(self):
+        return None if self.finished is None else self.finished - self.arrival
+
+
+def footprint(req):
+    "Device bytes a request needs (rings, state, parameters, edges), estimated."
+    from .engine import plan_ring
+    N, I = req.conn.nnode, req.couplings.size
+    d = req.conn.delays(float(np.min(req.speeds)), req.dt, 'ceil')
+    lognh = plan_ring(int(d.min()), int(d.max()))[0]
+    ring = N * ((1 << lognh) + 8) * 4
+    return I * (ring + N * 4 * 6 + 512) + req.conn.nnz * 8 * len(np.unique(req.speeds))
+
+
+class Server:
+    """
+    Continuous-batching server.  `hbm_budget` bounds the device bytes of the
+    admitted requests; `chunk` is the number of steps every active request
+    advances per tick.
+    """
+
+    def __init__(self, hbm_budget=180e9, chunk=2000, clock=time.perf_counter):
+        import torch
+        self.torch = torch
+        self.budget = float(hbm_budget)
+        self.chunk = int(chunk)
+        self.clock = clock
+        self.queue = []
+        self.active = []
+        self.done = []
+        self.used = 0
+        self.ticks = 0
+        self.node_steps = 0.0
+
+    def submit(self, req):
+        self.queue.append(req)
+
+    def _admit(self, now):
+        torch = self.torch
+        keep = []
+        for req in sorted(self.queue, key=lambda r: r.arrival):
+            if req.arrival > now:
+                keep.append(req)
+                continue
+            need = footprint(req)
+            free = torch.cuda.mem_get_info()[0]
+            if self.used + need > self.budget or need > free:
+                keep.append(req)
+                continue
+            M, C, noise = MODELS[req.model]
+            m = M()
+            cf = C(m)
+            scm = sch.EulerMaryuyamaStep(req.dt) if (noise and not req.want_grad) else sch.EulerStep(req.dt)
+            req.iset = InstanceSet(m, cf, scm, req.conn, dt=req.dt, couplings=req.couplings,
+                                   speeds=req.speeds, state0=req.x0, nparam=req.nparam,
+                                   seed=req.seed, blocked=False if req.want_grad else 'auto')
+            req.admitted = self.clock()
+            req.nbytes = need
+            self.used += need
+            self.active.append(req)
+        self.queue = keep
+
+    def _retire(self, req):
+        req.state = req.iset.state.cpu().numpy()
+        if req.want_grad and req.model == 'MPR' and req.target is not None:
+            from .adjoint import FCFit
+            prob = FCFit(req.conn, req.dt, float(req.speeds[0]), req.x0, req.target, req.nsteps)
+            prob.forward(req.couplings, np.asarray(req.nparam).reshape(req.couplings.size, -1))
+            req.grad = tuple(t.cpu().numpy() for t in prob.backward())
+        req.finished = self.clock()
+        self.used -= req.nbytes
+        req.iset = None
+        self.done.append(req)
+
+    def tick(self):
+        "Admit, advance every active request by one chunk, retire; returns work done."
+        self._admit(self.clock())
+        if not self.active:
+            return 0.0
+        by_model = {}
+        for req in self.active:
+            by_model.setdefault((req.model, req.want_grad), []).append(req)
+        batches = []
+        work = 0.0
+        for reqs in by_model.values():
+            steps = [min(self.chunk, r.nsteps - r.steps_done) for r in reqs]
+            b = Batch([r.iset for r in reqs], steps)
+            b.launch()
+            batches.append((b, reqs, steps))
+            work += sum(r.couplings.size * r.conn.nnode * n for r, n in zip(reqs, steps))
+        self.torch.cuda.synchronize()
+        for b, reqs, steps in batches:
+            b.status.check()
+            for r, n in zip(reqs, steps):
+                r.steps_done += n
+                r.iset.t += n
+        finished = [r for r in self.active if r.steps_done >= r.nsteps]
+        self.active = [r for r in self.active if r.steps_done < r.nsteps]
+        for r in finished:
+            self._retire(r)
+        self.ticks += 1
+        self.node_steps += work
+        return work
+
+    def run(self, until_empty=True, max_ticks=None):
+        while self.queue or self.active:
+            if max_ticks is not None and self.ticks >= max_ticks:
+                break
+            if not self.active and self.queue:
+                nxt = min(r.arrival for r in self.queue)
+                wait = nxt - self.clock()
+                if wait > 0:
+                    time.sleep(min(wait, 0.05))
+            self.tick()
+            if not until_empty:
+                break
+        return self.done
+
+    def stats(self):
+        lat = np.array([r.latency for r in self.done if r.latency is not None])
+        out = {'requests': len(self.done), 'ticks': self.ticks, 'node_steps': self.node_steps}
+        if lat.size:
+            out.update(p50_s=float(np.percentile(lat, 50)), p99_s=float(np.percentile(lat, 99)))
+        return out
+
+
+def random_requests(n, rate, rng, conns, models=('Kuramoto', 'G2DO', 'MPR'), inst=(1, 4096),
+                    steps=(1000, 100000), grad_frac=0.1, dt=0.1, t0=0.0):
+    """Poisson arrivals at `rate` per second; model uniform, connectome
+    uniform over `conns`, instance count and step count log-uniform."""
+    out = []
+    t = t0
+    for k in range(n):
+        t += rng.exponential(1.0 / rate)
+        name = models[rng.integers(len(models))]
+        conn = conns[rng.integers(len(conns))]
+        I = int(np.exp(rng.uniform(np.log(inst[0]), np.log(inst[1] + 1))))
+        I = max(1, min(I, inst[1]))
+        T = int(np.exp(rng.uniform(np.log(steps[0]), np.log(steps[1]))))
+        N = conn.nnode
+        want_grad = name == 'MPR' and rng.random() < grad_frac
+        if name == 'Kuramoto':
+            x0 = rng.uniform(0, 2 * np.pi, (I, N, 1))
+            nparam = rng.normal(2 * np.pi * 0.01, 0.001, (I, N, 1))
+            G = np.logspace(-2, 1, I)
+        elif name == 'G2DO':
+            x0 = rng.uniform(-0.5, 0.5, (I, N, 2))
+            nparam = None
+            G = np.logspace(-3, 0, I)
+        else:
+            x0 = np.stack([rng.uniform(0.05, 0.3, (I, N)), rng.uniform(-1.5, -0.5, (I, N))], -1)
+            nparam = rng.uniform(-6, -4, (I, N, 1))
+            G = np.logspace(-2, -0.5, I)
+        target = np.corrcoef(rng.normal(size=(N, 40))) if want_grad else None
+        out.append(Request(rid=k, model=name, conn=conn, couplings=G.astype(np.float32),
+                           speeds=np.full(I, 4.0, np.float32), x0=x0.astype(np.float32),
+                           nsteps=T, nparam=None if nparam is None else nparam.astype(np.float32),
+                           seed=1000 + k, dt=dt, want_grad=want_grad, target=target, arrival=t))
+    return out
