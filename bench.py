@@ -10,7 +10,8 @@ for all of its time steps, then the per-instance FC is computed.  The
 workload sizes are those of the benchmark configurations (seeded synthetic
 connectomes; there is no dataset):
 
-  grid   (default) dense parameter grid: generic 2-D oscillator (G2DO) with
+  grid   (default) dense parameter grid: generic 2-D oscillator (the CUDA DSL /
+         TVB form, cubic and coupling on V) with
          linear difference coupling and Euler-Maruyama noise (sigma 1e-3,
          Philox keyed by seed/instance/node/step), N = 84, 30% density,
          64 x 64 grid of G in logspace(-3, 0) x speed in linspace(1, 20)
@@ -63,7 +64,8 @@ def grid_workload(n_g=64, n_s=64, nsteps=100_000, N=84, seed=0):
     bold_period = 7200  # 720 ms at dt 0.1 ms
     return dict(name='grid', conn=conn, couplings=gg.ravel(), speeds=ss.ravel(), x0=x0,
                 nsteps=nsteps, dt=0.1, bold_period=bold_period,
-                bold_len=nsteps // bold_period, target=target, model='G2DO', cfun='Diff',
+                bold_len=nsteps // bold_period, target=target, model='Generic2dOscillator',
+                cfun='Diff',
                 noise=True, seed=12345)
 
 

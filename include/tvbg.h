@@ -58,6 +58,9 @@ extern "C" {
 #define TVBG_MODEL_G2DO 1     /* model.py:262-276  state W V, param a        */
 #define TVBG_MODEL_MPR 2      /* Montbrio-Pazo-Roxin 2015, state r V, param eta */
 #define TVBG_MODEL_LINEAR 3   /* model.py:250-259  state x, param lam        */
+#define TVBG_MODEL_G2DOSC 4   /* generic 2-D oscillator in the form of the CUDA
+                                 DSL (dsl/dsl_cuda/CUDAmodels/oscillator.c:149-150):
+                                 state V W, cubic in V, coupling into V */
 
 /* ---- coupling functions (tvb_hpc/coupling.py) --------------------------- */
 #define TVBG_CFUN_LINEAR 0    /* pre = x_j,                  post = a*sum + b */

@@ -71,7 +71,7 @@ def _p(a):
 
 
 def nstate(model):
-    return 2 if model in (1, 2) else 1
+    return 2 if model in (1, 2, 4) else 1
 
 
 def run(model, cfun, row, col, weights, nh, nsteps, dt, delays, cf_a, nparam, state, ring=None,

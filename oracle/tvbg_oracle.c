@@ -41,6 +41,7 @@
 #define ORC_MODEL_G2DO 1
 #define ORC_MODEL_MPR 2
 #define ORC_MODEL_LINEAR 3
+#define ORC_MODEL_G2DOSC 4 /* oscillator.c:149-150 */
 
 #define ORC_CFUN_LINEAR 0
 #define ORC_CFUN_DIFF 1
@@ -79,7 +80,9 @@ typedef struct orc_cfg {
     float dt_bold;
 } orc_cfg;
 
-static int nstate(int model) { return (model == ORC_MODEL_G2DO || model == ORC_MODEL_MPR) ? 2 : 1; }
+static int nstate(int model) {
+    return (model == ORC_MODEL_G2DO || model == ORC_MODEL_MPR || model == ORC_MODEL_G2DOSC) ? 2 : 1;
+}
 
 /* ---- Philox4x32-10 (Salmon et al. 2011) -------------------------------- */
 static void philox4x32_10(uint32_t c[4], uint32_t k0, uint32_t k1) {

@@ -72,7 +72,8 @@ def test_blocked_k4_and_global_ring(cuda):
 
 
 @pytest.mark.parametrize('model_name,cfun_name', [('MPR', 'Linear'), ('Linear', 'Diff'),
-                                                  ('G2DO', 'Sigmoidal'), ('Linear', 'Linear')])
+                                                  ('G2DO', 'Sigmoidal'), ('Linear', 'Linear'),
+                                                  ('Generic2dOscillator', 'Diff')])
 def test_blocked_other_pairs(cuda, model_name, cfun_name):
     sw, x0 = make(model_name, cfun_name, I=4, tpn=4)
     check(sw, x0, 400)
@@ -85,6 +86,21 @@ def test_blocked_bold_and_trace(cuda):
     assert rel_err(sw.bold_out.cpu().numpy(), ref['bold_out']) < TOL
     assert rel_err(sw.bold.cpu().numpy(), ref['bold']) < TOL
     assert rel_err(sw.trace.cpu().numpy(), ref['trace']) < TOL
+
+
+def test_blocked_bold_large_deviations(cuda):
+    """Balloon driven hard (|f-1|, |v-1| > 0.15): the kernel's exact-form
+    branch against the FP64 oracle."""
+    sw, x0 = make('Linear', 'Linear', I=3, noise=False, speeds=(6.0, ), tpn=4,
+                  bold_period=10, bold_len=60)
+    x0[:] = 2.5
+    sw.state.copy_(sw.torch.from_numpy(x0).cuda())
+    sw.nparam.zero_()
+    sw.cf_a[:] = 0.0
+    sw.run(600)
+    ref = orc.run_sweep_like(sw, x0, 600, real='f64')
+    assert np.abs(ref['bold'][:, 1:]).max() > 0.15
+    assert rel_err(sw.bold_out.cpu().numpy(), ref['bold_out']) < TOL
 
 
 def test_blocked_chunks_bit_exact(cuda):

@@ -125,6 +125,22 @@ def test_g2do_diff_noise_parity(cuda, tpn):
           % (rel_err(got, ref['state']), rel_err(got, ref64['state'])))
 
 
+def test_generic2d_oscillator_parity(cuda):
+    "The CUDA-DSL form of the 2-D oscillator (config-1 model), per-step kernel."
+    N, I = 84, 6
+    w, ln = network.synthetic_connectome(N, 0.3, seed=12)
+    conn = network.Connectivity.from_dense(w, ln)
+    x0 = np.random.default_rng(13).uniform(-0.5, 0.5, (I, N, 2)).astype(np.float32)
+    m = model.Generic2dOscillator()
+    sw = engine.Sweep(m, coupling.Diff(m), scheme.EulerMaryuyamaStep(0.1), conn, dt=0.1,
+                      couplings=np.logspace(-3, 0, I), speeds=[2.0, 9.0, 20.0] * 2, state0=x0,
+                      seed=5, tpn=2, blocked=False, bold_period=50, bold_len=20)
+    sw.run(1000)
+    ref = orc.run_sweep_like(sw, x0, 1000)
+    assert rel_err(sw.state.cpu().numpy(), ref['state']) < TOL
+    assert rel_err(sw.bold_out.cpu().numpy(), ref['bold_out']) < TOL
+
+
 def test_mpr_linear_noise_parity(cuda):
     "config-2/3 model: Montbrio-Pazo-Roxin with linear coupling on r."
     N, I = 84, 8

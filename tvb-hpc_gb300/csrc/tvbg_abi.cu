@@ -32,6 +32,7 @@ static StepKernel lookup(int model, int cfun, int tpn) {
         case TVBG_MODEL_G2DO: return step_kernel_g2do(cfun, tpn);
         case TVBG_MODEL_MPR: return step_kernel_mpr(cfun, tpn);
         case TVBG_MODEL_LINEAR: return step_kernel_linear(cfun, tpn);
+        case TVBG_MODEL_G2DOSC: return step_kernel_g2dosc(cfun, tpn);
         default: return nullptr;
     }
 }
@@ -41,12 +42,13 @@ static BlockedKernel lookup_blocked(int model, int cfun, int tpn, int k) {
         case TVBG_MODEL_G2DO: return blocked_kernel_g2do(cfun, tpn, k);
         case TVBG_MODEL_MPR: return blocked_kernel_mpr(cfun, tpn, k);
         case TVBG_MODEL_LINEAR: return blocked_kernel_linear(cfun, tpn, k);
+        case TVBG_MODEL_G2DOSC: return blocked_kernel_g2dosc(cfun, tpn, k);
         default: return nullptr;
     }
 }
 
 uint32_t blocked_aux_bytes(int model, int k, int nmax) {
-    const int ns = (model == TVBG_MODEL_G2DO || model == TVBG_MODEL_MPR) ? 2 : 1;
+    const int ns = (model == TVBG_MODEL_G2DO || model == TVBG_MODEL_MPR || model == TVBG_MODEL_G2DOSC) ? 2 : 1;
     return 4u * static_cast<uint32_t>(k * nmax * (2 + ns) + 4 * nmax) + 32u;
 }
 

@@ -136,6 +136,33 @@ struct G2DO {
     __device__ static __forceinline__ void limit(float*, uint32_t) {}
 };
 
+// Generic 2-D oscillator as the CUDA DSL writes it
+// (dsl/dsl_cuda/CUDAmodels/oscillator.c:149-150), state (V, W), param a,
+// constants as G2DO: K = [tau, I, b, c, d, e, f, g, alpha, beta, gamma]:
+//   V' = d tau (alpha W - f V^3 + e V^2 + g V + gamma I + gamma c)
+//   W' = d (a + b V + c V^2 - beta W) / tau
+// obsrv = V, W (coupling on V).  (tvb_hpc/model.py:262-276 attaches the
+// first equation to W instead, which makes the default fixed point a saddle.)
+struct G2DOsc {
+    static constexpr int ID = TVBG_MODEL_G2DOSC;
+    static constexpr int NS = 2;
+    static constexpr int NP = 1;
+    static constexpr int NOBS = 2;
+    __device__ static __forceinline__ void drift(const float* x, float c0, const float* p,
+                                                 const float* K, float* fo) {
+        const float V = x[0], W = x[1];
+        const float a = p[0];
+        const float tau = K[0], I = K[1], b = K[2], c = K[3], d = K[4], e = K[5];
+        const float f = K[6], g = K[7], alpha = K[8], beta = K[9], gamma = K[10];
+        const float V2 = V * V;
+        const float V3 = V2 * V;
+        fo[0] = d * tau * (alpha * W - f * V3 + e * V2 + g * V + gamma * I + gamma * c0);
+        fo[1] = d * (a + b * V + c * V2 - beta * W) / tau;
+    }
+    __device__ static __forceinline__ float obs(const float* x, int k) { return k == 0 ? x[0] : x[1]; }
+    __device__ static __forceinline__ void limit(float*, uint32_t) {}
+};
+
 // Montbrio, Pazo, Roxin (2015) firing-rate model, state (r, V), per-node eta,
 // K = [Delta, J, tau, I]:
 //   r' = (Delta / (pi tau) + 2 r V) / tau
@@ -243,33 +270,37 @@ struct Cfun<TVBG_CFUN_SIGMOIDAL> {
 // float32 form (increments of f, v, q ~ 1 fall below float resolution at the
 // 1e-4 s balloon step of a 0.1 ms simulation).
 // ---------------------------------------------------------------------------
-// log1p and expm1 for the small deviations of the balloon state, from
-// textbook series: log1p(v) = 2 atanh(u), u = v / (2 + v), atanh to u^9
-// (|v| <= 0.25 -> |u| <= 0.143, truncation < 3e-10); expm1 by its Taylor
-// series to y^9 / 9! (|y| <= 0.5, truncation < 3e-10).  Outside those
-// ranges the library functions are called.
-__device__ __forceinline__ float log1p_small(float v) {
-    if (fabsf(v) > 0.25f) return log1pf(v);
-    const float u = v / (2.0f + v);
-    const float u2 = u * u;
-    float q = fmaf(u2, 1.0f / 9.0f, 1.0f / 7.0f);
-    q = fmaf(u2, q, 1.0f / 5.0f);
-    q = fmaf(u2, q, 1.0f / 3.0f);
-    q = fmaf(u2, q, 1.0f);
-    return 2.0f * u * q;
-}
+// Polynomial forms of the balloon's non-linear terms for small deviations
+// from rest, generated by csrc/gen_balloon_series.py (binomial series of
+// (1+V)^p - 1 and the Taylor series of the oxygen-extraction term, to degree
+// 8; truncation < 1e-8 for |V|, |F| <= 0.15).  Outside that range the exact
+// forms with log1pf / expm1f are used.
+constexpr float kSeriesRange = 0.15f;
 
-__device__ __forceinline__ float expm1_small(float y) {
-    if (fabsf(y) > 0.5f) return expm1f(y);
-    float q = fmaf(y, 1.0f / 362880.0f, 1.0f / 40320.0f);
-    q = fmaf(y, q, 1.0f / 5040.0f);
-    q = fmaf(y, q, 1.0f / 720.0f);
-    q = fmaf(y, q, 1.0f / 120.0f);
-    q = fmaf(y, q, 1.0f / 24.0f);
-    q = fmaf(y, q, 1.0f / 6.0f);
-    q = fmaf(y, q, 0.5f);
-    q = fmaf(y, q, 1.0f);
-    return y * q;
+#define TVBG_HORNER8(y, c1, c2, c3, c4, c5, c6, c7, c8)                                         \
+    ((y) * fmaf(fmaf(fmaf(fmaf(fmaf(fmaf(fmaf((c8), (y), (c7)), (y), (c6)), (y), (c5)), (y), \
+                                    (c4)),                                                   \
+                               (y), (c3)),                                                   \
+                          (y), (c2)),                                                        \
+                     (y), (c1)))
+
+// (1 + V)^(1/alpha) - 1, alpha = 0.32
+__device__ __forceinline__ float pow_a_m1(float V) {
+    return TVBG_HORNER8(V, 3.125000000000e+00f, 3.320312500000e+00f, 1.245117187500e+00f,
+                        3.890991210938e-02f, -6.809234619141e-03f, 2.127885818481e-03f,
+                        -8.739531040192e-04f, 4.233210347593e-04f);
+}
+// (1 + V)^(1/alpha - 1) - 1
+__device__ __forceinline__ float pow_b_m1(float V) {
+    return TVBG_HORNER8(V, 2.125000000000e+00f, 1.195312500000e+00f, 4.980468750000e-02f,
+                        -1.089477539062e-02f, 4.085540771484e-03f, -1.957654953003e-03f,
+                        1.083701848984e-03f, -6.603808142245e-04f);
+}
+// (1+F)(1 - (1-E0)^(1/(1+F)))/E0 - 1, E0 = 0.4
+__device__ __forceinline__ float oxy_m1(float F) {
+    return TVBG_HORNER8(F, 2.337615643510e-01f, -1.957071134219e-01f, 1.623830439922e-01f,
+                        -1.333146717007e-01f, 1.080672127183e-01f, -8.624289966959e-02f,
+                        6.747828035329e-02f, -5.144168894908e-02f);
 }
 
 struct Balloon {
@@ -282,11 +313,22 @@ struct Balloon {
         const float ra = 1.0f / ALPHA;
         const float a = 1.0f - E0;
         const float neg_ln_a = 0.51082562376599068f;  // -ln(0.6)
-        const float lv = log1p_small(V);
-        const float vpow_m1 = expm1_small(ra * lv);
-        const float em = expm1_small(neg_ln_a * F / (1.0f + F));
-        const float t1 = F - (1.0f + F) * a * em * (1.0f / E0);
-        const float t2 = expm1_small((ra - 1.0f) * lv) * (1.0f + Q) + Q;
+        float vpow_m1, vpowb_m1, t1;
+        if (fabsf(V) <= kSeriesRange) {
+            vpow_m1 = pow_a_m1(V);
+            vpowb_m1 = pow_b_m1(V);
+        } else {
+            const float lv = log1pf(V);
+            vpow_m1 = expm1f(ra * lv);
+            vpowb_m1 = expm1f((ra - 1.0f) * lv);
+        }
+        if (fabsf(F) <= kSeriesRange) {
+            t1 = oxy_m1(F);
+        } else {
+            const float em = expm1f(neg_ln_a * F / (1.0f + F));
+            t1 = F - (1.0f + F) * a * em * (1.0f / E0);
+        }
+        const float t2 = vpowb_m1 * (1.0f + Q) + Q;
         const float ds = x - rts * s - rtf * F;
         const float dF = s;
         const float dV = rto * (F - vpow_m1);

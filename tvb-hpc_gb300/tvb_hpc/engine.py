@@ -400,10 +400,9 @@ class InstanceSet:
         return tab
 
     def bold_obs(self):
-        "Observable feeding the balloon: sin(theta) for Kuramoto, V for G2DO, r for MPR."
-        if self.model_id == nat.MODEL_KURAMOTO:
-            return 1
-        if self.model_id == nat.MODEL_G2DO:
+        """Observable feeding the balloon: sin(theta) for Kuramoto, V for the
+        2-D oscillators, r for MPR, x for Linear."""
+        if self.model_id in (nat.MODEL_KURAMOTO, nat.MODEL_G2DO):
             return 1
         return 0
 

@@ -260,6 +260,30 @@ class G2DO(BaseModel):
     _kernel_consts = ('tau', 'I', 'b', 'c', 'd', 'e', 'f', 'g', 'alpha', 'beta', 'gamma')
 
 
+class Generic2dOscillator(BaseModel):
+    """
+    Generic 2-D oscillator in the form of the CUDA DSL kernel
+    (dsl/dsl_cuda/CUDAmodels/oscillator.c:149-150) and of TVB: the cubic and
+    the coupling act on V.  tvb_hpc's G2DO (model.py:262-276) attaches that
+    equation to W instead; with the default constants its fixed point is a
+    saddle and trajectories diverge within ~10^4 steps of 0.1 ms, so the
+    benchmark's "2D generic oscillator" uses this form.
+    """
+    state = 'V W'
+    limit = (-2, 4), (-6, 6)
+    input = 'c_0'
+    param = 'a'
+    const = dict(G2DO.const)
+    drift = (
+        'd * tau * (alpha*W - f*V**3 + e*V**2 + g*V + gamma*I + gamma*c_0)',
+        'd * (a + b*V + c*V**2 - beta*W) / tau'
+    )
+    diffs = 1e-3, 1e-3
+    obsrv = 'V', 'W'
+    _kernel = nat.MODEL_G2DOSC
+    _kernel_consts = G2DO._kernel_consts
+
+
 class MPR(BaseModel):
     """
     Montbrio-Pazo-Roxin (2015) mean-field model of quadratic integrate-and-
@@ -284,4 +308,5 @@ class MPR(BaseModel):
     _kernel_consts = ('Delta', 'J', 'tau', 'I')
 
 
-_BUILTIN = {'Kuramoto': Kuramoto, 'G2DO': G2DO, 'MPR': MPR, 'Linear': Linear}
+_BUILTIN = {'Kuramoto': Kuramoto, 'G2DO': G2DO, 'MPR': MPR, 'Linear': Linear,
+            'Generic2dOscillator': Generic2dOscillator}

@@ -41,7 +41,7 @@ LOG = getLogger(__name__)
 
 MODELS = {
     'Kuramoto': (mdl.Kuramoto, cpl.Kuramoto, False),
-    'G2DO': (mdl.G2DO, cpl.Diff, True),
+    'G2DO': (mdl.Generic2dOscillator, cpl.Diff, True),
     'MPR': (mdl.MPR, cpl.Linear, True),
 }
 
