@@ -95,6 +95,7 @@ def kuramoto_workload(I=32, N=68, nsteps=1000, seed=0):
                 noise=False, seed=0)
 
 
+PLAIN_CHUNK = 1000
 MIXED_SPEC = [(68, 0.30, 1024), (84, 0.30, 1024), (192, 0.15, 256), (400, 0.08, 64),
               (998, 0.03, 16)]
 
@@ -254,15 +255,22 @@ class MixedStep:
         self.sw.tpn = self.batch.launches[0]['cfg'].tpn
         self.status = self.batch.status
         self.n_launch = len(self.batch.launches)
-        # plain path: one sweep launch per connectome
+        # plain path: per connectome, the per-step kernel (no time blocking),
+        # one sweep launched in chunks of PLAIN_CHUNK steps (as the
+        # reference's launcher chunks, dsl/dsl_cuda/example/cuda_run.py:124-142),
+        # connectomes one after the other; chunk tables are built up front
         self.plain = []
-        for s, p in zip(self.sets, wl['parts']):
-            sw = engine.Sweep.__new__(engine.Sweep)
-            sw.__dict__.update(s.__dict__)
-            sw.tpn = 4
-            sw.status = self.batch.status
-            sw._uploaded = None
-            self.plain.append((sw, sw.prepare(p['steps'])))
+        for p in wl['parts']:
+            sw = engine.Sweep(m, cf, scm, p['conn'], dt=wl['dt'], couplings=p['couplings'],
+                              speeds=p['speeds'], state0=p['x0'], nparam=p['nparam'],
+                              seed=p['seed'], blocked=False, tpn=2)
+            chunks = []
+            steps = np.asarray(p['steps'])
+            for c in range(int(np.ceil(steps.max() / PLAIN_CHUNK))):
+                sw.t[:] = c * PLAIN_CHUNK
+                chunks.append(sw.prepare(np.clip(steps - c * PLAIN_CHUNK, 0, PLAIN_CHUNK)))
+            sw.t[:] = 0
+            self.plain.append((sw, chunks, sw.state.clone()))
 
     def reset(self, x0=None):
         for s, x in zip(self.sets, self.x0 if x0 is None else x0):
@@ -284,8 +292,14 @@ class MixedStep:
         return evs, None
 
     def run_plain(self):
-        for sw, launches in self.plain:
-            sw.launch(launches, 4)
+        for sw, chunks, _ in self.plain:
+            for launches in chunks:
+                sw.launch(launches, 2)
+
+    def reset_plain(self):
+        for sw, _, x0 in self.plain:
+            sw.state.copy_(x0)
+            sw.ring.zero_()
 
     def launches_per_step(self):
         return self.n_launch
@@ -461,10 +475,10 @@ def gpu_arm(args):
     plain = None
     if wl['name'] == 'mixed':
         # the plain path on the same work: one sweep launch per connectome
-        gs.reset()
+        gs.reset_plain()
         gs.run_plain()
         torch.cuda.synchronize()
-        gs.reset()
+        gs.reset_plain()
         p0 = torch.cuda.Event(enable_timing=True)
         p1 = torch.cuda.Event(enable_timing=True)
         p0.record()
@@ -474,7 +488,8 @@ def gpu_arm(args):
         pms = p0.elapsed_time(p1)
         plain = {'value': round(node_steps(wl) / (pms / 1e3), 1), 'unit': UNIT,
                  'ms_per_step': round(pms, 3),
-                 'path': 'one tvbg_sweep launch per connectome, sequential'}
+                 'path': 'per-step kernel, one sweep per connectome in %d-step launches, '
+                         'connectomes in sequence' % PLAIN_CHUNK}
         return finish_mixed(args, wl, gs, world, rank, value, ms_per_step, clk, kern_ms, n_kern,
                             plain, torch, dist, barrier)
 

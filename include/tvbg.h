@@ -83,6 +83,10 @@ extern "C" {
 /* the trace carries one more column per node: the raw coupling sum S of the
  * step (written during the step; used by the adjoint's recomputation) */
 #define TVBG_F_TRACE_CSUM 256u
+/* time-blocked kernel, warp-specialised: owner warps update block i while
+ * the other warps gather block i+1 and integrate the balloon of block i-1
+ * (needs block_k <= (d_min + 1) / 2 and more warps than ceil(N/32)) */
+#define TVBG_F_PIPELINE 512u
 
 /*
  * Packed connectivity edge, one per CSR non-zero, rows = target node i:

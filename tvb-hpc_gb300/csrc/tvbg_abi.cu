@@ -49,7 +49,8 @@ static BlockedKernel lookup_blocked(int model, int cfun, int tpn, int k) {
 
 uint32_t blocked_aux_bytes(int model, int k, int nmax) {
     const int ns = (model == TVBG_MODEL_G2DO || model == TVBG_MODEL_MPR || model == TVBG_MODEL_G2DOSC) ? 2 : 1;
-    return 4u * static_cast<uint32_t>(k * nmax * (2 + ns) + 4 * nmax) + 32u;
+    // csum, z and xb are double-buffered for the pipelined loop
+    return 4u * static_cast<uint32_t>(2 * k * nmax * (2 + ns) + 4 * nmax) + 32u;
 }
 
 // Dynamic shared memory of a step launch: ring capacity + per-warp sums + mbarrier.

@@ -41,6 +41,7 @@ F_NO_WRAP = 32
 F_TRACKA = 64
 F_MIDSYNC = 128
 F_TRACE_CSUM = 256
+F_PIPELINE = 512
 
 GHOST = 8  # ghost slots per ring row of the time-blocked kernel
 

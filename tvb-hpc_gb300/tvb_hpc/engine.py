@@ -179,7 +179,8 @@ class InstanceSet:
                  nparam=None, delays=None, rounding='ceil', seed=0, inst_ids=None,
                  history='zero', bold_period=0, bold_len=0, trace_every=0, trace_len=0,
                  trace_nobs=None, flags=0, cf_b=None, nh_extra=0, t0=0, order='cuda',
-                 sync_every=None, blocked='auto', warps=None, trace_csum=False):
+                 sync_every=None, blocked='auto', warps=None, trace_csum=False,
+                 pipeline=True):
         _device_ok()
         torch = _torch()
         self.torch = torch
@@ -226,16 +227,20 @@ class InstanceSet:
         # time-blocked kernel where it applies (K steps per block)
         separable = self.cfun_id in (nat.CFUN_LINEAR, nat.CFUN_DIFF, nat.CFUN_SIGMOIDAL)
         can_block = separable and order == 'cuda' and self.model_id != nat.MODEL_KURAMOTO
-        tab_k = []
+        tab_k, tab_pipe = [], []
         for t, d in enumerate(tables):
             dmin = int(d.min()) if d.size else 0
-            k = 8 if dmin + 1 >= 8 else (4 if dmin + 1 >= 4 else 0)
+            # warp-specialised pipeline needs K <= (d_min + 1) / 2
+            kp = 8 if (dmin + 1) // 2 >= 8 else (4 if (dmin + 1) // 2 >= 4 else 0)
+            k = kp or (8 if dmin + 1 >= 8 else (4 if dmin + 1 >= 4 else 0))
             if blocked is False or not can_block or plans[t][0] > 16:
-                k = 0
+                k, kp = 0, 0
             elif blocked is True and k == 0:
                 raise ValueError('blocked kernel needs d_min + 1 >= 4 (d_min = %d)' % dmin)
             tab_k.append(k)
+            tab_pipe.append(bool(kp) and pipeline)
         self.block_k = np.array([tab_k[t] for t in tab_of], np.int32)
+        self.pipe = np.array([tab_pipe[t] for t in tab_of], bool)
         self.warps = warps
         # packed edges per (table), device
         ebufs, eoff = [], []
@@ -338,15 +343,15 @@ class InstanceSet:
     def threads(self, blocked_k=0):
         own = 32 * ((self.N + 31) // 32)
         if blocked_k and self.warps:
-            return max(own, 32 * int(self.warps))
+            return max(own + 32, 32 * int(self.warps))
         if blocked_k:
-            return max(own, 256)
+            return max(own + 32, 256)
         return own
 
     def smem_ring_limit(self, threads, blocked_k=0):
         if blocked_k:
             ns = self.ns
-            aux = 4 * (blocked_k * self.N * (2 + ns) + 4 * self.N) + 32
+            aux = 4 * (2 * blocked_k * self.N * (2 + ns) + 4 * self.N) + 32
             return self.smem_cap - aux - _SMEM_RESERVE
         return self.smem_cap - 4 * threads - 16 - _SMEM_RESERVE
 
@@ -378,6 +383,7 @@ class InstanceSet:
         limit = np.array([self.smem_ring_limit(self.threads(k), k) for k in self.block_k])
         fits = (self.ring_bytes <= limit) if smem_allowed else np.zeros(I, bool)
         fl = (self.flags | self.order_flags).astype(np.uint32)
+        fl = np.where(self.pipe, fl | nat.F_PIPELINE, fl).astype(np.uint32)
         tab['flags'] = np.where(fits, fl | nat.F_SMEM_RING, fl).astype(np.uint32)
         tab['sync_every'] = self.sync_every
         tab['trace_every'] = max(1, self.trace_every)
