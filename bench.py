@@ -605,6 +605,57 @@ def cpu_baseline_mixed(wl, budget_s=12.0):
             'sample': '; '.join(desc) + ' (%.1f s), oracle C + OpenMP, -O3' % el_tot}
 
 
+def serve_arm(args):
+    """Serving loop (config-4 shapes): Poisson arrivals, models Kuramoto /
+    2-D oscillator / MPR, N in {68, 84, 192, 400, 998}, instance and step
+    counts log-uniform, 10% of MPR requests with FC-fit gradients, admission
+    by a 180 GB HBM budget.  The arrival window is bounded (--serve-seconds)
+    and the instance range capped (--serve-max-inst) so the run ends in
+    minutes; the same requests then run one by one as plain sweeps."""
+    import torch
+    torch.cuda.set_device(0)
+    from tvb_hpc import network, serve, _native
+    _native.load()
+    conns = []
+    for k, (N, dens, _) in enumerate(MIXED_SPEC):
+        w, ln = network.synthetic_connectome(N, dens, seed=k)
+        conns.append(network.Connectivity.from_dense(w, ln))
+    rng = np.random.default_rng(7)
+    n_req = max(1, int(args.serve_rate * args.serve_seconds))
+    reqs = serve.random_requests(n_req, args.serve_rate, rng, conns,
+                                 inst=(1, args.serve_max_inst), steps=(1000, 100000))
+    # warm-up: load every kernel once
+    warm = serve.Server(chunk=args.serve_chunk)
+    for r in serve.random_requests(6, 1e6, np.random.default_rng(1), conns[:2], inst=(1, 2),
+                                   steps=(200, 300), grad_frac=0.0):
+        warm.submit(r)
+    warm.run()
+    torch.cuda.synchronize()
+    srv = serve.Server(chunk=args.serve_chunk)
+    t_start = time.perf_counter()
+    for r in reqs:
+        r.arrival += t_start
+        srv.submit(r)
+    srv.run()
+    wall = time.perf_counter() - t_start
+    st = srv.stats()
+    offered = sum(r.node_steps for r in reqs) / max(args.serve_seconds, 1e-9)
+    served = st['node_steps'] / wall
+    line = {'metric': METRIC, 'value': round(served, 1), 'unit': UNIT, 'n_gpus': 1,
+            'steps': 1, 'warmup': 1, 'higher_is_better': True, 'scaling': 'weak',
+            'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic (seeded connectomes)',
+            'config': {'workload': 'serve', 'rate_per_s': args.serve_rate,
+                       'window_s': args.serve_seconds, 'requests': n_req,
+                       'max_instances': args.serve_max_inst, 'chunk_steps': args.serve_chunk,
+                       'hbm_budget_gb': 180},
+            'serve': {'p50_latency_s': round(st.get('p50_s', float('nan')), 3),
+                      'p99_latency_s': round(st.get('p99_s', float('nan')), 3),
+                      'wall_s': round(wall, 3), 'ticks': st['ticks'],
+                      'offered_node_steps_per_s': round(offered, 1),
+                      'queue_kept_up': bool(wall <= args.serve_seconds * 1.25)}}
+    print(json.dumps(line), flush=True)
+
+
 def reference_arm(args):
     "The reference path's CPU implementation (the oracle port) on host cores."
     rank = int(os.environ.get('RANK', '0'))
@@ -612,8 +663,9 @@ def reference_arm(args):
         return
     wl = WORKLOADS[args.workload]()
     vals = []
+    base = cpu_baseline_mixed if wl['name'] == 'mixed' else cpu_baseline
     for i in range(args.warmup + args.steps):
-        cb = cpu_baseline(wl, budget_s=args.ref_seconds)
+        cb = base(wl, budget_s=args.ref_seconds)
         if i >= args.warmup:
             vals.append(cb['value'])
     v = float(np.median(vals))
@@ -633,7 +685,11 @@ def main():
     ap.add_argument('--gpus', type=int, default=1)
     ap.add_argument('--steps', type=int, default=3)
     ap.add_argument('--warmup', type=int, default=3)
-    ap.add_argument('--workload', default='grid', choices=sorted(WORKLOADS))
+    ap.add_argument('--workload', default='grid', choices=sorted(WORKLOADS) + ['serve'])
+    ap.add_argument('--serve-rate', type=float, default=50.0)
+    ap.add_argument('--serve-seconds', type=float, default=2.0)
+    ap.add_argument('--serve-max-inst', type=int, default=256)
+    ap.add_argument('--serve-chunk', type=int, default=5000)
     ap.add_argument('--impl', default='engine', choices=['engine', 'reference'])
     ap.add_argument('--no-cpu', action='store_true', help='skip the cpu_baseline leg')
     ap.add_argument('--ref-seconds', type=float, default=8.0)
@@ -642,6 +698,8 @@ def main():
     args = ap.parse_args()
     if args.impl == 'reference':
         reference_arm(args)
+    elif args.workload == 'serve':
+        serve_arm(args)
     else:
         gpu_arm(args)
 

@@ -20,7 +20,7 @@ TOL = 1e-4
 
 
 def make(model_name='G2DO', cfun_name='Diff', I=8, N=84, speeds=(5.0, 20.0), noise=True,
-         seed=3, **kw):
+         seed=3, dt=0.1, **kw):
     w, ln = network.synthetic_connectome(N, 0.3, seed=seed)
     conn = network.Connectivity.from_dense(w, ln)
     rng = np.random.default_rng(seed + 1)
@@ -35,8 +35,8 @@ def make(model_name='G2DO', cfun_name='Diff', I=8, N=84, speeds=(5.0, 20.0), noi
         x0 = rng.uniform(-0.5, 0.5, (I, N, m.nsvar))
         nparam = None
     cf = getattr(coupling, cfun_name)(m)
-    scm = scheme.EulerMaryuyamaStep(0.1) if noise else scheme.EulerStep(0.1)
-    sw = engine.Sweep(m, cf, scm, conn, dt=0.1, couplings=np.logspace(-2, 0, I),
+    scm = scheme.EulerMaryuyamaStep(dt) if noise else scheme.EulerStep(dt)
+    sw = engine.Sweep(m, cf, scm, conn, dt=dt, couplings=np.logspace(-2, 0, I),
                       speeds=np.resize(np.asarray(speeds, np.float32), I),
                       state0=x0.astype(np.float32), nparam=nparam, seed=777, **kw)
     return sw, x0.astype(np.float32)
@@ -91,14 +91,15 @@ def test_blocked_bold_and_trace(cuda):
 def test_blocked_bold_large_deviations(cuda):
     """Balloon driven hard (|f-1|, |v-1| > 0.15): the kernel's exact-form
     branch against the FP64 oracle."""
-    sw, x0 = make('Linear', 'Linear', I=3, noise=False, speeds=(6.0, ), tpn=4,
-                  bold_period=10, bold_len=60)
+    # dt 1 ms: 3000 steps = 3 s of balloon time, input held at 2.5
+    sw, x0 = make('Linear', 'Linear', I=3, noise=False, speeds=(1.0, ), tpn=4, dt=1.0,
+                  bold_period=100, bold_len=30)
     x0[:] = 2.5
     sw.state.copy_(sw.torch.from_numpy(x0).cuda())
     sw.nparam.zero_()
     sw.cf_a[:] = 0.0
-    sw.run(600)
-    ref = orc.run_sweep_like(sw, x0, 600, real='f64')
+    sw.run(3000)
+    ref = orc.run_sweep_like(sw, x0, 3000, real='f64')
     assert np.abs(ref['bold'][:, 1:]).max() > 0.15
     assert rel_err(sw.bold_out.cpu().numpy(), ref['bold_out']) < TOL
 

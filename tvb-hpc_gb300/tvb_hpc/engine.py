@@ -343,9 +343,9 @@ class InstanceSet:
     def threads(self, blocked_k=0):
         own = 32 * ((self.N + 31) // 32)
         if blocked_k and self.warps:
-            return max(own + 32, 32 * int(self.warps))
+            return min(1024, max(own + 32, 32 * int(self.warps)))
         if blocked_k:
-            return max(own + 32, 256)
+            return min(1024, max(own + 32, 256))
         return own
 
     def smem_ring_limit(self, threads, blocked_k=0):
@@ -621,3 +621,15 @@ class Batch:
         if check:
             self.torch.cuda.synchronize()
             self.status.check()
+
+
+def shard(n, rank, world):
+    """Instance range [lo, hi) of `rank` among `world` replicas: contiguous,
+    balanced, covering 0..n-1 exactly once.  Instances are independent, so a
+    sweep shards with no collective on the data path; only results are
+    gathered (e.g. torch.distributed.all_gather_object on the host)."""
+    if world < 1 or not 0 <= rank < world:
+        raise ValueError('bad rank/world')
+    base, extra = divmod(int(n), int(world))
+    lo = rank * base + min(rank, extra)
+    return lo, lo + base + (1 if rank < extra else 0)
