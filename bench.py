@@ -6,9 +6,17 @@ Benchmark of the GB300 brain-network step engine.
 
 One bench "step" is one full pass of the workload: every instance of the
 sweep is reset to its seeded initial state (device-resident copy) and run
-for all of its time steps, then the per-instance FC is computed.  The
-workload sizes are those of the benchmark configurations (seeded synthetic
-connectomes; there is no dataset):
+for all of its time steps (then, for the grid, the per-instance FC is
+computed).  The workload sizes are those of the benchmark configurations
+(seeded synthetic connectomes; there is no dataset):
+
+  mixed  (default) uneven batch: connectomes of N in {68, 84, 192, 400, 998}
+         (30/30/15/8/3% density), 1024/1024/256/64/16 instances, step counts
+         uniform in [5k, 50k], Montbrio-Pazo-Roxin with linear coupling and
+         Euler-Maruyama noise (sigma 1e-2), max delay 500 steps; run as one
+         CUDA graph of persistent batch kernels.  The plain path (per-step
+         kernel, one sweep per connectome in 1000-step launches, connectomes
+         in sequence) is timed on the same work and reported beside it.
 
   grid   (default) dense parameter grid: generic 2-D oscillator (the CUDA DSL /
          TVB form, cubic and coupling on V) with
@@ -685,7 +693,7 @@ def main():
     ap.add_argument('--gpus', type=int, default=1)
     ap.add_argument('--steps', type=int, default=3)
     ap.add_argument('--warmup', type=int, default=3)
-    ap.add_argument('--workload', default='grid', choices=sorted(WORKLOADS) + ['serve'])
+    ap.add_argument('--workload', default='mixed', choices=sorted(WORKLOADS) + ['serve'])
     ap.add_argument('--serve-rate', type=float, default=50.0)
     ap.add_argument('--serve-seconds', type=float, default=2.0)
     ap.add_argument('--serve-max-inst', type=int, default=256)
