@@ -557,7 +557,8 @@ class Batch:
                 bk = int(s.block_k[b])
                 thr = s.threads(bk)
                 smem = int(s.ring_bytes[b]) if tab['flags'][b] & nat.F_SMEM_RING else 0
-                rows.append((thr, bk, tab[b], float(s.N * ns[b]), smem, s.N))
+                rows.append((thr, bk, tab[b], float(s.N * ns[b]), smem, s.N,
+                             int(s.ring_bytes[b])))
         groups = {}
         for r in rows:
             groups.setdefault((r[0], r[1]), []).append(r)
@@ -566,14 +567,24 @@ class Batch:
         m0 = self.sets[0]
         for (thr, bk), rs in sorted(groups.items(), key=lambda kv: -sum(r[3] for r in kv[1])):
             rs.sort(key=lambda r: -r[3])               # longest first
+            nmax = max(r[5] for r in rs)
+            # the CTA's scratch is sized by the group's largest N: re-check
+            # which rings still fit shared memory next to it
+            cap = m0.smem_cap - _SMEM_RESERVE - (
+                4 * (2 * bk * nmax * (2 + m0.ns) + 4 * nmax) + 32 if bk else 4 * thr + 16)
             tab = np.array([r[2] for r in rs], dtype=nat.INSTANCE_DTYPE)
+            ring_b = np.array([r[6] for r in rs], np.int64)
+            smem_ok = ((tab['flags'] & nat.F_SMEM_RING) != 0) & (ring_b <= cap)
+            tab['flags'] = np.where(smem_ok, tab['flags'] | nat.F_SMEM_RING,
+                                    tab['flags'] & ~np.uint32(nat.F_SMEM_RING)).astype(np.uint32)
+            smem_ring = int(ring_b[smem_ok].max()) if smem_ok.any() else 0
             dev = torch.from_numpy(tab.view(np.uint8).copy()).cuda()
             cfg = nat.tvbg_launch()
             cfg.model, cfg.cfun, cfg.threads = m0.model_id, m0.cfun_id, thr
             cfg.tpn = int(self.tpn or (4 if bk else 2))
-            cfg.smem_ring = int((max(r[4] for r in rs) + 15) // 16 * 16)
+            cfg.smem_ring = int((smem_ring + 15) // 16 * 16)
             cfg.block_k = bk
-            cfg.nmax = max(r[5] for r in rs) if bk else 0
+            cfg.nmax = nmax if bk else 0
             counter = torch.zeros(1, dtype=torch.int32, device='cuda')
             cfg.d_counter = counter.data_ptr()
             cfg.d_status = self.status.t.data_ptr()
