@@ -228,11 +228,16 @@ class InstanceSet:
         separable = self.cfun_id in (nat.CFUN_LINEAR, nat.CFUN_DIFF, nat.CFUN_SIGMOIDAL)
         can_block = separable and order == 'cuda' and self.model_id != nat.MODEL_KURAMOTO
         tab_k, tab_pipe = [], []
+        smem_total = max_smem() - _SMEM_RESERVE
         for t, d in enumerate(tables):
             dmin = int(d.min()) if d.size else 0
             # warp-specialised pipeline needs K <= (d_min + 1) / 2
             kp = 8 if (dmin + 1) // 2 >= 8 else (4 if (dmin + 1) // 2 >= 4 else 0)
             k = kp or (8 if dmin + 1 >= 8 else (4 if dmin + 1 >= 4 else 0))
+            # the block's scratch (double-buffered sums, normals, BOLD inputs)
+            # must fit one CTA's shared memory next to the descriptor
+            while k and 4 * (2 * k * N * (2 + self.ns) + 4 * N) + 32 > smem_total:
+                k, kp = k // 2 if k > 4 else 0, kp // 2 if kp > 4 else 0
             if blocked is False or not can_block or plans[t][0] > 16:
                 k, kp = 0, 0
             elif blocked is True and k == 0:
