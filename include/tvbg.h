@@ -157,7 +157,7 @@ typedef struct tvbg_launch {
     int32_t block_k;       /* 0 or 1: per-step kernel; 4 or 8: time-blocked     */
                            /* kernel (K steps per block, padded ring layout)    */
     int32_t nmax;          /* largest N of the call (blocked kernel); 0 = threads */
-    int32_t reserved0;
+    int32_t cluster;       /* tvbg_group_run: CTAs per group (1, 2, 4 or 8; 0 = 1) */
     int32_t *d_status;     /* optional device int: first device error code      */
     int32_t *d_counter;    /* tvbg_batch_run work counter (zeroed by the call)  */
     const int32_t *d_order;/* tvbg_batch_run instance order (cost-descending)   */
@@ -328,6 +328,100 @@ int tvbg_philox_normal(uint64_t seed, uint32_t stream_id, float *d_out,
 int tvbg_philox_u32(uint32_t k0, uint32_t k1, uint32_t c1, uint32_t c2,
                     uint32_t c3, uint32_t *d_out, int64_t n_blocks,
                     void *stream);
+
+/*
+ * ---- lane-interleaved groups --------------------------------------------
+ * TVBG_GROUP_LANES instances that share a connectome, a delay table, the
+ * model constants, the coupling b and t0 run as one group: one instance per
+ * lane of an 8-lane slice, every per-node array interleaved over the 8
+ * instances, so one delayed read of an edge is one 32-byte sector for the
+ * group and the edge record is read once for 8 instances.  Same step (CUDA
+ * order) and Philox streams as tvbg_sweep; couplings LINEAR, DIFF and
+ * SIGMOIDAL; block_k (4 or 8) steps per barrier, which needs every delay
+ * >= block_k - 1 and nh >= max(delay) + 1 + block_k.
+ * Layouts (L = 8, R = nh + 8, l = lane):
+ *   ring     [N][R][L]  slot s of node j at (j*R + (s & (nh-1)))*L + l;
+ *                       positions < 8 are mirrored at +nh
+ *   state    [N][nsvar][L]      nparam  [N][npar][L]
+ *   bold     [4][N][L]          bold_out [bold_len][N][L]
+ *   trace    [trace_len][N][trace_nobs][L]
+ * A lane with nsteps = 0 is padding (its state and ring are not updated).
+ * This layout has no counterpart in tvb-hpc; it serves the sweeps of
+ * tvb_hpc/examples/hackathon.py:58-89 (a coupling x speed grid, one delay
+ * table per speed) and dsl/dsl_cuda/example/cuda_run.py:110-142 (one
+ * thread per parameter point).
+ */
+#define TVBG_GROUP_LANES 8
+
+typedef struct tvbg_lane {
+    float cf_a;          /* coupling a (global coupling G) of this instance */
+    int32_t nsteps;      /* steps this instance takes, <= the group's nsteps */
+    uint32_t inst_id;    /* Philox key word 1 */
+    int32_t reserved0;
+} tvbg_lane;
+
+typedef struct tvbg_group {
+    const tvbg_edge *edges;  /* [nnz] pk = (col << 16) | ((nh - d) & (nh-1)) */
+    const int32_t *row;      /* [N+1] CSR row offsets (in-edges of node i)    */
+    const float *wsum;       /* [N] sum of in-edge weights (DIFF), else NULL   */
+    const int32_t *nodes;    /* [N] node visiting order, NULL = 0..N-1         */
+    float *ring;             /* [N][nh + 8][8]                                */
+    float *state;            /* [N][nsvar][8]                                 */
+    const float *nparam;     /* [N][npar][8]                                  */
+    float *bold;             /* [4][N][8] balloon deviations, or NULL         */
+    float *bold_out;         /* [bold_len][N][8]                              */
+    float *trace;            /* [trace_len][N][trace_nobs][8], or NULL        */
+    int64_t t0;              /* absolute step index of the first step         */
+    int32_t nsteps;          /* steps of the longest lane                     */
+    int32_t N;               /* nodes (< 65536)                               */
+    int32_t nnz;
+    int32_t lognh;           /* 3..16                                         */
+    int32_t model;
+    int32_t cfun;
+    uint32_t flags;          /* NOISE, BOLD, TRACE, NO_WRAP, WRAP_FMOD         */
+    int32_t trace_every;
+    int32_t trace_len;
+    int32_t trace_nobs;
+    int32_t bold_period;
+    int32_t bold_len;
+    int32_t bold_obs;
+    uint32_t seed_lo;
+    uint32_t seed_hi;
+    int32_t reserved0;
+    float dt;
+    float sqrt_dt;
+    float dt_bold;
+    float cf_b;
+    float cf_p[3];
+    float reserved1;
+    float sigma[4];
+    float consts[16];
+    tvbg_lane lanes[TVBG_GROUP_LANES];
+} tvbg_group;
+
+size_t tvbg_group_size(void);
+
+/*
+ * Host helper for tvbg_group_run: pk = (col << 16) | ((nh - delay) & (nh-1)).
+ * Needs N <= 65536, lognh <= 16 and every delay < nh.
+ */
+int tvbg_pack_edges_group(int32_t N, int32_t nnz, const int32_t *row,
+                          const int32_t *col, const float *weights,
+                          const int32_t *delays, int32_t lognh,
+                          tvbg_edge *out);
+
+/*
+ * Run the groups d_groups[0..n_groups): cfg->cluster CTAs of cfg->threads
+ * threads per group (a thread-block cluster when > 1), group of cluster c =
+ * d_order[c] (or c).  cfg->block_k = 4 or 8; cfg->tpn, smem_ring, ctas,
+ * nmax and d_counter are not used.  Graph-capturable.
+ */
+int tvbg_group_run(const tvbg_group *d_groups, int32_t n_groups,
+                   const tvbg_launch *cfg, void *stream);
+
+/* Resident CTAs per SM of the group kernel of `cfg`, and the SM count. */
+int tvbg_group_occupancy(const tvbg_launch *cfg, int32_t *ctas_per_sm,
+                         int32_t *sms);
 
 #ifdef __cplusplus
 }

@@ -165,6 +165,41 @@ def run_sweep_like(sw, state0, nsteps, real='f32', t0=0, rings=None, bold=None, 
     return res
 
 
+def run_groups_like(gs, state0, nsteps, real='f32', nthreads=1):
+    """Run the oracle on the configuration of a lane-interleaved GroupSet
+    (CUDA step order): same delays, ring lengths, parameters, seeds and
+    monitors; `nsteps` scalar or per instance.  Returns state [I,N,ns],
+    rings (list of [nh, N]), bold_out [I,bold_len,N] and trace."""
+    I = gs.n
+    state0 = np.broadcast_to(np.asarray(state0), (I, gs.N, gs.ns))
+    steps = np.broadcast_to(np.asarray(nsteps, np.int64), (I, ))
+    nparam = gs.gnparam[gs._gi, :, :, gs._li].cpu().numpy()[:, :, 0]
+    flags = (int(gs.flags) & _SEMANTIC) | F_BOLD_DEV
+    lognh_i = gs.lognh[gs.grp_of]
+    tab_i = gs.gtab[gs.grp_of]
+    res = dict(state=None, rings=[None] * I, bold=None, bold_out=None, trace=None)
+    keys = sorted(set(zip(lognh_i.tolist(), steps.tolist())))
+    for lognh, n in keys:
+        idx = np.nonzero((lognh_i == lognh) & (steps == n))[0]
+        delays = np.stack([gs.delay_tables[int(tab_i[b])] for b in idx])
+        out = run(gs.model_id, gs.cfun_id, gs.row_np, gs.col_np, gs.w_np, 1 << lognh, int(n),
+                  gs.dt, delays, gs.cf_a[idx], nparam[idx], state0[idx], flags=flags,
+                  sigma=gs.sigma, consts=gs.consts, cf_b=float(gs.cf_b), cf_p=gs.cf_p,
+                  seed=gs.seed, inst_ids=gs.inst_ids[idx], trace_every=gs.trace_every,
+                  trace_len=gs.trace_len, trace_nobs=gs.trace_nobs,
+                  bold_period=gs.bold_period, bold_len=gs.bold_len, bold_obs=gs.bold_obs(),
+                  real=real, nthreads=nthreads)
+        for key in ('state', 'bold', 'bold_out', 'trace'):
+            if out[key] is None:
+                continue
+            if res[key] is None:
+                res[key] = np.zeros((I, ) + out[key].shape[1:], out[key].dtype)
+            res[key][idx] = out[key]
+        for k, b in enumerate(idx):
+            res['rings'][b] = out['ring'][k]
+    return res
+
+
 def philox_u32(k0, k1, n_blocks, c1=0, c2=0, c3=0):
     lib = load()
     out = np.zeros(4 * n_blocks, np.uint32)

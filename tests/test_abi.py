@@ -45,6 +45,8 @@ def test_struct_layouts_match():
     assert lib.tvbg_abi_version() == nat.ABI_VERSION
     assert lib.tvbg_instance_size() == ctypes.sizeof(nat.tvbg_instance) == nat.INSTANCE_DTYPE.itemsize
     assert lib.tvbg_launch_size() == ctypes.sizeof(nat.tvbg_launch)
+    assert lib.tvbg_group_size() == ctypes.sizeof(nat.tvbg_group) == nat.GROUP_DTYPE.itemsize
+    assert ctypes.sizeof(nat.tvbg_lane) == 16 and nat.GROUP_LANES == 8
 
 
 @pytest.mark.parametrize('rounding', ['trunc', 'ceil', 'dsl'])
@@ -119,6 +121,64 @@ def test_pack_edges_rejects_bad_input():
     dd = np.array([0], np.int32)
     assert lib.tvbg_pack_edges(1, 1, row.ctypes.data, bad_col.ctypes.data, w.ctypes.data,
                                dd.ctypes.data, 4, out.ctypes.data) == nat.TVBG_EINVAL
+
+
+def test_pack_edges_group_addressing_is_bit_exact():
+    """Group layout: pk = (col << 16) | ((nh - d) & mask); the read of slot
+    t - d of node col at ring position (tm + lo) & mask is the reference's
+    (t - d + nh) % nh (kuramoto.c:108)."""
+    lib = nat.load()
+    rng = np.random.default_rng(5)
+    N, lognh, nnz = 300, 9, 2000
+    nh = 1 << lognh
+    row = np.concatenate([[0], np.sort(rng.integers(0, nnz + 1, N - 1)), [nnz]]).astype(np.int32)
+    col = rng.integers(0, N, nnz).astype(np.int32)
+    d = rng.integers(0, nh, nnz).astype(np.int32)
+    w = rng.random(nnz).astype(np.float32)
+    out = np.zeros(nnz, np.dtype([('pk', '<u4'), ('w', '<f4')]))
+    nat.check(lib.tvbg_pack_edges_group(N, nnz, row.ctypes.data, col.ctypes.data, w.ctypes.data,
+                                        d.ctypes.data, lognh, out.ctypes.data))
+    pk = out['pk'].astype(np.int64)
+    np.testing.assert_array_equal(pk >> 16, col)
+    np.testing.assert_array_equal(out['w'], w)
+    for t in [0, 1, 7, nh - 1, nh, 5 * nh + 3, 987654321]:
+        pos = ((t & (nh - 1)) + (pk & 0xffff)) & (nh - 1)
+        np.testing.assert_array_equal(pos, (t - d.astype(np.int64) + nh) % nh)
+
+
+def test_pack_edges_group_rejects_bad_input():
+    lib = nat.load()
+    row = np.array([0, 1], np.int32)
+    col = np.array([0], np.int32)
+    w = np.array([1.0], np.float32)
+    out = np.zeros(1, np.dtype([('pk', '<u4'), ('w', '<f4')]))
+    for d, lognh in [(8, 3), (-1, 4), (0, 2), (0, 17)]:
+        dd = np.array([d], np.int32)
+        assert lib.tvbg_pack_edges_group(1, 1, row.ctypes.data, col.ctypes.data, w.ctypes.data,
+                                         dd.ctypes.data, lognh, out.ctypes.data) == nat.TVBG_EINVAL
+        assert lib.tvbg_last_error()
+    bad_col = np.array([1], np.int32)
+    dd = np.array([0], np.int32)
+    assert lib.tvbg_pack_edges_group(1, 1, row.ctypes.data, bad_col.ctypes.data, w.ctypes.data,
+                                     dd.ctypes.data, 4, out.ctypes.data) == nat.TVBG_EINVAL
+    big = np.zeros(65538, np.int32)
+    assert lib.tvbg_pack_edges_group(65537, 0, big.ctypes.data, None, None, None, 4,
+                                     None) == nat.TVBG_EINVAL
+
+
+def test_group_plan_and_shape():
+    from tvb_hpc import groups
+    for dmin, dmax in [(3, 3), (7, 500), (25, 500), (5, 2000), (100, 100)]:
+        k, lognh = groups.plan_group(dmin, dmax)
+        nh = 1 << lognh
+        assert k in (4, 8) and k <= dmin + 1 and nh >= dmax + 1 + k
+    with pytest.raises(ValueError):
+        groups.plan_group(2, 10)
+    with pytest.raises(ValueError):
+        groups.plan_group(5, 10, block_k=8)
+    for N, (thr, cl) in [(68, (544, 1)), (84, (672, 1)), (128, (1024, 1)), (192, (768, 2)),
+                         (400, (800, 4)), (998, (1024, 8))]:
+        assert groups.group_shape(N) == (thr, cl)
 
 
 def test_plan_ring_constraints():

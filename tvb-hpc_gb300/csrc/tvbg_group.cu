@@ -1,0 +1,114 @@
+// C ABI of the lane-interleaved group kernels (tvbg_group_run and helpers).
+#include <cstring>
+
+#include "tvbg_abi_internal.h"
+
+using namespace tvbg;
+
+namespace {
+
+GroupKernel lookup_group(int model, int cfun, int k) {
+    switch (model) {
+        case TVBG_MODEL_G2DO: return group_kernel_g2do(cfun, k);
+        case TVBG_MODEL_MPR: return group_kernel_mpr(cfun, k);
+        case TVBG_MODEL_LINEAR: return group_kernel_linear(cfun, k);
+        case TVBG_MODEL_G2DOSC: return group_kernel_g2dosc(cfun, k);
+        default: return nullptr;
+    }
+}
+
+int check_group_launch(const tvbg_launch* cfg, GroupKernel* kfn, int* cluster) {
+    if (!cfg) return set_error(TVBG_EINVAL, "null launch config");
+    if (cfg->threads < 32 || cfg->threads > 1024 || (cfg->threads & 31))
+        return set_error(TVBG_EINVAL, "threads must be a multiple of 32 in [32, 1024]");
+    if (cfg->block_k != 4 && cfg->block_k != 8)
+        return set_error(TVBG_EINVAL, "tvbg_group_run: block_k must be 4 or 8");
+    const int c = cfg->cluster <= 0 ? 1 : cfg->cluster;
+    if (c != 1 && c != 2 && c != 4 && c != 8)
+        return set_error(TVBG_EINVAL, "cluster must be 1, 2, 4 or 8");
+    *kfn = lookup_group(cfg->model, cfg->cfun, cfg->block_k);
+    if (!*kfn)
+        return set_error(TVBG_EUNSUPPORTED,
+                         "group kernel not built for this model/coupling/block_k");
+    *cluster = c;
+    return TVBG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+size_t tvbg_group_size(void) { return sizeof(tvbg_group); }
+
+int tvbg_pack_edges_group(int32_t N, int32_t nnz, const int32_t* row, const int32_t* col,
+                          const float* weights, const int32_t* delays, int32_t lognh,
+                          tvbg_edge* out) {
+    if (N < 0 || nnz < 0 || !row || (nnz > 0 && (!col || !weights || !delays || !out)))
+        return set_error(TVBG_EINVAL, "tvbg_pack_edges_group: bad arguments");
+    if (lognh < 3 || lognh > 16 || N > 65536)
+        return set_error(TVBG_EINVAL, "tvbg_pack_edges_group: needs lognh in [3, 16], N <= 65536");
+    if (row[0] != 0 || row[N] != nnz)
+        return set_error(TVBG_EINVAL, "tvbg_pack_edges_group: row must run from 0 to nnz");
+    const uint32_t nh = 1u << lognh;
+    const uint32_t mask = nh - 1u;
+    for (int32_t i = 0; i < N; ++i) {
+        if (row[i + 1] < row[i]) return set_error(TVBG_EINVAL, "tvbg_pack_edges_group: row not monotone");
+        for (int32_t e = row[i]; e < row[i + 1]; ++e) {
+            const int32_t c = col[e], d = delays[e];
+            if (c < 0 || c >= N) return set_error(TVBG_EINVAL, "tvbg_pack_edges_group: col out of range");
+            if (d < 0 || static_cast<uint32_t>(d) >= nh)
+                return set_error(TVBG_EINVAL, "tvbg_pack_edges_group: delay outside [0, nh)");
+            out[e].pk = (static_cast<uint32_t>(c) << 16) | ((nh - static_cast<uint32_t>(d)) & mask);
+            out[e].w = weights[e];
+        }
+    }
+    return TVBG_OK;
+}
+
+int tvbg_group_run(const tvbg_group* d_groups, int32_t n_groups, const tvbg_launch* cfg,
+                   void* stream) {
+    GroupKernel kfn = nullptr;
+    int cluster = 1;
+    int rc = check_group_launch(cfg, &kfn, &cluster);
+    if (rc) return rc;
+    if (n_groups < 0 || (n_groups > 0 && !d_groups))
+        return set_error(TVBG_EINVAL, "tvbg_group_run: bad group array");
+    if (n_groups == 0) return TVBG_OK;
+    cudaLaunchConfig_t lc;
+    std::memset(&lc, 0, sizeof(lc));
+    lc.gridDim = dim3(static_cast<unsigned>(n_groups) * static_cast<unsigned>(cluster), 1, 1);
+    lc.blockDim = dim3(static_cast<unsigned>(cfg->threads), 1, 1);
+    lc.dynamicSmemBytes = 0;
+    lc.stream = static_cast<cudaStream_t>(stream);
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = static_cast<unsigned>(cluster);
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    lc.attrs = attr;
+    lc.numAttrs = cluster > 1 ? 1 : 0;
+    cudaError_t e = cudaLaunchKernelEx(&lc, kfn, d_groups, n_groups, cfg->d_order, cfg->d_status);
+    if (e != cudaSuccess) return set_cuda_error(e, "group kernel launch");
+    return TVBG_OK;
+}
+
+int tvbg_group_occupancy(const tvbg_launch* cfg, int32_t* ctas_per_sm, int32_t* sms) {
+    if (!ctas_per_sm || !sms) return set_error(TVBG_EINVAL, "tvbg_group_occupancy: null");
+    GroupKernel kfn = nullptr;
+    int cluster = 1;
+    int rc = check_group_launch(cfg, &kfn, &cluster);
+    if (rc) return rc;
+    int n = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &n, reinterpret_cast<const void*>(kfn), cfg->threads, 0);
+    if (e != cudaSuccess) return set_cuda_error(e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
+    int dev = 0, nsm = 0;
+    e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return set_cuda_error(e, "tvbg_group_occupancy: SM count");
+    *ctas_per_sm = n;
+    *sms = nsm;
+    return TVBG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,301 @@
+// Lane-interleaved group kernel: TVBG_GROUP_LANES (8) instances that share a
+// connectome, a delay table, the model constants and t0 run together, one
+// instance per lane of an 8-lane slice of a warp.
+//
+// Canonical step (CUDA order, the same as tvbg_step.cuh and
+// tvbg_step_blocked.cuh; tvb_hpc/network.py:115-143, coupling.py:103-116,
+// model.py:131-155, scheme.py:88-107, ring addressing of
+// dsl/dsl_cuda/CUDAmodels/kuramoto.c:92,108,128):
+//   S     = sum_e w_e pre(ring[t - d_e][col_e])          (CSR order)
+//   c     = post(S, obs0(x_i), sum_e w_e)
+//   x'    = limit(x + dt f(x, c, p) + sqrt(dt) sigma z)   z: Philox(seed_lo, inst; node, t/SPC, seed_hi)
+//   ring[t+1][i] = obs0(x')
+//
+// Layout.  Every per-node quantity is interleaved over the 8 instances of
+// the group, so a lane slice reading "node j, slot s" reads 32 contiguous
+// bytes -- one DRAM/L2 sector -- and the edge record (column, delay,
+// weight) is the same for the 8 lanes:
+//   ring   [N][R][8], R = nh + 8: slot s of node j at (j R + (s & (nh-1))) 8 + l,
+//          positions < 8 mirrored at +nh so a run of K <= 8 slots never wraps
+//   state  [N][NS][8], nparam [N][NP][8], bold [4][N][8],
+//   bold_out [bold_len][N][8], trace [trace_len][N][trace_nobs][8].
+//
+// Thread mapping.  Thread t of CTA r (cluster of C CTAs) is lane l = t % 8
+// of node slot s = t / 8; node slot s of CTA r serves the node positions
+// q = s C + r, s C + r + C P, ... (P = blockDim / 8) of the group's node
+// order (the host sorts nodes by in-degree, so the 4 slots of a warp see
+// similar edge counts, and the C CTAs of a cluster see the same work).
+//
+// Time blocking.  A value written at step t is first read at t + 1 + d_min,
+// so the K <= d_min + 1 steps of a block read only slots that exist when the
+// block starts; with nh >= d_max + 1 + K no slot written in a block aliases
+// one read in it.  Each thread therefore gathers the K coupling sums of its
+// node (one edge record and address per K steps, K independent sector loads
+// per edge), runs the K updates from registers, and the cluster meets at one
+// barrier per block.  Ring loads bypass L1 (ld.global.cg): with C > 1 the
+// values come from other SMs, ordered by the cluster barrier's
+// release/acquire.
+#pragma once
+
+#include "tvbg_step_blocked.cuh"
+
+namespace tvbg {
+
+constexpr int kLanes = TVBG_GROUP_LANES;
+
+__device__ __forceinline__ float ld_cg(const float* p) {
+    float v;
+    asm volatile("ld.global.cg.f32 %0, [%1];" : "=f"(v) : "l"(p));
+    return v;
+}
+
+__device__ __forceinline__ uint32_t cluster_nranks() {
+    uint32_t n;
+    asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(n));
+    return n;
+}
+__device__ __forceinline__ uint32_t cluster_rank() {
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+__device__ __forceinline__ uint32_t cluster_id_x() {
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%clusterid.x;" : "=r"(r));
+    return r;
+}
+
+// Block barrier of the group: the CTA, or every CTA of the cluster.
+__device__ __forceinline__ void group_barrier(bool cluster) {
+    if (cluster) {
+        asm volatile("barrier.cluster.arrive.release.aligned;\n\t"
+                     "barrier.cluster.wait.acquire.aligned;" ::: "memory");
+    } else {
+        __syncthreads();
+    }
+}
+
+// Copy a group descriptor into shared memory (word-parallel).
+__device__ __forceinline__ void stage_group(const tvbg_group* src, tvbg_group* dst) {
+    static_assert(sizeof(tvbg_group) % 4 == 0, "descriptor size");
+    const uint32_t* s = reinterpret_cast<const uint32_t*>(src);
+    uint32_t* d = reinterpret_cast<uint32_t*>(dst);
+    for (int i = threadIdx.x; i < static_cast<int>(sizeof(tvbg_group) / 4); i += blockDim.x)
+        d[i] = __ldg(s + i);
+    __syncthreads();
+}
+
+// Normal number r (0..3) of one Philox call, without dynamic indexing.
+__device__ __forceinline__ float pick4(const float z[4], int r) {
+    const float a = (r & 1) ? z[1] : z[0];
+    const float b = (r & 1) ? z[3] : z[2];
+    return (r & 2) ? b : a;
+}
+
+template <int CF>
+__device__ __forceinline__ float lane_pre(float xj, const tvbg_group& g) {
+    if constexpr (CF == TVBG_CFUN_SIGMOIDAL) {
+        return g.cf_p[0] / (1.0f + expf(g.cf_p[2] * (g.cf_p[1] - xj)));
+    } else {
+        return xj;
+    }
+}
+
+template <int CF>
+__device__ __forceinline__ float lane_post(float S, float xi, float wsum, float a, float b) {
+    if constexpr (CF == TVBG_CFUN_DIFF) {
+        return a * (S - xi * wsum) + b;
+    } else if constexpr (CF == TVBG_CFUN_SIGMOIDAL) {
+        return a * S;
+    } else {
+        return a * S + b;
+    }
+}
+
+// K coupling sums of node n for the block starting at ring position tm.
+// U = 8 / K edges per iteration keep 8 independent sector loads in flight
+// per thread within the register budget of a 1024-thread CTA.
+template <int CF, int K>
+__device__ __forceinline__ void lane_gather(const tvbg_group& g, int n, uint32_t tm, uint32_t mask,
+                                            uint32_t R, int l, float acc[K]) {
+    constexpr int U = K >= 8 ? 1 : 8 / K;
+    const float* __restrict__ ring = g.ring + l;
+    const uint2* __restrict__ edges = reinterpret_cast<const uint2*>(g.edges);
+    const int lo = __ldg(g.row + n), hi = __ldg(g.row + n + 1);
+#pragma unroll
+    for (int k = 0; k < K; ++k) acc[k] = 0.0f;
+    auto addr = [&](uint32_t pk) {
+        return ring + (static_cast<size_t>(pk >> 16) * R + ((tm + (pk & 0xffffu)) & mask)) * kLanes;
+    };
+    int e = lo;
+    for (; e + U <= hi; e += U) {
+        uint2 ed[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) ed[u] = __ldg(edges + e + u);
+        float v[U][K];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const float* p = addr(ed[u].x);
+#pragma unroll
+            for (int k = 0; k < K; ++k) v[u][k] = ld_cg(p + k * kLanes);
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const float w = __uint_as_float(ed[u].y);
+#pragma unroll
+            for (int k = 0; k < K; ++k) acc[k] = fmaf(w, lane_pre<CF>(v[u][k], g), acc[k]);
+        }
+    }
+    for (; e < hi; ++e) {
+        const uint2 e0 = __ldg(edges + e);
+        const float* p = addr(e0.x);
+        const float w = __uint_as_float(e0.y);
+#pragma unroll
+        for (int k = 0; k < K; ++k) acc[k] = fmaf(w, lane_pre<CF>(ld_cg(p + k * kLanes), g), acc[k]);
+    }
+}
+
+template <class M, int CF, int K>
+__device__ __forceinline__ void run_group(const tvbg_group& g, int32_t* status) {
+    constexpr int NS = M::NS;
+    constexpr int NP = M::NP;
+    constexpr int SPC = 4 / NS;
+    const int N = g.N;
+    const uint32_t C = cluster_nranks();
+    const uint32_t rank = cluster_rank();
+    const bool cluster = C > 1;
+    if (N <= 0 || N > 65535 || g.lognh < 3 || g.lognh > 16 || g.model != M::ID || g.cfun != CF ||
+        g.nsteps < 0 || (g.flags & (TVBG_F_TRACKA | TVBG_F_MIDSYNC | TVBG_F_TRACE_CSUM))) {
+        if (threadIdx.x == 0) report(status, TVBG_EINVAL);
+        return;  // every CTA of the cluster reads the same descriptor and leaves here
+    }
+    const int l = threadIdx.x % kLanes;
+    const int slot = threadIdx.x / kLanes;
+    const int P = blockDim.x / kLanes;
+    const int stride = static_cast<int>(C) * P;
+    const uint32_t nh = 1u << g.lognh;
+    const uint32_t mask = nh - 1u;
+    const uint32_t R = nh + kGhost;
+    const uint32_t flags = g.flags;
+    const bool noise = (flags & TVBG_F_NOISE) != 0;
+    const bool bold = (flags & TVBG_F_BOLD) != 0 && g.bold != nullptr && g.bold_out != nullptr;
+    const bool trace = (flags & TVBG_F_TRACE) != 0 && g.trace != nullptr;
+    const float dt = g.dt, sqrt_dt = g.sqrt_dt;
+    const float cf_a = g.lanes[l].cf_a;
+    const int my_steps = g.lanes[l].nsteps < g.nsteps ? g.lanes[l].nsteps : g.nsteps;
+    const uint32_t inst_id = g.lanes[l].inst_id;
+    const long long t0 = g.t0;
+    const long long t_end = t0 + my_steps;  // this lane updates while t < t_end
+    float* __restrict__ ring = g.ring;
+    float* __restrict__ state = g.state;
+    const int q0 = slot * static_cast<int>(C) + static_cast<int>(rank);
+
+    // seed: slot t0 holds obs0 of the state at t0
+    {
+        const uint32_t pos = static_cast<uint32_t>(t0) & mask;
+        for (int q = q0; q < N; q += stride) {
+            const int n = g.nodes ? __ldg(g.nodes + q) : q;
+            float x[NS];
+#pragma unroll
+            for (int v = 0; v < NS; ++v) x[v] = state[(n * NS + v) * kLanes + l];
+            const size_t idx = (static_cast<size_t>(n) * R + pos) * kLanes + l;
+            const float o = M::obs(x, 0);
+            ring[idx] = o;
+            if (pos < kGhost) ring[idx + static_cast<size_t>(nh) * kLanes] = o;
+        }
+    }
+    group_barrier(cluster);
+
+    for (long long tb = t0; tb < t0 + g.nsteps; tb += K) {
+        const int cnt = (t0 + g.nsteps - tb) < K ? static_cast<int>(t0 + g.nsteps - tb) : K;
+        const uint32_t tm = static_cast<uint32_t>(tb) & mask;
+        for (int q = q0; q < N; q += stride) {
+            const int n = g.nodes ? __ldg(g.nodes + q) : q;
+            float x[NS], p[NP];
+#pragma unroll
+            for (int v = 0; v < NS; ++v) x[v] = state[(n * NS + v) * kLanes + l];
+#pragma unroll
+            for (int v = 0; v < NP; ++v) p[v] = __ldg(g.nparam + (n * NP + v) * kLanes + l);
+            const float wsum = (CF == TVBG_CFUN_DIFF && g.wsum) ? __ldg(g.wsum + n) : 0.0f;
+            float bs = 0.0f, bF = 0.0f, bV = 0.0f, bQ = 0.0f;
+            if (bold) {
+                bs = g.bold[(0 * N + n) * kLanes + l];
+                bF = g.bold[(1 * N + n) * kLanes + l];
+                bV = g.bold[(2 * N + n) * kLanes + l];
+                bQ = g.bold[(3 * N + n) * kLanes + l];
+            }
+            float acc[K];
+            lane_gather<CF, K>(g, n, tm, mask, R, l, acc);
+            float obs0 = M::obs(x, 0);
+            float zz[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll
+            for (int k = 0; k < K; ++k) {
+                const long long t = tb + k;
+                if (k < cnt && t < t_end) {
+                    if (trace && t % g.trace_every == 0) {
+                        const long long row = (t / g.trace_every) % g.trace_len;
+                        float* dst = g.trace + ((row * N + n) * g.trace_nobs) * kLanes + l;
+                        for (int o = 0; o < g.trace_nobs; ++o) dst[o * kLanes] = M::obs(x, o);
+                    }
+                    const float xbold = bold ? M::obs(x, g.bold_obs) : 0.0f;
+                    const float c = lane_post<CF>(acc[k], obs0, wsum, cf_a, g.cf_b);
+                    float f[NS];
+                    M::drift(x, c, p, g.consts, f);
+#pragma unroll
+                    for (int v = 0; v < NS; ++v) x[v] = fmaf(dt, f[v], x[v]);
+                    if (noise) {
+                        const int r0 = static_cast<int>(t % SPC);
+                        if (k == 0 || r0 == 0) {
+                            const u32x4 w = philox4x32_10(static_cast<uint32_t>(n),
+                                                          static_cast<uint32_t>(t / SPC), g.seed_hi,
+                                                          0u, g.seed_lo, inst_id);
+                            box_muller(w.v[0], w.v[1], zz[0], zz[1]);
+                            box_muller(w.v[2], w.v[3], zz[2], zz[3]);
+                        }
+#pragma unroll
+                        for (int v = 0; v < NS; ++v)
+                            x[v] = fmaf(sqrt_dt * pick4(zz, r0 * NS + v), g.sigma[v], x[v]);
+                    }
+                    M::limit(x, flags);
+                    obs0 = M::obs(x, 0);
+                    const uint32_t pos = (static_cast<uint32_t>(t) + 1u) & mask;
+                    const size_t idx = (static_cast<size_t>(n) * R + pos) * kLanes + l;
+                    ring[idx] = obs0;
+                    if (pos < kGhost) ring[idx + static_cast<size_t>(nh) * kLanes] = obs0;
+                    if (bold) {
+                        Balloon::step(bs, bF, bV, bQ, xbold, g.dt_bold);
+                        if ((t + 1) % g.bold_period == 0) {
+                            const long long row = (t + 1) / g.bold_period - 1;
+                            if (row >= 0 && row < g.bold_len)
+                                g.bold_out[(row * N + n) * kLanes + l] = Balloon::signal(bV, bQ);
+                        }
+                    }
+                }
+            }
+#pragma unroll
+            for (int v = 0; v < NS; ++v) state[(n * NS + v) * kLanes + l] = x[v];
+            if (bold) {
+                g.bold[(0 * N + n) * kLanes + l] = bs;
+                g.bold[(1 * N + n) * kLanes + l] = bF;
+                g.bold[(2 * N + n) * kLanes + l] = bV;
+                g.bold[(3 * N + n) * kLanes + l] = bQ;
+            }
+        }
+        group_barrier(cluster);
+    }
+}
+
+// One group per CTA (or per cluster of CTAs): group index = order[cluster id].
+template <class M, int CF, int K>
+__global__ void __launch_bounds__(1024, 1)
+    group_kernel(const tvbg_group* __restrict__ groups, int32_t n_groups,
+                 const int32_t* __restrict__ order, int32_t* __restrict__ status) {
+    __shared__ __align__(16) tvbg_group s_grp;
+    const int cid = static_cast<int>(cluster_id_x());
+    if (cid >= n_groups) return;  // uniform over the cluster
+    const int idx = order ? __ldg(order + cid) : cid;
+    stage_group(groups + idx, &s_grp);
+    run_group<M, CF, K>(s_grp, status);
+}
+
+}  // namespace tvbg

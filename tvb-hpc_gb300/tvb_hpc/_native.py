@@ -101,11 +101,64 @@ class tvbg_launch(ctypes.Structure):
         ('ctas', ctypes.c_int32),
         ('block_k', ctypes.c_int32),
         ('nmax', ctypes.c_int32),
-        ('reserved0', ctypes.c_int32),
+        ('cluster', ctypes.c_int32),
         ('d_status', ctypes.c_void_p),
         ('d_counter', ctypes.c_void_p),
         ('d_order', ctypes.c_void_p),
     ]
+
+
+GROUP_LANES = 8  # instances per lane-interleaved group (TVBG_GROUP_LANES)
+
+
+class tvbg_lane(ctypes.Structure):
+    _fields_ = [('cf_a', ctypes.c_float), ('nsteps', ctypes.c_int32),
+                ('inst_id', ctypes.c_uint32), ('reserved0', ctypes.c_int32)]
+
+
+class tvbg_group(ctypes.Structure):
+    _fields_ = [
+        ('edges', ctypes.c_void_p),
+        ('row', ctypes.c_void_p),
+        ('wsum', ctypes.c_void_p),
+        ('nodes', ctypes.c_void_p),
+        ('ring', ctypes.c_void_p),
+        ('state', ctypes.c_void_p),
+        ('nparam', ctypes.c_void_p),
+        ('bold', ctypes.c_void_p),
+        ('bold_out', ctypes.c_void_p),
+        ('trace', ctypes.c_void_p),
+        ('t0', ctypes.c_int64),
+        ('nsteps', ctypes.c_int32),
+        ('N', ctypes.c_int32),
+        ('nnz', ctypes.c_int32),
+        ('lognh', ctypes.c_int32),
+        ('model', ctypes.c_int32),
+        ('cfun', ctypes.c_int32),
+        ('flags', ctypes.c_uint32),
+        ('trace_every', ctypes.c_int32),
+        ('trace_len', ctypes.c_int32),
+        ('trace_nobs', ctypes.c_int32),
+        ('bold_period', ctypes.c_int32),
+        ('bold_len', ctypes.c_int32),
+        ('bold_obs', ctypes.c_int32),
+        ('seed_lo', ctypes.c_uint32),
+        ('seed_hi', ctypes.c_uint32),
+        ('reserved0', ctypes.c_int32),
+        ('dt', ctypes.c_float),
+        ('sqrt_dt', ctypes.c_float),
+        ('dt_bold', ctypes.c_float),
+        ('cf_b', ctypes.c_float),
+        ('cf_p', ctypes.c_float * 3),
+        ('reserved1', ctypes.c_float),
+        ('sigma', ctypes.c_float * 4),
+        ('consts', ctypes.c_float * 16),
+        ('lanes', tvbg_lane * GROUP_LANES),
+    ]
+
+
+#: numpy view of tvbg_group (group tables are built in bulk)
+GROUP_DTYPE = np.dtype(tvbg_group)
 
 
 class tvbg_adjoint(ctypes.Structure):
@@ -149,6 +202,10 @@ SIGNATURES = {
     'tvbg_philox_normal': (ctypes.c_int, [_u64, _u32, _vp, _i64, _vp]),
     'tvbg_adjoint_mpr': (ctypes.c_int, [_vp, _i32, _i32, _vp]),
     'tvbg_philox_u32': (ctypes.c_int, [_u32, _u32, _u32, _u32, _u32, _vp, _i64, _vp]),
+    'tvbg_group_size': (_sz, []),
+    'tvbg_pack_edges_group': (ctypes.c_int, [_i32, _i32, _vp, _vp, _vp, _vp, _i32, _vp]),
+    'tvbg_group_run': (ctypes.c_int, [_vp, _i32, ctypes.POINTER(tvbg_launch), _vp]),
+    'tvbg_group_occupancy': (ctypes.c_int, [ctypes.c_void_p, _ip, _ip]),
 }
 
 
@@ -184,6 +241,8 @@ def load():
             lib.tvbg_instance_size(), ctypes.sizeof(tvbg_instance)))
     if lib.tvbg_launch_size() != ctypes.sizeof(tvbg_launch):
         raise RuntimeError('tvbg_launch layout mismatch')
+    if lib.tvbg_group_size() != ctypes.sizeof(tvbg_group):
+        raise RuntimeError('tvbg_group layout mismatch')
     _lib = lib
     return lib
 

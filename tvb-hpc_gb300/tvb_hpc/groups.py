@@ -1,0 +1,443 @@
+"""
+Lane-interleaved instance groups (tvbg_group_run): the sweep layout for many
+instances of one connectome.
+
+Instances that share a delay table (one conduction speed) are packed eight
+to a group, one instance per lane of an 8-lane slice; every per-node array
+of a group is interleaved over its eight instances (include/tvbg.h, "lane-
+interleaved groups"), so a delayed read of one edge is one 32-byte sector
+for the group and the edge record is read once for eight instances.  A
+group runs on one CTA, or on a cluster of 2, 4 or 8 CTAs that split its
+nodes (N > 128), with one barrier every K = 4 or 8 steps.
+
+The step is the CUDA-order step of the per-instance kernels (same Philox
+streams, same ring semantics); the coupling sums are taken in CSR order.
+This is the layout of the reference's sweeps -- one parameter point per
+GPU thread over a (coupling x speed) grid,
+dsl/dsl_cuda/example/cuda_run.py:110-142 and
+tvb_hpc/examples/hackathon.py:58-89 -- with the history interleaved by
+instance so reads coalesce, CSR edges instead of the dense N x N scan, and
+time blocking.
+"""
+
+import ctypes
+
+import numpy as np
+
+from . import _native as nat
+from .engine import DeviceStatus, _device_ok, _torch
+from .network import delays_f32
+from .utils import next_pow2
+
+L = nat.GROUP_LANES
+
+
+def plan_group(dmin, dmax, block_k=None):
+    """(K, lognh) for delays in [dmin, dmax]: K = 8 or 4 steps per barrier
+    (K <= dmin + 1), nh the smallest power of two >= dmax + 1 + K."""
+    dmin, dmax = int(dmin), int(dmax)
+    k = int(block_k) if block_k else (8 if dmin + 1 >= 8 else (4 if dmin + 1 >= 4 else 0))
+    if k not in (4, 8) or k > dmin + 1:
+        raise ValueError('group kernel needs K in (4, 8) and K <= d_min + 1 (d_min = %d)' % dmin)
+    nh = max(8, next_pow2(dmax + 1 + k))
+    return k, int(np.log2(nh))
+
+
+def group_shape(N, threads=None, cluster=None):
+    """(threads, cluster) of a group launch: by default one node per thread,
+    clusters of 2/4/8 CTAs for N > 128."""
+    if cluster is None:
+        cluster = 1
+        while L * -(-N // cluster) > 1024 and cluster < 8:
+            cluster *= 2
+    if threads is None:
+        per = -(-N // cluster)
+        threads = min(1024, 32 * -(-(L * per) // 32))
+    return int(threads), int(cluster)
+
+
+def group_occupancy(cfg):
+    lib = nat.load()
+    per, sms = ctypes.c_int32(0), ctypes.c_int32(0)
+    nat.check(lib.tvbg_group_occupancy(ctypes.byref(cfg), ctypes.byref(per), ctypes.byref(sms)))
+    return int(per.value), int(sms.value)
+
+
+class GroupSet:
+    """
+    Device-resident instances of one connectome in lane-interleaved groups.
+
+    Same parameters as engine.InstanceSet (model, cfun, scheme, conn, dt,
+    couplings, speeds, state0, nparam, delays, rounding, seed, inst_ids,
+    bold_period, bold_len, trace_every, trace_len, trace_nobs, flags, cf_b,
+    t0); further:
+      nsteps  : optional (I,) step counts, used to put instances of similar
+                length into the same group (longest first);
+      block_k : 4 or 8 steps per barrier (default: 8 when d_min >= 7);
+      threads, cluster : launch shape (default: group_shape).
+    Couplings must be separable (Linear, Diff, Sigmoidal); the Kuramoto
+    model and the Track-A order run on the per-instance kernels.
+
+    A lane that takes fewer steps than its group is finished after its run;
+    the group's clock advances by the longest lane.
+    """
+
+    def __init__(self, model, cfun, scheme, conn, dt, couplings, speeds=None, state0=None,
+                 nparam=None, delays=None, rounding='ceil', seed=0, inst_ids=None,
+                 bold_period=0, bold_len=0, trace_every=0, trace_len=0, trace_nobs=None,
+                 flags=0, cf_b=None, t0=0, nsteps=None, block_k=None, threads=None,
+                 cluster=None, history='zero'):
+        _device_ok()
+        torch = _torch()
+        self.torch = torch
+        lib = nat.load()
+        self.model, self.cfun, self.scheme = model, cfun, scheme
+        self.model_id, self.consts, self.sigma = model.engine_spec()
+        self.cfun_id, cf_a0, cf_b0, self.cf_p = cfun.engine_spec()
+        if self.cfun_id not in (nat.CFUN_LINEAR, nat.CFUN_DIFF, nat.CFUN_SIGMOIDAL):
+            raise ValueError('group kernel needs a separable coupling (Linear, Diff, Sigmoidal)')
+        if self.model_id == nat.MODEL_KURAMOTO:
+            raise ValueError('Kuramoto runs on the per-instance kernels')
+        self.N = N = int(conn.nnode)
+        if N > 65535:
+            raise ValueError('group kernel: N < 65536')
+        self.ns = model.nsvar
+        self.nobs = model.nobs
+        self.npar = len(model.param_sym)
+        couplings = np.atleast_1d(np.asarray(couplings, np.float32))
+        I = self.n = couplings.size
+        self.dt = float(dt)
+        row = np.asarray(conn.row, np.int64).astype(np.int32)
+        col = np.asarray(conn.col, np.int64).astype(np.int32)
+        w = np.asarray(conn.wnz, np.float32)
+        self.nnz = int(col.size)
+        self.row_np, self.col_np, self.w_np = row, col, w
+        # delay tables, one per distinct speed
+        if delays is not None:
+            tables = [np.asarray(delays, np.int64).astype(np.int32)]
+            tab_of = np.zeros(I, np.int64)
+        else:
+            sp = np.broadcast_to(np.asarray(speeds, np.float32), (I, )).copy()
+            uniq, tab_of = np.unique(sp, return_inverse=True)
+            tables = [delays_f32(conn.lnz, s, dt, rounding) for s in uniq]
+        self.delay_tables = tables
+        plans = [plan_group(d.min() if d.size else 7, d.max() if d.size else 0, block_k)
+                 for d in tables]
+        # per-node constants shared by every table: in-edge weight sums
+        # (float32, CSR order) and the visiting order (in-degree, descending)
+        wsum = np.zeros(N, np.float32)
+        for i in range(N):
+            s = np.float32(0.0)
+            for x in w[row[i]:row[i + 1]]:
+                s = np.float32(s + x)
+            wsum[i] = s
+        deg = np.diff(row)
+        nodes = np.argsort(-deg, kind='stable').astype(np.int32)
+        self.row = torch.from_numpy(row).cuda()
+        self.wsum = torch.from_numpy(wsum).cuda()
+        self.nodes = torch.from_numpy(nodes).cuda()
+        eb = []
+        for d, (k, lognh) in zip(tables, plans):
+            out = np.zeros(max(1, col.size), dtype=np.dtype([('pk', '<u4'), ('w', '<f4')]))
+            if col.size:
+                nat.check(lib.tvbg_pack_edges_group(N, col.size, row.ctypes.data, col.ctypes.data,
+                                                    w.ctypes.data, np.ascontiguousarray(d).ctypes.data,
+                                                    lognh, out.ctypes.data))
+            eb.append(out)
+        self.edges = torch.from_numpy(np.concatenate(eb).view(np.uint8).copy()).cuda()
+        self.edge_stride = max(1, col.size)
+        # groups: per table, instances longest-first, eight per group
+        order_key = (np.zeros(I) if nsteps is None
+                     else -np.broadcast_to(np.asarray(nsteps, np.int64), (I, )).astype(np.float64))
+        members, gtab = [], []
+        for t in range(len(tables)):
+            idx = np.nonzero(tab_of == t)[0]
+            idx = idx[np.argsort(order_key[idx], kind='stable')]
+            for g0 in range(0, idx.size, L):
+                members.append(idx[g0:g0 + L])
+                gtab.append(t)
+        G = self.n_groups = len(members)
+        self.members = members
+        self.gtab = np.array(gtab, np.int64)
+        self.grp_of = np.zeros(I, np.int64)
+        self.lane_of = np.zeros(I, np.int64)
+        for g, m in enumerate(members):
+            self.grp_of[m] = g
+            self.lane_of[m] = np.arange(m.size)
+        self.block_k = np.array([plans[t][0] for t in self.gtab], np.int32)
+        self.lognh = np.array([plans[t][1] for t in self.gtab], np.int32)
+        R = (1 << self.lognh.astype(np.int64)) + 8
+        ring_len = N * R * L
+        self.ring_off = np.concatenate([[0], np.cumsum(ring_len)[:-1]]).astype(np.int64)
+        self.ring = torch.zeros(int(ring_len.sum()), dtype=torch.float32, device='cuda')
+        self.R = R
+        self._gi = torch.from_numpy(self.grp_of).cuda()
+        self._li = torch.from_numpy(self.lane_of).cuda()
+        # state / parameters [G, N, ns, L]
+        self.gstate = torch.zeros((G, N, self.ns, L), dtype=torch.float32, device='cuda')
+        if state0 is not None:
+            st = np.broadcast_to(np.asarray(state0, np.float32), (I, N, self.ns))
+            self.set_state(torch.from_numpy(np.ascontiguousarray(st)).cuda())
+        if nparam is None:
+            npm = np.broadcast_to(model.node_params(N), (I, N, self.npar))
+        else:
+            npm = np.asarray(nparam, np.float32)
+            if npm.ndim == 1:
+                npm = npm.reshape(N, 1)
+            if npm.ndim == 2 and npm.shape == (I, N) and self.npar == 1 and I != N:
+                npm = npm[:, :, None]
+            npm = np.broadcast_to(npm, (I, N, self.npar))
+        self.gnparam = torch.zeros((G, N, self.npar, L), dtype=torch.float32, device='cuda')
+        self.gnparam[self._gi, :, :, self._li] = torch.from_numpy(
+            np.ascontiguousarray(npm, np.float32)).cuda()
+        if history == 'fill':
+            self.fill_history()
+        elif history != 'zero':
+            raise ValueError("history must be 'zero' or 'fill'")
+        # monitors
+        fl = int(flags)
+        self.bold_period, self.bold_len = int(bold_period), int(bold_len)
+        self.gbold = self.gbold_out = None
+        if self.bold_period > 0:
+            self.gbold = torch.zeros((G, 4, N, L), dtype=torch.float32, device='cuda')
+            self.gbold_out = torch.full((G, max(1, self.bold_len), N, L), float('nan'),
+                                        dtype=torch.float32, device='cuda')
+            fl |= nat.F_BOLD
+        self.trace_every, self.trace_len = int(trace_every), int(trace_len)
+        self.trace_nobs = int(trace_nobs if trace_nobs is not None else self.nobs)
+        self.gtrace = None
+        if self.trace_every > 0:
+            self.gtrace = torch.zeros((G, max(1, self.trace_len), N, self.trace_nobs, L),
+                                      dtype=torch.float32, device='cuda')
+            fl |= nat.F_TRACE
+        if getattr(scheme, 'noise', False):
+            fl |= nat.F_NOISE
+        self.flags = fl
+        self.seed = int(seed) & ((1 << 64) - 1)
+        self.inst_ids = (np.arange(I, dtype=np.uint32) if inst_ids is None
+                         else np.asarray(inst_ids, np.uint32))
+        self.cf_a = couplings
+        self.cf_b = np.float32(cf_b if cf_b is not None else
+                               (cf_b0 if isinstance(cf_b0, (int, float, np.number)) else 0.0))
+        self.t = np.full(G, int(t0), np.int64)
+        self.threads, self.cluster = group_shape(N, threads, cluster)
+        self.status = DeviceStatus()
+        self._uploaded = None
+
+    def bold_obs(self):
+        "Observable feeding the balloon: V for G2DO (tvb_hpc order W, V), else obs 0."
+        return 1 if self.model_id == nat.MODEL_G2DO else 0
+
+    # -- per-instance views ------------------------------------------------------
+    @property
+    def state(self):
+        "(I, N, nsvar) copy of the states."
+        return self.gstate[self._gi, :, :, self._li]
+
+    def set_state(self, x):
+        self.gstate[self._gi, :, :, self._li] = x.to(self.gstate.dtype)
+
+    @property
+    def bold_out(self):
+        "(I, bold_len, N) BOLD samples."
+        return None if self.gbold_out is None else self.gbold_out[self._gi, :, :, self._li]
+
+    @property
+    def trace(self):
+        "(I, trace_len, N, trace_nobs) observable trace."
+        return None if self.gtrace is None else self.gtrace[self._gi, :, :, :, self._li]
+
+    def reset(self, state=None):
+        "Zero rings and monitors; optionally set the state; clocks back to 0."
+        self.ring.zero_()
+        if self.gbold is not None:
+            self.gbold.zero_()
+        if state is not None:
+            self.set_state(state)
+        self.t[:] = 0
+
+    def fill_history(self):
+        "Every ring slot of every lane holds obs0 of the current state."
+        N = self.N
+        o0 = self.gstate[:, :, 0, :]                                  # [G, N, L]
+        for g in range(self.n_groups):
+            R = int(self.R[g])
+            o = int(self.ring_off[g])
+            self.ring[o:o + N * R * L].view(N, R, L).copy_(o0[g][:, None, :].expand(N, R, L))
+
+    def ring_plain(self, b):
+        "Ring of instance b as numpy [nh, N] slot-major (the oracle's layout)."
+        g, l = int(self.grp_of[b]), int(self.lane_of[b])
+        R = int(self.R[g])
+        nh = 1 << int(self.lognh[g])
+        o = int(self.ring_off[g])
+        r = self.ring[o:o + self.N * R * L].view(self.N, R, L)[:, :nh, l]
+        return r.t().contiguous().cpu().numpy()
+
+    # -- launches -------------------------------------------------------------------
+    def build_table(self, nsteps):
+        "Numpy tvbg_group table for the next nsteps (scalar or (I,))."
+        G, N = self.n_groups, self.N
+        steps = np.broadcast_to(np.asarray(nsteps, np.int64), (self.n, )).astype(np.int64)
+        tab = np.zeros(G, dtype=nat.GROUP_DTYPE)
+        gi = np.arange(G, dtype=np.int64)
+        tab['edges'] = self.edges.data_ptr() + 8 * self.edge_stride * self.gtab
+        tab['row'] = self.row.data_ptr()
+        tab['wsum'] = self.wsum.data_ptr()
+        tab['nodes'] = self.nodes.data_ptr()
+        tab['ring'] = self.ring.data_ptr() + 4 * self.ring_off
+        tab['state'] = self.gstate.data_ptr() + 4 * gi * N * self.ns * L
+        tab['nparam'] = self.gnparam.data_ptr() + 4 * gi * N * self.npar * L
+        if self.gbold is not None:
+            tab['bold'] = self.gbold.data_ptr() + 4 * gi * 4 * N * L
+            tab['bold_out'] = self.gbold_out.data_ptr() + 4 * gi * self.gbold_out.shape[1] * N * L
+        if self.gtrace is not None:
+            tab['trace'] = (self.gtrace.data_ptr()
+                            + 4 * gi * self.gtrace.shape[1] * N * self.trace_nobs * L)
+        tab['t0'] = self.t
+        tab['N'] = N
+        tab['nnz'] = self.nnz
+        tab['lognh'] = self.lognh
+        tab['model'] = self.model_id
+        tab['cfun'] = self.cfun_id
+        tab['flags'] = self.flags
+        tab['trace_every'] = max(1, self.trace_every)
+        tab['trace_len'] = max(1, self.trace_len)
+        tab['trace_nobs'] = self.trace_nobs
+        tab['bold_period'] = max(1, self.bold_period)
+        tab['bold_len'] = self.bold_len
+        tab['bold_obs'] = self.bold_obs()
+        tab['seed_lo'] = self.seed & 0xffffffff
+        tab['seed_hi'] = (self.seed >> 32) & 0xffffffff
+        tab['dt'] = np.float32(self.dt)
+        tab['sqrt_dt'] = np.sqrt(np.float32(self.dt)).astype(np.float32)
+        tab['dt_bold'] = np.float32(self.dt / 1000.0)
+        tab['cf_b'] = self.cf_b
+        tab['cf_p'] = np.asarray(self.cf_p, np.float32)
+        tab['sigma'] = self.sigma
+        tab['consts'] = self.consts
+        gmax = np.zeros(G, np.int64)
+        for g, m in enumerate(self.members):
+            ln = tab['lanes'][g]
+            ln['cf_a'][:m.size] = self.cf_a[m]
+            ln['nsteps'][:m.size] = steps[m]
+            ln['inst_id'][:m.size] = self.inst_ids[m]
+            tab['lanes'][g] = ln
+            gmax[g] = steps[m].max()
+        tab['nsteps'] = gmax
+        return tab, gmax
+
+    def launch_cfg(self, block_k, order=None):
+        cfg = nat.tvbg_launch()
+        cfg.model, cfg.cfun = self.model_id, self.cfun_id
+        cfg.threads, cfg.cluster = self.threads, self.cluster
+        cfg.block_k = int(block_k)
+        cfg.d_status = self.status.t.data_ptr()
+        cfg.d_order = order.data_ptr() if order is not None else None
+        return cfg
+
+    def prepare(self, nsteps):
+        """Upload the group tables for the next nsteps: one launch per block
+        length, groups in longest-first order.  Returns the launch list."""
+        torch = self.torch
+        tab, gmax = self.build_table(nsteps)
+        dev = torch.from_numpy(tab.view(np.uint8).copy()).cuda()
+        launches = []
+        for k in sorted(set(self.block_k.tolist())):
+            idx = np.nonzero(self.block_k == k)[0]
+            idx = idx[np.argsort(-gmax[idx], kind='stable')].astype(np.int32)
+            order = torch.from_numpy(idx).cuda()
+            launches.append((dev, order, int(idx.size), self.launch_cfg(k, order)))
+        self._uploaded = (launches, gmax)
+        return launches, gmax
+
+    def launch(self, launches=None, stream=None):
+        lib = nat.load()
+        launches = launches if launches is not None else self._uploaded[0]
+        sh = nat.stream_handle(stream)
+        for dev, order, n, cfg in launches:
+            nat.check(lib.tvbg_group_run(dev.data_ptr(), n, ctypes.byref(cfg), sh))
+
+    def advance(self, gmax):
+        "Move the group clocks after a launch of the prepared tables."
+        self.t += gmax
+
+    def run(self, nsteps, stream=None, check=True):
+        "Advance every instance by nsteps (scalar or per instance)."
+        launches, gmax = self.prepare(nsteps)
+        self.launch(launches, stream)
+        self.advance(gmax)
+        if check:
+            self.torch.cuda.synchronize()
+            self.status.check()
+
+    @property
+    def node_steps_per_step(self):
+        return float(self.n * self.N)
+
+
+class GroupBatch:
+    """
+    Several GroupSets (different connectomes, N and step counts) in one
+    launch set: every set's launches go on their own forked stream and the
+    whole batch can be captured into one CUDA graph.
+    """
+
+    def __init__(self, sets, nsteps):
+        torch = _torch()
+        self.torch = torch
+        self.sets = list(sets)
+        self.nsteps = [np.broadcast_to(np.asarray(n, np.int64), (s.n, )).astype(np.int64)
+                       for s, n in zip(self.sets, nsteps)]
+        self.status = DeviceStatus()
+        self.plans = []
+        for s, n in zip(self.sets, self.nsteps):
+            launches, gmax = s.prepare(n)
+            for _, _, _, cfg in launches:
+                cfg.d_status = self.status.t.data_ptr()
+            self.plans.append((s, launches, gmax))
+        # longest sets first (their streams are forked first)
+        self.plans.sort(key=lambda p: -float(p[2].max(initial=0)) * p[0].N)
+        self.streams = [torch.cuda.Stream() for _ in self.plans]
+        self.graph = None
+
+    @property
+    def node_steps(self):
+        return float(sum((s.N * n).sum() for s, n in zip(self.sets, self.nsteps)))
+
+    @property
+    def n_launches(self):
+        return sum(len(p[1]) for p in self.plans)
+
+    def launch(self, stream=None):
+        torch = self.torch
+        main = stream or torch.cuda.current_stream()
+        for (s, launches, _), st in zip(self.plans, self.streams):
+            st.wait_stream(main)
+            with torch.cuda.stream(st):
+                s.launch(launches, st)
+        for st in self.streams:
+            main.wait_stream(st)
+
+    def capture(self):
+        torch = self.torch
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        cap = torch.cuda.Stream()
+        with torch.cuda.stream(cap):
+            with torch.cuda.graph(g, stream=cap):
+                self.launch(cap)
+        self.graph = g
+        return g
+
+    def replay(self):
+        self.graph.replay()
+
+    def run(self, check=True):
+        if self.graph is not None:
+            self.replay()
+        else:
+            self.launch()
+        if check:
+            self.torch.cuda.synchronize()
+            self.status.check()
