@@ -143,8 +143,7 @@ def workload_config(wl):
                 'instances': [int(p['couplings'].size) for p in wl['parts']],
                 'time_steps': 'uniform 5k-50k per instance', 'dt_ms': wl['dt'],
                 'noise': 'philox-em', 'max_delay_steps': 500,
-                'l2': 'inputs larger than L2 (rings+state)', 'parallelism': 'replicas',
-                'path': 'persistent batch, one CUDA graph'}
+                'l2': 'inputs larger than L2 (rings+state)', 'parallelism': 'replicas'}
     c = wl['conn']
     return {'workload': wl['name'], 'model': wl['model'], 'coupling': wl['cfun'],
             'nodes': int(c.nnode), 'edges': int(c.nnz), 'instances': int(wl['couplings'].size),
@@ -240,29 +239,40 @@ def build_sweep(wl, tpn=None, warps=None):
 
 class MixedStep:
     """One bench step of the uneven batch: reset every instance from resident
-    copies and run the whole batch as one CUDA-graph launch (persistent
-    kernels on forked streams).  `run_plain` runs the same work as one
+    copies and run the whole batch as one CUDA-graph launch.  The batch runs
+    either as lane-interleaved groups (tvbg_group_run: eight instances per
+    lane slice, clusters for large N; default) or as per-instance persistent
+    kernels (tvbg_batch_run).  `run_plain` runs the same work as one
     tvbg_sweep per connectome, sequentially (the plain path)."""
 
-    def __init__(self, wl, torch):
-        from tvb_hpc import model, coupling, scheme, engine
+    def __init__(self, wl, torch, path='groups', graph=True):
+        from tvb_hpc import model, coupling, scheme, engine, groups
         self.torch = torch
         self.wl = wl
+        self.path = path
         m = getattr(model, wl['model'])()
         cf = getattr(coupling, wl['cfun'])(m)
         scm = scheme.EulerMaryuyamaStep(wl['dt'])
         self.sets = []
         for p in wl['parts']:
-            self.sets.append(engine.InstanceSet(
-                m, cf, scm, p['conn'], dt=wl['dt'], couplings=p['couplings'], speeds=p['speeds'],
-                state0=p['x0'], nparam=p['nparam'], seed=p['seed']))
+            kw = dict(dt=wl['dt'], couplings=p['couplings'], speeds=p['speeds'], state0=p['x0'],
+                      nparam=p['nparam'], seed=p['seed'])
+            if path == 'groups':
+                self.sets.append(groups.GroupSet(m, cf, scm, p['conn'], nsteps=p['steps'], **kw))
+            else:
+                self.sets.append(engine.InstanceSet(m, cf, scm, p['conn'], **kw))
         self.x0 = [s.state.clone() for s in self.sets]
-        self.batch = engine.Batch(self.sets, [p['steps'] for p in wl['parts']])
-        self.batch.capture()
-        self.sw = self.sets[0]
-        self.sw.tpn = self.batch.launches[0]['cfg'].tpn
+        steps = [p['steps'] for p in wl['parts']]
+        if path == 'groups':
+            self.batch = groups.GroupBatch(self.sets, steps)
+            self.n_launch = self.batch.n_launches
+        else:
+            self.batch = engine.Batch(self.sets, steps)
+            self.n_launch = len(self.batch.launches)
+        if graph:
+            self.batch.capture()
+        self.ns = m.nsvar
         self.status = self.batch.status
-        self.n_launch = len(self.batch.launches)
         # plain path: per connectome, the per-step kernel (no time blocking),
         # one sweep launched in chunks of PLAIN_CHUNK steps (as the
         # reference's launcher chunks, dsl/dsl_cuda/example/cuda_run.py:124-142),
@@ -282,21 +292,25 @@ class MixedStep:
 
     def reset(self, x0=None):
         for s, x in zip(self.sets, self.x0 if x0 is None else x0):
-            s.state.copy_(x)
+            if self.path == 'groups':
+                s.set_state(x)
+            else:
+                s.state.copy_(x)
             s.ring.zero_()
 
     def run(self, time_kernels=False):
         evs = []
         torch = self.torch
+        go = self.batch.replay if self.batch.graph is not None else self.batch.launch
         if time_kernels:
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record()
-            self.batch.replay()
+            go()
             e1.record()
             evs.append((e0, e1))
         else:
-            self.batch.replay()
+            go()
         return evs, None
 
     def run_plain(self):
@@ -439,7 +453,7 @@ def gpu_arm(args):
     from tvb_hpc import _native
     _native.load()
     wl = WORKLOADS[args.workload]()
-    gs = (MixedStep(wl, torch) if wl['name'] == 'mixed'
+    gs = (MixedStep(wl, torch, args.mixed_path, not args.no_graph) if wl['name'] == 'mixed'
           else GpuStep(wl, torch, args.tpn, args.warps))
 
     def barrier():
@@ -571,9 +585,13 @@ def finish_mixed(args, wl, gs, world, rank, value, ms_per_step, clk, kern_ms, n_
             'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': round(ms_per_step, 3),
             'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32',
             'data': 'synthetic (seeded connectomes, config recipe)',
-            'config': workload_config(wl), 'e2e': e2e,
+            'config': dict(workload_config(wl), path=(
+                'lane-interleaved groups (8 instances per lane slice, CTA clusters for N > 128), '
+                if gs.path == 'groups' else 'per-instance persistent kernels, ')
+                + ('one CUDA graph' if gs.batch.graph is not None else 'direct launches')),
+            'e2e': e2e,
             'gpu_launches': gs.launches_per_step() * args.steps,
-            'roofline': roofline_entry(wl, gs.sw.ns, kern_ms, args.steps),
+            'roofline': roofline_entry(wl, gs.ns, kern_ms, args.steps),
             'clocks': clk, 'plain': plain,
             'batched_vs_plain': round(value / plain['value'], 3) if plain else None}
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -703,6 +721,10 @@ def main():
     ap.add_argument('--ref-seconds', type=float, default=8.0)
     ap.add_argument('--tpn', type=int, default=None, help='fix the gather width (skip autotune)')
     ap.add_argument('--warps', type=int, default=None, help='fix the CTA width of the blocked kernel')
+    ap.add_argument('--mixed-path', default='groups', choices=['groups', 'instances'],
+                    help='uneven batch as lane-interleaved groups or per-instance kernels')
+    ap.add_argument('--no-graph', action='store_true',
+                    help='launch the batch directly instead of replaying a CUDA graph')
     args = ap.parse_args()
     if args.impl == 'reference':
         reference_arm(args)

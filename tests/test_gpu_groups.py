@@ -61,8 +61,9 @@ def check(gs, x0, nsteps):
     return ref
 
 
-def test_groups_g2dosc_diff_noise(cuda):
-    gs, x0 = make()
+@pytest.mark.parametrize('depth', [2, 4])
+def test_groups_g2dosc_diff_noise(cuda, depth):
+    gs, x0 = make(gkw=dict(depth=depth))
     assert set(gs.block_k) == {4, 8}          # speed 20: d_min = 5 -> K = 4
     assert gs.n_groups == 4                    # 10 + 10 instances -> 8 + 2 per speed
     assert gs.cluster == 1
@@ -95,11 +96,12 @@ def test_groups_ragged_steps(cuda):
     assert rel_err(gs.state.cpu().numpy(), ref['state']) < TOL
 
 
-@pytest.mark.parametrize('N,threads,cluster', [(300, None, None), (300, 1024, 2),
-                                               (998, None, None), (84, 128, 1), (84, 96, 2)])
-def test_groups_clusters_and_multinode_threads(cuda, N, threads, cluster):
+@pytest.mark.parametrize('N,threads,cluster,depth', [(300, None, None, 2), (300, 1024, 2, 4),
+                                                     (998, None, None, 4), (84, 128, 1, 2),
+                                                     (84, 96, 2, 4)])
+def test_groups_clusters_and_multinode_threads(cuda, N, threads, cluster, depth):
     gs, x0 = make('MPR', 'Linear', I=9, N=N, density=0.05 if N > 500 else 0.15, speeds=(4.0, ),
-                  gkw=dict(threads=threads, cluster=cluster))
+                  gkw=dict(threads=threads, cluster=cluster, depth=depth))
     if cluster:
         assert gs.cluster == cluster
     check(gs, x0, 200)

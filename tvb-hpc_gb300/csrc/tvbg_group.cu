@@ -7,14 +7,19 @@ using namespace tvbg;
 
 namespace {
 
-GroupKernel lookup_group(int model, int cfun, int k) {
+GroupKernel lookup_group(int model, int cfun, int k, int depth) {
     switch (model) {
-        case TVBG_MODEL_G2DO: return group_kernel_g2do(cfun, k);
-        case TVBG_MODEL_MPR: return group_kernel_mpr(cfun, k);
-        case TVBG_MODEL_LINEAR: return group_kernel_linear(cfun, k);
-        case TVBG_MODEL_G2DOSC: return group_kernel_g2dosc(cfun, k);
+        case TVBG_MODEL_G2DO: return group_kernel_g2do(cfun, k, depth);
+        case TVBG_MODEL_MPR: return group_kernel_mpr(cfun, k, depth);
+        case TVBG_MODEL_LINEAR: return group_kernel_linear(cfun, k, depth);
+        case TVBG_MODEL_G2DOSC: return group_kernel_g2dosc(cfun, k, depth);
         default: return nullptr;
     }
+}
+
+// Dynamic shared memory of a group launch: the K coupling sums of every thread.
+size_t group_smem_bytes(const tvbg_launch* cfg) {
+    return 4u * static_cast<size_t>(cfg->block_k) * static_cast<size_t>(cfg->threads);
 }
 
 int check_group_launch(const tvbg_launch* cfg, GroupKernel* kfn, int* cluster) {
@@ -26,10 +31,13 @@ int check_group_launch(const tvbg_launch* cfg, GroupKernel* kfn, int* cluster) {
     const int c = cfg->cluster <= 0 ? 1 : cfg->cluster;
     if (c != 1 && c != 2 && c != 4 && c != 8)
         return set_error(TVBG_EINVAL, "cluster must be 1, 2, 4 or 8");
-    *kfn = lookup_group(cfg->model, cfg->cfun, cfg->block_k);
+    const int depth = cfg->tpn <= 0 ? 4 : cfg->tpn;
+    if (depth != 2 && depth != 4)
+        return set_error(TVBG_EINVAL, "tvbg_group_run: tpn (gather depth) must be 0, 2 or 4");
+    *kfn = lookup_group(cfg->model, cfg->cfun, cfg->block_k, depth);
     if (!*kfn)
         return set_error(TVBG_EUNSUPPORTED,
-                         "group kernel not built for this model/coupling/block_k");
+                         "group kernel not built for this model/coupling/block_k/depth");
     *cluster = c;
     return TVBG_OK;
 }
@@ -78,7 +86,7 @@ int tvbg_group_run(const tvbg_group* d_groups, int32_t n_groups, const tvbg_laun
     std::memset(&lc, 0, sizeof(lc));
     lc.gridDim = dim3(static_cast<unsigned>(n_groups) * static_cast<unsigned>(cluster), 1, 1);
     lc.blockDim = dim3(static_cast<unsigned>(cfg->threads), 1, 1);
-    lc.dynamicSmemBytes = 0;
+    lc.dynamicSmemBytes = group_smem_bytes(cfg);
     lc.stream = static_cast<cudaStream_t>(stream);
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -100,7 +108,7 @@ int tvbg_group_occupancy(const tvbg_launch* cfg, int32_t* ctas_per_sm, int32_t* 
     if (rc) return rc;
     int n = 0;
     cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-        &n, reinterpret_cast<const void*>(kfn), cfg->threads, 0);
+        &n, reinterpret_cast<const void*>(kfn), cfg->threads, group_smem_bytes(cfg));
     if (e != cudaSuccess) return set_cuda_error(e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
     int dev = 0, nsm = 0;
     e = cudaGetDevice(&dev);

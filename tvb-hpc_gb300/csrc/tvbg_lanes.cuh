@@ -113,12 +113,13 @@ __device__ __forceinline__ float lane_post(float S, float xi, float wsum, float 
 }
 
 // K coupling sums of node n for the block starting at ring position tm.
-// U = 8 / K edges per iteration keep 8 independent sector loads in flight
-// per thread within the register budget of a 1024-thread CTA.
-template <int CF, int K>
+// U = D / K edges per iteration: D independent sector loads in flight per
+// thread (the gather is bound by memory latency, not issue).  The sums are
+// accumulated in CSR order.
+template <int CF, int K, int D>
 __device__ __forceinline__ void lane_gather(const tvbg_group& g, int n, uint32_t tm, uint32_t mask,
                                             uint32_t R, int l, float acc[K]) {
-    constexpr int U = K >= 8 ? 1 : 8 / K;
+    constexpr int U = D / K;
     const float* __restrict__ ring = g.ring + l;
     const uint2* __restrict__ edges = reinterpret_cast<const uint2*>(g.edges);
     const int lo = __ldg(g.row + n), hi = __ldg(g.row + n + 1);
@@ -129,34 +130,49 @@ __device__ __forceinline__ void lane_gather(const tvbg_group& g, int n, uint32_t
     };
     int e = lo;
     for (; e + U <= hi; e += U) {
-        uint2 ed[U];
-#pragma unroll
-        for (int u = 0; u < U; ++u) ed[u] = __ldg(edges + e + u);
         float v[U][K];
+        float w[U];
 #pragma unroll
         for (int u = 0; u < U; ++u) {
-            const float* p = addr(ed[u].x);
+            const uint2 ed = __ldg(edges + e + u);
+            const float* p = addr(ed.x);
+            w[u] = __uint_as_float(ed.y);
 #pragma unroll
             for (int k = 0; k < K; ++k) v[u][k] = ld_cg(p + k * kLanes);
         }
 #pragma unroll
         for (int u = 0; u < U; ++u) {
-            const float w = __uint_as_float(ed[u].y);
 #pragma unroll
-            for (int k = 0; k < K; ++k) acc[k] = fmaf(w, lane_pre<CF>(v[u][k], g), acc[k]);
+            for (int k = 0; k < K; ++k) acc[k] = fmaf(w[u], lane_pre<CF>(v[u][k], g), acc[k]);
         }
     }
-    for (; e < hi; ++e) {
-        const uint2 e0 = __ldg(edges + e);
-        const float* p = addr(e0.x);
-        const float w = __uint_as_float(e0.y);
+    // remainder: fewer than U edges, loads still issued together
+    const int rem = hi - e;
+    if (rem > 0) {
+        float v[U][K];
+        float w[U];
 #pragma unroll
-        for (int k = 0; k < K; ++k) acc[k] = fmaf(w, lane_pre<CF>(ld_cg(p + k * kLanes), g), acc[k]);
+        for (int u = 0; u < U; ++u) {
+            if (u < rem) {
+                const uint2 ed = __ldg(edges + e + u);
+                const float* p = addr(ed.x);
+                w[u] = __uint_as_float(ed.y);
+#pragma unroll
+                for (int k = 0; k < K; ++k) v[u][k] = ld_cg(p + k * kLanes);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            if (u < rem) {
+#pragma unroll
+                for (int k = 0; k < K; ++k) acc[k] = fmaf(w[u], lane_pre<CF>(v[u][k], g), acc[k]);
+            }
+        }
     }
 }
 
-template <class M, int CF, int K>
-__device__ __forceinline__ void run_group(const tvbg_group& g, int32_t* status) {
+template <class M, int CF, int K, int D>
+__device__ __forceinline__ void run_group(const tvbg_group& g, float* csum, int32_t* status) {
     constexpr int NS = M::NS;
     constexpr int NP = M::NP;
     constexpr int SPC = 4 / NS;
@@ -224,51 +240,55 @@ __device__ __forceinline__ void run_group(const tvbg_group& g, int32_t* status) 
                 bV = g.bold[(2 * N + n) * kLanes + l];
                 bQ = g.bold[(3 * N + n) * kLanes + l];
             }
-            float acc[K];
-            lane_gather<CF, K>(g, n, tm, mask, R, l, acc);
+            {
+                float acc[K];
+                lane_gather<CF, K, D>(g, n, tm, mask, R, l, acc);
+#pragma unroll
+                for (int k = 0; k < K; ++k) csum[k * blockDim.x + threadIdx.x] = acc[k];
+            }
             float obs0 = M::obs(x, 0);
             float zz[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-#pragma unroll
-            for (int k = 0; k < K; ++k) {
+#pragma unroll 1
+            for (int k = 0; k < cnt; ++k) {
                 const long long t = tb + k;
-                if (k < cnt && t < t_end) {
-                    if (trace && t % g.trace_every == 0) {
-                        const long long row = (t / g.trace_every) % g.trace_len;
-                        float* dst = g.trace + ((row * N + n) * g.trace_nobs) * kLanes + l;
-                        for (int o = 0; o < g.trace_nobs; ++o) dst[o * kLanes] = M::obs(x, o);
-                    }
-                    const float xbold = bold ? M::obs(x, g.bold_obs) : 0.0f;
-                    const float c = lane_post<CF>(acc[k], obs0, wsum, cf_a, g.cf_b);
-                    float f[NS];
-                    M::drift(x, c, p, g.consts, f);
+                if (t >= t_end) break;
+                if (trace && t % g.trace_every == 0) {
+                    const long long row = (t / g.trace_every) % g.trace_len;
+                    float* dst = g.trace + ((row * N + n) * g.trace_nobs) * kLanes + l;
+                    for (int o = 0; o < g.trace_nobs; ++o) dst[o * kLanes] = M::obs(x, o);
+                }
+                const float xbold = bold ? M::obs(x, g.bold_obs) : 0.0f;
+                const float c = lane_post<CF>(csum[k * blockDim.x + threadIdx.x], obs0, wsum, cf_a,
+                                              g.cf_b);
+                float f[NS];
+                M::drift(x, c, p, g.consts, f);
 #pragma unroll
-                    for (int v = 0; v < NS; ++v) x[v] = fmaf(dt, f[v], x[v]);
-                    if (noise) {
-                        const int r0 = static_cast<int>(t % SPC);
-                        if (k == 0 || r0 == 0) {
-                            const u32x4 w = philox4x32_10(static_cast<uint32_t>(n),
-                                                          static_cast<uint32_t>(t / SPC), g.seed_hi,
-                                                          0u, g.seed_lo, inst_id);
-                            box_muller(w.v[0], w.v[1], zz[0], zz[1]);
-                            box_muller(w.v[2], w.v[3], zz[2], zz[3]);
-                        }
-#pragma unroll
-                        for (int v = 0; v < NS; ++v)
-                            x[v] = fmaf(sqrt_dt * pick4(zz, r0 * NS + v), g.sigma[v], x[v]);
+                for (int v = 0; v < NS; ++v) x[v] = fmaf(dt, f[v], x[v]);
+                if (noise) {
+                    const int r0 = static_cast<int>(t % SPC);
+                    if (k == 0 || r0 == 0) {
+                        const u32x4 w = philox4x32_10(static_cast<uint32_t>(n),
+                                                      static_cast<uint32_t>(t / SPC), g.seed_hi, 0u,
+                                                      g.seed_lo, inst_id);
+                        box_muller(w.v[0], w.v[1], zz[0], zz[1]);
+                        box_muller(w.v[2], w.v[3], zz[2], zz[3]);
                     }
-                    M::limit(x, flags);
-                    obs0 = M::obs(x, 0);
-                    const uint32_t pos = (static_cast<uint32_t>(t) + 1u) & mask;
-                    const size_t idx = (static_cast<size_t>(n) * R + pos) * kLanes + l;
-                    ring[idx] = obs0;
-                    if (pos < kGhost) ring[idx + static_cast<size_t>(nh) * kLanes] = obs0;
-                    if (bold) {
-                        Balloon::step(bs, bF, bV, bQ, xbold, g.dt_bold);
-                        if ((t + 1) % g.bold_period == 0) {
-                            const long long row = (t + 1) / g.bold_period - 1;
-                            if (row >= 0 && row < g.bold_len)
-                                g.bold_out[(row * N + n) * kLanes + l] = Balloon::signal(bV, bQ);
-                        }
+#pragma unroll
+                    for (int v = 0; v < NS; ++v)
+                        x[v] = fmaf(sqrt_dt * pick4(zz, r0 * NS + v), g.sigma[v], x[v]);
+                }
+                M::limit(x, flags);
+                obs0 = M::obs(x, 0);
+                const uint32_t pos = (static_cast<uint32_t>(t) + 1u) & mask;
+                const size_t idx = (static_cast<size_t>(n) * R + pos) * kLanes + l;
+                ring[idx] = obs0;
+                if (pos < kGhost) ring[idx + static_cast<size_t>(nh) * kLanes] = obs0;
+                if (bold) {
+                    Balloon::step(bs, bF, bV, bQ, xbold, g.dt_bold);
+                    if ((t + 1) % g.bold_period == 0) {
+                        const long long row = (t + 1) / g.bold_period - 1;
+                        if (row >= 0 && row < g.bold_len)
+                            g.bold_out[(row * N + n) * kLanes + l] = Balloon::signal(bV, bQ);
                     }
                 }
             }
@@ -286,16 +306,18 @@ __device__ __forceinline__ void run_group(const tvbg_group& g, int32_t* status) 
 }
 
 // One group per CTA (or per cluster of CTAs): group index = order[cluster id].
-template <class M, int CF, int K>
+// D = sector loads in flight per thread in the gather (16 or 32).
+template <class M, int CF, int K, int D>
 __global__ void __launch_bounds__(1024, 1)
     group_kernel(const tvbg_group* __restrict__ groups, int32_t n_groups,
                  const int32_t* __restrict__ order, int32_t* __restrict__ status) {
     __shared__ __align__(16) tvbg_group s_grp;
+    extern __shared__ float csum[];  // [K][blockDim]: the block's coupling sums per thread
     const int cid = static_cast<int>(cluster_id_x());
     if (cid >= n_groups) return;  // uniform over the cluster
     const int idx = order ? __ldg(order + cid) : cid;
     stage_group(groups + idx, &s_grp);
-    run_group<M, CF, K>(s_grp, status);
+    run_group<M, CF, K, D>(s_grp, csum, status);
 }
 
 }  // namespace tvbg

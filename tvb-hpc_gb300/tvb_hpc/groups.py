@@ -74,7 +74,9 @@ class GroupSet:
       nsteps  : optional (I,) step counts, used to put instances of similar
                 length into the same group (longest first);
       block_k : 4 or 8 steps per barrier (default: 8 when d_min >= 7);
-      threads, cluster : launch shape (default: group_shape).
+      threads, cluster : launch shape (default: group_shape);
+      depth   : gather depth, 2 or 4 (16 or 32 sector loads in flight per
+                thread; the sigmoidal coupling always uses 2).
     Couplings must be separable (Linear, Diff, Sigmoidal); the Kuramoto
     model and the Track-A order run on the per-instance kernels.
 
@@ -86,7 +88,7 @@ class GroupSet:
                  nparam=None, delays=None, rounding='ceil', seed=0, inst_ids=None,
                  bold_period=0, bold_len=0, trace_every=0, trace_len=0, trace_nobs=None,
                  flags=0, cf_b=None, t0=0, nsteps=None, block_k=None, threads=None,
-                 cluster=None, history='zero'):
+                 cluster=None, history='zero', depth=2):
         _device_ok()
         torch = _torch()
         self.torch = torch
@@ -221,6 +223,7 @@ class GroupSet:
                                (cf_b0 if isinstance(cf_b0, (int, float, np.number)) else 0.0))
         self.t = np.full(G, int(t0), np.int64)
         self.threads, self.cluster = group_shape(N, threads, cluster)
+        self.depth = 2 if self.cfun_id == nat.CFUN_SIGMOIDAL else int(depth)
         self.status = DeviceStatus()
         self._uploaded = None
 
@@ -332,6 +335,7 @@ class GroupSet:
         cfg.model, cfg.cfun = self.model_id, self.cfun_id
         cfg.threads, cfg.cluster = self.threads, self.cluster
         cfg.block_k = int(block_k)
+        cfg.tpn = self.depth
         cfg.d_status = self.status.t.data_ptr()
         cfg.d_order = order.data_ptr() if order is not None else None
         return cfg
