@@ -176,9 +176,13 @@ def test_group_plan_and_shape():
         groups.plan_group(2, 10)
     with pytest.raises(ValueError):
         groups.plan_group(5, 10, block_k=8)
-    for N, (thr, cl) in [(68, (544, 1)), (84, (672, 1)), (128, (1024, 1)), (192, (768, 2)),
-                         (400, (800, 4)), (998, (1024, 8))]:
-        assert groups.group_shape(N) == (thr, cl)
+    for N, shape in [(68, (544, 4, 4)), (84, (672, 4, 4)), (128, (1024, 4, 4)),
+                     (192, (768, 4, 2)), (400, (800, 8, 2)), (998, (1024, 8, 1))]:
+        assert groups.group_shape(N) == shape
+    for N, sl in [(68, 1), (84, 2), (400, 1)]:
+        thr, cl, s = groups.group_shape(N, slices=sl)
+        assert s == sl and thr % (8 * sl) == 0 and thr <= 1024
+        assert cl * (thr // (8 * sl)) >= N
 
 
 def test_plan_ring_constraints():

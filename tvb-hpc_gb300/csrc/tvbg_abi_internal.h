@@ -34,12 +34,12 @@ BlockedKernel blocked_kernel_mpr(int cfun, int tpn, int k);
 BlockedKernel blocked_kernel_linear(int cfun, int tpn, int k);
 BlockedKernel blocked_kernel_g2dosc(int cfun, int tpn, int k);
 // Lane-interleaved group kernel signature and per-model lookup for (cfun, K,
-// gather depth 2 or 4 = 16 or 32 loads in flight per thread).
+// edge slices per node 1, 2 or 4).
 using GroupKernel = void (*)(const tvbg_group*, int32_t, const int32_t*, int32_t*);
-GroupKernel group_kernel_g2do(int cfun, int k, int depth);
-GroupKernel group_kernel_mpr(int cfun, int k, int depth);
-GroupKernel group_kernel_linear(int cfun, int k, int depth);
-GroupKernel group_kernel_g2dosc(int cfun, int k, int depth);
+GroupKernel group_kernel_g2do(int cfun, int k, int slices);
+GroupKernel group_kernel_mpr(int cfun, int k, int slices);
+GroupKernel group_kernel_linear(int cfun, int k, int slices);
+GroupKernel group_kernel_g2dosc(int cfun, int k, int slices);
 // Shared memory of the blocked kernel beyond the ring (floats): K * nmax * (2 + NS) + 4 * nmax.
 uint32_t blocked_aux_bytes(int model, int k, int nmax);
 

@@ -7,12 +7,12 @@ using namespace tvbg;
 
 namespace {
 
-GroupKernel lookup_group(int model, int cfun, int k, int depth) {
+GroupKernel lookup_group(int model, int cfun, int k, int slices) {
     switch (model) {
-        case TVBG_MODEL_G2DO: return group_kernel_g2do(cfun, k, depth);
-        case TVBG_MODEL_MPR: return group_kernel_mpr(cfun, k, depth);
-        case TVBG_MODEL_LINEAR: return group_kernel_linear(cfun, k, depth);
-        case TVBG_MODEL_G2DOSC: return group_kernel_g2dosc(cfun, k, depth);
+        case TVBG_MODEL_G2DO: return group_kernel_g2do(cfun, k, slices);
+        case TVBG_MODEL_MPR: return group_kernel_mpr(cfun, k, slices);
+        case TVBG_MODEL_LINEAR: return group_kernel_linear(cfun, k, slices);
+        case TVBG_MODEL_G2DOSC: return group_kernel_g2dosc(cfun, k, slices);
         default: return nullptr;
     }
 }
@@ -31,13 +31,15 @@ int check_group_launch(const tvbg_launch* cfg, GroupKernel* kfn, int* cluster) {
     const int c = cfg->cluster <= 0 ? 1 : cfg->cluster;
     if (c != 1 && c != 2 && c != 4 && c != 8)
         return set_error(TVBG_EINVAL, "cluster must be 1, 2, 4 or 8");
-    const int depth = cfg->tpn <= 0 ? 4 : cfg->tpn;
-    if (depth != 2 && depth != 4)
-        return set_error(TVBG_EINVAL, "tvbg_group_run: tpn (gather depth) must be 0, 2 or 4");
-    *kfn = lookup_group(cfg->model, cfg->cfun, cfg->block_k, depth);
+    const int slices = cfg->tpn <= 0 ? 1 : cfg->tpn;
+    if (slices != 1 && slices != 2 && slices != 4)
+        return set_error(TVBG_EINVAL, "tvbg_group_run: tpn (edge slices per node) must be 0, 1, 2 or 4");
+    if (cfg->threads % (8 * slices))
+        return set_error(TVBG_EINVAL, "tvbg_group_run: threads must be a multiple of 8 * tpn");
+    *kfn = lookup_group(cfg->model, cfg->cfun, cfg->block_k, slices);
     if (!*kfn)
         return set_error(TVBG_EUNSUPPORTED,
-                         "group kernel not built for this model/coupling/block_k/depth");
+                         "group kernel not built for this model/coupling/block_k/slices");
     *cluster = c;
     return TVBG_OK;
 }

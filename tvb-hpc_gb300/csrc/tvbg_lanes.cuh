@@ -20,11 +20,14 @@
 //   state  [N][NS][8], nparam [N][NP][8], bold [4][N][8],
 //   bold_out [bold_len][N][8], trace [trace_len][N][trace_nobs][8].
 //
-// Thread mapping.  Thread t of CTA r (cluster of C CTAs) is lane l = t % 8
-// of node slot s = t / 8; node slot s of CTA r serves the node positions
-// q = s C + r, s C + r + C P, ... (P = blockDim / 8) of the group's node
-// order (the host sorts nodes by in-degree, so the 4 slots of a warp see
-// similar edge counts, and the C CTAs of a cluster see the same work).
+// Thread mapping.  Thread t of CTA r (cluster of C CTAs) is lane l = t % 8,
+// edge slice s = (t / 8) % S of node slot q = t / (8 S).  The S slices of a
+// node (consecutive lanes of one warp) each sum every S-th in-edge and
+// combine by shuffles; slice 0 then updates the node.  Node slot q of CTA r
+// serves the node positions q C + r, q C + r + C P, ... (P = blockDim /
+// (8 S)) of the group's node order (the host sorts nodes by in-degree, so
+// the slots of a warp see similar edge counts and the C CTAs of a cluster
+// the same work).
 //
 // Time blocking.  A value written at step t is first read at t + 1 + d_min,
 // so the K <= d_min + 1 steps of a block read only slots that exist when the
@@ -112,29 +115,29 @@ __device__ __forceinline__ float lane_post(float S, float xi, float wsum, float 
     }
 }
 
-// K coupling sums of node n for the block starting at ring position tm.
-// U = D / K edges per iteration: D independent sector loads in flight per
-// thread (the gather is bound by memory latency, not issue).  The sums are
-// accumulated in CSR order.
-template <int CF, int K, int D>
-__device__ __forceinline__ void lane_gather(const tvbg_group& g, int n, uint32_t tm, uint32_t mask,
-                                            uint32_t R, int l, float acc[K]) {
-    constexpr int U = D / K;
+// Partial coupling sums of node n for the K steps of the block starting at
+// ring position tm, over the in-edges lo + s, lo + s + S, ... of slice s:
+// U = 16 / K edges per iteration keep 16 independent sector loads in flight
+// per thread (the gather is bound by memory latency, not issue).
+template <int CF, int K, int S>
+__device__ __forceinline__ void lane_gather(const tvbg_group& g, int lo, int hi, int s,
+                                            uint32_t tm, uint32_t mask, uint32_t R, int l,
+                                            float acc[K]) {
+    constexpr int U = 16 / K;
     const float* __restrict__ ring = g.ring + l;
     const uint2* __restrict__ edges = reinterpret_cast<const uint2*>(g.edges);
-    const int lo = __ldg(g.row + n), hi = __ldg(g.row + n + 1);
 #pragma unroll
     for (int k = 0; k < K; ++k) acc[k] = 0.0f;
     auto addr = [&](uint32_t pk) {
         return ring + (static_cast<size_t>(pk >> 16) * R + ((tm + (pk & 0xffffu)) & mask)) * kLanes;
     };
-    int e = lo;
-    for (; e + U <= hi; e += U) {
+    int e = lo + s;
+    for (; e + (U - 1) * S < hi; e += U * S) {
         float v[U][K];
         float w[U];
 #pragma unroll
         for (int u = 0; u < U; ++u) {
-            const uint2 ed = __ldg(edges + e + u);
+            const uint2 ed = __ldg(edges + e + u * S);
             const float* p = addr(ed.x);
             w[u] = __uint_as_float(ed.y);
 #pragma unroll
@@ -146,15 +149,14 @@ __device__ __forceinline__ void lane_gather(const tvbg_group& g, int n, uint32_t
             for (int k = 0; k < K; ++k) acc[k] = fmaf(w[u], lane_pre<CF>(v[u][k], g), acc[k]);
         }
     }
-    // remainder: fewer than U edges, loads still issued together
-    const int rem = hi - e;
-    if (rem > 0) {
+    // remainder: fewer than U edges of this slice, loads still issued together
+    if (e < hi) {
         float v[U][K];
         float w[U];
 #pragma unroll
         for (int u = 0; u < U; ++u) {
-            if (u < rem) {
-                const uint2 ed = __ldg(edges + e + u);
+            if (e + u * S < hi) {
+                const uint2 ed = __ldg(edges + e + u * S);
                 const float* p = addr(ed.x);
                 w[u] = __uint_as_float(ed.y);
 #pragma unroll
@@ -163,7 +165,7 @@ __device__ __forceinline__ void lane_gather(const tvbg_group& g, int n, uint32_t
         }
 #pragma unroll
         for (int u = 0; u < U; ++u) {
-            if (u < rem) {
+            if (e + u * S < hi) {
 #pragma unroll
                 for (int k = 0; k < K; ++k) acc[k] = fmaf(w[u], lane_pre<CF>(v[u][k], g), acc[k]);
             }
@@ -171,7 +173,7 @@ __device__ __forceinline__ void lane_gather(const tvbg_group& g, int n, uint32_t
     }
 }
 
-template <class M, int CF, int K, int D>
+template <class M, int CF, int K, int S>
 __device__ __forceinline__ void run_group(const tvbg_group& g, float* csum, int32_t* status) {
     constexpr int NS = M::NS;
     constexpr int NP = M::NP;
@@ -186,9 +188,11 @@ __device__ __forceinline__ void run_group(const tvbg_group& g, float* csum, int3
         return;  // every CTA of the cluster reads the same descriptor and leaves here
     }
     const int l = threadIdx.x % kLanes;
-    const int slot = threadIdx.x / kLanes;
-    const int P = blockDim.x / kLanes;
+    const int sl = (threadIdx.x / kLanes) % S;          // edge slice
+    const int slot = threadIdx.x / (kLanes * S);
+    const int P = blockDim.x / (kLanes * S);
     const int stride = static_cast<int>(C) * P;
+    const int rounds = (N + stride - 1) / stride;       // warp-uniform node loop
     const uint32_t nh = 1u << g.lognh;
     const uint32_t mask = nh - 1u;
     const uint32_t R = nh + kGhost;
@@ -207,7 +211,7 @@ __device__ __forceinline__ void run_group(const tvbg_group& g, float* csum, int3
     const int q0 = slot * static_cast<int>(C) + static_cast<int>(rank);
 
     // seed: slot t0 holds obs0 of the state at t0
-    {
+    if (sl == 0) {
         const uint32_t pos = static_cast<uint32_t>(t0) & mask;
         for (int q = q0; q < N; q += stride) {
             const int n = g.nodes ? __ldg(g.nodes + q) : q;
@@ -225,8 +229,24 @@ __device__ __forceinline__ void run_group(const tvbg_group& g, float* csum, int3
     for (long long tb = t0; tb < t0 + g.nsteps; tb += K) {
         const int cnt = (t0 + g.nsteps - tb) < K ? static_cast<int>(t0 + g.nsteps - tb) : K;
         const uint32_t tm = static_cast<uint32_t>(tb) & mask;
-        for (int q = q0; q < N; q += stride) {
-            const int n = g.nodes ? __ldg(g.nodes + q) : q;
+        for (int r = 0; r < rounds; ++r) {
+            const int q = q0 + r * stride;
+            const bool valid = q < N;
+            const int n = valid ? (g.nodes ? __ldg(g.nodes + q) : q) : 0;
+            {
+                const int lo = valid ? __ldg(g.row + n) : 0;
+                const int hi = valid ? __ldg(g.row + n + 1) : 0;
+                float acc[K];
+                lane_gather<CF, K, S>(g, lo, hi, sl, tm, mask, R, l, acc);
+#pragma unroll
+                for (int k = 0; k < K; ++k) {
+#pragma unroll
+                    for (int off = kLanes; off < kLanes * S; off <<= 1)
+                        acc[k] += __shfl_xor_sync(kFullMask, acc[k], off);
+                    csum[k * blockDim.x + threadIdx.x] = acc[k];
+                }
+            }
+            if (!valid || sl != 0) continue;
             float x[NS], p[NP];
 #pragma unroll
             for (int v = 0; v < NS; ++v) x[v] = state[(n * NS + v) * kLanes + l];
@@ -239,12 +259,6 @@ __device__ __forceinline__ void run_group(const tvbg_group& g, float* csum, int3
                 bF = g.bold[(1 * N + n) * kLanes + l];
                 bV = g.bold[(2 * N + n) * kLanes + l];
                 bQ = g.bold[(3 * N + n) * kLanes + l];
-            }
-            {
-                float acc[K];
-                lane_gather<CF, K, D>(g, n, tm, mask, R, l, acc);
-#pragma unroll
-                for (int k = 0; k < K; ++k) csum[k * blockDim.x + threadIdx.x] = acc[k];
             }
             float obs0 = M::obs(x, 0);
             float zz[4] = {0.0f, 0.0f, 0.0f, 0.0f};
@@ -306,8 +320,8 @@ __device__ __forceinline__ void run_group(const tvbg_group& g, float* csum, int3
 }
 
 // One group per CTA (or per cluster of CTAs): group index = order[cluster id].
-// D = sector loads in flight per thread in the gather (16 or 32).
-template <class M, int CF, int K, int D>
+// S = edge slices per node (1, 2 or 4).
+template <class M, int CF, int K, int S>
 __global__ void __launch_bounds__(1024, 1)
     group_kernel(const tvbg_group* __restrict__ groups, int32_t n_groups,
                  const int32_t* __restrict__ order, int32_t* __restrict__ status) {
@@ -317,7 +331,7 @@ __global__ void __launch_bounds__(1024, 1)
     if (cid >= n_groups) return;  // uniform over the cluster
     const int idx = order ? __ldg(order + cid) : cid;
     stage_group(groups + idx, &s_grp);
-    run_group<M, CF, K, D>(s_grp, csum, status);
+    run_group<M, CF, K, S>(s_grp, csum, status);
 }
 
 }  // namespace tvbg

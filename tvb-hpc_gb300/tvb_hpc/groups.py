@@ -43,17 +43,31 @@ def plan_group(dmin, dmax, block_k=None):
     return k, int(np.log2(nh))
 
 
-def group_shape(N, threads=None, cluster=None):
-    """(threads, cluster) of a group launch: by default one node per thread,
-    clusters of 2/4/8 CTAs for N > 128."""
+def group_shape(N, threads=None, cluster=None, slices=None):
+    """(threads, cluster, slices) of a group launch.  By default one node per
+    slot, with the most edge slices (4, 2, 1) that keep the cluster within 4
+    CTAs (4 slices) or 8 CTAs (2 slices, 1 slice)."""
+    def need(s):
+        c = 1
+        while L * s * -(-N // c) > 1024 and c < 8:
+            c *= 2
+        return c, L * s * -(-N // c) <= 1024
+    if slices is None:
+        slices = 1
+        for s, cmax in ((4, 4), (2, 8)):
+            c, ok = need(s)
+            if ok and c <= cmax:
+                slices = s
+                break
+    slices = int(slices)
     if cluster is None:
-        cluster = 1
-        while L * -(-N // cluster) > 1024 and cluster < 8:
-            cluster *= 2
+        cluster = need(slices)[0]
     if threads is None:
         per = -(-N // cluster)
-        threads = min(1024, 32 * -(-(L * per) // 32))
-    return int(threads), int(cluster)
+        threads = min(1024, 32 * -(-(L * slices * per) // 32))
+    if threads % (L * slices):
+        raise ValueError('threads must be a multiple of 8 * slices')
+    return int(threads), int(cluster), slices
 
 
 def group_occupancy(cfg):
@@ -74,9 +88,9 @@ class GroupSet:
       nsteps  : optional (I,) step counts, used to put instances of similar
                 length into the same group (longest first);
       block_k : 4 or 8 steps per barrier (default: 8 when d_min >= 7);
-      threads, cluster : launch shape (default: group_shape);
-      depth   : gather depth, 2 or 4 (16 or 32 sector loads in flight per
-                thread; the sigmoidal coupling always uses 2).
+      threads, cluster, slices : launch shape (default: group_shape);
+                slices = threads per (node, instance) in the gather (1, 2,
+                4; the sigmoidal coupling uses 1).
     Couplings must be separable (Linear, Diff, Sigmoidal); the Kuramoto
     model and the Track-A order run on the per-instance kernels.
 
@@ -88,7 +102,7 @@ class GroupSet:
                  nparam=None, delays=None, rounding='ceil', seed=0, inst_ids=None,
                  bold_period=0, bold_len=0, trace_every=0, trace_len=0, trace_nobs=None,
                  flags=0, cf_b=None, t0=0, nsteps=None, block_k=None, threads=None,
-                 cluster=None, history='zero', depth=2):
+                 cluster=None, history='zero', slices=None):
         _device_ok()
         torch = _torch()
         self.torch = torch
@@ -222,8 +236,9 @@ class GroupSet:
         self.cf_b = np.float32(cf_b if cf_b is not None else
                                (cf_b0 if isinstance(cf_b0, (int, float, np.number)) else 0.0))
         self.t = np.full(G, int(t0), np.int64)
-        self.threads, self.cluster = group_shape(N, threads, cluster)
-        self.depth = 2 if self.cfun_id == nat.CFUN_SIGMOIDAL else int(depth)
+        if self.cfun_id == nat.CFUN_SIGMOIDAL:
+            slices = 1
+        self.threads, self.cluster, self.slices = group_shape(N, threads, cluster, slices)
         self.status = DeviceStatus()
         self._uploaded = None
 
@@ -335,7 +350,7 @@ class GroupSet:
         cfg.model, cfg.cfun = self.model_id, self.cfun_id
         cfg.threads, cfg.cluster = self.threads, self.cluster
         cfg.block_k = int(block_k)
-        cfg.tpn = self.depth
+        cfg.tpn = self.slices
         cfg.d_status = self.status.t.data_ptr()
         cfg.d_order = order.data_ptr() if order is not None else None
         return cfg
