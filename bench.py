@@ -327,28 +327,66 @@ class MixedStep:
         return self.n_launch
 
 
+def build_groups(wl, slices=None):
+    from tvb_hpc import model, coupling, scheme, groups
+    m = getattr(model, wl['model'])()
+    cf = getattr(coupling, wl['cfun'])(m)
+    scm = scheme.EulerMaryuyamaStep(wl['dt']) if wl['noise'] else scheme.EulerStep(wl['dt'])
+    return groups.GroupSet(m, cf, scm, wl['conn'], dt=wl['dt'], couplings=wl['couplings'],
+                           speeds=wl['speeds'], state0=wl['x0'], nparam=wl.get('nparam'),
+                           seed=wl['seed'], bold_period=wl['bold_period'],
+                           bold_len=wl['bold_len'], slices=slices)
+
+
+def groups_supported(wl):
+    return wl['cfun'] in ('Linear', 'Diff', 'Sigmoidal') and wl['model'] != 'Kuramoto'
+
+
 class GpuStep:
     """One bench step on the device: reset state/ring/balloon from resident
-    copies, run every instance for all steps, compute FC."""
+    copies, run every instance for all steps, compute FC.  Separable
+    couplings run as lane-interleaved groups (tvbg_group_run), the others on
+    the per-instance kernels (tvbg_sweep)."""
 
-    def __init__(self, wl, torch, tpn=None, warps=None):
+    def __init__(self, wl, torch, tpn=None, warps=None, path='groups'):
         self.torch = torch
         self.wl = wl
-        self.sw = build_sweep(wl, tpn, warps)
-        self.sw.pick_tpn()
+        self.groups = path == 'groups' and groups_supported(wl)
+        if self.groups:
+            self.sw = build_groups(wl, tpn)
+            self.launches = self.sw.prepare(wl['nsteps'])[0]
+            self.tpn = self.sw.slices
+        else:
+            self.sw = build_sweep(wl, tpn, warps)
+            self.sw.pick_tpn()
+            self.launches = self.sw.prepare(wl['nsteps'])
+            self.tpn = self.sw.tpn
+        self.path = ('lane-interleaved groups' if self.groups else 'per-instance kernels')
         self.x0 = self.sw.state.clone()
+        self.ns = self.sw.ns
+        self.status = self.sw.status
         self.target = (torch.from_numpy(wl['target']).cuda() if wl['target'] is not None
                        else None)
-        self.launches = self.sw.prepare(wl['nsteps'])
         self.n_launch = len(self.launches)
-        self.kernel_ms = []
 
     def reset(self, x0=None):
         sw = self.sw
-        sw.state.copy_(self.x0 if x0 is None else x0)
+        x = self.x0 if x0 is None else x0
         sw.ring.zero_()
-        if sw.bold is not None:
-            sw.bold.zero_()
+        if self.groups:
+            sw.set_state(x)
+            if sw.gbold is not None:
+                sw.gbold.zero_()
+        else:
+            sw.state.copy_(x)
+            if sw.bold is not None:
+                sw.bold.zero_()
+
+    def _launch(self, launches):
+        if self.groups:
+            self.sw.launch(launches)
+        else:
+            self.sw.launch(launches, self.sw.tpn)
 
     def run(self, time_kernels=False):
         from tvb_hpc import metric  # noqa: F401
@@ -360,18 +398,18 @@ class GpuStep:
                 e0 = torch.cuda.Event(enable_timing=True)
                 e1 = torch.cuda.Event(enable_timing=True)
                 e0.record()
-                sw.launch([launch], sw.tpn)
+                self._launch([launch])
                 e1.record()
                 evs.append((e0, e1))
         else:
-            sw.launch(self.launches, sw.tpn)
+            self._launch(self.launches)
         fc = None
-        if sw.bold is not None and self.target is not None:
+        if sw.bold_out is not None and self.target is not None:
             fc = metric.fc(sw.bold_out, self.target)
         return evs, fc
 
     def launches_per_step(self):
-        fc_launches = 1 if (self.sw.bold is not None and self.target is not None) else 0
+        fc_launches = 1 if (self.wl['bold_period'] > 0 and self.target is not None) else 0
         return self.n_launch + fc_launches
 
 
@@ -453,8 +491,8 @@ def gpu_arm(args):
     from tvb_hpc import _native
     _native.load()
     wl = WORKLOADS[args.workload]()
-    gs = (MixedStep(wl, torch, args.mixed_path, not args.no_graph) if wl['name'] == 'mixed'
-          else GpuStep(wl, torch, args.tpn, args.warps))
+    gs = (MixedStep(wl, torch, args.path, not args.no_graph) if wl['name'] == 'mixed'
+          else GpuStep(wl, torch, args.tpn, args.warps, args.path))
 
     def barrier():
         if world > 1:
@@ -492,7 +530,7 @@ def gpu_arm(args):
     total_ms = float(t.item())
     ms_per_step = total_ms / args.steps
     value = world * node_steps(wl) * args.steps / (total_ms / 1e3)
-    (gs.status if hasattr(gs, 'status') else gs.sw.status).check()
+    gs.status.check()
 
     plain = None
     if wl['name'] == 'mixed':
@@ -548,8 +586,9 @@ def gpu_arm(args):
             'data': 'synthetic (seeded connectomes, config recipe)',
             'config': workload_config(wl), 'e2e': e2e,
             'gpu_launches': gs.launches_per_step() * args.steps,
-            'roofline': roofline_entry(wl, gs.sw.ns, kern_ms, args.steps),
-            'clocks': clk, 'tpn': gs.sw.tpn}
+            'roofline': roofline_entry(wl, gs.ns, kern_ms, args.steps),
+            'clocks': clk, 'tpn': gs.tpn}
+    line['config']['path'] = gs.path
     if rank == 0 and world == 1 and not args.no_cpu:
         line['cpu_baseline'] = cpu_baseline(wl)
     if world > 1:
@@ -721,8 +760,8 @@ def main():
     ap.add_argument('--ref-seconds', type=float, default=8.0)
     ap.add_argument('--tpn', type=int, default=None, help='fix the gather width (skip autotune)')
     ap.add_argument('--warps', type=int, default=None, help='fix the CTA width of the blocked kernel')
-    ap.add_argument('--mixed-path', default='groups', choices=['groups', 'instances'],
-                    help='uneven batch as lane-interleaved groups or per-instance kernels')
+    ap.add_argument('--path', default='groups', choices=['groups', 'instances'],
+                    help='lane-interleaved groups (separable couplings) or per-instance kernels')
     ap.add_argument('--no-graph', action='store_true',
                     help='launch the batch directly instead of replaying a CUDA graph')
     args = ap.parse_args()

@@ -176,13 +176,15 @@ def test_group_plan_and_shape():
         groups.plan_group(2, 10)
     with pytest.raises(ValueError):
         groups.plan_group(5, 10, block_k=8)
-    for N, shape in [(68, (544, 4, 4)), (84, (672, 4, 4)), (128, (1024, 4, 4)),
-                     (192, (768, 4, 2)), (400, (800, 8, 2)), (998, (1024, 8, 1))]:
-        assert groups.group_shape(N) == shape
-    for N, sl in [(68, 1), (84, 2), (400, 1)]:
-        thr, cl, s = groups.group_shape(N, slices=sl)
-        assert s == sl and thr % (8 * sl) == 0 and thr <= 1024
-        assert cl * (thr // (8 * sl)) >= N
+    for N in (1, 4, 20, 68, 84, 128, 192, 300, 400, 998):
+        for sl in (None, 1, 2, 4):
+            thr, cl, s = groups.group_shape(N, slices=sl)
+            assert s == (sl or 1) and thr % (8 * s) == 0 and 32 <= thr <= 1024 and 1 <= cl <= 8
+            assert cl * (thr // (8 * s)) >= N or thr == 1024
+    # the planner fills the SM: 3-CTA clusters of 192 threads for N = 68
+    assert groups.group_shape(68) == (192, 3, 1)
+    assert groups.group_shape(998) == (1024, 8, 1)
+    assert groups.group_shape(84, threads=672) == (672, 1, 1)
 
 
 def test_plan_ring_constraints():

@@ -43,29 +43,45 @@ def plan_group(dmin, dmax, block_k=None):
     return k, int(np.log2(nh))
 
 
+CLUSTER_COST = 0.03
+
+
 def group_shape(N, threads=None, cluster=None, slices=None):
-    """(threads, cluster, slices) of a group launch.  By default one node per
-    slot, with the most edge slices (4, 2, 1) that keep the cluster within 4
-    CTAs (4 slices) or 8 CTAs (2 slices, 1 slice)."""
-    def need(s):
-        c = 1
-        while L * s * -(-N // c) > 1024 and c < 8:
-            c *= 2
-        return c, L * s * -(-N // c) <= 1024
-    if slices is None:
-        slices = 1
-        for s, cmax in ((4, 4), (2, 8)):
-            c, ok = need(s)
-            if ok and c <= cmax:
-                slices = s
-                break
-    slices = int(slices)
-    if cluster is None:
-        cluster = need(slices)[0]
+    """(threads, cluster, slices) of a group launch.
+
+    The kernel holds 64 registers per thread, so an SM keeps floor(1024 / T)
+    CTAs of T threads; the gather is bound by loads in flight, so the
+    planner maximises the *useful* threads resident per SM:
+        floor(1024 / T) * T * N / (C T / (8 S)),
+    over T = 32..1024 and clusters C <= 8 with one node per slot, discounted
+    by CLUSTER_COST per extra CTA of the cluster.  slices defaults to 1 (extra slices shorten a
+    group's critical path but cost throughput when the GPU is full)."""
+    slices = 1 if slices is None else int(slices)
+    lanes = L * slices
+    if threads is not None and cluster is None:
+        slots = int(threads) // lanes
+        cluster = min(8, -(-N // slots))
     if threads is None:
-        per = -(-N // cluster)
-        threads = min(1024, 32 * -(-(L * slices * per) // 32))
-    if threads % (L * slices):
+        best = None
+        for T in range(32, 1025, 32):
+            if T % lanes:
+                continue
+            slots = T // lanes
+            C = -(-N // slots) if cluster is None else int(cluster)
+            if C > 8:
+                continue
+            if cluster is not None and C * slots < N and T < 1024:
+                continue
+            useful = (1024 // T) * T * min(1.0, N / float(C * slots))
+            # each extra CTA of a cluster costs a little (barrier, placement)
+            key = (round(useful * (1.0 - CLUSTER_COST * (C - 1)), 3), -C, T)
+            if best is None or key > best[0]:
+                best = (key, T, C)
+        if best is None:      # very large N: widest CTAs, 8-CTA clusters, several nodes per slot
+            threads, cluster = 1024 // lanes * lanes, 8 if cluster is None else cluster
+        else:
+            threads, cluster = best[1], best[2]
+    if int(threads) % lanes:
         raise ValueError('threads must be a multiple of 8 * slices')
     return int(threads), int(cluster), slices
 
