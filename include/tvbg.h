@@ -157,7 +157,7 @@ typedef struct tvbg_launch {
     int32_t block_k;       /* 0 or 1: per-step kernel; 4 or 8: time-blocked     */
                            /* kernel (K steps per block, padded ring layout)    */
     int32_t nmax;          /* largest N of the call (blocked kernel); 0 = threads */
-    int32_t cluster;       /* tvbg_group_run: CTAs per group (1, 2, 4 or 8; 0 = 1) */
+    int32_t cluster;       /* tvbg_group_run: CTAs per group (1..8; 0 = 1)        */
     int32_t *d_status;     /* optional device int: first device error code      */
     int32_t *d_counter;    /* tvbg_batch_run work counter (zeroed by the call)  */
     const int32_t *d_order;/* tvbg_batch_run instance order (cost-descending)   */

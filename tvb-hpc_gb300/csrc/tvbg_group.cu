@@ -29,8 +29,7 @@ int check_group_launch(const tvbg_launch* cfg, GroupKernel* kfn, int* cluster) {
     if (cfg->block_k != 4 && cfg->block_k != 8)
         return set_error(TVBG_EINVAL, "tvbg_group_run: block_k must be 4 or 8");
     const int c = cfg->cluster <= 0 ? 1 : cfg->cluster;
-    if (c != 1 && c != 2 && c != 4 && c != 8)
-        return set_error(TVBG_EINVAL, "cluster must be 1, 2, 4 or 8");
+    if (c < 1 || c > 8) return set_error(TVBG_EINVAL, "cluster must be in [1, 8]");
     const int slices = cfg->tpn <= 0 ? 1 : cfg->tpn;
     if (slices != 1 && slices != 2 && slices != 4)
         return set_error(TVBG_EINVAL, "tvbg_group_run: tpn (edge slices per node) must be 0, 1, 2 or 4");

@@ -10,9 +10,11 @@ memory and advances all of them together:
   tick:
     1. admit queued requests (arrival time <= now) while their device
        footprint fits the HBM budget;
-    2. advance every active request by min(chunk, steps left): one
-       persistent batch launch per model (tvbg_batch_run, forked streams),
-       instances of all requests interleaved longest-first;
+    2. advance every active request by min(chunk, steps left): requests on
+       separable couplings run as lane-interleaved groups (tvbg_group_run,
+       one forked stream per request), the others (Kuramoto, gradient
+       requests) as one persistent batch launch per model (tvbg_batch_run),
+       all on the device at once;
     3. retire requests that reached their step count: copy the final state
        (and gradients) to the host, free the device memory, record latency.
 
@@ -35,6 +37,7 @@ import numpy as np
 
 from . import model as mdl, coupling as cpl, scheme as sch
 from .engine import InstanceSet, Batch
+from .groups import GroupSet, GroupBatch
 from .utils import getLogger
 
 LOG = getLogger(__name__)
@@ -84,7 +87,7 @@ def footprint(req):
     from .engine import plan_ring
     N, I = req.conn.nnode, req.couplings.size
     d = req.conn.delays(float(np.min(req.speeds)), req.dt, 'ceil')
-    lognh = plan_ring(int(d.min()), int(d.max()))[0]
+    lognh = plan_ring(int(d.min()), int(d.max()), extra=8)[0]
     ring = N * ((1 << lognh) + 8) * 4
     return I * (ring + N * 4 * 6 + 512) + req.conn.nnz * 8 * len(np.unique(req.speeds))
 
@@ -124,18 +127,29 @@ class Server:
             if self.used + need > self.budget or need > free:
                 keep.append(req)
                 continue
-            M, C, noise = MODELS[req.model]
-            m = M()
-            cf = C(m)
-            scm = sch.EulerMaryuyamaStep(req.dt) if (noise and not req.want_grad) else sch.EulerStep(req.dt)
-            req.iset = InstanceSet(m, cf, scm, req.conn, dt=req.dt, couplings=req.couplings,
-                                   speeds=req.speeds, state0=req.x0, nparam=req.nparam,
-                                   seed=req.seed, blocked=False if req.want_grad else 'auto')
+            req.iset = self._make_set(req)
             req.admitted = self.clock()
             req.nbytes = need
             self.used += need
             self.active.append(req)
         self.queue = keep
+
+    @staticmethod
+    def _make_set(req):
+        "Lane-interleaved groups where the coupling is separable, else per-instance."
+        M, C, noise = MODELS[req.model]
+        m = M()
+        cf = C(m)
+        scm = (sch.EulerMaryuyamaStep(req.dt) if (noise and not req.want_grad)
+               else sch.EulerStep(req.dt))
+        kw = dict(dt=req.dt, couplings=req.couplings, speeds=req.speeds, state0=req.x0,
+                  nparam=req.nparam, seed=req.seed)
+        if not req.want_grad and req.model != 'Kuramoto':
+            try:
+                return GroupSet(m, cf, scm, req.conn, **kw)
+            except ValueError:      # delays too short for the group kernel's blocks
+                pass
+        return InstanceSet(m, cf, scm, req.conn, blocked=False if req.want_grad else 'auto', **kw)
 
     def _retire(self, req):
         req.state = req.iset.state.cpu().numpy()
@@ -154,16 +168,25 @@ class Server:
         self._admit(self.clock())
         if not self.active:
             return 0.0
-        by_model = {}
+        by_model, grouped = {}, []
         for req in self.active:
-            by_model.setdefault((req.model, req.want_grad), []).append(req)
+            if isinstance(req.iset, GroupSet):
+                grouped.append(req)
+            else:
+                by_model.setdefault((req.model, req.want_grad), []).append(req)
         batches = []
         work = 0.0
+        if grouped:
+            steps = [min(self.chunk, r.nsteps - r.steps_done) for r in grouped]
+            gb = GroupBatch([r.iset for r in grouped], steps)
+            gb.launch()
+            batches.append((gb, grouped, steps))
         for reqs in by_model.values():
             steps = [min(self.chunk, r.nsteps - r.steps_done) for r in reqs]
             b = Batch([r.iset for r in reqs], steps)
             b.launch()
             batches.append((b, reqs, steps))
+        for b, reqs, steps in batches:
             work += sum(r.couplings.size * r.conn.nnode * n for r, n in zip(reqs, steps))
         self.torch.cuda.synchronize()
         for b, reqs, steps in batches:
