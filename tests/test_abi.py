@@ -181,9 +181,9 @@ def test_group_plan_and_shape():
             thr, cl, s = groups.group_shape(N, slices=sl)
             assert s == (sl or 1) and thr % (8 * s) == 0 and 32 <= thr <= 1024 and 1 <= cl <= 8
             assert cl * (thr // (8 * s)) >= N or thr == 1024
-    # the planner fills the SM: 3-CTA clusters of 192 threads for N = 68
-    assert groups.group_shape(68) == (192, 3, 1)
-    assert groups.group_shape(998) == (1024, 8, 1)
+    for N, shape in [(68, (544, 1, 1)), (84, (672, 1, 1)), (128, (1024, 1, 1)),
+                     (192, (768, 2, 1)), (400, (800, 4, 1)), (998, (1024, 8, 1))]:
+        assert groups.group_shape(N) == shape
     assert groups.group_shape(84, threads=672) == (672, 1, 1)
 
 

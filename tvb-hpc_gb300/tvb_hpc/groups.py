@@ -43,44 +43,26 @@ def plan_group(dmin, dmax, block_k=None):
     return k, int(np.log2(nh))
 
 
-CLUSTER_COST = 0.03
-
-
 def group_shape(N, threads=None, cluster=None, slices=None):
-    """(threads, cluster, slices) of a group launch.
-
-    The kernel holds 64 registers per thread, so an SM keeps floor(1024 / T)
-    CTAs of T threads; the gather is bound by loads in flight, so the
-    planner maximises the *useful* threads resident per SM:
-        floor(1024 / T) * T * N / (C T / (8 S)),
-    over T = 32..1024 and clusters C <= 8 with one node per slot, discounted
-    by CLUSTER_COST per extra CTA of the cluster.  slices defaults to 1 (extra slices shorten a
-    group's critical path but cost throughput when the GPU is full)."""
+    """(threads, cluster, slices) of a group launch: one node per slot of
+    8 * slices lanes, on the smallest cluster (<= 8 CTAs) whose CTAs stay
+    within 1024 threads; beyond 8 CTAs the slots take several nodes.
+    Measured on the uneven batch and the 64 x 64 grid, this beats packing
+    more, smaller CTAs per SM (the gather is bound by the memory system,
+    not by resident threads), and one slice beats more when the GPU is full
+    (extra slices only shorten a single group's critical path)."""
     slices = 1 if slices is None else int(slices)
     lanes = L * slices
-    if threads is not None and cluster is None:
-        slots = int(threads) // lanes
-        cluster = min(8, -(-N // slots))
-    if threads is None:
-        best = None
-        for T in range(32, 1025, 32):
-            if T % lanes:
-                continue
-            slots = T // lanes
-            C = -(-N // slots) if cluster is None else int(cluster)
-            if C > 8:
-                continue
-            if cluster is not None and C * slots < N and T < 1024:
-                continue
-            useful = (1024 // T) * T * min(1.0, N / float(C * slots))
-            # each extra CTA of a cluster costs a little (barrier, placement)
-            key = (round(useful * (1.0 - CLUSTER_COST * (C - 1)), 3), -C, T)
-            if best is None or key > best[0]:
-                best = (key, T, C)
-        if best is None:      # very large N: widest CTAs, 8-CTA clusters, several nodes per slot
-            threads, cluster = 1024 // lanes * lanes, 8 if cluster is None else cluster
+    if cluster is None:
+        if threads is not None:
+            cluster = min(8, -(-N // (int(threads) // lanes)))
         else:
-            threads, cluster = best[1], best[2]
+            cluster = 1
+            while lanes * -(-N // cluster) > 1024 and cluster < 8:
+                cluster *= 2
+    if threads is None:
+        per = -(-N // int(cluster))
+        threads = min(1024 // lanes * lanes, 32 * -(-(lanes * per) // 32))
     if int(threads) % lanes:
         raise ValueError('threads must be a multiple of 8 * slices')
     return int(threads), int(cluster), slices
