@@ -226,9 +226,18 @@ __device__ __forceinline__ void run_group(const tvbg_group& g, float* csum, int3
     }
     group_barrier(cluster);
 
+    const int bper = g.bold_period > 0 ? g.bold_period : 1;
+    const int tev = g.trace_every > 0 ? g.trace_every : 1;
     for (long long tb = t0; tb < t0 + g.nsteps; tb += K) {
         const int cnt = (t0 + g.nsteps - tb) < K ? static_cast<int>(t0 + g.nsteps - tb) : K;
         const uint32_t tm = static_cast<uint32_t>(tb) & mask;
+        // monitor schedule of the block (one 64-bit division per block, not per step):
+        // BOLD sample after step t when (t + 1) % bold_period == 0, trace before step t
+        // when t % trace_every == 0
+        const int b_first = static_cast<int>((bper - 1) - tb % bper);       // k of the first sample
+        const long long b_row0 = (tb + b_first + 1) / bper - 1;
+        const int tr_first = static_cast<int>((tev - tb % tev) % tev);
+        const long long tr_row0 = (tb + tr_first) / tev;
         for (int r = 0; r < rounds; ++r) {
             const int q = q0 + r * stride;
             const bool valid = q < N;
@@ -260,16 +269,20 @@ __device__ __forceinline__ void run_group(const tvbg_group& g, float* csum, int3
                 bV = g.bold[(2 * N + n) * kLanes + l];
                 bQ = g.bold[(3 * N + n) * kLanes + l];
             }
+            float* __restrict__ rrow = ring + static_cast<size_t>(n) * R * kLanes + l;
             float obs0 = M::obs(x, 0);
             float zz[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+            int b_next = b_first, tr_next = tr_first;
+            long long b_row = b_row0, tr_row = tr_row0;
+            const int kend = (t_end - tb) < cnt ? static_cast<int>(t_end - tb) : cnt;
 #pragma unroll 1
-            for (int k = 0; k < cnt; ++k) {
+            for (int k = 0; k < kend; ++k) {
                 const long long t = tb + k;
-                if (t >= t_end) break;
-                if (trace && t % g.trace_every == 0) {
-                    const long long row = (t / g.trace_every) % g.trace_len;
-                    float* dst = g.trace + ((row * N + n) * g.trace_nobs) * kLanes + l;
+                if (trace && k == tr_next) {
+                    float* dst = g.trace + (((tr_row % g.trace_len) * N + n) * g.trace_nobs) * kLanes + l;
                     for (int o = 0; o < g.trace_nobs; ++o) dst[o * kLanes] = M::obs(x, o);
+                    tr_next += tev;
+                    tr_row += 1;
                 }
                 const float xbold = bold ? M::obs(x, g.bold_obs) : 0.0f;
                 const float c = lane_post<CF>(csum[k * blockDim.x + threadIdx.x], obs0, wsum, cf_a,
@@ -279,7 +292,7 @@ __device__ __forceinline__ void run_group(const tvbg_group& g, float* csum, int3
 #pragma unroll
                 for (int v = 0; v < NS; ++v) x[v] = fmaf(dt, f[v], x[v]);
                 if (noise) {
-                    const int r0 = static_cast<int>(t % SPC);
+                    const int r0 = static_cast<int>(t & (SPC - 1));
                     if (k == 0 || r0 == 0) {
                         const u32x4 w = philox4x32_10(static_cast<uint32_t>(n),
                                                       static_cast<uint32_t>(t / SPC), g.seed_hi, 0u,
@@ -294,15 +307,15 @@ __device__ __forceinline__ void run_group(const tvbg_group& g, float* csum, int3
                 M::limit(x, flags);
                 obs0 = M::obs(x, 0);
                 const uint32_t pos = (static_cast<uint32_t>(t) + 1u) & mask;
-                const size_t idx = (static_cast<size_t>(n) * R + pos) * kLanes + l;
-                ring[idx] = obs0;
-                if (pos < kGhost) ring[idx + static_cast<size_t>(nh) * kLanes] = obs0;
+                rrow[pos * kLanes] = obs0;
+                if (pos < kGhost) rrow[(pos + nh) * kLanes] = obs0;
                 if (bold) {
                     Balloon::step(bs, bF, bV, bQ, xbold, g.dt_bold);
-                    if ((t + 1) % g.bold_period == 0) {
-                        const long long row = (t + 1) / g.bold_period - 1;
-                        if (row >= 0 && row < g.bold_len)
-                            g.bold_out[(row * N + n) * kLanes + l] = Balloon::signal(bV, bQ);
+                    if (k == b_next) {
+                        if (b_row >= 0 && b_row < g.bold_len)
+                            g.bold_out[(b_row * N + n) * kLanes + l] = Balloon::signal(bV, bQ);
+                        b_next += bper;
+                        b_row += 1;
                     }
                 }
             }

@@ -239,6 +239,7 @@ class GroupSet:
         self.threads, self.cluster, self.slices = group_shape(N, threads, cluster, slices)
         self.status = DeviceStatus()
         self._uploaded = None
+        self._streams = None
 
     def bold_obs(self):
         "Observable feeding the balloon: V for G2DO (tvb_hpc order W, V), else obs 0."
@@ -369,11 +370,24 @@ class GroupSet:
         return launches, gmax
 
     def launch(self, launches=None, stream=None):
+        """Enqueue the prepared launches on `stream` (a torch stream, default
+        the current one); launches of different block lengths run
+        concurrently on forked streams joined back into `stream`."""
+        torch = self.torch
         lib = nat.load()
         launches = launches if launches is not None else self._uploaded[0]
-        sh = nat.stream_handle(stream)
-        for dev, order, n, cfg in launches:
-            nat.check(lib.tvbg_group_run(dev.data_ptr(), n, ctypes.byref(cfg), sh))
+        main = stream if stream is not None else torch.cuda.current_stream()
+        if len(launches) == 1:
+            dev, order, n, cfg = launches[0]
+            nat.check(lib.tvbg_group_run(dev.data_ptr(), n, ctypes.byref(cfg), main.cuda_stream))
+            return
+        if self._streams is None or len(self._streams) < len(launches):
+            self._streams = [torch.cuda.Stream() for _ in launches]
+        for (dev, order, n, cfg), st in zip(launches, self._streams):
+            st.wait_stream(main)
+            nat.check(lib.tvbg_group_run(dev.data_ptr(), n, ctypes.byref(cfg), st.cuda_stream))
+        for st in self._streams[:len(launches)]:
+            main.wait_stream(st)
 
     def advance(self, gmax):
         "Move the group clocks after a launch of the prepared tables."
