@@ -226,18 +226,19 @@ __device__ __forceinline__ void run_group(const tvbg_group& g, float* csum, int3
     }
     group_barrier(cluster);
 
+    // monitor schedule as 32-bit counters carried across blocks (the 64-bit
+    // divisions run once per kernel): BOLD sample after step t when
+    // (t + 1) % bold_period == 0, trace row before step t when
+    // t % trace_every == 0
     const int bper = g.bold_period > 0 ? g.bold_period : 1;
     const int tev = g.trace_every > 0 ? g.trace_every : 1;
+    int b_until = bold ? static_cast<int>((bper - 1) - t0 % bper) : 0;  // steps to the next sample
+    int b_row = bold ? static_cast<int>((t0 + b_until + 1) / bper - 1) : 0;
+    int tr_until = trace ? static_cast<int>((tev - t0 % tev) % tev) : 0;
+    int tr_row = trace ? static_cast<int>(((t0 + tr_until) / tev) % g.trace_len) : 0;
     for (long long tb = t0; tb < t0 + g.nsteps; tb += K) {
         const int cnt = (t0 + g.nsteps - tb) < K ? static_cast<int>(t0 + g.nsteps - tb) : K;
         const uint32_t tm = static_cast<uint32_t>(tb) & mask;
-        // monitor schedule of the block (one 64-bit division per block, not per step):
-        // BOLD sample after step t when (t + 1) % bold_period == 0, trace before step t
-        // when t % trace_every == 0
-        const int b_first = static_cast<int>((bper - 1) - tb % bper);       // k of the first sample
-        const long long b_row0 = (tb + b_first + 1) / bper - 1;
-        const int tr_first = static_cast<int>((tev - tb % tev) % tev);
-        const long long tr_row0 = (tb + tr_first) / tev;
         for (int r = 0; r < rounds; ++r) {
             const int q = q0 + r * stride;
             const bool valid = q < N;
@@ -272,17 +273,17 @@ __device__ __forceinline__ void run_group(const tvbg_group& g, float* csum, int3
             float* __restrict__ rrow = ring + static_cast<size_t>(n) * R * kLanes + l;
             float obs0 = M::obs(x, 0);
             float zz[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-            int b_next = b_first, tr_next = tr_first;
-            long long b_row = b_row0, tr_row = tr_row0;
+            int b_next = b_until, tr_next = tr_until;
+            int brow = b_row, trow = tr_row;
             const int kend = (t_end - tb) < cnt ? static_cast<int>(t_end - tb) : cnt;
 #pragma unroll 1
             for (int k = 0; k < kend; ++k) {
                 const long long t = tb + k;
                 if (trace && k == tr_next) {
-                    float* dst = g.trace + (((tr_row % g.trace_len) * N + n) * g.trace_nobs) * kLanes + l;
+                    float* dst = g.trace + ((static_cast<size_t>(trow) * N + n) * g.trace_nobs) * kLanes + l;
                     for (int o = 0; o < g.trace_nobs; ++o) dst[o * kLanes] = M::obs(x, o);
                     tr_next += tev;
-                    tr_row += 1;
+                    trow = trow + 1 == g.trace_len ? 0 : trow + 1;
                 }
                 const float xbold = bold ? M::obs(x, g.bold_obs) : 0.0f;
                 const float c = lane_post<CF>(csum[k * blockDim.x + threadIdx.x], obs0, wsum, cf_a,
@@ -312,10 +313,11 @@ __device__ __forceinline__ void run_group(const tvbg_group& g, float* csum, int3
                 if (bold) {
                     Balloon::step(bs, bF, bV, bQ, xbold, g.dt_bold);
                     if (k == b_next) {
-                        if (b_row >= 0 && b_row < g.bold_len)
-                            g.bold_out[(b_row * N + n) * kLanes + l] = Balloon::signal(bV, bQ);
+                        if (brow >= 0 && brow < g.bold_len)
+                            g.bold_out[(static_cast<size_t>(brow) * N + n) * kLanes + l] =
+                                Balloon::signal(bV, bQ);
                         b_next += bper;
-                        b_row += 1;
+                        brow += 1;
                     }
                 }
             }
@@ -327,6 +329,21 @@ __device__ __forceinline__ void run_group(const tvbg_group& g, float* csum, int3
                 g.bold[(2 * N + n) * kLanes + l] = bV;
                 g.bold[(3 * N + n) * kLanes + l] = bQ;
             }
+        }
+        // advance the monitor counters past this block
+        if (bold) {
+            while (b_until < cnt) {
+                b_until += bper;
+                b_row += 1;
+            }
+            b_until -= cnt;
+        }
+        if (trace) {
+            while (tr_until < cnt) {
+                tr_until += tev;
+                tr_row = tr_row + 1 == g.trace_len ? 0 : tr_row + 1;
+            }
+            tr_until -= cnt;
         }
         group_barrier(cluster);
     }
