@@ -177,14 +177,14 @@ def test_group_plan_and_shape():
     with pytest.raises(ValueError):
         groups.plan_group(5, 10, block_k=8)
     for N in (1, 4, 20, 68, 84, 128, 192, 300, 400, 998):
-        for sl in (None, 1, 2, 4):
-            thr, cl, s = groups.group_shape(N, slices=sl)
-            assert s == (sl or 1) and thr % (8 * s) == 0 and 32 <= thr <= 1024 and 1 <= cl <= 8
-            assert cl * (thr // (8 * s)) >= N or thr == 1024
-    for N, shape in [(68, (544, 1, 1)), (84, (672, 1, 1)), (128, (1024, 1, 1)),
-                     (192, (768, 2, 1)), (400, (800, 4, 1)), (998, (1024, 8, 1))]:
+        thr, cl = groups.group_shape(N)
+        assert thr % 32 == 0 and 32 <= thr <= 1024 and 1 <= cl <= 8
+        assert cl * (thr // 8) >= N or thr == 1024
+    for N, shape in [(68, (544, 1)), (84, (672, 1)), (128, (1024, 1)),
+                     (192, (768, 2)), (400, (800, 4)), (998, (1024, 8))]:
         assert groups.group_shape(N) == shape
-    assert groups.group_shape(84, threads=672) == (672, 1, 1)
+    assert groups.group_shape(84, threads=672) == (672, 1)
+    assert groups.group_shape(84, threads=128) == (128, 6)
 
 
 def test_plan_ring_constraints():

@@ -61,12 +61,11 @@ def check(gs, x0, nsteps):
     return ref
 
 
-@pytest.mark.parametrize('slices', [1, 2, 4])
-def test_groups_g2dosc_diff_noise(cuda, slices):
-    gs, x0 = make(gkw=dict(slices=slices))
+@pytest.mark.parametrize('runs', [0, 1, 3])
+def test_groups_g2dosc_diff_noise(cuda, runs):
+    gs, x0 = make(gkw=dict(runs=runs))
     assert set(gs.block_k) == {4, 8}          # speed 20: d_min = 5 -> K = 4
     assert gs.n_groups == 4                    # 10 + 10 instances -> 8 + 2 per speed
-    assert gs.slices == slices
     check(gs, x0, 403)
 
 
@@ -96,13 +95,12 @@ def test_groups_ragged_steps(cuda):
     assert rel_err(gs.state.cpu().numpy(), ref['state']) < TOL
 
 
-@pytest.mark.parametrize('N,threads,cluster,slices', [(300, None, None, None), (300, 1024, 2, 1),
-                                                      (998, None, None, None), (84, 128, 1, 1),
-                                                      (84, 96, 2, 2), (84, 64, 4, 4),
-                                                      (192, None, 8, 4)])
-def test_groups_clusters_and_multinode_threads(cuda, N, threads, cluster, slices):
+@pytest.mark.parametrize('N,threads,cluster', [(300, None, None), (300, 1024, 2),
+                                               (998, None, None), (84, 128, 1), (84, 96, 2),
+                                               (84, 64, 4), (192, None, 8)])
+def test_groups_clusters_and_multinode_threads(cuda, N, threads, cluster):
     gs, x0 = make('MPR', 'Linear', I=9, N=N, density=0.05 if N > 500 else 0.15, speeds=(4.0, ),
-                  gkw=dict(threads=threads, cluster=cluster, slices=slices))
+                  gkw=dict(threads=threads, cluster=cluster))
     if cluster:
         assert gs.cluster == cluster
     check(gs, x0, 200)

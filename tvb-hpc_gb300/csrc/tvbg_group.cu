@@ -2,27 +2,29 @@
 #include <cstring>
 
 #include "tvbg_abi_internal.h"
+#include "tvbg_lanes.cuh"
 
 using namespace tvbg;
 
 namespace {
 
-GroupKernel lookup_group(int model, int cfun, int k, int slices) {
+GroupKernel lookup_group(int model, int cfun, int k) {
     switch (model) {
-        case TVBG_MODEL_G2DO: return group_kernel_g2do(cfun, k, slices);
-        case TVBG_MODEL_MPR: return group_kernel_mpr(cfun, k, slices);
-        case TVBG_MODEL_LINEAR: return group_kernel_linear(cfun, k, slices);
-        case TVBG_MODEL_G2DOSC: return group_kernel_g2dosc(cfun, k, slices);
+        case TVBG_MODEL_G2DO: return group_kernel_g2do(cfun, k);
+        case TVBG_MODEL_MPR: return group_kernel_mpr(cfun, k);
+        case TVBG_MODEL_LINEAR: return group_kernel_linear(cfun, k);
+        case TVBG_MODEL_G2DOSC: return group_kernel_g2dosc(cfun, k);
         default: return nullptr;
     }
 }
 
-// Dynamic shared memory of a group launch: the K coupling sums of every thread.
-size_t group_smem_bytes(const tvbg_launch* cfg) {
-    return 4u * static_cast<size_t>(cfg->block_k) * static_cast<size_t>(cfg->threads);
-}
+constexpr int kMaxRunsPerStage = 8;
+constexpr size_t kStaticSlack = 1024;  // the kernel's static shared memory (descriptor) + slack
 
-int check_group_launch(const tvbg_launch* cfg, GroupKernel* kfn, int* cluster) {
+// Validate a group launch and size its dynamic shared memory: `ec` edge runs
+// per stage (cfg->nmax, or the most that fit, at most 8).
+int check_group_launch(const tvbg_launch* cfg, GroupKernel* kfn, int* cluster, int* ec,
+                       size_t* smem) {
     if (!cfg) return set_error(TVBG_EINVAL, "null launch config");
     if (cfg->threads < 32 || cfg->threads > 1024 || (cfg->threads & 31))
         return set_error(TVBG_EINVAL, "threads must be a multiple of 32 in [32, 1024]");
@@ -30,16 +32,27 @@ int check_group_launch(const tvbg_launch* cfg, GroupKernel* kfn, int* cluster) {
         return set_error(TVBG_EINVAL, "tvbg_group_run: block_k must be 4 or 8");
     const int c = cfg->cluster <= 0 ? 1 : cfg->cluster;
     if (c < 1 || c > 8) return set_error(TVBG_EINVAL, "cluster must be in [1, 8]");
-    const int slices = cfg->tpn <= 0 ? 1 : cfg->tpn;
-    if (slices != 1 && slices != 2 && slices != 4)
-        return set_error(TVBG_EINVAL, "tvbg_group_run: tpn (edge slices per node) must be 0, 1, 2 or 4");
-    if (cfg->threads % (8 * slices))
-        return set_error(TVBG_EINVAL, "tvbg_group_run: threads must be a multiple of 8 * tpn");
-    *kfn = lookup_group(cfg->model, cfg->cfun, cfg->block_k, slices);
+    if (cfg->tpn > 1) return set_error(TVBG_EINVAL, "tvbg_group_run: tpn must be 0 or 1");
+    if (cfg->nmax < 0 || cfg->nmax > kMaxRunsPerStage)
+        return set_error(TVBG_EINVAL, "tvbg_group_run: nmax (edge runs per stage) must be in [0, 8]");
+    *kfn = lookup_group(cfg->model, cfg->cfun, cfg->block_k);
     if (!*kfn)
-        return set_error(TVBG_EUNSUPPORTED,
-                         "group kernel not built for this model/coupling/block_k/slices");
+        return set_error(TVBG_EUNSUPPORTED, "group kernel not built for this model/coupling/block_k");
+    int dev = 0, optin = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (e != cudaSuccess) return set_cuda_error(e, "tvbg_group_run: device attributes");
+    int runs = cfg->nmax;
+    if (runs == 0) {
+        for (runs = kMaxRunsPerStage; runs > 0; --runs)
+            if (group_smem_bytes(cfg->block_k, cfg->threads, runs) + kStaticSlack <= static_cast<size_t>(optin))
+                break;
+    }
+    if (runs < 1 || group_smem_bytes(cfg->block_k, cfg->threads, runs) + kStaticSlack > static_cast<size_t>(optin))
+        return set_error(TVBG_EINVAL, "tvbg_group_run: the gather stages do not fit shared memory");
     *cluster = c;
+    *ec = runs;
+    *smem = group_smem_bytes(cfg->block_k, cfg->threads, runs);
     return TVBG_OK;
 }
 
@@ -77,17 +90,22 @@ int tvbg_pack_edges_group(int32_t N, int32_t nnz, const int32_t* row, const int3
 int tvbg_group_run(const tvbg_group* d_groups, int32_t n_groups, const tvbg_launch* cfg,
                    void* stream) {
     GroupKernel kfn = nullptr;
-    int cluster = 1;
-    int rc = check_group_launch(cfg, &kfn, &cluster);
+    int cluster = 1, ec = 0;
+    size_t smem = 0;
+    int rc = check_group_launch(cfg, &kfn, &cluster, &ec, &smem);
     if (rc) return rc;
     if (n_groups < 0 || (n_groups > 0 && !d_groups))
         return set_error(TVBG_EINVAL, "tvbg_group_run: bad group array");
     if (n_groups == 0) return TVBG_OK;
+    cudaError_t e = cudaFuncSetAttribute(reinterpret_cast<const void*>(kfn),
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(smem));
+    if (e != cudaSuccess) return set_cuda_error(e, "tvbg_group_run: smem attribute");
     cudaLaunchConfig_t lc;
     std::memset(&lc, 0, sizeof(lc));
     lc.gridDim = dim3(static_cast<unsigned>(n_groups) * static_cast<unsigned>(cluster), 1, 1);
     lc.blockDim = dim3(static_cast<unsigned>(cfg->threads), 1, 1);
-    lc.dynamicSmemBytes = group_smem_bytes(cfg);
+    lc.dynamicSmemBytes = smem;
     lc.stream = static_cast<cudaStream_t>(stream);
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -96,7 +114,8 @@ int tvbg_group_run(const tvbg_group* d_groups, int32_t n_groups, const tvbg_laun
     attr[0].val.clusterDim.z = 1;
     lc.attrs = attr;
     lc.numAttrs = cluster > 1 ? 1 : 0;
-    cudaError_t e = cudaLaunchKernelEx(&lc, kfn, d_groups, n_groups, cfg->d_order, cfg->d_status);
+    e = cudaLaunchKernelEx(&lc, kfn, d_groups, n_groups, cfg->d_order, cfg->d_status,
+                           static_cast<int32_t>(ec));
     if (e != cudaSuccess) return set_cuda_error(e, "group kernel launch");
     return TVBG_OK;
 }
@@ -104,12 +123,17 @@ int tvbg_group_run(const tvbg_group* d_groups, int32_t n_groups, const tvbg_laun
 int tvbg_group_occupancy(const tvbg_launch* cfg, int32_t* ctas_per_sm, int32_t* sms) {
     if (!ctas_per_sm || !sms) return set_error(TVBG_EINVAL, "tvbg_group_occupancy: null");
     GroupKernel kfn = nullptr;
-    int cluster = 1;
-    int rc = check_group_launch(cfg, &kfn, &cluster);
+    int cluster = 1, ec = 0;
+    size_t smem = 0;
+    int rc = check_group_launch(cfg, &kfn, &cluster, &ec, &smem);
     if (rc) return rc;
+    cudaError_t e = cudaFuncSetAttribute(reinterpret_cast<const void*>(kfn),
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(smem));
+    if (e != cudaSuccess) return set_cuda_error(e, "tvbg_group_occupancy: smem attribute");
     int n = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-        &n, reinterpret_cast<const void*>(kfn), cfg->threads, group_smem_bytes(cfg));
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, reinterpret_cast<const void*>(kfn),
+                                                      cfg->threads, smem);
     if (e != cudaSuccess) return set_cuda_error(e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
     int dev = 0, nsm = 0;
     e = cudaGetDevice(&dev);

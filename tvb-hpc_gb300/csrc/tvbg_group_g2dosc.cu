@@ -1,40 +1,24 @@
 // Lane-interleaved group kernels for the G2DOsc model: separable couplings
-// (LINEAR, DIFF, SIGMOIDAL) x block length 4, 8 x edge slices 1, 2, 4.
+// (LINEAR, DIFF, SIGMOIDAL) x block length 4, 8 (TMA-staged gather).
 #include "tvbg_abi_internal.h"
 #include "tvbg_lanes.cuh"
 
 namespace tvbg {
 
-// slices: edge slices per node (1, 2 or 4); the sigmoidal coupling (an
-// expf per value) is built with one slice only
-template <int CF, int K>
-static GroupKernel pick_s(int slices) {
-    if constexpr (CF == TVBG_CFUN_SIGMOIDAL) {
-        return slices == 1 ? group_kernel<G2DOsc, CF, K, 1> : nullptr;
-    } else {
-        switch (slices) {
-            case 1: return group_kernel<G2DOsc, CF, K, 1>;
-            case 2: return group_kernel<G2DOsc, CF, K, 2>;
-            case 4: return group_kernel<G2DOsc, CF, K, 4>;
-            default: return nullptr;
-        }
-    }
-}
-
 template <int CF>
-static GroupKernel pick_k(int k, int slices) {
+static GroupKernel pick_k(int k) {
     switch (k) {
-        case 4: return pick_s<CF, 4>(slices);
-        case 8: return pick_s<CF, 8>(slices);
+        case 4: return group_kernel<G2DOsc, CF, 4>;
+        case 8: return group_kernel<G2DOsc, CF, 8>;
         default: return nullptr;
     }
 }
 
-GroupKernel group_kernel_g2dosc(int cfun, int k, int slices) {
+GroupKernel group_kernel_g2dosc(int cfun, int k) {
     switch (cfun) {
-        case TVBG_CFUN_LINEAR: return pick_k<TVBG_CFUN_LINEAR>(k, slices);
-        case TVBG_CFUN_DIFF: return pick_k<TVBG_CFUN_DIFF>(k, slices);
-        case TVBG_CFUN_SIGMOIDAL: return pick_k<TVBG_CFUN_SIGMOIDAL>(k, slices);
+        case TVBG_CFUN_LINEAR: return pick_k<TVBG_CFUN_LINEAR>(k);
+        case TVBG_CFUN_DIFF: return pick_k<TVBG_CFUN_DIFF>(k);
+        case TVBG_CFUN_SIGMOIDAL: return pick_k<TVBG_CFUN_SIGMOIDAL>(k);
         default: return nullptr;
     }
 }

@@ -43,29 +43,22 @@ def plan_group(dmin, dmax, block_k=None):
     return k, int(np.log2(nh))
 
 
-def group_shape(N, threads=None, cluster=None, slices=None):
-    """(threads, cluster, slices) of a group launch: one node per slot of
-    8 * slices lanes, on the smallest cluster (<= 8 CTAs) whose CTAs stay
-    within 1024 threads; beyond 8 CTAs the slots take several nodes.
-    Measured on the uneven batch and the 64 x 64 grid, this beats packing
-    more, smaller CTAs per SM (the gather is bound by the memory system,
-    not by resident threads), and one slice beats more when the GPU is full
-    (extra slices only shorten a single group's critical path)."""
-    slices = 1 if slices is None else int(slices)
-    lanes = L * slices
+def group_shape(N, threads=None, cluster=None):
+    """(threads, cluster) of a group launch: one node per 8-lane slot, on the
+    smallest cluster (<= 8 CTAs) whose CTAs stay within 1024 threads; beyond
+    8 CTAs the slots take several nodes.  Measured on the uneven batch and
+    the 64 x 64 grid, this beats packing more, smaller CTAs per SM."""
     if cluster is None:
         if threads is not None:
-            cluster = min(8, -(-N // (int(threads) // lanes)))
+            cluster = min(8, -(-N // (int(threads) // L)))
         else:
             cluster = 1
-            while lanes * -(-N // cluster) > 1024 and cluster < 8:
+            while L * -(-N // cluster) > 1024 and cluster < 8:
                 cluster *= 2
     if threads is None:
         per = -(-N // int(cluster))
-        threads = min(1024 // lanes * lanes, 32 * -(-(lanes * per) // 32))
-    if int(threads) % lanes:
-        raise ValueError('threads must be a multiple of 8 * slices')
-    return int(threads), int(cluster), slices
+        threads = min(1024, 32 * -(-(L * per) // 32))
+    return int(threads), int(cluster)
 
 
 def group_occupancy(cfg):
@@ -86,9 +79,9 @@ class GroupSet:
       nsteps  : optional (I,) step counts, used to put instances of similar
                 length into the same group (longest first);
       block_k : 4 or 8 steps per barrier (default: 8 when d_min >= 7);
-      threads, cluster, slices : launch shape (default: group_shape);
-                slices = threads per (node, instance) in the gather (1, 2,
-                4; the sigmoidal coupling uses 1).
+      threads, cluster : launch shape (default: group_shape);
+      runs    : edge runs per stage of the TMA gather (default: the most
+                that fit shared memory, at most 8).
     Couplings must be separable (Linear, Diff, Sigmoidal); the Kuramoto
     model and the Track-A order run on the per-instance kernels.
 
@@ -100,7 +93,7 @@ class GroupSet:
                  nparam=None, delays=None, rounding='ceil', seed=0, inst_ids=None,
                  bold_period=0, bold_len=0, trace_every=0, trace_len=0, trace_nobs=None,
                  flags=0, cf_b=None, t0=0, nsteps=None, block_k=None, threads=None,
-                 cluster=None, history='zero', slices=None):
+                 cluster=None, history='zero', runs=0):
         _device_ok()
         torch = _torch()
         self.torch = torch
@@ -234,9 +227,8 @@ class GroupSet:
         self.cf_b = np.float32(cf_b if cf_b is not None else
                                (cf_b0 if isinstance(cf_b0, (int, float, np.number)) else 0.0))
         self.t = np.full(G, int(t0), np.int64)
-        if self.cfun_id == nat.CFUN_SIGMOIDAL:
-            slices = 1
-        self.threads, self.cluster, self.slices = group_shape(N, threads, cluster, slices)
+        self.threads, self.cluster = group_shape(N, threads, cluster)
+        self.runs = int(runs)
         self.status = DeviceStatus()
         self._uploaded = None
         self._streams = None
@@ -349,7 +341,7 @@ class GroupSet:
         cfg.model, cfg.cfun = self.model_id, self.cfun_id
         cfg.threads, cfg.cluster = self.threads, self.cluster
         cfg.block_k = int(block_k)
-        cfg.tpn = self.slices
+        cfg.nmax = self.runs
         cfg.d_status = self.status.t.data_ptr()
         cfg.d_order = order.data_ptr() if order is not None else None
         return cfg
