@@ -327,7 +327,7 @@ class MixedStep:
         return self.n_launch
 
 
-def build_groups(wl, runs=0):
+def build_groups(wl):
     from tvb_hpc import model, coupling, scheme, groups
     m = getattr(model, wl['model'])()
     cf = getattr(coupling, wl['cfun'])(m)
@@ -335,7 +335,7 @@ def build_groups(wl, runs=0):
     return groups.GroupSet(m, cf, scm, wl['conn'], dt=wl['dt'], couplings=wl['couplings'],
                            speeds=wl['speeds'], state0=wl['x0'], nparam=wl.get('nparam'),
                            seed=wl['seed'], bold_period=wl['bold_period'],
-                           bold_len=wl['bold_len'], runs=runs)
+                           bold_len=wl['bold_len'])
 
 
 def groups_supported(wl):
@@ -353,9 +353,9 @@ class GpuStep:
         self.wl = wl
         self.groups = path == 'groups' and groups_supported(wl)
         if self.groups:
-            self.sw = build_groups(wl, tpn or 0)
+            self.sw = build_groups(wl)
             self.launches = self.sw.prepare(wl['nsteps'])[0]
-            self.tpn = self.sw.runs
+            self.tpn = None
         else:
             self.sw = build_sweep(wl, tpn, warps)
             self.sw.pick_tpn()

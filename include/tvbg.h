@@ -413,10 +413,8 @@ int tvbg_pack_edges_group(int32_t N, int32_t nnz, const int32_t *row,
 /*
  * Run the groups d_groups[0..n_groups): cfg->cluster CTAs of cfg->threads
  * threads per group (a thread-block cluster when > 1), group of cluster c =
- * d_order[c] (or c).  cfg->block_k = 4 or 8; cfg->nmax = edge runs per
- * stage of the TMA gather (1..8; 0 = the most that fit the CTA's shared
- * memory); cfg->tpn must be 0 or 1; smem_ring, ctas and d_counter are not
- * used.  Graph-capturable.
+ * d_order[c] (or c).  cfg->block_k = 4 or 8; cfg->tpn must be 0 or 1;
+ * smem_ring, ctas, nmax and d_counter are not used.  Graph-capturable.
  */
 int tvbg_group_run(const tvbg_group *d_groups, int32_t n_groups,
                    const tvbg_launch *cfg, void *stream);

@@ -61,9 +61,8 @@ def check(gs, x0, nsteps):
     return ref
 
 
-@pytest.mark.parametrize('runs', [0, 1, 3])
-def test_groups_g2dosc_diff_noise(cuda, runs):
-    gs, x0 = make(gkw=dict(runs=runs))
+def test_groups_g2dosc_diff_noise(cuda):
+    gs, x0 = make()
     assert set(gs.block_k) == {4, 8}          # speed 20: d_min = 5 -> K = 4
     assert gs.n_groups == 4                    # 10 + 10 instances -> 8 + 2 per speed
     check(gs, x0, 403)

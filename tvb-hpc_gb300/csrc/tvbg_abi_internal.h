@@ -33,9 +33,8 @@ BlockedKernel blocked_kernel_g2do(int cfun, int tpn, int k);
 BlockedKernel blocked_kernel_mpr(int cfun, int tpn, int k);
 BlockedKernel blocked_kernel_linear(int cfun, int tpn, int k);
 BlockedKernel blocked_kernel_g2dosc(int cfun, int tpn, int k);
-// Lane-interleaved group kernel signature (last argument: edge runs per
-// stage of the TMA gather) and per-model lookup for (cfun, K).
-using GroupKernel = void (*)(const tvbg_group*, int32_t, const int32_t*, int32_t*, int32_t);
+// Lane-interleaved group kernel signature and per-model lookup for (cfun, K).
+using GroupKernel = void (*)(const tvbg_group*, int32_t, const int32_t*, int32_t*);
 GroupKernel group_kernel_g2do(int cfun, int k);
 GroupKernel group_kernel_mpr(int cfun, int k);
 GroupKernel group_kernel_linear(int cfun, int k);

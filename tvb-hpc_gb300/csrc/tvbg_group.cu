@@ -18,13 +18,9 @@ GroupKernel lookup_group(int model, int cfun, int k) {
     }
 }
 
-constexpr int kMaxRunsPerStage = 8;
-constexpr size_t kStaticSlack = 1024;  // the kernel's static shared memory (descriptor) + slack
-
-// Validate a group launch and size its dynamic shared memory: `ec` edge runs
-// per stage (cfg->nmax, or the most that fit, at most 8).
-int check_group_launch(const tvbg_launch* cfg, GroupKernel* kfn, int* cluster, int* ec,
-                       size_t* smem) {
+// Validate a group launch; its dynamic shared memory holds the K coupling
+// sums of every thread.
+int check_group_launch(const tvbg_launch* cfg, GroupKernel* kfn, int* cluster, size_t* smem) {
     if (!cfg) return set_error(TVBG_EINVAL, "null launch config");
     if (cfg->threads < 32 || cfg->threads > 1024 || (cfg->threads & 31))
         return set_error(TVBG_EINVAL, "threads must be a multiple of 32 in [32, 1024]");
@@ -33,26 +29,11 @@ int check_group_launch(const tvbg_launch* cfg, GroupKernel* kfn, int* cluster, i
     const int c = cfg->cluster <= 0 ? 1 : cfg->cluster;
     if (c < 1 || c > 8) return set_error(TVBG_EINVAL, "cluster must be in [1, 8]");
     if (cfg->tpn > 1) return set_error(TVBG_EINVAL, "tvbg_group_run: tpn must be 0 or 1");
-    if (cfg->nmax < 0 || cfg->nmax > kMaxRunsPerStage)
-        return set_error(TVBG_EINVAL, "tvbg_group_run: nmax (edge runs per stage) must be in [0, 8]");
     *kfn = lookup_group(cfg->model, cfg->cfun, cfg->block_k);
     if (!*kfn)
         return set_error(TVBG_EUNSUPPORTED, "group kernel not built for this model/coupling/block_k");
-    int dev = 0, optin = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    if (e != cudaSuccess) return set_cuda_error(e, "tvbg_group_run: device attributes");
-    int runs = cfg->nmax;
-    if (runs == 0) {
-        for (runs = kMaxRunsPerStage; runs > 0; --runs)
-            if (group_smem_bytes(cfg->block_k, cfg->threads, runs) + kStaticSlack <= static_cast<size_t>(optin))
-                break;
-    }
-    if (runs < 1 || group_smem_bytes(cfg->block_k, cfg->threads, runs) + kStaticSlack > static_cast<size_t>(optin))
-        return set_error(TVBG_EINVAL, "tvbg_group_run: the gather stages do not fit shared memory");
     *cluster = c;
-    *ec = runs;
-    *smem = group_smem_bytes(cfg->block_k, cfg->threads, runs);
+    *smem = group_smem_bytes(cfg->block_k, cfg->threads);
     return TVBG_OK;
 }
 
@@ -90,17 +71,14 @@ int tvbg_pack_edges_group(int32_t N, int32_t nnz, const int32_t* row, const int3
 int tvbg_group_run(const tvbg_group* d_groups, int32_t n_groups, const tvbg_launch* cfg,
                    void* stream) {
     GroupKernel kfn = nullptr;
-    int cluster = 1, ec = 0;
+    int cluster = 1;
     size_t smem = 0;
-    int rc = check_group_launch(cfg, &kfn, &cluster, &ec, &smem);
+    int rc = check_group_launch(cfg, &kfn, &cluster, &smem);
     if (rc) return rc;
     if (n_groups < 0 || (n_groups > 0 && !d_groups))
         return set_error(TVBG_EINVAL, "tvbg_group_run: bad group array");
     if (n_groups == 0) return TVBG_OK;
-    cudaError_t e = cudaFuncSetAttribute(reinterpret_cast<const void*>(kfn),
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         static_cast<int>(smem));
-    if (e != cudaSuccess) return set_cuda_error(e, "tvbg_group_run: smem attribute");
+    cudaError_t e = cudaSuccess;
     cudaLaunchConfig_t lc;
     std::memset(&lc, 0, sizeof(lc));
     lc.gridDim = dim3(static_cast<unsigned>(n_groups) * static_cast<unsigned>(cluster), 1, 1);
@@ -114,8 +92,7 @@ int tvbg_group_run(const tvbg_group* d_groups, int32_t n_groups, const tvbg_laun
     attr[0].val.clusterDim.z = 1;
     lc.attrs = attr;
     lc.numAttrs = cluster > 1 ? 1 : 0;
-    e = cudaLaunchKernelEx(&lc, kfn, d_groups, n_groups, cfg->d_order, cfg->d_status,
-                           static_cast<int32_t>(ec));
+    e = cudaLaunchKernelEx(&lc, kfn, d_groups, n_groups, cfg->d_order, cfg->d_status);
     if (e != cudaSuccess) return set_cuda_error(e, "group kernel launch");
     return TVBG_OK;
 }
@@ -123,15 +100,12 @@ int tvbg_group_run(const tvbg_group* d_groups, int32_t n_groups, const tvbg_laun
 int tvbg_group_occupancy(const tvbg_launch* cfg, int32_t* ctas_per_sm, int32_t* sms) {
     if (!ctas_per_sm || !sms) return set_error(TVBG_EINVAL, "tvbg_group_occupancy: null");
     GroupKernel kfn = nullptr;
-    int cluster = 1, ec = 0;
+    int cluster = 1;
     size_t smem = 0;
-    int rc = check_group_launch(cfg, &kfn, &cluster, &ec, &smem);
+    int rc = check_group_launch(cfg, &kfn, &cluster, &smem);
     if (rc) return rc;
-    cudaError_t e = cudaFuncSetAttribute(reinterpret_cast<const void*>(kfn),
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         static_cast<int>(smem));
-    if (e != cudaSuccess) return set_cuda_error(e, "tvbg_group_occupancy: smem attribute");
     int n = 0;
+    cudaError_t e = cudaSuccess;
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, reinterpret_cast<const void*>(kfn),
                                                       cfg->threads, smem);
     if (e != cudaSuccess) return set_cuda_error(e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor");

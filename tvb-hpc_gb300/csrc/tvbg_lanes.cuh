@@ -31,18 +31,15 @@
 // block starts; with nh >= d_max + 1 + K no slot written in a block aliases
 // one read in it.  The cluster meets at one barrier per block.
 //
-// Gather by TMA.  The K slots of one edge for the 8 lanes are one
-// contiguous run of K * 32 bytes of the source node's ring row.  Lane 0 of
-// each node slot stages the runs of its node's in-edges into shared memory
-// with cp.async.bulk (one copy per edge, completion on an mbarrier), in
-// chunks of `ec` edges through two stages, so 2 ec runs per node are in
-// flight while the 8 lanes accumulate the chunk before; the sums of the
-// block's K steps are then parked in shared memory and the node's K updates
-// run from registers.  In-flight data lives in shared memory, not in
-// registers: the gather is bound by memory latency, and this keeps several
-// times more of it in flight than register loads could.  The ring is
-// written by generic stores, so the issuing lane fences the generic and
-// async proxies (fence.proxy.async.global) after the block barrier.
+// Gather.  Each thread sums its node's in-edges for the K steps of the
+// block: one edge record and one address per K steps, K sector loads per
+// edge (cache-global, __ldcg: with C > 1 the values come from other SMs,
+// ordered by the cluster barrier's release/acquire), 16 independent loads
+// in flight per thread.  The sums are parked in shared memory and the
+// node's K updates run from registers.  (Staging the edges' K-slot runs in
+// shared memory with cp.async.bulk instead was measured slower on the
+// benchmark workloads: the kernel is bound by instruction issue and latency,
+// not by bytes in flight.)
 #pragma once
 
 #include "tvbg_step_blocked.cuh"
@@ -50,10 +47,6 @@
 namespace tvbg {
 
 constexpr int kLanes = TVBG_GROUP_LANES;
-
-__device__ __forceinline__ void fence_proxy_async_global() {
-    asm volatile("fence.proxy.async.global;" ::: "memory");
-}
 
 __device__ __forceinline__ uint32_t cluster_nranks() {
     uint32_t n;
@@ -118,98 +111,68 @@ __device__ __forceinline__ float lane_post(float S, float xi, float wsum, float 
     }
 }
 
-// Shared memory of one node slot: two stages of `ec` runs (K * 8 floats
-// each) and their two mbarriers; `phase` holds the two parity bits and
-// `pend` the stages with a copy in flight (identical in the slot's 8 lanes).
-struct SlotStage {
-    float* buf;        // stage 0 at buf, stage 1 at buf + stf
-    uint32_t buf_addr; // shared address of buf
-    uint32_t mbar;     // stage s barrier at mbar + 8 s
-    int stf;           // floats per stage
-};
-
-// Wait (bounded) for stage st of the slot; every lane polls, and the slot
-// proceeds once any lane saw the phase complete.
-__device__ __forceinline__ bool slot_wait(const SlotStage& ss, int st, uint32_t& phase,
-                                          unsigned wmask) {
-    const uint32_t bar = ss.mbar + 8u * static_cast<uint32_t>(st);
-    const uint32_t par = (phase >> st) & 1u;
-    bool done = false;
-    for (long long it = 0; it < kWaitLimit && !done; ++it) done = mbar_try_wait(bar, par);
-    done = __any_sync(wmask, done);
-    if (done) phase ^= (1u << st);  // a stage that timed out keeps its parity for a later wait
-    return done;
-}
-
 // Coupling sums of node n (in-edges [lo, hi)) for the K steps of the block
-// starting at ring position tm, accumulated in CSR order.  Returns false if
-// a bounded wait gave up (the slot then stops issuing copies).
+// starting at ring position tm, accumulated in CSR order.  U = 16 / K edges
+// per iteration: 16 independent sector loads in flight per thread.
 template <int CF, int K>
-__device__ __forceinline__ bool bulk_gather(const tvbg_group& g, int lo, int hi, uint32_t tm,
-                                            uint32_t mask, uint32_t R, int l, int ec,
-                                            const SlotStage& ss, uint32_t& phase, uint32_t& pend,
-                                            unsigned wmask, float acc[K]) {
-    constexpr uint32_t kRunBytes = K * kLanes * 4;
+__device__ __forceinline__ void lane_gather(const tvbg_group& g, int lo, int hi, uint32_t tm,
+                                            uint32_t mask, uint32_t R, int l, float acc[K]) {
+    constexpr int U = 16 / K;
+    const float* __restrict__ ring = g.ring + l;
     const uint2* __restrict__ edges = reinterpret_cast<const uint2*>(g.edges);
 #pragma unroll
     for (int k = 0; k < K; ++k) acc[k] = 0.0f;
-    const int nE = hi - lo;
-    if (nE <= 0) return true;
-    const int nch = (nE + ec - 1) / ec;
-    auto issue = [&](int c) {
-        const int st = c & 1;
-        const int e0 = lo + c * ec;
-        const int m = (hi - e0) < ec ? (hi - e0) : ec;
-        const uint32_t bar = ss.mbar + 8u * static_cast<uint32_t>(st);
-        if (l == 0) {
-            mbar_expect_tx(bar, static_cast<uint32_t>(m) * kRunBytes);
-            for (int i = 0; i < m; ++i) {
-                const uint32_t pk = __ldg(&edges[e0 + i].x);
-                const float* src =
-                    g.ring + (static_cast<size_t>(pk >> 16) * R + ((tm + (pk & 0xffffu)) & mask)) * kLanes;
-                bulk_g2s(ss.buf_addr + 4u * static_cast<uint32_t>(st * ss.stf + i * K * kLanes), src,
-                         kRunBytes, bar);
-            }
-        }
-        pend |= (1u << st);
+    auto addr = [&](uint32_t pk) {
+        return ring + (static_cast<size_t>(pk >> 16) * R + ((tm + (pk & 0xffffu)) & mask)) * kLanes;
     };
-    if (l == 0) fence_proxy_async_global();
-    issue(0);
-    for (int c = 0; c < nch; ++c) {
-        const int st = c & 1;
-        if (c + 1 < nch) {
-            __syncwarp(wmask);  // the slot's lanes are done with stage (c + 1) & 1
-            issue(c + 1);
-        }
-        if (!slot_wait(ss, st, phase, wmask)) return false;
-        pend &= ~(1u << st);
-        const int e0 = lo + c * ec;
-        const int m = (hi - e0) < ec ? (hi - e0) : ec;
-        const float* b = ss.buf + st * ss.stf + l;
-        for (int i = 0; i < m; ++i) {
-            const float w = __uint_as_float(__ldg(&edges[e0 + i].y));
+    int e = lo;
+    for (; e + U <= hi; e += U) {
+        float v[U][K];
+        float w[U];
 #pragma unroll
-            for (int k = 0; k < K; ++k) acc[k] = fmaf(w, lane_pre<CF>(b[(i * K + k) * kLanes], g), acc[k]);
+        for (int u = 0; u < U; ++u) {
+            const uint2 ed = __ldg(edges + e + u);
+            const float* p = addr(ed.x);
+            w[u] = __uint_as_float(ed.y);
+#pragma unroll
+            for (int k = 0; k < K; ++k) v[u][k] = __ldcg(p + k * kLanes);
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+#pragma unroll
+            for (int k = 0; k < K; ++k) acc[k] = fmaf(w[u], lane_pre<CF>(v[u][k], g), acc[k]);
         }
     }
-    return true;
+    if (e < hi) {  // fewer than U edges left, loads still issued together
+        float v[U][K];
+        float w[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            if (e + u < hi) {
+                const uint2 ed = __ldg(edges + e + u);
+                const float* p = addr(ed.x);
+                w[u] = __uint_as_float(ed.y);
+#pragma unroll
+                for (int k = 0; k < K; ++k) v[u][k] = __ldcg(p + k * kLanes);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            if (e + u < hi) {
+#pragma unroll
+                for (int k = 0; k < K; ++k) acc[k] = fmaf(w[u], lane_pre<CF>(v[u][k], g), acc[k]);
+            }
+        }
+    }
 }
 
-// Dynamic shared memory of a group CTA of `threads` threads, block length
-// K and `ec` edge runs per stage: [csum K*threads floats][2 mbarriers per
-// slot][per slot: 2 stages of ec*K*8 floats + 8 floats of padding, which
-// puts the 4 slots of a warp on different banks].
-__host__ __device__ constexpr uint32_t group_slot_floats(int K, int ec) {
-    return static_cast<uint32_t>(2 * ec * K * kLanes + 8);
-}
-__host__ __device__ constexpr uint32_t group_smem_bytes(int K, int threads, int ec) {
-    return static_cast<uint32_t>(4 * K * threads) + static_cast<uint32_t>(16 * (threads / kLanes)) +
-           4u * static_cast<uint32_t>(threads / kLanes) * group_slot_floats(K, ec) + 16u;
+// Dynamic shared memory of a group CTA: the K coupling sums of every thread.
+__host__ __device__ constexpr uint32_t group_smem_bytes(int K, int threads) {
+    return static_cast<uint32_t>(4 * K * threads);
 }
 
 template <class M, int CF, int K>
-__device__ __forceinline__ void run_group(const tvbg_group& g, unsigned char* smem, int ec,
-                                          int32_t* status) {
+__device__ __forceinline__ void run_group(const tvbg_group& g, float* csum, int32_t* status) {
     constexpr int NS = M::NS;
     constexpr int NP = M::NP;
     constexpr int SPC = 4 / NS;
@@ -243,26 +206,6 @@ __device__ __forceinline__ void run_group(const tvbg_group& g, unsigned char* sm
     float* __restrict__ ring = g.ring;
     float* __restrict__ state = g.state;
     const int q0 = slot * static_cast<int>(C) + static_cast<int>(rank);
-    const unsigned wmask = 0xffu << (threadIdx.x & 24u);   // the 8 lanes of this slot
-
-    // shared memory: csum | mbarriers | stage buffers
-    float* csum = reinterpret_cast<float*>(smem);
-    const uint32_t mbar0 = (smem_addr(smem + 4 * K * blockDim.x) + 15u) & ~15u;
-    SlotStage ss;
-    ss.stf = ec * K * kLanes;
-    {
-        const uint32_t bufs = mbar0 + 16u * static_cast<uint32_t>(P);
-        ss.buf_addr = bufs + 4u * static_cast<uint32_t>(slot) * group_slot_floats(K, ec);
-        ss.buf = reinterpret_cast<float*>(smem + (ss.buf_addr - smem_addr(smem)));
-        ss.mbar = mbar0 + 16u * static_cast<uint32_t>(slot);
-    }
-    if (l == 0) {
-        mbar_init(ss.mbar, 1);
-        mbar_init(ss.mbar + 8u, 1);
-    }
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    uint32_t phase = 0, pend = 0;
-    bool live = true;  // false once a bounded wait gave up
 
     // seed: slot t0 holds obs0 of the state at t0
     {
@@ -305,13 +248,10 @@ __device__ __forceinline__ void run_group(const tvbg_group& g, unsigned char* sm
             for (int v = 0; v < NP; ++v) p[v] = __ldg(g.nparam + (n * NP + v) * kLanes + l);
             const float wsum = (CF == TVBG_CFUN_DIFF && g.wsum) ? __ldg(g.wsum + n) : 0.0f;
             {
-                const int lo = (valid && live) ? __ldg(g.row + n) : 0;
-                const int hi = (valid && live) ? __ldg(g.row + n + 1) : 0;
+                const int lo = valid ? __ldg(g.row + n) : 0;
+                const int hi = valid ? __ldg(g.row + n + 1) : 0;
                 float acc[K];
-                if (!bulk_gather<CF, K>(g, lo, hi, tm, mask, R, l, ec, ss, phase, pend, wmask, acc)) {
-                    live = false;
-                    if (l == 0) report(status, TVBG_ETIMEOUT);
-                }
+                lane_gather<CF, K>(g, lo, hi, tm, mask, R, l, acc);
 #pragma unroll
                 for (int k = 0; k < K; ++k) csum[k * blockDim.x + threadIdx.x] = acc[k];
             }
@@ -400,25 +340,20 @@ __device__ __forceinline__ void run_group(const tvbg_group& g, unsigned char* sm
         }
         group_barrier(cluster);
     }
-    // a slot whose wait gave up may still have copies in flight: wait for
-    // them (bounded) before the CTA's shared memory goes away
-    for (int st = 0; st < 2; ++st)
-        if (pend & (1u << st)) slot_wait(ss, st, phase, wmask);
 }
 
-// One group per CTA (or per cluster of CTAs): group index = order[cluster id];
-// `ec` edge runs per stage of the TMA gather.
+// One group per CTA (or per cluster of CTAs): group index = order[cluster id].
 template <class M, int CF, int K>
 __global__ void __launch_bounds__(1024, 1)
     group_kernel(const tvbg_group* __restrict__ groups, int32_t n_groups,
-                 const int32_t* __restrict__ order, int32_t* __restrict__ status, int32_t ec) {
+                 const int32_t* __restrict__ order, int32_t* __restrict__ status) {
     __shared__ __align__(16) tvbg_group s_grp;
-    extern __shared__ __align__(128) unsigned char gsmem[];
+    extern __shared__ float csum[];  // [K][blockDim]: the block's coupling sums per thread
     const int cid = static_cast<int>(cluster_id_x());
     if (cid >= n_groups) return;  // uniform over the cluster
     const int idx = order ? __ldg(order + cid) : cid;
     stage_group(groups + idx, &s_grp);
-    run_group<M, CF, K>(s_grp, gsmem, ec, status);
+    run_group<M, CF, K>(s_grp, csum, status);
 }
 
 }  // namespace tvbg

@@ -79,9 +79,7 @@ class GroupSet:
       nsteps  : optional (I,) step counts, used to put instances of similar
                 length into the same group (longest first);
       block_k : 4 or 8 steps per barrier (default: 8 when d_min >= 7);
-      threads, cluster : launch shape (default: group_shape);
-      runs    : edge runs per stage of the TMA gather (default: the most
-                that fit shared memory, at most 8).
+      threads, cluster : launch shape (default: group_shape).
     Couplings must be separable (Linear, Diff, Sigmoidal); the Kuramoto
     model and the Track-A order run on the per-instance kernels.
 
@@ -93,7 +91,7 @@ class GroupSet:
                  nparam=None, delays=None, rounding='ceil', seed=0, inst_ids=None,
                  bold_period=0, bold_len=0, trace_every=0, trace_len=0, trace_nobs=None,
                  flags=0, cf_b=None, t0=0, nsteps=None, block_k=None, threads=None,
-                 cluster=None, history='zero', runs=0):
+                 cluster=None, history='zero'):
         _device_ok()
         torch = _torch()
         self.torch = torch
@@ -228,7 +226,6 @@ class GroupSet:
                                (cf_b0 if isinstance(cf_b0, (int, float, np.number)) else 0.0))
         self.t = np.full(G, int(t0), np.int64)
         self.threads, self.cluster = group_shape(N, threads, cluster)
-        self.runs = int(runs)
         self.status = DeviceStatus()
         self._uploaded = None
         self._streams = None
@@ -341,7 +338,6 @@ class GroupSet:
         cfg.model, cfg.cfun = self.model_id, self.cfun_id
         cfg.threads, cfg.cluster = self.threads, self.cluster
         cfg.block_k = int(block_k)
-        cfg.nmax = self.runs
         cfg.d_status = self.status.t.data_ptr()
         cfg.d_order = order.data_ptr() if order is not None else None
         return cfg
