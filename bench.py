@@ -706,6 +706,7 @@ def serve_arm(args):
     st = srv.stats()
     offered = sum(r.node_steps for r in reqs) / max(args.serve_seconds, 1e-9)
     served = st['node_steps'] / wall
+    plain = serve_plain(reqs, budget_s=args.serve_plain_seconds)
     line = {'metric': METRIC, 'value': round(served, 1), 'unit': UNIT, 'n_gpus': 1,
             'steps': 1, 'warmup': 1, 'higher_is_better': True, 'scaling': 'weak',
             'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic (seeded connectomes)',
@@ -717,8 +718,45 @@ def serve_arm(args):
                       'p99_latency_s': round(st.get('p99_s', float('nan')), 3),
                       'wall_s': round(wall, 3), 'ticks': st['ticks'],
                       'offered_node_steps_per_s': round(offered, 1),
-                      'queue_kept_up': bool(wall <= args.serve_seconds * 1.25)}}
+                      'queue_kept_up': bool(wall <= args.serve_seconds * 1.25)},
+            'plain': plain,
+            'served_vs_plain': round(served / plain['value'], 3) if plain['value'] else None}
     print(json.dumps(line), flush=True)
+
+
+def serve_plain(reqs, budget_s=20.0):
+    """The plain path on the same requests: each request alone, as one
+    sweep of the per-step kernel launched in PLAIN_CHUNK-step chunks and
+    synchronised after each chunk (the reference launcher's loop,
+    dsl/dsl_cuda/example/cuda_run.py:124-142), requests one after the other
+    in arrival order, until `budget_s` of GPU time is spent; returns the
+    measured node-steps/s (gradient requests run forward only)."""
+    import torch
+    from tvb_hpc import engine, scheme, serve
+    done, el, n_req = 0.0, 0.0, 0
+    for r in sorted(reqs, key=lambda r: r.arrival):
+        if el >= budget_s:
+            break
+        M, C, noise = serve.MODELS[r.model]
+        m = M()
+        cf = C(m)
+        scm = scheme.EulerMaryuyamaStep(r.dt) if noise else scheme.EulerStep(r.dt)
+        sw = engine.Sweep(m, cf, scm, r.conn, dt=r.dt, couplings=r.couplings, speeds=r.speeds,
+                          state0=r.x0, nparam=r.nparam, seed=r.seed, blocked=False, tpn=2)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        left = r.nsteps
+        while left > 0 and el + (time.perf_counter() - t0) < budget_s:
+            n = min(PLAIN_CHUNK, left)
+            sw.run(n)          # synchronises and checks the status word
+            left -= n
+        el += time.perf_counter() - t0
+        done += float(r.couplings.size) * r.conn.nnode * (r.nsteps - left)
+        n_req += 1
+    return {'value': round(done / el, 1) if el > 0 else None, 'unit': UNIT, 'requests': n_req,
+            'seconds': round(el, 3),
+            'path': 'each request alone: per-step kernel, %d-step launches, host sync per launch'
+                    % PLAIN_CHUNK}
 
 
 def reference_arm(args):
@@ -755,6 +793,7 @@ def main():
     ap.add_argument('--serve-seconds', type=float, default=2.0)
     ap.add_argument('--serve-max-inst', type=int, default=256)
     ap.add_argument('--serve-chunk', type=int, default=5000)
+    ap.add_argument('--serve-plain-seconds', type=float, default=20.0)
     ap.add_argument('--impl', default='engine', choices=['engine', 'reference'])
     ap.add_argument('--no-cpu', action='store_true', help='skip the cpu_baseline leg')
     ap.add_argument('--ref-seconds', type=float, default=8.0)
