@@ -240,13 +240,6 @@ __device__ __forceinline__ void run_group(const tvbg_group& g, float* csum, int3
             const int q = q0 + r * stride;
             const bool valid = q < N;
             const int n = valid ? (g.nodes ? __ldg(g.nodes + q) : q) : 0;
-            // state and parameters first: their loads overlap the gather's
-            float x[NS], p[NP];
-#pragma unroll
-            for (int v = 0; v < NS; ++v) x[v] = state[(n * NS + v) * kLanes + l];
-#pragma unroll
-            for (int v = 0; v < NP; ++v) p[v] = __ldg(g.nparam + (n * NP + v) * kLanes + l);
-            const float wsum = (CF == TVBG_CFUN_DIFF && g.wsum) ? __ldg(g.wsum + n) : 0.0f;
             {
                 const int lo = valid ? __ldg(g.row + n) : 0;
                 const int hi = valid ? __ldg(g.row + n + 1) : 0;
@@ -256,6 +249,12 @@ __device__ __forceinline__ void run_group(const tvbg_group& g, float* csum, int3
                 for (int k = 0; k < K; ++k) csum[k * blockDim.x + threadIdx.x] = acc[k];
             }
             if (!valid) continue;
+            float x[NS], p[NP];
+#pragma unroll
+            for (int v = 0; v < NS; ++v) x[v] = state[(n * NS + v) * kLanes + l];
+#pragma unroll
+            for (int v = 0; v < NP; ++v) p[v] = __ldg(g.nparam + (n * NP + v) * kLanes + l);
+            const float wsum = (CF == TVBG_CFUN_DIFF && g.wsum) ? __ldg(g.wsum + n) : 0.0f;
             float bs = 0.0f, bF = 0.0f, bV = 0.0f, bQ = 0.0f;
             if (bold) {
                 bs = g.bold[(0 * N + n) * kLanes + l];
@@ -263,15 +262,14 @@ __device__ __forceinline__ void run_group(const tvbg_group& g, float* csum, int3
                 bV = g.bold[(2 * N + n) * kLanes + l];
                 bQ = g.bold[(3 * N + n) * kLanes + l];
             }
-            float* __restrict__ rrow = ring + static_cast<size_t>(n) * R * kLanes + l;
             float obs0 = M::obs(x, 0);
             float zz[4] = {0.0f, 0.0f, 0.0f, 0.0f};
             int b_next = b_until, tr_next = tr_until;
             int brow = b_row, trow = tr_row;
-            const int kend = (t_end - tb) < cnt ? static_cast<int>(t_end - tb) : cnt;
 #pragma unroll 1
-            for (int k = 0; k < kend; ++k) {
+            for (int k = 0; k < cnt; ++k) {
                 const long long t = tb + k;
+                if (t >= t_end) break;
                 if (trace && k == tr_next) {
                     float* dst = g.trace + ((static_cast<size_t>(trow) * N + n) * g.trace_nobs) * kLanes + l;
                     for (int o = 0; o < g.trace_nobs; ++o) dst[o * kLanes] = M::obs(x, o);
@@ -301,8 +299,9 @@ __device__ __forceinline__ void run_group(const tvbg_group& g, float* csum, int3
                 M::limit(x, flags);
                 obs0 = M::obs(x, 0);
                 const uint32_t pos = (static_cast<uint32_t>(t) + 1u) & mask;
-                rrow[pos * kLanes] = obs0;
-                if (pos < kGhost) rrow[(pos + nh) * kLanes] = obs0;
+                const size_t idx = (static_cast<size_t>(n) * R + pos) * kLanes + l;
+                ring[idx] = obs0;
+                if (pos < kGhost) ring[idx + static_cast<size_t>(nh) * kLanes] = obs0;
                 if (bold) {
                     Balloon::step(bs, bF, bV, bQ, xbold, g.dt_bold);
                     if (k == b_next) {
