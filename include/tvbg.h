@@ -61,6 +61,11 @@ extern "C" {
 #define TVBG_MODEL_G2DOSC 4   /* generic 2-D oscillator in the form of the CUDA
                                  DSL (dsl/dsl_cuda/CUDAmodels/oscillator.c:149-150):
                                  state V W, cubic in V, coupling into V */
+#define TVBG_MODEL_RWW 5      /* model.py:209-223 reduced Wong-Wang, state S,
+                                 params w io */
+#define TVBG_MODEL_JANSENRIT 6 /* model.py:226-247 Jansen-Rit, state y0..y5,
+                                 params v0 r, observable y0 - y1; no noise
+                                 (more than 4 state variables) */
 
 /* ---- coupling functions (tvb_hpc/coupling.py) --------------------------- */
 #define TVBG_CFUN_LINEAR 0    /* pre = x_j,                  post = a*sum + b */

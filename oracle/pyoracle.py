@@ -35,7 +35,7 @@ class OrcCfg(ctypes.Structure):
         ('trace_every', ctypes.c_int32), ('trace_len', ctypes.c_int32),
         ('trace_nobs', ctypes.c_int32),
         ('bold_period', ctypes.c_int32), ('bold_len', ctypes.c_int32), ('bold_obs', ctypes.c_int32),
-        ('dt_bold', ctypes.c_float),
+        ('dt_bold', ctypes.c_float), ('npar', ctypes.c_int32),
     ]
 
 
@@ -71,7 +71,7 @@ def _p(a):
 
 
 def nstate(model):
-    return 2 if model in (1, 2, 4) else 1
+    return {1: 2, 2: 2, 4: 2, 6: 6}.get(model, 1)
 
 
 def run(model, cfun, row, col, weights, nh, nsteps, dt, delays, cf_a, nparam, state, ring=None,
@@ -80,7 +80,7 @@ def run(model, cfun, row, col, weights, nh, nsteps, dt, delays, cf_a, nparam, st
         bold_len=0, bold_obs=0, real='f32', nthreads=1):
     """
     Run the oracle for I instances.  delays [I, nnz] int, cf_a [I],
-    nparam [I, N], state [I, N, ns], ring [I, nh, N] (plain slot-major),
+    nparam [I, N] or [I, N, npar], state [I, N, ns], ring [I, nh, N] (plain slot-major),
     bold [I, 4, N].  Returns dict of the updated arrays.
     """
     lib = load()
@@ -93,13 +93,20 @@ def run(model, cfun, row, col, weights, nh, nsteps, dt, delays, cf_a, nparam, st
     I = state.shape[0]
     delays = np.ascontiguousarray(np.broadcast_to(np.asarray(delays, np.int32), (I, col.size)))
     cf_a = np.ascontiguousarray(np.broadcast_to(np.asarray(cf_a, dtype), (I, )))
-    nparam = np.ascontiguousarray(np.broadcast_to(np.asarray(nparam, dtype).reshape(-1, N), (I, N)))
+    nparam = np.asarray(nparam, dtype)
+    if nparam.ndim == 3:                       # [I, N, npar]
+        npar = nparam.shape[2]
+    else:                                      # [I, N] or [N]: one parameter per node
+        npar = 1
+        nparam = nparam.reshape(-1, N, 1)
+    nparam = np.ascontiguousarray(np.broadcast_to(nparam, (I, N, npar)))
     ring = (np.zeros((I, nh, N), dtype) if ring is None
             else np.array(ring, dtype, copy=True).reshape(I, nh, N))
     cfg = OrcCfg()
     cfg.model, cfg.cfun, cfg.N, cfg.nnz = model, cfun, N, col.size
     cfg.row, cfg.col, cfg.weights = row.ctypes.data, col.ctypes.data, w.ctypes.data
     cfg.nh, cfg.nsteps, cfg.t0, cfg.dt, cfg.flags = nh, nsteps, t0, dt, flags
+    cfg.npar = npar
     cfg.sigma[:] = list(np.asarray(sigma, np.float32))
     cfg.consts[:] = list(np.asarray(consts if consts is not None else np.zeros(16), np.float32))
     cfg.cf_b = cf_b
@@ -138,7 +145,7 @@ def run_sweep_like(sw, state0, nsteps, real='f32', t0=0, rings=None, bold=None, 
     Returns state [I,N,ns], rings (list of [nh, N]), bold, bold_out, trace."""
     I = sw.n
     state0 = np.broadcast_to(np.asarray(state0), (I, sw.N, sw.ns))
-    nparam = sw.nparam.cpu().numpy()[:, :, 0]
+    nparam = sw.nparam.cpu().numpy()
     flags = (int(sw.flags) & _SEMANTIC) | F_BOLD_DEV
     res = dict(state=None, rings=[None] * I, bold=None, bold_out=None, trace=None)
     for lognh in sorted(set(int(x) for x in sw.lognh)):
@@ -173,7 +180,7 @@ def run_groups_like(gs, state0, nsteps, real='f32', nthreads=1):
     I = gs.n
     state0 = np.broadcast_to(np.asarray(state0), (I, gs.N, gs.ns))
     steps = np.broadcast_to(np.asarray(nsteps, np.int64), (I, ))
-    nparam = gs.gnparam[gs._gi, :, :, gs._li].cpu().numpy()[:, :, 0]
+    nparam = gs.gnparam[gs._gi, :, :, gs._li].cpu().numpy()
     flags = (int(gs.flags) & _SEMANTIC) | F_BOLD_DEV
     lognh_i = gs.lognh[gs.grp_of]
     tab_i = gs.gtab[gs.grp_of]

@@ -42,6 +42,8 @@
 #define ORC_MODEL_MPR 2
 #define ORC_MODEL_LINEAR 3
 #define ORC_MODEL_G2DOSC 4 /* oscillator.c:149-150 */
+#define ORC_MODEL_RWW 5       /* tvb_hpc/model.py:209-223 */
+#define ORC_MODEL_JANSENRIT 6 /* tvb_hpc/model.py:226-247 */
 
 #define ORC_CFUN_LINEAR 0
 #define ORC_CFUN_DIFF 1
@@ -78,9 +80,11 @@ typedef struct orc_cfg {
     int32_t trace_every, trace_len, trace_nobs;
     int32_t bold_period, bold_len, bold_obs;
     float dt_bold;
+    int32_t npar; /* parameters per node (nparam is [N][npar] per instance); 0 = 1 */
 } orc_cfg;
 
 static int nstate(int model) {
+    if (model == ORC_MODEL_JANSENRIT) return 6;
     return (model == ORC_MODEL_G2DO || model == ORC_MODEL_MPR || model == ORC_MODEL_G2DOSC) ? 2 : 1;
 }
 

@@ -41,9 +41,18 @@ def test_models_parse_and_prep_arrays():
 
 
 def test_engine_spec_rejects_unbuilt_or_edited():
-    for M in (model.RWW, model.JansenRit, model.HMJE):
-        with pytest.raises(NotImplementedError):
-            M().engine_spec()
+    with pytest.raises(NotImplementedError):
+        model.HMJE().engine_spec()
+    kid, consts, sigma = model.RWW().engine_spec()
+    assert kid == 5 and consts[5] == np.float32(0.2609) and sigma[0] == np.float32(0.01)
+    kid, consts, sigma = model.JansenRit().engine_spec()
+    assert kid == 6 and consts[0] == np.float32(3.25) and consts[10] == np.float32(0.22)
+    assert np.all(sigma == 0)
+
+    class NoisyJR(model.JansenRit):
+        diffs = 0, 0, 0, 0, 0, 1e-3
+    with pytest.raises(NotImplementedError):
+        NoisyJR().engine_spec()
 
     class Edited(model.Kuramoto):
         drift = 'omega + 2 * I',

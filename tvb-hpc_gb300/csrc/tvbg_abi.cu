@@ -33,6 +33,8 @@ static StepKernel lookup(int model, int cfun, int tpn) {
         case TVBG_MODEL_MPR: return step_kernel_mpr(cfun, tpn);
         case TVBG_MODEL_LINEAR: return step_kernel_linear(cfun, tpn);
         case TVBG_MODEL_G2DOSC: return step_kernel_g2dosc(cfun, tpn);
+        case TVBG_MODEL_RWW: return step_kernel_rww(cfun, tpn);
+        case TVBG_MODEL_JANSENRIT: return step_kernel_jansenrit(cfun, tpn);
         default: return nullptr;
     }
 }

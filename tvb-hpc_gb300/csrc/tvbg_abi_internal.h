@@ -28,6 +28,8 @@ StepKernel step_kernel_g2do(int cfun, int tpn);
 StepKernel step_kernel_mpr(int cfun, int tpn);
 StepKernel step_kernel_linear(int cfun, int tpn);
 StepKernel step_kernel_g2dosc(int cfun, int tpn);
+StepKernel step_kernel_rww(int cfun, int tpn);
+StepKernel step_kernel_jansenrit(int cfun, int tpn);
 // Per-model lookup of the time-blocked kernel for (cfun, tpn, K); nullptr if not built.
 BlockedKernel blocked_kernel_g2do(int cfun, int tpn, int k);
 BlockedKernel blocked_kernel_mpr(int cfun, int tpn, int k);
@@ -39,6 +41,8 @@ GroupKernel group_kernel_g2do(int cfun, int k);
 GroupKernel group_kernel_mpr(int cfun, int k);
 GroupKernel group_kernel_linear(int cfun, int k);
 GroupKernel group_kernel_g2dosc(int cfun, int k);
+GroupKernel group_kernel_rww(int cfun, int k);
+GroupKernel group_kernel_jansenrit(int cfun, int k);
 // Shared memory of the blocked kernel beyond the ring (floats): K * nmax * (2 + NS) + 4 * nmax.
 uint32_t blocked_aux_bytes(int model, int k, int nmax);
 

@@ -203,6 +203,70 @@ struct Linear {
     __device__ static __forceinline__ void limit(float*, uint32_t) {}
 };
 
+// tvb_hpc/model.py:209-223 (RWW), state S, params (w, io),
+// K = [a, b, d, g, ts, J]:
+//   x = w J S + io + J c;   h = (a x - b) / (1 - exp(-d (a x - b)))
+//   S' = -S / ts + (1 - S) h g;   obsrv = S.
+// (h has a removable singularity at a x = b, where both the reference and
+// this form give 0/0.)
+struct RWW {
+    static constexpr int ID = TVBG_MODEL_RWW;
+    static constexpr int NS = 1;
+    static constexpr int NP = 2;
+    static constexpr int NOBS = 1;
+    __device__ static __forceinline__ void drift(const float* x, float c, const float* p,
+                                                 const float* K, float* f) {
+        const float S = x[0], w = p[0], io = p[1];
+        const float a = K[0], b = K[1], d = K[2], g = K[3], ts = K[4], J = K[5];
+        const float xx = w * J * S + io + J * c;
+        const float y = a * xx - b;
+        const float h = y / (1.0f - expf(-d * y));
+        f[0] = -(S / ts) + (1.0f - S) * h * g;
+    }
+    __device__ static __forceinline__ float obs(const float* x, int) { return x[0]; }
+    __device__ static __forceinline__ void limit(float*, uint32_t) {}
+};
+
+// tvb_hpc/model.py:226-247 (Jansen-Rit), state y0..y5, params (v0, r),
+// K = [A, B, a, b, nu_max, J, a_1, a_2, a_3, a_4, mu]:
+//   sigm(u) = 2 nu_max / (1 + exp(r (v0 - u)))
+//   y0' = y3, y1' = y4, y2' = y5
+//   y3' = A a sigm(y1 - y2) - 2 a y3 - a^2 y0
+//   y4' = A a (mu + a_2 J sigm(a_1 J y0) + c) - 2 a y4 - a^2 y1
+//   y5' = B b a_4 J sigm(a_3 J y0) - 2 b y5 - b^2 y2
+// obsrv = y0 - y1.  The model has no noise (diffs are zero).
+struct JansenRit {
+    static constexpr int ID = TVBG_MODEL_JANSENRIT;
+    static constexpr int NS = 6;
+    static constexpr int NP = 2;
+    static constexpr int NOBS = 1;
+    __device__ static __forceinline__ void drift(const float* x, float c, const float* p,
+                                                 const float* K, float* f) {
+        const float v0 = p[0], r = p[1];
+        const float A = K[0], B = K[1], a = K[2], b = K[3], nu_max = K[4], J = K[5];
+        const float a_1 = K[6], a_2 = K[7], a_3 = K[8], a_4 = K[9], mu = K[10];
+        const float s12 = 2.0f * nu_max / (1.0f + expf(r * (v0 - (x[1] - x[2]))));
+        const float s01 = 2.0f * nu_max / (1.0f + expf(r * (v0 - (a_1 * J * x[0]))));
+        const float s03 = 2.0f * nu_max / (1.0f + expf(r * (v0 - (a_3 * J * x[0]))));
+        f[0] = x[3];
+        f[1] = x[4];
+        f[2] = x[5];
+        f[3] = A * a * s12 - 2.0f * a * x[3] - a * a * x[0];
+        f[4] = A * a * (mu + a_2 * J * s01 + c) - 2.0f * a * x[4] - a * a * x[1];
+        f[5] = B * b * (a_4 * J * s03) - 2.0f * b * x[5] - b * b * x[2];
+    }
+    __device__ static __forceinline__ float obs(const float* x, int) { return x[0] - x[1]; }
+    __device__ static __forceinline__ void limit(float*, uint32_t) {}
+};
+
+// Philox calls serve 4 normals: a model with NS <= 4 state variables takes
+// 4 / NS steps per call; models with more state variables run without noise.
+template <class M>
+struct Noise {
+    static constexpr bool kOK = M::NS <= 4;
+    static constexpr int SPC = M::NS <= 4 ? 4 / M::NS : 1;
+};
+
 // ---------------------------------------------------------------------------
 // Coupling functions, tvb_hpc/coupling.py:103-121 and network.py:115-136:
 //   input_i = post( sum_e w_e * pre(obsrv_j(t - d_e), obsrv_i(t)) ),

@@ -14,6 +14,8 @@ GroupKernel lookup_group(int model, int cfun, int k) {
         case TVBG_MODEL_MPR: return group_kernel_mpr(cfun, k);
         case TVBG_MODEL_LINEAR: return group_kernel_linear(cfun, k);
         case TVBG_MODEL_G2DOSC: return group_kernel_g2dosc(cfun, k);
+        case TVBG_MODEL_RWW: return group_kernel_rww(cfun, k);
+        case TVBG_MODEL_JANSENRIT: return group_kernel_jansenrit(cfun, k);
         default: return nullptr;
     }
 }

@@ -1,0 +1,26 @@
+// Lane-interleaved group kernels for the JansenRit model: separable couplings
+// (LINEAR, DIFF, SIGMOIDAL) x block length 4, 8.
+#include "tvbg_abi_internal.h"
+#include "tvbg_lanes.cuh"
+
+namespace tvbg {
+
+template <int CF>
+static GroupKernel pick_k(int k) {
+    switch (k) {
+        case 4: return group_kernel<JansenRit, CF, 4>;
+        case 8: return group_kernel<JansenRit, CF, 8>;
+        default: return nullptr;
+    }
+}
+
+GroupKernel group_kernel_jansenrit(int cfun, int k) {
+    switch (cfun) {
+        case TVBG_CFUN_LINEAR: return pick_k<TVBG_CFUN_LINEAR>(k);
+        case TVBG_CFUN_DIFF: return pick_k<TVBG_CFUN_DIFF>(k);
+        case TVBG_CFUN_SIGMOIDAL: return pick_k<TVBG_CFUN_SIGMOIDAL>(k);
+        default: return nullptr;
+    }
+}
+
+}  // namespace tvbg

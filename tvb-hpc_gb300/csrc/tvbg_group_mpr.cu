@@ -1,5 +1,5 @@
 // Lane-interleaved group kernels for the MPR model: separable couplings
-// (LINEAR, DIFF, SIGMOIDAL) x block length 4, 8 (TMA-staged gather).
+// (LINEAR, DIFF, SIGMOIDAL) x block length 4, 8.
 #include "tvbg_abi_internal.h"
 #include "tvbg_lanes.cuh"
 

@@ -175,13 +175,14 @@ template <class M, int CF, int K>
 __device__ __forceinline__ void run_group(const tvbg_group& g, float* csum, int32_t* status) {
     constexpr int NS = M::NS;
     constexpr int NP = M::NP;
-    constexpr int SPC = 4 / NS;
+    constexpr int SPC = Noise<M>::SPC;
     const int N = g.N;
     const uint32_t C = cluster_nranks();
     const uint32_t rank = cluster_rank();
     const bool cluster = C > 1;
     if (N <= 0 || N > 65535 || g.lognh < 3 || g.lognh > 16 || g.model != M::ID || g.cfun != CF ||
-        g.nsteps < 0 || (g.flags & (TVBG_F_TRACKA | TVBG_F_MIDSYNC | TVBG_F_TRACE_CSUM))) {
+        g.nsteps < 0 || (g.flags & (TVBG_F_TRACKA | TVBG_F_MIDSYNC | TVBG_F_TRACE_CSUM)) ||
+        (!Noise<M>::kOK && (g.flags & TVBG_F_NOISE))) {
         if (threadIdx.x == 0) report(status, TVBG_EINVAL);
         return;  // every CTA of the cluster reads the same descriptor and leaves here
     }
@@ -283,18 +284,20 @@ __device__ __forceinline__ void run_group(const tvbg_group& g, float* csum, int3
                 M::drift(x, c, p, g.consts, f);
 #pragma unroll
                 for (int v = 0; v < NS; ++v) x[v] = fmaf(dt, f[v], x[v]);
-                if (noise) {
-                    const int r0 = static_cast<int>(t & (SPC - 1));
-                    if (k == 0 || r0 == 0) {
-                        const u32x4 w = philox4x32_10(static_cast<uint32_t>(n),
-                                                      static_cast<uint32_t>(t / SPC), g.seed_hi, 0u,
-                                                      g.seed_lo, inst_id);
-                        box_muller(w.v[0], w.v[1], zz[0], zz[1]);
-                        box_muller(w.v[2], w.v[3], zz[2], zz[3]);
-                    }
+                if constexpr (Noise<M>::kOK) {
+                    if (noise) {
+                        const int r0 = static_cast<int>(t & (SPC - 1));
+                        if (k == 0 || r0 == 0) {
+                            const u32x4 w = philox4x32_10(static_cast<uint32_t>(n),
+                                                          static_cast<uint32_t>(t / SPC), g.seed_hi, 0u,
+                                                          g.seed_lo, inst_id);
+                            box_muller(w.v[0], w.v[1], zz[0], zz[1]);
+                            box_muller(w.v[2], w.v[3], zz[2], zz[3]);
+                        }
 #pragma unroll
-                    for (int v = 0; v < NS; ++v)
-                        x[v] = fmaf(sqrt_dt * pick4(zz, r0 * NS + v), g.sigma[v], x[v]);
+                        for (int v = 0; v < NS; ++v)
+                            x[v] = fmaf(sqrt_dt * pick4(zz, r0 * NS + v), g.sigma[v], x[v]);
+                    }
                 }
                 M::limit(x, flags);
                 obs0 = M::obs(x, 0);

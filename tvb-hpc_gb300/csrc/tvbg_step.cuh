@@ -165,7 +165,7 @@ __device__ __forceinline__ void run_steps(const tvbg_instance& d, const Ring<SME
                                           float* bs) {
     using C = Cfun<CF>;
     constexpr int G = 32 / TPN;
-    constexpr int SPC = 4 / M::NS;  // steps served by one Philox call
+    constexpr int SPC = Noise<M>::SPC;  // steps served by one Philox call
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     const int N = d.N;
@@ -289,19 +289,21 @@ __device__ __forceinline__ void run_steps(const tvbg_instance& d, const Ring<SME
                 M::drift(x, c, p, K, f);
 #pragma unroll
                 for (int v = 0; v < M::NS; ++v) x[v] = fmaf(dt, f[v], x[v]);
-                if (noise) {
-                    const uint32_t tt = static_cast<uint32_t>(t);
-                    const uint32_t ph = tt % SPC;
-                    if (ph == 0 || s == 0)
-                        philox_normals4(static_cast<uint32_t>(my), tt / SPC, d.seed_hi, d.seed_lo,
-                                        d.inst_id, z);
+                if constexpr (Noise<M>::kOK) {
+                    if (noise) {
+                        const uint32_t tt = static_cast<uint32_t>(t);
+                        const uint32_t ph = tt % SPC;
+                        if (ph == 0 || s == 0)
+                            philox_normals4(static_cast<uint32_t>(my), tt / SPC, d.seed_hi,
+                                            d.seed_lo, d.inst_id, z);
 #pragma unroll
-                    for (int v = 0; v < M::NS; ++v) {
-                        float zv = z[0];
+                        for (int v = 0; v < M::NS; ++v) {
+                            float zv = z[0];
 #pragma unroll
-                        for (int q = 0; q < 4; ++q)
-                            if (q == static_cast<int>(ph) * M::NS + v) zv = z[q];
-                        x[v] = fmaf(sqrt_dt * zv, d.sigma[v], x[v]);
+                            for (int q = 0; q < 4; ++q)
+                                if (q == static_cast<int>(ph) * M::NS + v) zv = z[q];
+                            x[v] = fmaf(sqrt_dt * zv, d.sigma[v], x[v]);
+                        }
                     }
                 }
                 M::limit(x, flags);
@@ -329,7 +331,7 @@ __device__ __forceinline__ void run_instance(const tvbg_instance& d, const SmemP
     const int my = threadIdx.x;
     const bool own = my < N;
     if (N > static_cast<int>(blockDim.x) || N <= 0 || d.lognh < 2 || d.lognh > 24 ||
-        d.model != M::ID || d.cfun != CF) {
+        d.model != M::ID || d.cfun != CF || (!Noise<M>::kOK && (d.flags & TVBG_F_NOISE))) {
         if (threadIdx.x == 0) report(status, TVBG_EINVAL);
         return;
     }

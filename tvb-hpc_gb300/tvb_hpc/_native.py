@@ -30,6 +30,7 @@ TVBG_EDEVICE = -5
 FC_NOALLOC_MAX_DOUBLES = 1048576
 
 MODEL_KURAMOTO, MODEL_G2DO, MODEL_MPR, MODEL_LINEAR, MODEL_G2DOSC = 0, 1, 2, 3, 4
+MODEL_RWW, MODEL_JANSENRIT = 5, 6
 CFUN_LINEAR, CFUN_DIFF, CFUN_KURAMOTO, CFUN_SIGMOIDAL = 0, 1, 2, 3
 
 F_NOISE = 1

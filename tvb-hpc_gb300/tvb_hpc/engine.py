@@ -226,7 +226,8 @@ class InstanceSet:
             self.sync_every = np.minimum(self.sync_every, int(sync_every)).astype(np.int32)
         # time-blocked kernel where it applies (K steps per block)
         separable = self.cfun_id in (nat.CFUN_LINEAR, nat.CFUN_DIFF, nat.CFUN_SIGMOIDAL)
-        can_block = separable and order == 'cuda' and self.model_id != nat.MODEL_KURAMOTO
+        can_block = (separable and order == 'cuda' and self.model_id in (
+            nat.MODEL_G2DO, nat.MODEL_MPR, nat.MODEL_LINEAR, nat.MODEL_G2DOSC))
         tab_k, tab_pipe = [], []
         smem_total = max_smem() - _SMEM_RESERVE
         for t, d in enumerate(tables):
@@ -316,7 +317,8 @@ class InstanceSet:
             fl |= nat.F_TRACE
             if trace_csum:
                 fl |= nat.F_TRACE_CSUM
-        if getattr(scheme, 'noise', False):
+        # an Euler-Maruyama scheme on a model whose diffusion is zero is Euler
+        if getattr(scheme, 'noise', False) and np.any(self.sigma != 0):
             fl |= nat.F_NOISE
         self.flags = fl
         self.seed = int(seed) & ((1 << 64) - 1)

@@ -215,7 +215,8 @@ class GroupSet:
             self.gtrace = torch.zeros((G, max(1, self.trace_len), N, self.trace_nobs, L),
                                       dtype=torch.float32, device='cuda')
             fl |= nat.F_TRACE
-        if getattr(scheme, 'noise', False):
+        # an Euler-Maruyama scheme on a model whose diffusion is zero is Euler
+        if getattr(scheme, 'noise', False) and np.any(self.sigma != 0):
             fl |= nat.F_NOISE
         self.flags = fl
         self.seed = int(seed) & ((1 << 64) - 1)

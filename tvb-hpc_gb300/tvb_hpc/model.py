@@ -106,10 +106,12 @@ class BaseModel:
         consts = np.zeros(16, np.float32)
         for i, name in enumerate(self._kernel_consts):
             consts[i] = float(self.const[name])
-        sigma = np.zeros(4, np.float32)
+        sig = np.zeros(max(4, len(self.diffs)), np.float32)
         for i, g in enumerate(self.diffs):
-            sigma[i] = float(parse(g).subs({k: v for k, v in self.const.items()}))
-        return self._kernel, consts, sigma
+            sig[i] = float(parse(g).subs({k: v for k, v in self.const.items()}))
+        if self.nsvar > 4 and np.any(sig != 0):
+            raise NotImplementedError('noise on more than 4 state variables is not built')
+        return self._kernel, consts, sig[:4].copy()
 
     def node_params(self, nnode):
         "Per-node parameter array [nnode, npar] from const (prep_arrays)."
@@ -201,6 +203,8 @@ class RWW(BaseModel):
     drift = '- (S / ts) + (1 - S) * h * g',
     diffs = 0.01,
     obsrv = 'S',
+    _kernel = nat.MODEL_RWW
+    _kernel_consts = ('a', 'b', 'd', 'g', 'ts', 'J')
 
 
 class JansenRit(BaseModel):
@@ -225,6 +229,8 @@ class JansenRit(BaseModel):
     )
     diffs = 0, 0, 0, 0, 0, 0
     obsrv = 'y0 - y1',
+    _kernel = nat.MODEL_JANSENRIT
+    _kernel_consts = ('A', 'B', 'a', 'b', 'nu_max', 'J', 'a_1', 'a_2', 'a_3', 'a_4', 'mu')
 
 
 class Linear(BaseModel):
@@ -309,4 +315,4 @@ class MPR(BaseModel):
 
 
 _BUILTIN = {'Kuramoto': Kuramoto, 'G2DO': G2DO, 'MPR': MPR, 'Linear': Linear,
-            'Generic2dOscillator': Generic2dOscillator}
+            'Generic2dOscillator': Generic2dOscillator, 'RWW': RWW, 'JansenRit': JansenRit}

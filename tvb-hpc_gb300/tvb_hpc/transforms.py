@@ -139,7 +139,7 @@ class NetworkTimeStep:
         tab['model'] = self.model_id
         tab['cfun'] = self.cfun_id
         fl = nat.F_TRACE | oflags | (nat.F_SMEM_RING if smem_ok else 0)
-        if getattr(self.scheme, 'noise', False):
+        if getattr(self.scheme, 'noise', False) and np.any(np.asarray(self.sigma) != 0):
             fl |= nat.F_NOISE
         tab['flags'] = fl
         tab['sync_every'] = sync
