@@ -131,13 +131,32 @@ def mixed_workload(seed=0, scale=1.0, steps_lo=5000, steps_hi=50000):
                 bold_period=0, bold_len=0, target=None, seed=seed)
 
 
-WORKLOADS = {'grid': grid_workload, 'grid_small': grid_small_workload,
-             'kuramoto': kuramoto_workload, 'mixed': mixed_workload}
+def grid_1k_workload():
+    """Profiling case of the group kernel: the full 64 x 64 grid (same
+    instances, rings and BOLD schedule) for 1000 steps; BOLD sampled every
+    200 steps so the FC has five rows."""
+    wl = grid_workload(nsteps=1000)
+    wl.update(name='grid_1k', bold_period=200, bold_len=5)
+    return wl
+
+
+def mixed_small_workload():
+    """Traffic-capture case of the uneven batch: every connectome of the
+    mixed workload with 1/8 of its instances (128/128/32/8/2), same step
+    distribution."""
+    wl = mixed_workload(scale=0.125)
+    wl['name'] = 'mixed_small'
+    return wl
+
+
+WORKLOADS = {'grid': grid_workload, 'grid_small': grid_small_workload, 'grid_1k': grid_1k_workload,
+             'kuramoto': kuramoto_workload, 'mixed': mixed_workload,
+             'mixed_small': mixed_small_workload}
 
 
 def workload_config(wl):
-    if wl['name'] == 'mixed':
-        return {'workload': 'mixed', 'model': wl['model'], 'coupling': wl['cfun'],
+    if wl['name'].startswith('mixed'):
+        return {'workload': wl['name'], 'model': wl['model'], 'coupling': wl['cfun'],
                 'nodes': [int(p['conn'].nnode) for p in wl['parts']],
                 'edges': [int(p['conn'].nnz) for p in wl['parts']],
                 'instances': [int(p['couplings'].size) for p in wl['parts']],
@@ -154,16 +173,16 @@ def workload_config(wl):
 
 
 def node_steps(wl):
-    if wl['name'] == 'mixed':
+    if wl['name'].startswith('mixed'):
         return float(sum(p['conn'].nnode * p['steps'].sum() for p in wl['parts']))
     return float(wl['couplings'].size) * wl['conn'].nnode * wl['nsteps']
 
 
 def algorithmic_bytes_per_node_step(wl, nsvar):
-    """Data touched per node-step (SURVEY 8(d) accounting): 4 B per delayed
-    read of the coupled variable, 8 B per state variable (read + write),
-    32 B for the balloon state when BOLD is on."""
-    if wl['name'] == 'mixed':
+    """Algorithmic bytes per node-step: 4 B per delayed read of the coupled
+    variable, 8 B per state variable (read + write), 32 B for the balloon
+    state when BOLD is on."""
+    if wl['name'].startswith('mixed'):
         tot = sum(p['conn'].nnode * p['steps'].sum() for p in wl['parts'])
         E = sum(p['conn'].nnz * p['steps'].sum() for p in wl['parts']) / tot
         return 4.0 * E + 8.0 * nsvar
@@ -426,17 +445,22 @@ def roofline_entry(wl, nsvar, kernel_ms_total, steps):
     hbm = hbm or 6800.0
     bpn = algorithmic_bytes_per_node_step(wl, nsvar)
     achieved = bpn * node_steps(wl) * steps / (kernel_ms_total / 1e3) / 1e9
-    traffic = None
+    # DRAM traffic of the step kernel from an ncu capture (profiles/traffic.json:
+    # bytes per node-step measured on a capture case of this workload), per
+    # bench step
+    traffic, tsrc = None, None
     tp = os.path.join(ROOT, 'profiles', 'traffic.json')
     if os.path.exists(tp):
-        t = json.load(open(tp)).get(wl['name'])
+        key = 'mixed' if wl['name'].startswith('mixed') else wl['name'].split('_')[0]
+        t = json.load(open(tp)).get(key)
         if t:
-            traffic = t.get('dram_bytes_per_launch')
+            traffic = round(t['dram_bytes_per_node_step'] * node_steps(wl))
+            tsrc = t.get('source')
     return {'bound': 'hbm', 'achieved': round(achieved, 1), 'peak': hbm, 'unit': 'GB/s',
-            'frac': round(achieved / hbm, 4), 'traffic': traffic, 'peak_source': src,
-            'algorithmic_bytes_per_node_step': round(bpn, 2),
-            'note': 'rings staged in shared memory move no HBM bytes; frac > 1 means '
-                    'on-chip reuse beyond an HBM-streaming step'}
+            'frac': round(achieved / hbm, 4), 'traffic': traffic, 'traffic_source': tsrc,
+            'peak_source': src, 'algorithmic_bytes_per_node_step': round(bpn, 2),
+            'note': 'achieved = algorithmic bytes / event-timed kernel time; traffic = DRAM '
+                    'bytes per bench step (part of the ring reads hit L2)'}
 
 
 def cpu_baseline(wl, budget_s=12.0):
@@ -491,7 +515,7 @@ def gpu_arm(args):
     from tvb_hpc import _native
     _native.load()
     wl = WORKLOADS[args.workload]()
-    gs = (MixedStep(wl, torch, args.path, not args.no_graph) if wl['name'] == 'mixed'
+    gs = (MixedStep(wl, torch, args.path, not args.no_graph) if wl['name'].startswith('mixed')
           else GpuStep(wl, torch, args.tpn, args.warps, args.path))
 
     def barrier():
@@ -533,7 +557,7 @@ def gpu_arm(args):
     gs.status.check()
 
     plain = None
-    if wl['name'] == 'mixed':
+    if wl['name'].startswith('mixed'):
         # the plain path on the same work: one sweep launch per connectome
         gs.reset_plain()
         gs.run_plain()
@@ -766,7 +790,7 @@ def reference_arm(args):
         return
     wl = WORKLOADS[args.workload]()
     vals = []
-    base = cpu_baseline_mixed if wl['name'] == 'mixed' else cpu_baseline
+    base = cpu_baseline_mixed if wl['name'].startswith('mixed') else cpu_baseline
     for i in range(args.warmup + args.steps):
         cb = base(wl, budget_s=args.ref_seconds)
         if i >= args.warmup:
