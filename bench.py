@@ -797,7 +797,7 @@ def reference_arm(args):
             vals.append(cb['value'])
     v = float(np.median(vals))
     cb['value'] = round(v, 1)
-    line = {'metric': METRIC, 'value': round(v, 1), 'unit': UNIT, 'n_gpus': 0,
+    line = {'metric': METRIC, 'value': round(v, 1), 'unit': UNIT, 'n_gpus': args.gpus,
             'steps': args.steps, 'warmup': args.warmup, 'higher_is_better': True,
             'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32',
             'data': 'synthetic (seeded connectomes, config recipe)', 'impl': 'reference',
