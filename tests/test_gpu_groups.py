@@ -10,7 +10,7 @@ with one long run) and agreement with the per-step kernel.
 import numpy as np
 import pytest
 
-from conftest import rel_err
+from conftest import rel_err, circ_rel_err
 
 import pyoracle as orc
 from tvb_hpc import model, coupling, scheme, network, engine, groups
@@ -141,3 +141,45 @@ def test_group_batch_graph(cuda):
     for s, o, st in zip(sets, solo, steps):
         o.run(st)
         assert np.array_equal(s.state.cpu().numpy(), o.state.cpu().numpy())
+
+
+def kuramoto_setup(I=20, N=68, speeds=(4.0, 10.0), seed=11, dt=0.1):
+    w, ln = network.synthetic_connectome(N, 0.3, seed=seed)
+    conn = network.Connectivity.from_dense(w, ln)
+    rng = np.random.default_rng(seed)
+    m = model.Kuramoto()
+    cf = coupling.Kuramoto(m)
+    x0 = rng.uniform(0, 2 * np.pi, (I, N, 1)).astype(np.float32)
+    omega = rng.normal(2 * np.pi * 0.01, 0.001, (I, N, 1)).astype(np.float32)
+    kw = dict(dt=dt, couplings=np.logspace(-2, 1, I).astype(np.float32),
+              speeds=np.resize(np.asarray(speeds, np.float32), I), state0=x0, nparam=omega, seed=5)
+    return (m, cf, scheme.EulerStep(dt), conn), kw, x0
+
+
+def test_groups_kuramoto_sin_cos_ring(cuda):
+    """The Kuramoto coupling on the group kernel: the ring keeps sin and cos
+    of the phase and the coupling sum is cos(x_i) S_sin - sin(x_i) S_cos,
+    algebraically the reference's sum of sin(x_j - x_i)."""
+    args, kw, x0 = kuramoto_setup()
+    gs = groups.GroupSet(*args, **kw)
+    assert gs.channels == 2 and set(gs.block_k) == {8}
+    gs.run(1000)
+    ref = orc.run_groups_like(gs, x0, 1000)
+    assert circ_rel_err(gs.state.cpu().numpy(), ref['state']) < TOL
+    for b in range(gs.n):
+        got, r = gs.ring_plain(b), ref['rings'][b]
+        np.testing.assert_array_equal(got == 0, r == 0)
+        assert circ_rel_err(got, r) < TOL
+
+
+def test_groups_kuramoto_matches_per_instance_kernel_and_chunks(cuda):
+    args, kw, x0 = kuramoto_setup(I=10, speeds=(4.0, ))
+    a = groups.GroupSet(*args, **kw)
+    b = engine.Sweep(*args, **kw, tpn=2)
+    c = groups.GroupSet(*args, **kw)
+    a.run(600)
+    b.run(600)
+    for n in (250, 1, 349):
+        c.run(n)
+    assert circ_rel_err(a.state.cpu().numpy(), b.state.cpu().numpy()) < TOL
+    assert np.array_equal(a.state.cpu().numpy(), c.state.cpu().numpy())

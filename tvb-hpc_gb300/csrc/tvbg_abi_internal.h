@@ -37,6 +37,7 @@ BlockedKernel blocked_kernel_linear(int cfun, int tpn, int k);
 BlockedKernel blocked_kernel_g2dosc(int cfun, int tpn, int k);
 // Lane-interleaved group kernel signature and per-model lookup for (cfun, K).
 using GroupKernel = void (*)(const tvbg_group*, int32_t, const int32_t*, int32_t*);
+GroupKernel group_kernel_kuramoto(int cfun, int k);
 GroupKernel group_kernel_g2do(int cfun, int k);
 GroupKernel group_kernel_mpr(int cfun, int k);
 GroupKernel group_kernel_linear(int cfun, int k);

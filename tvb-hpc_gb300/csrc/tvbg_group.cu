@@ -10,6 +10,7 @@ namespace {
 
 GroupKernel lookup_group(int model, int cfun, int k) {
     switch (model) {
+        case TVBG_MODEL_KURAMOTO: return group_kernel_kuramoto(cfun, k);
         case TVBG_MODEL_G2DO: return group_kernel_g2do(cfun, k);
         case TVBG_MODEL_MPR: return group_kernel_mpr(cfun, k);
         case TVBG_MODEL_LINEAR: return group_kernel_linear(cfun, k);
@@ -35,7 +36,7 @@ int check_group_launch(const tvbg_launch* cfg, GroupKernel* kfn, int* cluster, s
     if (!*kfn)
         return set_error(TVBG_EUNSUPPORTED, "group kernel not built for this model/coupling/block_k");
     *cluster = c;
-    *smem = group_smem_bytes(cfg->block_k, cfg->threads);
+    *smem = group_smem_bytes(cfg->block_k, cfg->threads, cfg->cfun == TVBG_CFUN_KURAMOTO ? 2 : 1);
     return TVBG_OK;
 }
 
@@ -81,6 +82,11 @@ int tvbg_group_run(const tvbg_group* d_groups, int32_t n_groups, const tvbg_laun
         return set_error(TVBG_EINVAL, "tvbg_group_run: bad group array");
     if (n_groups == 0) return TVBG_OK;
     cudaError_t e = cudaSuccess;
+    if (smem > 48u * 1024u) {
+        e = cudaFuncSetAttribute(reinterpret_cast<const void*>(kfn),
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+        if (e != cudaSuccess) return set_cuda_error(e, "tvbg_group_run: smem attribute");
+    }
     cudaLaunchConfig_t lc;
     std::memset(&lc, 0, sizeof(lc));
     lc.gridDim = dim3(static_cast<unsigned>(n_groups) * static_cast<unsigned>(cluster), 1, 1);
@@ -108,6 +114,11 @@ int tvbg_group_occupancy(const tvbg_launch* cfg, int32_t* ctas_per_sm, int32_t* 
     if (rc) return rc;
     int n = 0;
     cudaError_t e = cudaSuccess;
+    if (smem > 48u * 1024u) {
+        e = cudaFuncSetAttribute(reinterpret_cast<const void*>(kfn),
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+        if (e != cudaSuccess) return set_cuda_error(e, "tvbg_group_occupancy: smem attribute");
+    }
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, reinterpret_cast<const void*>(kfn),
                                                       cfg->threads, smem);
     if (e != cudaSuccess) return set_cuda_error(e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor");

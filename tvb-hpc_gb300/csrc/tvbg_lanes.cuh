@@ -16,7 +16,8 @@
 // bytes -- one DRAM/L2 sector -- and the edge record (column, delay,
 // weight) is the same for the 8 lanes:
 //   ring   [N][R][8], R = nh + 8: slot s of node j at (j R + (s & (nh-1))) 8 + l,
-//          positions < 8 mirrored at +nh so a run of K <= 8 slots never wraps
+//          positions < 8 mirrored at +nh so a run of K <= 8 slots never wraps;
+//          with the Kuramoto coupling [N][R][2][8]: sin and cos of the observable
 //   state  [N][NS][8], nparam [N][NP][8], bold [4][N][8],
 //   bold_out [bold_len][N][8], trace [trace_len][N][trace_nobs][8].
 //
@@ -166,9 +167,63 @@ __device__ __forceinline__ void lane_gather(const tvbg_group& g, int lo, int hi,
     }
 }
 
-// Dynamic shared memory of a group CTA: the K coupling sums of every thread.
-__host__ __device__ constexpr uint32_t group_smem_bytes(int K, int threads) {
-    return static_cast<uint32_t>(4 * K * threads);
+// Kuramoto coupling, sum_e w_e sin(x_j - x_i) = cos x_i sum_e w_e sin x_j
+// - sin x_i sum_e w_e cos x_j: the ring carries two channels, sin and cos
+// of the observable ([N][R][2][8]), and the gather sums both for the K steps
+// (16 independent loads in flight per thread, CSR order).
+template <int K>
+__device__ __forceinline__ void lane_gather_sc(const tvbg_group& g, int lo, int hi, uint32_t tm,
+                                               uint32_t mask, uint32_t R, int l, float accs[K],
+                                               float accc[K]) {
+    constexpr int RL = 2 * kLanes;
+    constexpr int U = 8 / K;
+    const float* __restrict__ ring = g.ring + l;
+    const uint2* __restrict__ edges = reinterpret_cast<const uint2*>(g.edges);
+#pragma unroll
+    for (int k = 0; k < K; ++k) accs[k] = accc[k] = 0.0f;
+    auto addr = [&](uint32_t pk) {
+        return ring + (static_cast<size_t>(pk >> 16) * R + ((tm + (pk & 0xffffu)) & mask)) * RL;
+    };
+    int e = lo;
+    for (; e < hi; e += U) {
+        float vs[U][K], vc[U][K];
+        float w[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            if (e + u < hi) {
+                const uint2 ed = __ldg(edges + e + u);
+                const float* p = addr(ed.x);
+                w[u] = __uint_as_float(ed.y);
+#pragma unroll
+                for (int k = 0; k < K; ++k) {
+                    vs[u][k] = __ldcg(p + k * RL);
+                    vc[u][k] = __ldcg(p + k * RL + kLanes);
+                }
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            if (e + u < hi) {
+#pragma unroll
+                for (int k = 0; k < K; ++k) {
+                    accs[k] = fmaf(w[u], vs[u][k], accs[k]);
+                    accc[k] = fmaf(w[u], vc[u][k], accc[k]);
+                }
+            }
+        }
+    }
+}
+
+// Ring channels per (node, slot): 2 (sin, cos) for the Kuramoto coupling, else 1.
+template <int CF>
+__host__ __device__ constexpr int ring_channels() {
+    return CF == TVBG_CFUN_KURAMOTO ? 2 : 1;
+}
+
+// Dynamic shared memory of a group CTA: the K coupling sums (per ring
+// channel) of every thread.
+__host__ __device__ constexpr uint32_t group_smem_bytes(int K, int threads, int nc) {
+    return static_cast<uint32_t>(4 * K * threads * nc);
 }
 
 template <class M, int CF, int K>
@@ -176,6 +231,8 @@ __device__ __forceinline__ void run_group(const tvbg_group& g, float* csum, int3
     constexpr int NS = M::NS;
     constexpr int NP = M::NP;
     constexpr int SPC = Noise<M>::SPC;
+    constexpr int NC = ring_channels<CF>();
+    constexpr int RL = kLanes * NC;  // floats per (node, slot)
     const int N = g.N;
     const uint32_t C = cluster_nranks();
     const uint32_t rank = cluster_rank();
@@ -216,10 +273,21 @@ __device__ __forceinline__ void run_group(const tvbg_group& g, float* csum, int3
             float x[NS];
 #pragma unroll
             for (int v = 0; v < NS; ++v) x[v] = state[(n * NS + v) * kLanes + l];
-            const size_t idx = (static_cast<size_t>(n) * R + pos) * kLanes + l;
+            const size_t idx = (static_cast<size_t>(n) * R + pos) * RL + l;
             const float o = M::obs(x, 0);
-            ring[idx] = o;
-            if (pos < kGhost) ring[idx + static_cast<size_t>(nh) * kLanes] = o;
+            if constexpr (NC == 2) {
+                float sn, cs;
+                sincosf(o, &sn, &cs);
+                ring[idx] = sn;
+                ring[idx + kLanes] = cs;
+                if (pos < kGhost) {
+                    ring[idx + static_cast<size_t>(nh) * RL] = sn;
+                    ring[idx + static_cast<size_t>(nh) * RL + kLanes] = cs;
+                }
+            } else {
+                ring[idx] = o;
+                if (pos < kGhost) ring[idx + static_cast<size_t>(nh) * kLanes] = o;
+            }
         }
     }
     group_barrier(cluster);
@@ -244,10 +312,20 @@ __device__ __forceinline__ void run_group(const tvbg_group& g, float* csum, int3
             {
                 const int lo = valid ? __ldg(g.row + n) : 0;
                 const int hi = valid ? __ldg(g.row + n + 1) : 0;
-                float acc[K];
-                lane_gather<CF, K>(g, lo, hi, tm, mask, R, l, acc);
+                if constexpr (NC == 2) {
+                    float accs[K], accc[K];
+                    lane_gather_sc<K>(g, lo, hi, tm, mask, R, l, accs, accc);
 #pragma unroll
-                for (int k = 0; k < K; ++k) csum[k * blockDim.x + threadIdx.x] = acc[k];
+                    for (int k = 0; k < K; ++k) {
+                        csum[k * blockDim.x + threadIdx.x] = accs[k];
+                        csum[(K + k) * blockDim.x + threadIdx.x] = accc[k];
+                    }
+                } else {
+                    float acc[K];
+                    lane_gather<CF, K>(g, lo, hi, tm, mask, R, l, acc);
+#pragma unroll
+                    for (int k = 0; k < K; ++k) csum[k * blockDim.x + threadIdx.x] = acc[k];
+                }
             }
             if (!valid) continue;
             float x[NS], p[NP];
@@ -264,6 +342,8 @@ __device__ __forceinline__ void run_group(const tvbg_group& g, float* csum, int3
                 bQ = g.bold[(3 * N + n) * kLanes + l];
             }
             float obs0 = M::obs(x, 0);
+            float sn0 = 0.0f, cs0 = 0.0f;  // sin, cos of obs0 (Kuramoto coupling)
+            if constexpr (NC == 2) sincosf(obs0, &sn0, &cs0);
             float zz[4] = {0.0f, 0.0f, 0.0f, 0.0f};
             int b_next = b_until, tr_next = tr_until;
             int brow = b_row, trow = tr_row;
@@ -278,8 +358,15 @@ __device__ __forceinline__ void run_group(const tvbg_group& g, float* csum, int3
                     trow = trow + 1 == g.trace_len ? 0 : trow + 1;
                 }
                 const float xbold = bold ? M::obs(x, g.bold_obs) : 0.0f;
-                const float c = lane_post<CF>(csum[k * blockDim.x + threadIdx.x], obs0, wsum, cf_a,
-                                              g.cf_b);
+                float c;
+                if constexpr (NC == 2) {
+                    // sum_e w sin(x_j - x_i); post = a * mean (coupling.py:119-121)
+                    const float S = cs0 * csum[k * blockDim.x + threadIdx.x] -
+                                    sn0 * csum[(K + k) * blockDim.x + threadIdx.x];
+                    c = cf_a * (S / static_cast<float>(N));
+                } else {
+                    c = lane_post<CF>(csum[k * blockDim.x + threadIdx.x], obs0, wsum, cf_a, g.cf_b);
+                }
                 float f[NS];
                 M::drift(x, c, p, g.consts, f);
 #pragma unroll
@@ -302,9 +389,19 @@ __device__ __forceinline__ void run_group(const tvbg_group& g, float* csum, int3
                 M::limit(x, flags);
                 obs0 = M::obs(x, 0);
                 const uint32_t pos = (static_cast<uint32_t>(t) + 1u) & mask;
-                const size_t idx = (static_cast<size_t>(n) * R + pos) * kLanes + l;
-                ring[idx] = obs0;
-                if (pos < kGhost) ring[idx + static_cast<size_t>(nh) * kLanes] = obs0;
+                const size_t idx = (static_cast<size_t>(n) * R + pos) * RL + l;
+                if constexpr (NC == 2) {
+                    sincosf(obs0, &sn0, &cs0);
+                    ring[idx] = sn0;
+                    ring[idx + kLanes] = cs0;
+                    if (pos < kGhost) {
+                        ring[idx + static_cast<size_t>(nh) * RL] = sn0;
+                        ring[idx + static_cast<size_t>(nh) * RL + kLanes] = cs0;
+                    }
+                } else {
+                    ring[idx] = obs0;
+                    if (pos < kGhost) ring[idx + static_cast<size_t>(nh) * kLanes] = obs0;
+                }
                 if (bold) {
                     Balloon::step(bs, bF, bV, bQ, xbold, g.dt_bold);
                     if (k == b_next) {
@@ -350,7 +447,7 @@ __global__ void __launch_bounds__(1024, 1)
     group_kernel(const tvbg_group* __restrict__ groups, int32_t n_groups,
                  const int32_t* __restrict__ order, int32_t* __restrict__ status) {
     __shared__ __align__(16) tvbg_group s_grp;
-    extern __shared__ float csum[];  // [K][blockDim]: the block's coupling sums per thread
+    extern __shared__ float csum[];  // [channels][K][blockDim]: the block's coupling sums
     const int cid = static_cast<int>(cluster_id_x());
     if (cid >= n_groups) return;  // uniform over the cluster
     const int idx = order ? __ldg(order + cid) : cid;

@@ -68,6 +68,12 @@ def group_occupancy(cfg):
     return int(per.value), int(sms.value)
 
 
+def torch_stack_sc(x):
+    "(sin x, cos x) stacked on a new axis before the last one."
+    import torch
+    return torch.stack([torch.sin(x), torch.cos(x)], dim=-2)
+
+
 class GroupSet:
     """
     Device-resident instances of one connectome in lane-interleaved groups.
@@ -80,8 +86,9 @@ class GroupSet:
                 length into the same group (longest first);
       block_k : 4 or 8 steps per barrier (default: 8 when d_min >= 7);
       threads, cluster : launch shape (default: group_shape).
-    Couplings must be separable (Linear, Diff, Sigmoidal); the Kuramoto
-    model and the Track-A order run on the per-instance kernels.
+    Couplings must be separable (Linear, Diff, Sigmoidal), or the Kuramoto
+    coupling with the Kuramoto model (whose ring keeps sin and cos of the
+    phase); the Track-A order runs on the per-instance kernels.
 
     A lane that takes fewer steps than its group is finished after its run;
     the group's clock advances by the longest lane.
@@ -99,10 +106,13 @@ class GroupSet:
         self.model, self.cfun, self.scheme = model, cfun, scheme
         self.model_id, self.consts, self.sigma = model.engine_spec()
         self.cfun_id, cf_a0, cf_b0, self.cf_p = cfun.engine_spec()
-        if self.cfun_id not in (nat.CFUN_LINEAR, nat.CFUN_DIFF, nat.CFUN_SIGMOIDAL):
-            raise ValueError('group kernel needs a separable coupling (Linear, Diff, Sigmoidal)')
-        if self.model_id == nat.MODEL_KURAMOTO:
-            raise ValueError('Kuramoto runs on the per-instance kernels')
+        separable = self.cfun_id in (nat.CFUN_LINEAR, nat.CFUN_DIFF, nat.CFUN_SIGMOIDAL)
+        kuramoto = (self.model_id, self.cfun_id) == (nat.MODEL_KURAMOTO, nat.CFUN_KURAMOTO)
+        if not (separable or kuramoto):
+            raise ValueError('group kernel: a separable coupling (Linear, Diff, Sigmoidal), or the '
+                             'Kuramoto model with the Kuramoto coupling')
+        # the Kuramoto coupling keeps sin and cos of the observable in the ring
+        self.channels = 2 if self.cfun_id == nat.CFUN_KURAMOTO else 1
         self.N = N = int(conn.nnode)
         if N > 65535:
             raise ValueError('group kernel: N < 65536')
@@ -172,7 +182,7 @@ class GroupSet:
         self.block_k = np.array([plans[t][0] for t in self.gtab], np.int32)
         self.lognh = np.array([plans[t][1] for t in self.gtab], np.int32)
         R = (1 << self.lognh.astype(np.int64)) + 8
-        ring_len = N * R * L
+        ring_len = N * R * L * self.channels
         self.ring_off = np.concatenate([[0], np.cumsum(ring_len)[:-1]]).astype(np.int64)
         self.ring = torch.zeros(int(ring_len.sum()), dtype=torch.float32, device='cuda')
         self.R = R
@@ -232,8 +242,9 @@ class GroupSet:
         self._streams = None
 
     def bold_obs(self):
-        "Observable feeding the balloon: V for G2DO (tvb_hpc order W, V), else obs 0."
-        return 1 if self.model_id == nat.MODEL_G2DO else 0
+        """Observable feeding the balloon: sin(theta) for Kuramoto, V for G2DO
+        (tvb_hpc order W, V), else obs 0 (as engine.InstanceSet)."""
+        return 1 if self.model_id in (nat.MODEL_KURAMOTO, nat.MODEL_G2DO) else 0
 
     # -- per-instance views ------------------------------------------------------
     @property
@@ -265,21 +276,32 @@ class GroupSet:
 
     def fill_history(self):
         "Every ring slot of every lane holds obs0 of the current state."
-        N = self.N
+        N, C = self.N, self.channels
         o0 = self.gstate[:, :, 0, :]                                  # [G, N, L]
+        if C == 2:
+            o0 = torch_stack_sc(o0)                                   # [G, N, 2, L]
+        else:
+            o0 = o0[:, :, None, :]
         for g in range(self.n_groups):
             R = int(self.R[g])
             o = int(self.ring_off[g])
-            self.ring[o:o + N * R * L].view(N, R, L).copy_(o0[g][:, None, :].expand(N, R, L))
+            self.ring[o:o + N * R * L * C].view(N, R, C, L).copy_(
+                o0[g][:, None, :, :].expand(N, R, C, L))
 
     def ring_plain(self, b):
-        "Ring of instance b as numpy [nh, N] slot-major (the oracle's layout)."
+        """Ring of instance b as numpy [nh, N] slot-major (the oracle's layout);
+        with the Kuramoto coupling the phase is recovered from (sin, cos) into
+        [0, 2 pi) (slots never written read 0)."""
         g, l = int(self.grp_of[b]), int(self.lane_of[b])
-        R = int(self.R[g])
+        R, C = int(self.R[g]), self.channels
         nh = 1 << int(self.lognh[g])
         o = int(self.ring_off[g])
-        r = self.ring[o:o + self.N * R * L].view(self.N, R, L)[:, :nh, l]
-        return r.t().contiguous().cpu().numpy()
+        r = self.ring[o:o + self.N * R * L * C].view(self.N, R, C, L)[:, :nh, :, l]
+        r = r.cpu().numpy()
+        if C == 2:
+            th = np.mod(np.arctan2(r[:, :, 0], r[:, :, 1]), 2 * np.pi)
+            return np.ascontiguousarray(th.T.astype(np.float32))
+        return np.ascontiguousarray(r[:, :, 0].T)
 
     # -- launches -------------------------------------------------------------------
     def build_table(self, nsteps):

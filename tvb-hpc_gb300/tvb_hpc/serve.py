@@ -10,11 +10,10 @@ memory and advances all of them together:
   tick:
     1. admit queued requests (arrival time <= now) while their device
        footprint fits the HBM budget;
-    2. advance every active request by min(chunk, steps left): requests on
-       separable couplings run as lane-interleaved groups (tvbg_group_run,
-       one forked stream per request), the others (Kuramoto, gradient
-       requests) as one persistent batch launch per model (tvbg_batch_run),
-       all on the device at once;
+    2. advance every active request by min(chunk, steps left): requests run
+       as lane-interleaved groups (tvbg_group_run, one forked stream per
+       request), gradient requests as one persistent batch launch per model
+       (tvbg_batch_run), all on the device at once;
     3. retire requests that reached their step count: copy the final state
        (and gradients) to the host, free the device memory, record latency.
 
@@ -144,7 +143,7 @@ class Server:
                else sch.EulerStep(req.dt))
         kw = dict(dt=req.dt, couplings=req.couplings, speeds=req.speeds, state0=req.x0,
                   nparam=req.nparam, seed=req.seed)
-        if not req.want_grad and req.model != 'Kuramoto':
+        if not req.want_grad:
             try:
                 return GroupSet(m, cf, scm, req.conn, **kw)
             except ValueError:      # delays too short for the group kernel's blocks
