@@ -313,9 +313,10 @@ class MixedStep:
         for s, x in zip(self.sets, self.x0 if x0 is None else x0):
             if self.path == 'groups':
                 s.set_state(x)
+                s.clear_history()
             else:
                 s.state.copy_(x)
-            s.ring.zero_()
+                s.ring.zero_()
 
     def run(self, time_kernels=False):
         evs = []
@@ -391,12 +392,13 @@ class GpuStep:
     def reset(self, x0=None):
         sw = self.sw
         x = self.x0 if x0 is None else x0
-        sw.ring.zero_()
         if self.groups:
+            sw.clear_history()
             sw.set_state(x)
             if sw.gbold is not None:
                 sw.gbold.zero_()
         else:
+            sw.ring.zero_()
             sw.state.copy_(x)
             if sw.bold is not None:
                 sw.bold.zero_()

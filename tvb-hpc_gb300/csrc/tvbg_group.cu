@@ -82,7 +82,7 @@ int tvbg_group_run(const tvbg_group* d_groups, int32_t n_groups, const tvbg_laun
         return set_error(TVBG_EINVAL, "tvbg_group_run: bad group array");
     if (n_groups == 0) return TVBG_OK;
     cudaError_t e = cudaSuccess;
-    if (smem > 48u * 1024u) {
+    if (smem + sizeof(tvbg_group) > 48u * 1024u) {  // beyond the default: opt in
         e = cudaFuncSetAttribute(reinterpret_cast<const void*>(kfn),
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
         if (e != cudaSuccess) return set_cuda_error(e, "tvbg_group_run: smem attribute");
@@ -114,7 +114,7 @@ int tvbg_group_occupancy(const tvbg_launch* cfg, int32_t* ctas_per_sm, int32_t* 
     if (rc) return rc;
     int n = 0;
     cudaError_t e = cudaSuccess;
-    if (smem > 48u * 1024u) {
+    if (smem + sizeof(tvbg_group) > 48u * 1024u) {  // beyond the default: opt in
         e = cudaFuncSetAttribute(reinterpret_cast<const void*>(kfn),
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
         if (e != cudaSuccess) return set_cuda_error(e, "tvbg_group_occupancy: smem attribute");

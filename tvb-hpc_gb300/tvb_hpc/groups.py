@@ -186,6 +186,7 @@ class GroupSet:
         self.ring_off = np.concatenate([[0], np.cumsum(ring_len)[:-1]]).astype(np.int64)
         self.ring = torch.zeros(int(ring_len.sum()), dtype=torch.float32, device='cuda')
         self.R = R
+        self.clear_history()
         self._gi = torch.from_numpy(self.grp_of).cuda()
         self._li = torch.from_numpy(self.lane_of).cuda()
         # state / parameters [G, N, ns, L]
@@ -266,13 +267,24 @@ class GroupSet:
         return None if self.gtrace is None else self.gtrace[self._gi, :, :, :, self._li]
 
     def reset(self, state=None):
-        "Zero rings and monitors; optionally set the state; clocks back to 0."
-        self.ring.zero_()
+        "Zero history and monitors; optionally set the state; clocks back to 0."
+        self.clear_history()
         if self.gbold is not None:
             self.gbold.zero_()
         if state is not None:
             self.set_state(state)
         self.t[:] = 0
+
+    def clear_history(self):
+        """Zero history (every slot holds the observable 0): zeros, or with the
+        Kuramoto coupling (sin 0, cos 0) = (0, 1) in every slot."""
+        self.ring.zero_()
+        if self.channels == 2:
+            N = self.N
+            for g in range(self.n_groups):
+                R = int(self.R[g])
+                o = int(self.ring_off[g])
+                self.ring[o:o + N * R * L * 2].view(N, R, 2, L)[:, :, 1, :] = 1.0
 
     def fill_history(self):
         "Every ring slot of every lane holds obs0 of the current state."
