@@ -342,11 +342,14 @@ int tvbg_philox_u32(uint32_t k0, uint32_t k1, uint32_t c1, uint32_t c2,
  * instances, so one delayed read of an edge is one 32-byte sector for the
  * group and the edge record is read once for 8 instances.  Same step (CUDA
  * order) and Philox streams as tvbg_sweep; couplings LINEAR, DIFF and
- * SIGMOIDAL; block_k (4 or 8) steps per barrier, which needs every delay
+ * SIGMOIDAL, and KURAMOTO with the Kuramoto model; block_k (4 or 8) steps
+ * per barrier, which needs every delay
  * >= block_k - 1 and nh >= max(delay) + 1 + block_k.
  * Layouts (L = 8, R = nh + 8, l = lane):
  *   ring     [N][R][L]  slot s of node j at (j*R + (s & (nh-1)))*L + l;
- *                       positions < 8 are mirrored at +nh
+ *                       positions < 8 are mirrored at +nh; with the
+ *                       KURAMOTO coupling (Kuramoto model) [N][R][2][L]:
+ *                       sin and cos of the observable, zero history (0, 1)
  *   state    [N][nsvar][L]      nparam  [N][npar][L]
  *   bold     [4][N][L]          bold_out [bold_len][N][L]
  *   trace    [trace_len][N][trace_nobs][L]
