@@ -138,15 +138,13 @@ class GroupSet:
         self.delay_tables = tables
         plans = [plan_group(d.min() if d.size else 7, d.max() if d.size else 0, block_k)
                  for d in tables]
-        # per-node constants shared by every table: in-edge weight sums
-        # (float32, CSR order) and the visiting order (in-degree, descending)
-        wsum = np.zeros(N, np.float32)
-        for i in range(N):
-            s = np.float32(0.0)
-            for x in w[row[i]:row[i + 1]]:
-                s = np.float32(s + x)
-            wsum[i] = s
+        # per-node constants shared by every table: in-edge weight sums and
+        # the visiting order (in-degree, descending)
         deg = np.diff(row)
+        wsum = np.zeros(N, np.float32)
+        nz = deg > 0
+        if col.size:
+            wsum[nz] = np.add.reduceat(w, row[:-1][nz]).astype(np.float32)
         nodes = np.argsort(-deg, kind='stable').astype(np.int32)
         self.row = torch.from_numpy(row).cuda()
         self.wsum = torch.from_numpy(wsum).cuda()
@@ -357,14 +355,14 @@ class GroupSet:
         tab['cf_p'] = np.asarray(self.cf_p, np.float32)
         tab['sigma'] = self.sigma
         tab['consts'] = self.consts
-        gmax = np.zeros(G, np.int64)
-        for g, m in enumerate(self.members):
-            ln = tab['lanes'][g]
-            ln['cf_a'][:m.size] = self.cf_a[m]
-            ln['nsteps'][:m.size] = steps[m]
-            ln['inst_id'][:m.size] = self.inst_ids[m]
-            tab['lanes'][g] = ln
-            gmax[g] = steps[m].max()
+        # lanes: instance b sits in group grp_of[b], lane lane_of[b]; padding
+        # lanes keep nsteps = 0
+        lanes = tab['lanes']
+        gi_, li_ = self.grp_of, self.lane_of
+        lanes['cf_a'][gi_, li_] = self.cf_a
+        lanes['nsteps'][gi_, li_] = steps
+        lanes['inst_id'][gi_, li_] = self.inst_ids
+        gmax = lanes['nsteps'].max(axis=1).astype(np.int64)
         tab['nsteps'] = gmax
         return tab, gmax
 
