@@ -742,7 +742,7 @@ def serve_arm(args):
                        'hbm_budget_gb': 180},
             'serve': {'p50_latency_s': round(st.get('p50_s', float('nan')), 3),
                       'p99_latency_s': round(st.get('p99_s', float('nan')), 3),
-                      'wall_s': round(wall, 3), 'ticks': st['ticks'],
+                      'wall_s': round(wall, 3), 'ticks': st['ticks'], 'phase_s': st['phase_s'],
                       'offered_node_steps_per_s': round(offered, 1),
                       'queue_kept_up': bool(wall <= args.serve_seconds * 1.25)},
             'plain': plain,

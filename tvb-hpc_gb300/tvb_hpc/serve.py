@@ -110,6 +110,9 @@ class Server:
         self.used = 0
         self.ticks = 0
         self.node_steps = 0.0
+        # wall time split per phase (admission incl. set-up, launch
+        # preparation, device, retirement)
+        self.phase_s = dict(admit=0.0, prepare=0.0, device=0.0, retire=0.0)
 
     def submit(self, req):
         self.queue.append(req)
@@ -164,7 +167,10 @@ class Server:
 
     def tick(self):
         "Admit, advance every active request by one chunk, retire; returns work done."
+        t_a = time.perf_counter()
         self._admit(self.clock())
+        t_p = time.perf_counter()
+        self.phase_s['admit'] += t_p - t_a
         if not self.active:
             return 0.0
         by_model, grouped = {}, []
@@ -187,7 +193,11 @@ class Server:
             batches.append((b, reqs, steps))
         for b, reqs, steps in batches:
             work += sum(r.couplings.size * r.conn.nnode * n for r, n in zip(reqs, steps))
+        t_d = time.perf_counter()
         self.torch.cuda.synchronize()
+        t_r = time.perf_counter()
+        self.phase_s['prepare'] += t_d - t_p
+        self.phase_s['device'] += t_r - t_d
         for b, reqs, steps in batches:
             b.status.check()
             for r, n in zip(reqs, steps):
@@ -197,6 +207,7 @@ class Server:
         self.active = [r for r in self.active if r.steps_done < r.nsteps]
         for r in finished:
             self._retire(r)
+        self.phase_s['retire'] += time.perf_counter() - t_r
         self.ticks += 1
         self.node_steps += work
         return work
@@ -217,7 +228,8 @@ class Server:
 
     def stats(self):
         lat = np.array([r.latency for r in self.done if r.latency is not None])
-        out = {'requests': len(self.done), 'ticks': self.ticks, 'node_steps': self.node_steps}
+        out = {'requests': len(self.done), 'ticks': self.ticks, 'node_steps': self.node_steps,
+               'phase_s': {k: round(v, 3) for k, v in self.phase_s.items()}}
         if lat.size:
             out.update(p50_s=float(np.percentile(lat, 50)), p99_s=float(np.percentile(lat, 99)))
         return out
