@@ -17,10 +17,12 @@ memory and advances all of them together:
     3. retire requests that reached their step count: copy the final state
        (and gradients) to the host, free the device memory, record latency.
 
-Requests that arrive while a tick runs join at the next tick, as slots and
-memory free up; their work overlaps on the device with the requests already
-running.  Chunk boundaries are exact (the step kernels resume bit-for-bit
-from the resident state and ring), and every request keeps its own Philox
+Requests that arrive while a tick runs are admitted while the device runs
+that tick (their state is built on a side stream) and join at the next
+tick, as slots and memory free up; their work overlaps on the device with
+the requests already running.  Chunk boundaries are exact (the step kernels
+resume bit-for-bit from the resident state and ring), and every request
+keeps its own Philox
 key (request seed, request-local instance id) and launch shape, so a
 request's result is the same alone and in any mix.
 
@@ -113,12 +115,17 @@ class Server:
         # wall time split per phase (admission incl. set-up, launch
         # preparation, device, retirement)
         self.phase_s = dict(admit=0.0, prepare=0.0, device=0.0, retire=0.0)
+        self.side = torch.cuda.Stream()
 
     def submit(self, req):
         self.queue.append(req)
 
-    def _admit(self, now):
+    def _admit(self, now, into=None):
+        """Admit queued requests that have arrived and fit the budget; their
+        device state is built on the current stream and appended to `into`
+        (default: the active list)."""
         torch = self.torch
+        into = self.active if into is None else into
         keep = []
         for req in sorted(self.queue, key=lambda r: r.arrival):
             if req.arrival > now:
@@ -133,12 +140,15 @@ class Server:
             req.admitted = self.clock()
             req.nbytes = need
             self.used += need
-            self.active.append(req)
+            into.append(req)
         self.queue = keep
 
     @staticmethod
     def _make_set(req):
-        "Lane-interleaved groups where the coupling is separable, else per-instance."
+        """Lane-interleaved groups (every model/coupling pair the server offers),
+        per-instance kernels for gradient requests (the adjoint recomputes
+        from per-instance rings) and where the group kernel's blocks do not
+        fit the delays."""
         M, C, noise = MODELS[req.model]
         m = M()
         cf = C(m)
@@ -194,17 +204,26 @@ class Server:
         for b, reqs, steps in batches:
             work += sum(r.couplings.size * r.conn.nnode * n for r, n in zip(reqs, steps))
         t_d = time.perf_counter()
+        self.phase_s['prepare'] += t_d - t_p
+        # while the device runs this chunk, admit what has arrived meanwhile:
+        # the new requests' device state is built on a side stream and they
+        # join at the next tick
+        fresh = []
+        if self.queue:
+            with self.torch.cuda.stream(self.side):
+                self._admit(self.clock(), into=fresh)
+        t_s = time.perf_counter()
+        self.phase_s['admit'] += t_s - t_d
         self.torch.cuda.synchronize()
         t_r = time.perf_counter()
-        self.phase_s['prepare'] += t_d - t_p
-        self.phase_s['device'] += t_r - t_d
+        self.phase_s['device'] += t_r - t_s
         for b, reqs, steps in batches:
             b.status.check()
             for r, n in zip(reqs, steps):
                 r.steps_done += n
                 r.iset.t += n
         finished = [r for r in self.active if r.steps_done >= r.nsteps]
-        self.active = [r for r in self.active if r.steps_done < r.nsteps]
+        self.active = [r for r in self.active if r.steps_done < r.nsteps] + fresh
         for r in finished:
             self._retire(r)
         self.phase_s['retire'] += time.perf_counter() - t_r
