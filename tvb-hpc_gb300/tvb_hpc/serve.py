@@ -22,9 +22,8 @@ that tick (their state is built on a side stream) and join at the next
 tick, as slots and memory free up; their work overlaps on the device with
 the requests already running.  Chunk boundaries are exact (the step kernels
 resume bit-for-bit from the resident state and ring), and every request
-keeps its own Philox
-key (request seed, request-local instance id) and launch shape, so a
-request's result is the same alone and in any mix.
+keeps its own Philox key (request seed, request-local instance id) and
+launch shape, so a request's result is the same alone and in any mix.
 
 The reference has no serving layer; its CUDA launcher runs one sweep per
 call and copies results back after every chunk
