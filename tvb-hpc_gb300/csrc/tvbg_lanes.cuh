@@ -9,6 +9,7 @@
 //   S     = sum_e w_e pre(ring[t - d_e][col_e])          (CSR order)
 //   c     = post(S, obs0(x_i), sum_e w_e)
 //   x'    = limit(x + dt f(x, c, p) + sqrt(dt) sigma z)   z: Philox(seed_lo, inst; node, t/SPC, seed_hi)
+//           (Box-Muller with CUDA's fast intrinsics, box_muller_fast)
 //   ring[t+1][i] = obs0(x')
 //
 // Layout.  Every per-node quantity is interleaved over the 8 instances of
@@ -378,8 +379,8 @@ __device__ __forceinline__ void run_group(const tvbg_group& g, float* csum, int3
                             const u32x4 w = philox4x32_10(static_cast<uint32_t>(n),
                                                           static_cast<uint32_t>(t / SPC), g.seed_hi, 0u,
                                                           g.seed_lo, inst_id);
-                            box_muller(w.v[0], w.v[1], zz[0], zz[1]);
-                            box_muller(w.v[2], w.v[3], zz[2], zz[3]);
+                            box_muller_fast(w.v[0], w.v[1], zz[0], zz[1]);
+                            box_muller_fast(w.v[2], w.v[3], zz[2], zz[3]);
                         }
 #pragma unroll
                         for (int v = 0; v < NS; ++v)
