@@ -322,6 +322,25 @@ int tvbg_fc_noalloc(const float *d_x, int32_t n_inst, int32_t T, int32_t N,
                     double *d_err, void *stream);
 
 /*
+ * Streaming covariance for long runs: fold one sample per instance into an
+ * FP64 running state (Welford update).  d_x: sample of instance b at
+ * d_x + b * x_stride (N floats); n: samples already folded (0 starts a new
+ * state -- the state arrays need no clearing); d_mean: double [n_inst][N];
+ * d_m2: double [n_inst][N][N], the co-moment
+ * sum_s (x_si - mean_i)(x_sj - mean_j) over the samples folded so far.
+ * N <= 3000.  Replaces tvb_hpc/metric.py:87-108 (OnlineCov) and
+ * dsl/dsl_cuda/CUDAmodels/refs/covar.c:9-68 (update_cov).
+ */
+int tvbg_cov_update(const float *d_x, int64_t x_stride, int32_t n_inst,
+                    int32_t N, int64_t n, double *d_mean, double *d_m2,
+                    void *stream);
+
+/* Pearson correlation of a streaming state: corr_ij = m2_ij / sqrt(m2_ii
+ * m2_jj), float [n_inst][N][N].  Replaces refs/covar.c:73-109 (cov_to_corr). */
+int tvbg_cov_corr(const double *d_m2, int32_t n_inst, int32_t N, float *d_corr,
+                  void *stream);
+
+/*
  * Fill d_out[0..n) with standard normals from Philox4x32-10 (Salmon et al.
  * 2011) + Box-Muller: key = (seed_lo, stream_id), counter = (i/4, 0,
  * seed_hi, 0) for output i.  Replaces tvb_hpc/rng.py:30-96 (RNG.fill).

@@ -204,6 +204,8 @@ SIGNATURES = {
     'tvbg_adjoint_mpr': (ctypes.c_int, [_vp, _i32, _i32, _vp]),
     'tvbg_philox_u32': (ctypes.c_int, [_u32, _u32, _u32, _u32, _u32, _vp, _i64, _vp]),
     'tvbg_group_size': (_sz, []),
+    'tvbg_cov_update': (ctypes.c_int, [_vp, _i64, _i32, _i32, _i64, _vp, _vp, _vp]),
+    'tvbg_cov_corr': (ctypes.c_int, [_vp, _i32, _i32, _vp, _vp]),
     'tvbg_pack_edges_group': (ctypes.c_int, [_i32, _i32, _vp, _vp, _vp, _vp, _i32, _vp]),
     'tvbg_group_run': (ctypes.c_int, [_vp, _i32, ctypes.POINTER(tvbg_launch), _vp]),
     'tvbg_group_occupancy': (ctypes.c_int, [ctypes.c_void_p, _ip, _ip]),

@@ -92,3 +92,51 @@ class OnlineCov:
         self.cov += np.outer(x - u1, x - self.u)
         self.u = u1
         self.t += 1
+
+
+class StreamingFC:
+    """
+    Device-resident streaming covariance / FC of many instances for long
+    runs (tvbg_cov_update, tvbg_cov_corr): fold one sample per instance at a
+    time -- e.g. each new BOLD row -- with FP64 Welford updates, read the
+    Pearson FC at any point; the time series itself need not be kept.  The
+    GPU counterpart of OnlineCov (metric.py:87-108) and
+    dsl/dsl_cuda/CUDAmodels/refs/covar.c:9-109.
+    """
+
+    def __init__(self, n_inst, N, device='cuda'):
+        import torch
+        self.torch = torch
+        self.n_inst, self.N = int(n_inst), int(N)
+        self.n = 0
+        self.mean = torch.empty((n_inst, N), dtype=torch.float64, device=device)
+        self.m2 = torch.empty((n_inst, N, N), dtype=torch.float64, device=device)
+
+    def update(self, x, stream=None):
+        "x: float32 CUDA [n_inst, N] (rows may be strided); one sample per instance."
+        lib = nat.load()
+        torch = self.torch
+        if x.dtype != torch.float32:
+            x = x.float()
+        if x.shape != (self.n_inst, self.N):
+            raise ValueError('sample shape %s, expected %s' % (tuple(x.shape), (self.n_inst, self.N)))
+        if x.stride(1) != 1 or x.stride(0) < self.N:
+            x = x.contiguous()
+        nat.check(lib.tvbg_cov_update(x.data_ptr(), x.stride(0), self.n_inst, self.N, self.n,
+                                      self.mean.data_ptr(), self.m2.data_ptr(),
+                                      nat.stream_handle(stream)))
+        self.n += 1
+
+    def update_rows(self, xs, rows, stream=None):
+        "Fold rows `rows` of xs [n_inst, T, N] in order."
+        for r in rows:
+            self.update(xs[:, r, :], stream)
+
+    def corr(self, stream=None):
+        "Pearson FC [n_inst, N, N] float32 of the samples folded so far."
+        lib = nat.load()
+        out = self.torch.empty((self.n_inst, self.N, self.N), dtype=self.torch.float32,
+                               device=self.m2.device)
+        nat.check(lib.tvbg_cov_corr(self.m2.data_ptr(), self.n_inst, self.N, out.data_ptr(),
+                                    nat.stream_handle(stream)))
+        return out
