@@ -22,7 +22,7 @@ def test_streaming_fc_matches_two_pass(cuda, I, T, N):
     s = metric.StreamingFC(I, N)
     s.update_rows(xd, range(T))         # strided rows of [I, T, N]
     got = s.corr().cpu().numpy()
-    ref, _ = metric.fc(xd)
+    ref = metric.fc(xd)
     np.testing.assert_allclose(got, ref.cpu().numpy(), atol=1e-6)
     np.testing.assert_allclose(got[0], orc.fc(x[0]), atol=1e-6)
     # means are the sample means
@@ -38,4 +38,4 @@ def test_streaming_fc_restart_needs_no_clearing(cuda):
     s.update_rows(a, range(25))
     s.n = 0                             # a new stream reuses the state arrays
     s.update_rows(b, range(25))
-    np.testing.assert_allclose(s.corr().cpu().numpy(), metric.fc(b)[0].cpu().numpy(), atol=1e-6)
+    np.testing.assert_allclose(s.corr().cpu().numpy(), metric.fc(b).cpu().numpy(), atol=1e-6)
