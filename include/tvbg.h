@@ -322,6 +322,52 @@ int tvbg_fc_noalloc(const float *d_x, int32_t n_inst, int32_t T, int32_t N,
                     double *d_err, void *stream);
 
 /*
+ * ---- one very large network ----------------------------------------------
+ * A single instance with up to millions of nodes (the case of
+ * tvb_hpc/examples/sim515k.py: one network of 515 056 nodes), node-parallel:
+ * one thread per node, node-major ring [N][nh + 8] (slot s of node j at
+ * j*(nh+8) + (s & (nh-1)), positions < 8 mirrored at +nh), one launch per
+ * block of block_k (4 or 8) steps.  Needs every delay >= block_k - 1 and
+ * nh >= max(delay) + 1 + block_k; couplings LINEAR, DIFF, SIGMOIDAL; models
+ * G2DO, G2DOSC, MPR, LINEAR.  Same step (CUDA order) and Philox stream as
+ * instance 0 of tvbg_sweep.  The descriptor is host memory (it is passed to
+ * the kernels by value).
+ */
+typedef struct tvbg_net {
+    const int32_t *row;     /* [N+1] CSR offsets (in-edges of node i)          */
+    const int32_t *col;     /* [nnz] source node of each edge                  */
+    const float *w;         /* [nnz] weight                                    */
+    const uint16_t *off;    /* [nnz] (nh - delay) & (nh - 1)                   */
+    const float *wsum;      /* [N] sum of in-edge weights (DIFF), else NULL    */
+    float *ring;            /* [N][nh + 8]                                     */
+    float *state;           /* [N][nsvar], updated in place                    */
+    const float *nparam;    /* [N][npar]                                       */
+    int64_t N;
+    int32_t lognh;          /* 3..16                                           */
+    int32_t model;
+    int32_t cfun;
+    uint32_t flags;         /* NOISE, NO_WRAP                                  */
+    uint32_t seed_lo;
+    uint32_t seed_hi;
+    float dt;
+    float sqrt_dt;
+    float cf_a;
+    float cf_b;
+    float cf_p[3];
+    float reserved0;
+    float sigma[4];
+    float consts[16];
+} tvbg_net;
+
+size_t tvbg_net_size(void);
+
+/* Advance the network from step t0 by nsteps: one seed launch (slot t0
+ * holds obs0 of the state) and ceil(nsteps / cfg->block_k) step launches of
+ * cfg->threads threads per CTA on `stream`.  Graph-capturable. */
+int tvbg_net_run(const tvbg_net *net, int64_t t0, int32_t nsteps,
+                 const tvbg_launch *cfg, void *stream);
+
+/*
  * Streaming covariance for long runs: fold one sample per instance into an
  * FP64 running state (Welford update).  d_x: sample of instance b at
  * d_x + b * x_stride (N floats); n: samples already folded (0 starts a new

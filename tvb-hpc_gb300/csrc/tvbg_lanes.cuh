@@ -94,9 +94,9 @@ __device__ __forceinline__ float pick4(const float z[4], int r) {
 }
 
 template <int CF>
-__device__ __forceinline__ float lane_pre(float xj, const tvbg_group& g) {
+__device__ __forceinline__ float lane_pre(float xj, const float* cf_p) {
     if constexpr (CF == TVBG_CFUN_SIGMOIDAL) {
-        return g.cf_p[0] / (1.0f + expf(g.cf_p[2] * (g.cf_p[1] - xj)));
+        return cf_p[0] / (1.0f + expf(cf_p[2] * (cf_p[1] - xj)));
     } else {
         return xj;
     }
@@ -142,7 +142,7 @@ __device__ __forceinline__ void lane_gather(const tvbg_group& g, int lo, int hi,
 #pragma unroll
         for (int u = 0; u < U; ++u) {
 #pragma unroll
-            for (int k = 0; k < K; ++k) acc[k] = fmaf(w[u], lane_pre<CF>(v[u][k], g), acc[k]);
+            for (int k = 0; k < K; ++k) acc[k] = fmaf(w[u], lane_pre<CF>(v[u][k], g.cf_p), acc[k]);
         }
     }
     if (e < hi) {  // fewer than U edges left, loads still issued together
@@ -162,7 +162,7 @@ __device__ __forceinline__ void lane_gather(const tvbg_group& g, int lo, int hi,
         for (int u = 0; u < U; ++u) {
             if (e + u < hi) {
 #pragma unroll
-                for (int k = 0; k < K; ++k) acc[k] = fmaf(w[u], lane_pre<CF>(v[u][k], g), acc[k]);
+                for (int k = 0; k < K; ++k) acc[k] = fmaf(w[u], lane_pre<CF>(v[u][k], g.cf_p), acc[k]);
             }
         }
     }

@@ -158,6 +158,20 @@ class tvbg_group(ctypes.Structure):
     ]
 
 
+class tvbg_net(ctypes.Structure):
+    _fields_ = [
+        ('row', ctypes.c_void_p), ('col', ctypes.c_void_p), ('w', ctypes.c_void_p),
+        ('off', ctypes.c_void_p), ('wsum', ctypes.c_void_p), ('ring', ctypes.c_void_p),
+        ('state', ctypes.c_void_p), ('nparam', ctypes.c_void_p),
+        ('N', ctypes.c_int64), ('lognh', ctypes.c_int32), ('model', ctypes.c_int32),
+        ('cfun', ctypes.c_int32), ('flags', ctypes.c_uint32), ('seed_lo', ctypes.c_uint32),
+        ('seed_hi', ctypes.c_uint32), ('dt', ctypes.c_float), ('sqrt_dt', ctypes.c_float),
+        ('cf_a', ctypes.c_float), ('cf_b', ctypes.c_float), ('cf_p', ctypes.c_float * 3),
+        ('reserved0', ctypes.c_float), ('sigma', ctypes.c_float * 4),
+        ('consts', ctypes.c_float * 16),
+    ]
+
+
 #: numpy view of tvbg_group (group tables are built in bulk)
 GROUP_DTYPE = np.dtype(tvbg_group)
 
@@ -204,6 +218,9 @@ SIGNATURES = {
     'tvbg_adjoint_mpr': (ctypes.c_int, [_vp, _i32, _i32, _vp]),
     'tvbg_philox_u32': (ctypes.c_int, [_u32, _u32, _u32, _u32, _u32, _vp, _i64, _vp]),
     'tvbg_group_size': (_sz, []),
+    'tvbg_net_size': (_sz, []),
+    'tvbg_net_run': (ctypes.c_int, [ctypes.POINTER(tvbg_net), _i64, _i32,
+                                    ctypes.POINTER(tvbg_launch), _vp]),
     'tvbg_cov_update': (ctypes.c_int, [_vp, _i64, _i32, _i32, _i64, _vp, _vp, _vp]),
     'tvbg_cov_corr': (ctypes.c_int, [_vp, _i32, _i32, _vp, _vp]),
     'tvbg_pack_edges_group': (ctypes.c_int, [_i32, _i32, _vp, _vp, _vp, _vp, _i32, _vp]),
@@ -246,6 +263,8 @@ def load():
         raise RuntimeError('tvbg_launch layout mismatch')
     if lib.tvbg_group_size() != ctypes.sizeof(tvbg_group):
         raise RuntimeError('tvbg_group layout mismatch')
+    if lib.tvbg_net_size() != ctypes.sizeof(tvbg_net):
+        raise RuntimeError('tvbg_net layout mismatch')
     _lib = lib
     return lib
 

@@ -121,6 +121,34 @@ def synthetic_connectome(N, density, seed, mu=-1.0, sigma=1.0, len_lo=10.0, len_
     return w.astype(np.float32), ln.astype(np.float32)
 
 
+def synthetic_sparse_connectome(N, mean_degree, seed, mu=-1.0, sigma=1.0, len_lo=10.0,
+                                len_hi=200.0):
+    """
+    Seeded synthetic sparse connectivity for networks too large for a dense
+    matrix (the 515 056-node case of tvb_hpc/examples/sim515k.py, whose data
+    file is not available): every node gets Poisson(mean_degree) in-edges
+    from uniformly drawn distinct sources (no self-edges), log-normal(mu,
+    sigma) weights normalised to max 1, tract lengths U(len_lo, len_hi) mm.
+    Returns a Connectivity (CSR, columns sorted within each row).
+    """
+    rng = np.random.default_rng(seed)
+    deg = np.minimum(rng.poisson(mean_degree, N), N - 1).astype(np.int64)
+    row = np.concatenate([[0], np.cumsum(deg)]).astype(np.int64)
+    nnz = int(row[-1])
+    tgt = np.repeat(np.arange(N, dtype=np.int64), deg)
+    src = rng.integers(0, N - 1, nnz)
+    src = src + (src >= tgt)                      # skip the diagonal
+    # sort and de-duplicate the sources of each row
+    key = tgt * N + src
+    key = np.unique(key)
+    tgt, src = key // N, key % N
+    row = np.concatenate([[0], np.cumsum(np.bincount(tgt, minlength=N))]).astype(np.int32)
+    w = rng.lognormal(mu, sigma, src.size)
+    w = (w / w.max()).astype(np.float32)
+    ln = rng.uniform(len_lo, len_hi, src.size).astype(np.float32)
+    return Connectivity(N, None, int(src.size), src.astype(np.int32), row, w, ln)
+
+
 class Network:
     """
     Network implementing sparse time-delay coupling with pre/post summation

@@ -15,7 +15,9 @@ memory and advances all of them together:
        request), gradient requests as one persistent batch launch per model
        (tvbg_batch_run), all on the device at once;
     3. retire requests that reached their step count: copy the final state
-       (and gradients) to the host, free the device memory, record latency.
+       to the host, free the device memory, record latency; FC-fit gradient
+       requests then run their recomputation and adjoint on a worker thread
+       (own stream) and finish when it does.
 
 Requests that arrive while a tick runs are admitted while the device runs
 that tick (their state is built on a side stream) and join at the next
@@ -30,6 +32,7 @@ call and copies results back after every chunk
 (dsl/dsl_cuda/example/cuda_run.py:124-142).
 """
 
+import concurrent.futures
 import time
 from dataclasses import dataclass, field
 
@@ -115,6 +118,9 @@ class Server:
         # preparation, device, retirement)
         self.phase_s = dict(admit=0.0, prepare=0.0, device=0.0, retire=0.0)
         self.side = torch.cuda.Stream()
+        self.grad_stream = torch.cuda.Stream()
+        self.pool = concurrent.futures.ThreadPoolExecutor(max_workers=1)
+        self.pending = []
 
     def submit(self, req):
         self.queue.append(req)
@@ -164,15 +170,35 @@ class Server:
 
     def _retire(self, req):
         req.state = req.iset.state.cpu().numpy()
-        if req.want_grad and req.model == 'MPR' and req.target is not None:
-            from .adjoint import FCFit
-            prob = FCFit(req.conn, req.dt, float(req.speeds[0]), req.x0, req.target, req.nsteps)
-            prob.forward(req.couplings, np.asarray(req.nparam).reshape(req.couplings.size, -1))
-            req.grad = tuple(t.cpu().numpy() for t in prob.backward())
-        req.finished = self.clock()
         self.used -= req.nbytes
         req.iset = None
+        if req.want_grad and req.model == 'MPR' and req.target is not None:
+            # FC-fit gradients (recomputed forward + adjoint) run on a worker
+            # thread with its own stream, so they hold up no tick
+            self.pending.append((req, self.pool.submit(self._gradient, req)))
+            return
+        req.finished = self.clock()
         self.done.append(req)
+
+    def _gradient(self, req):
+        from .adjoint import FCFit
+        torch = self.torch
+        with torch.cuda.stream(self.grad_stream):
+            prob = FCFit(req.conn, req.dt, float(req.speeds[0]), req.x0, req.target, req.nsteps)
+            prob.forward(req.couplings, np.asarray(req.nparam).reshape(req.couplings.size, -1))
+            return tuple(t.cpu().numpy() for t in prob.backward())
+
+    def _collect(self, wait=False):
+        "Finish the gradient requests whose worker job is done."
+        keep = []
+        for req, fut in self.pending:
+            if wait or fut.done():
+                req.grad = fut.result()
+                req.finished = self.clock()
+                self.done.append(req)
+            else:
+                keep.append((req, fut))
+        self.pending = keep
 
     def tick(self):
         "Admit, advance every active request by one chunk, retire; returns work done."
@@ -202,6 +228,8 @@ class Server:
             batches.append((b, reqs, steps))
         for b, reqs, steps in batches:
             work += sum(r.couplings.size * r.conn.nnode * n for r, n in zip(reqs, steps))
+        done = self.torch.cuda.Event()
+        done.record()          # after every launch (forked streams join the current one)
         t_d = time.perf_counter()
         self.phase_s['prepare'] += t_d - t_p
         # while the device runs this chunk, admit what has arrived meanwhile:
@@ -213,7 +241,10 @@ class Server:
                 self._admit(self.clock(), into=fresh)
         t_s = time.perf_counter()
         self.phase_s['admit'] += t_s - t_d
-        self.torch.cuda.synchronize()
+        # wait for this tick's launches and the admissions' copies only (a
+        # gradient job may be running on its own stream)
+        done.synchronize()
+        self.side.synchronize()
         t_r = time.perf_counter()
         self.phase_s['device'] += t_r - t_s
         for b, reqs, steps in batches:
@@ -225,14 +256,18 @@ class Server:
         self.active = [r for r in self.active if r.steps_done < r.nsteps] + fresh
         for r in finished:
             self._retire(r)
+        self._collect()
         self.phase_s['retire'] += time.perf_counter() - t_r
         self.ticks += 1
         self.node_steps += work
         return work
 
     def run(self, until_empty=True, max_ticks=None):
-        while self.queue or self.active:
+        while self.queue or self.active or self.pending:
             if max_ticks is not None and self.ticks >= max_ticks:
+                break
+            if not self.active and not self.queue:
+                self._collect(wait=True)     # only gradient jobs are left
                 break
             if not self.active and self.queue:
                 nxt = min(r.arrival for r in self.queue)
