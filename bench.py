@@ -14,20 +14,24 @@ computed).  The workload sizes are those of the benchmark configurations
          (30/30/15/8/3% density), 1024/1024/256/64/16 instances, step counts
          uniform in [5k, 50k], Montbrio-Pazo-Roxin with linear coupling and
          Euler-Maruyama noise (sigma 1e-2), max delay 500 steps; run as one
-         CUDA graph of persistent batch kernels.  The plain path (per-step
-         kernel, one sweep per connectome in 1000-step launches, connectomes
-         in sequence) is timed on the same work and reported beside it.
-
-  grid   (default) dense parameter grid: generic 2-D oscillator (the CUDA DSL /
-         TVB form, cubic and coupling on V) with
-         linear difference coupling and Euler-Maruyama noise (sigma 1e-3,
-         Philox keyed by seed/instance/node/step), N = 84, 30% density,
-         64 x 64 grid of G in logspace(-3, 0) x speed in linspace(1, 20)
-         mm/ms = 4096 instances, dt 0.1 ms, 100k steps, Balloon-Windkessel
-         BOLD sampled every 720 ms, 84 x 84 Pearson FC per instance against a
-         seeded target FC.
+         CUDA graph of lane-interleaved group launches (one per connectome,
+         forked streams).  The plain path (per-step kernel, one sweep per
+         connectome in 1000-step launches, connectomes in sequence) is timed
+         on the same work and reported beside it.
+  grid   dense parameter grid: generic 2-D oscillator (the CUDA DSL / TVB
+         form, cubic and coupling on V) with linear difference coupling and
+         Euler-Maruyama noise (sigma 1e-3, Philox keyed by
+         seed/instance/node/step), N = 84, 30% density, 64 x 64 grid of G in
+         logspace(-3, 0) x speed in linspace(1, 20) mm/ms = 4096 instances,
+         dt 0.1 ms, 100k steps, Balloon-Windkessel BOLD sampled every 720 ms,
+         84 x 84 Pearson FC per instance against a seeded target FC.
   kuramoto  plain Kuramoto sweep, N = 68, 32 instances, 1000 steps (the
          CPU-runnable parity case).
+  net515k   one network of 515 056 nodes (sparse synthetic connectivity),
+         node-parallel, 1000 steps.
+  serve  the serving loop: Poisson arrivals of sweep requests, p50/p99
+         latency, served vs plain.
+  grid_1k, mixed_small, grid_small: profiling cases.
 
 Metric: node-steps/s (one node x one instance x one time step).  `value`
 is device-resident throughput (CUDA events on the launching stream, max
@@ -149,9 +153,27 @@ def mixed_small_workload():
     return wl
 
 
+def net515k_workload(N=515056, degree=64, nsteps=1000, seed=0):
+    """One very large network, the single simulation of
+    tvb_hpc/examples/sim515k.py (515 056 nodes, linear coupling, Euler): its
+    connectivity file is not available, so a seeded sparse synthetic one
+    stands in (Poisson(64) in-edges per node, log-normal weights, lengths
+    U(10, 200) mm at 4 mm/ms, dt 0.1 ms: delays 25-500 steps); the 2-D
+    oscillator in its CUDA-DSL form (tvb_hpc's G2DO diverges within 10^4
+    steps); 1000 steps per bench step."""
+    from tvb_hpc import network
+    conn = network.synthetic_sparse_connectome(N, degree, seed=seed)
+    rng = np.random.default_rng(seed + 1)
+    x0 = rng.uniform(-0.5, 0.5, (1, N, 2)).astype(np.float32)
+    return dict(name='net515k', conn=conn, couplings=np.array([0.05], np.float32),
+                speeds=np.array([4.0], np.float32), x0=x0, nsteps=nsteps, dt=0.1, bold_period=0,
+                bold_len=0, target=None, model='Generic2dOscillator', cfun='Linear', noise=False,
+                seed=seed)
+
+
 WORKLOADS = {'grid': grid_workload, 'grid_small': grid_small_workload, 'grid_1k': grid_1k_workload,
              'kuramoto': kuramoto_workload, 'mixed': mixed_workload,
-             'mixed_small': mixed_small_workload}
+             'mixed_small': mixed_small_workload, 'net515k': net515k_workload}
 
 
 def workload_config(wl):
@@ -434,6 +456,51 @@ class GpuStep:
         return self.n_launch + fc_launches
 
 
+class NetStep:
+    """One bench step of the single large network: reset state and ring
+    from resident copies, advance nsteps (one seed launch and one launch per
+    block of K steps, node-parallel)."""
+
+    def __init__(self, wl, torch):
+        from tvb_hpc import model, coupling, scheme, bignet
+        self.torch = torch
+        self.wl = wl
+        m = getattr(model, wl['model'])()
+        cf = getattr(coupling, wl['cfun'])(m)
+        scm = scheme.EulerMaryuyamaStep(wl['dt']) if wl['noise'] else scheme.EulerStep(wl['dt'])
+        self.sw = bignet.SingleNetwork(m, cf, scm, wl['conn'], wl['dt'],
+                                       coupling=float(wl['couplings'][0]),
+                                       speed=float(wl['speeds'][0]), state0=wl['x0'][0],
+                                       seed=wl['seed'])
+        self.x0 = self.sw.state.clone()
+        self.ns = self.sw.ns
+        self.status = self.sw.status
+        self.tpn = None
+        self.path = 'node-parallel single network, one launch per block of %d steps' % self.sw.block_k
+
+    def reset(self, x0=None):
+        self.sw.state.copy_(self.x0 if x0 is None else x0)
+        self.sw.ring.zero_()
+        self.sw.t = 0
+
+    def run(self, time_kernels=False):
+        torch = self.torch
+        evs = []
+        if time_kernels:
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            self.sw.launch(self.wl['nsteps'])
+            e1.record()
+            evs.append((e0, e1))
+        else:
+            self.sw.launch(self.wl['nsteps'])
+        return evs, None
+
+    def launches_per_step(self):
+        return 1 + -(-self.wl['nsteps'] // self.sw.block_k)
+
+
 def roofline_entry(wl, nsvar, kernel_ms_total, steps):
     """Roofline of the step kernel: algorithmic bytes of the timed steps over
     the step kernels' event-timed duration (for the uneven batch, the graph
@@ -467,6 +534,9 @@ def roofline_entry(wl, nsvar, kernel_ms_total, steps):
 
 def cpu_baseline(wl, budget_s=12.0):
     "The oracle (C restatement, OpenMP over instances) on a bounded sample."
+    if wl['conn'].nnode > 1024:
+        return {'value': None, 'unit': UNIT, 'cores': 0, 'kind': 'port',
+                'sample': 'not run: the oracle steps networks of up to 1024 nodes'}
     sys.path.insert(0, os.path.join(ROOT, 'oracle'))
     import pyoracle as orc
     from tvb_hpc import network, model as mdl
@@ -517,8 +587,12 @@ def gpu_arm(args):
     from tvb_hpc import _native
     _native.load()
     wl = WORKLOADS[args.workload]()
-    gs = (MixedStep(wl, torch, args.path, not args.no_graph) if wl['name'].startswith('mixed')
-          else GpuStep(wl, torch, args.tpn, args.warps, args.path))
+    if wl['name'].startswith('mixed'):
+        gs = MixedStep(wl, torch, args.path, not args.no_graph)
+    elif wl['name'] == 'net515k':
+        gs = NetStep(wl, torch)
+    else:
+        gs = GpuStep(wl, torch, args.tpn, args.warps, args.path)
 
     def barrier():
         if world > 1:

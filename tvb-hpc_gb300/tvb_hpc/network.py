@@ -133,15 +133,22 @@ def synthetic_sparse_connectome(N, mean_degree, seed, mu=-1.0, sigma=1.0, len_lo
     """
     rng = np.random.default_rng(seed)
     deg = np.minimum(rng.poisson(mean_degree, N), N - 1).astype(np.int64)
-    row = np.concatenate([[0], np.cumsum(deg)]).astype(np.int64)
-    nnz = int(row[-1])
-    tgt = np.repeat(np.arange(N, dtype=np.int64), deg)
-    src = rng.integers(0, N - 1, nnz)
-    src = src + (src >= tgt)                      # skip the diagonal
-    # sort and de-duplicate the sources of each row
-    key = tgt * N + src
-    key = np.unique(key)
-    tgt, src = key // N, key % N
+    # sorted sources per row without a global sort: the normalised cumulative
+    # sums of d + 1 exponential gaps are d sorted uniforms on (0, 1)
+    seg = np.repeat(np.arange(N, dtype=np.int64), deg + 1)
+    cs = np.cumsum(rng.exponential(1.0, seg.size))
+    ends = np.cumsum(deg + 1) - 1                       # last element of each segment
+    base = np.concatenate([[0.0], cs[ends[:-1]]])
+    total = cs[ends] - base
+    keep = np.ones(seg.size, bool)
+    keep[ends] = False
+    tgt = seg[keep]
+    u = (cs[keep] - base[tgt]) / total[tgt]
+    src = np.minimum((u * (N - 1)).astype(np.int64), N - 2)
+    src = src + (src >= tgt)                            # skip the diagonal (order kept)
+    dup = np.zeros(src.size, bool)
+    dup[1:] = (src[1:] == src[:-1]) & (tgt[1:] == tgt[:-1])
+    tgt, src = tgt[~dup], src[~dup]
     row = np.concatenate([[0], np.cumsum(np.bincount(tgt, minlength=N))]).astype(np.int32)
     w = rng.lognormal(mu, sigma, src.size)
     w = (w / w.max()).astype(np.float32)
