@@ -96,16 +96,25 @@ class FCFit:
                            trace_len=trace_len, trace_nobs=trace_nobs, trace_csum=trace_csum)
 
     @staticmethod
-    def _run(iset, nsteps, tpn=2):
-        from .engine import Sweep
+    def _sweep(iset, tpn=2):
+        "A Sweep view of an InstanceSet (same device arrays)."
+        from .engine import Sweep, DeviceStatus
         sw = Sweep.__new__(Sweep)
         sw.__dict__.update(iset.__dict__)
         sw.tpn = tpn
-        from .engine import DeviceStatus
         sw.status = DeviceStatus()
         sw._uploaded = None
-        sw.run(nsteps)
-        iset.t = sw.t
+        return sw
+
+    @staticmethod
+    def _plan(sw, segs):
+        """Launch tables of every segment (t0, n), built and uploaded up
+        front so the segments then run back to back without host syncs."""
+        plans = []
+        for t0, n in segs:
+            sw.t[:] = t0
+            plans.append(sw.prepare(n))
+        return plans
 
     def forward(self, G, eta):
         "Loss [I] (FP64); keeps checkpoints and the rate series for backward."
@@ -114,13 +123,16 @@ class FCFit:
         eta = np.asarray(eta, np.float32).reshape(self.I, self.N)
         self.G, self.eta = G, eta
         fw = self._set(G, eta, self.T, 1, False)
+        sw = self._sweep(fw)
+        segs = [(t, min(self.C, self.T - t)) for t in range(0, self.T, self.C)]
+        plans = self._plan(sw, segs)
         self.ckpt = []
-        t = 0
-        while t < self.T:
-            n = min(self.C, self.T - t)
-            self.ckpt.append((t, n, fw.state.clone(), fw.ring.clone()))
-            self._run(fw, n)
-            t += n
+        for (t0, n), pl in zip(segs, plans):
+            self.ckpt.append((t0, n, fw.state.clone(), fw.ring.clone()))
+            sw.launch(pl, 2)
+        fw.t[:] = self.T
+        torch.cuda.synchronize()
+        sw.status.check()
         r_tr = fw.trace[:, :, :, 0]                     # r(t), t = 0..T-1
         X = torch.cat([r_tr[:, 1:], fw.state[:, None, :, 0]], 1).double()   # X[s] = r(s+1)
         self.fw = fw
@@ -162,33 +174,42 @@ class FCFit:
         deta = torch.zeros((I, N), dtype=torch.float64, device='cuda')
         dGn = torch.zeros((I, N), dtype=torch.float64, device='cuda')
         rec = self._set(self.G, self.eta, self.C, 2, True)
+        sw = self._sweep(rec)
+        rev = list(reversed(self.ckpt))
+        plans = self._plan(sw, [(t0, n) for (t0, n, _, _) in rev])
         threads = 32 * ((N + 31) // 32)
-        for (t0, n, st, rg) in reversed(self.ckpt):
+        seg = rec.trace                                  # [I, C, N, 3]: r, V, S of a segment
+        tab = np.zeros((len(rev), I), dtype=nat.ADJOINT_DTYPE)
+        b = np.arange(I, dtype=np.int64)
+        for k, (t0, n, _, _) in enumerate(rev):
+            tk = tab[k]
+            tk['edges_t'] = self.edges_t.data_ptr()
+            tk['row_t'] = self.row_t.data_ptr()
+            tk['seg'] = seg.data_ptr() + 4 * b * seg.shape[1] * N * 3
+            tk['dr'] = dr.data_ptr() + 4 * (b * (T + 1) * N + t0 * N)
+            tk['lam'] = lam.data_ptr() + 4 * b * N * 2
+            tk['ring'] = ring.data_ptr() + 4 * b * N * nh
+            tk['deta'] = deta.data_ptr() + 8 * b * N
+            tk['dG'] = dGn.data_ptr() + 8 * b * N
+            tk['t0'] = t0
+            tk['len'] = n
+            tk['N'] = N
+            tk['lognh'] = self.lognh
+            tk['dt'] = np.float32(self.dt)
+            tk['G'] = self.G
+            tk['consts'] = self.consts[:4]
+        dev = torch.from_numpy(tab.view(np.uint8).reshape(-1).copy()).cuda()
+        row_bytes = I * nat.ADJOINT_DTYPE.itemsize
+        # segments last first: recompute from the checkpoint (bit-identical to
+        # the forward), then the reverse-time kernel over it, back to back
+        for k, ((t0, n, st, rg), pl) in enumerate(zip(rev, plans)):
             rec.state.copy_(st)
             rec.ring.copy_(rg)
-            rec.t[:] = t0
-            self._run(rec, n)
-            seg = rec.trace                              # [I, C, N, 3]: r, V, S of steps t0..
-            tab = np.zeros(I, dtype=nat.ADJOINT_DTYPE)
-            b = np.arange(I, dtype=np.int64)
-            tab['edges_t'] = self.edges_t.data_ptr()
-            tab['row_t'] = self.row_t.data_ptr()
-            tab['seg'] = seg.data_ptr() + 4 * b * seg.shape[1] * N * 3
-            tab['dr'] = dr.data_ptr() + 4 * (b * (T + 1) * N + t0 * N)
-            tab['lam'] = lam.data_ptr() + 4 * b * N * 2
-            tab['ring'] = ring.data_ptr() + 4 * b * N * nh
-            tab['deta'] = deta.data_ptr() + 8 * b * N
-            tab['dG'] = dGn.data_ptr() + 8 * b * N
-            tab['t0'] = t0
-            tab['len'] = n
-            tab['N'] = N
-            tab['lognh'] = self.lognh
-            tab['dt'] = np.float32(self.dt)
-            tab['G'] = self.G
-            tab['consts'] = self.consts[:4]
-            dev = torch.from_numpy(tab.view(np.uint8).copy()).cuda()
-            nat.check(lib.tvbg_adjoint_mpr(dev.data_ptr(), I, threads, nat.stream_handle()))
+            sw.launch(pl, 2)
+            nat.check(lib.tvbg_adjoint_mpr(dev.data_ptr() + k * row_bytes, I, threads,
+                                           nat.stream_handle()))
         torch.cuda.synchronize()
+        sw.status.check()
         return dGn.sum(1), deta
 
 
