@@ -363,7 +363,10 @@ size_t tvbg_net_size(void);
 
 /* Advance the network from step t0 by nsteps: one seed launch (slot t0
  * holds obs0 of the state) and ceil(nsteps / cfg->block_k) step launches of
- * cfg->threads threads per CTA on `stream`.  Graph-capturable. */
+ * cfg->threads threads per CTA on `stream`.  cfg->tpn selects the thread
+ * mapping: 0 or 1 = one thread per node, block_k = block_k lanes per node
+ * (lane k gathers step k); both give bit-identical results.
+ * Graph-capturable. */
 int tvbg_net_run(const tvbg_net *net, int64_t t0, int32_t nsteps,
                  const tvbg_launch *cfg, void *stream);
 

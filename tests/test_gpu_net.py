@@ -67,6 +67,19 @@ def test_net_matches_group_kernel_at_large_n(cuda):
     assert rel_err(net.state.cpu().numpy(), gs.state.cpu().numpy()[0]) < 1e-5
 
 
+@pytest.mark.parametrize('name,cfun_name,noise,k', [('MPR', 'Linear', True, 8),
+                                                    ('G2DO', 'Diff', True, 4),
+                                                    ('Linear', 'Sigmoidal', False, 8)])
+def test_net_thread_mappings_bit_identical(cuda, name, cfun_name, noise, k):
+    "K lanes per node and one thread per node: same sums, same updates."
+    a, _, _, _ = make(name, cfun_name, noise=noise, block_k=k, lanes=True)
+    b, _, _, _ = make(name, cfun_name, noise=noise, block_k=k, lanes=False)
+    a.run(301)
+    b.run(301)
+    assert np.array_equal(a.state.cpu().numpy(), b.state.cpu().numpy())
+    assert np.array_equal(a.ring.cpu().numpy(), b.ring.cpu().numpy())
+
+
 def test_net_chunks_bit_exact(cuda):
     a, _, _, _ = make(noise=True, name='MPR')
     b, _, _, _ = make(noise=True, name='MPR')

@@ -9,31 +9,38 @@ namespace {
 using NetKernel = void (*)(const tvbg_net, long long, int, int32_t*);
 using SeedKernel = void (*)(const tvbg_net, long long);
 
+// lanes == 1: one thread per node; lanes == K: K lanes per node.
 template <class M, int CF>
-NetKernel pick_k(int k) {
+NetKernel pick_k(int k, bool lanes) {
     switch (k) {
-        case 4: return net_kernel<M, CF, 4>;
-        case 8: return net_kernel<M, CF, 8>;
+        case 4: return lanes ? net_kernel_lanes<M, CF, 4> : net_kernel<M, CF, 4>;
+        case 8: return lanes ? net_kernel_lanes<M, CF, 8> : net_kernel<M, CF, 8>;
         default: return nullptr;
     }
 }
 
 template <class M>
-NetKernel pick_cf(int cfun, int k) {
+NetKernel pick_cf(int cfun, int k, bool lanes) {
     switch (cfun) {
-        case TVBG_CFUN_LINEAR: return pick_k<M, TVBG_CFUN_LINEAR>(k);
-        case TVBG_CFUN_DIFF: return pick_k<M, TVBG_CFUN_DIFF>(k);
-        case TVBG_CFUN_SIGMOIDAL: return pick_k<M, TVBG_CFUN_SIGMOIDAL>(k);
+        case TVBG_CFUN_LINEAR: return pick_k<M, TVBG_CFUN_LINEAR>(k, lanes);
+        case TVBG_CFUN_DIFF: return pick_k<M, TVBG_CFUN_DIFF>(k, lanes);
+        case TVBG_CFUN_SIGMOIDAL: return pick_k<M, TVBG_CFUN_SIGMOIDAL>(k, lanes);
         default: return nullptr;
     }
 }
 
-int lookup(int model, int cfun, int k, NetKernel* kfn, SeedKernel* sfn) {
+int lookup(int model, int cfun, int k, bool lanes, NetKernel* kfn, SeedKernel* sfn) {
     switch (model) {
-        case TVBG_MODEL_G2DO: *kfn = pick_cf<G2DO>(cfun, k); *sfn = net_seed_kernel<G2DO>; break;
-        case TVBG_MODEL_G2DOSC: *kfn = pick_cf<G2DOsc>(cfun, k); *sfn = net_seed_kernel<G2DOsc>; break;
-        case TVBG_MODEL_MPR: *kfn = pick_cf<MPR>(cfun, k); *sfn = net_seed_kernel<MPR>; break;
-        case TVBG_MODEL_LINEAR: *kfn = pick_cf<Linear>(cfun, k); *sfn = net_seed_kernel<Linear>; break;
+        case TVBG_MODEL_G2DO: *kfn = pick_cf<G2DO>(cfun, k, lanes); *sfn = net_seed_kernel<G2DO>; break;
+        case TVBG_MODEL_G2DOSC:
+            *kfn = pick_cf<G2DOsc>(cfun, k, lanes);
+            *sfn = net_seed_kernel<G2DOsc>;
+            break;
+        case TVBG_MODEL_MPR: *kfn = pick_cf<MPR>(cfun, k, lanes); *sfn = net_seed_kernel<MPR>; break;
+        case TVBG_MODEL_LINEAR:
+            *kfn = pick_cf<Linear>(cfun, k, lanes);
+            *sfn = net_seed_kernel<Linear>;
+            break;
         default: *kfn = nullptr;
     }
     return *kfn ? TVBG_OK : set_error(TVBG_EUNSUPPORTED, "tvbg_net_run: model/coupling/block_k not built");
@@ -56,14 +63,18 @@ extern "C" int tvbg_net_run(const tvbg_net* net, int64_t t0, int32_t nsteps, con
         return set_error(TVBG_EINVAL, "threads must be a multiple of 32 in [32, 1024]");
     if (net->model != cfg->model || net->cfun != cfg->cfun)
         return set_error(TVBG_EINVAL, "tvbg_net_run: descriptor and launch disagree on model/coupling");
+    const int lanes = cfg->tpn > 1 ? cfg->tpn : 1;
+    if (lanes != 1 && lanes != cfg->block_k)
+        return set_error(TVBG_EINVAL, "tvbg_net_run: tpn must be 0, 1 or block_k");
     NetKernel kfn = nullptr;
     SeedKernel sfn = nullptr;
-    int rc = lookup(net->model, net->cfun, cfg->block_k, &kfn, &sfn);
+    int rc = lookup(net->model, net->cfun, cfg->block_k, lanes > 1, &kfn, &sfn);
     if (rc) return rc;
-    const long long blocks = (net->N + cfg->threads - 1) / cfg->threads;
+    const long long seed_blocks = (net->N + cfg->threads - 1) / cfg->threads;
+    const long long blocks = (net->N * lanes + cfg->threads - 1) / cfg->threads;
     if (blocks > 0x7fffffffLL) return set_error(TVBG_EINVAL, "tvbg_net_run: N too large");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    sfn<<<static_cast<unsigned>(blocks), cfg->threads, 0, st>>>(*net, t0);
+    sfn<<<static_cast<unsigned>(seed_blocks), cfg->threads, 0, st>>>(*net, t0);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return set_cuda_error(e, "tvbg_net_run: seed launch");
     for (long long tb = t0; tb < t0 + nsteps; tb += cfg->block_k) {

@@ -4,11 +4,13 @@ case of tvb_hpc/examples/sim515k.py (one G2DO network of 515 056 nodes with
 linear coupling, CSR connectivity), where instances cannot fill the GPU and
 the parallelism is over nodes.
 
-One thread per node; the history ring is node-major ([N][nh + 8]) so the
-K slots an edge reads in a block of K steps are contiguous; one kernel
-launch per block (the launch boundary is the grid-wide barrier).  The step
-is the CUDA-order step of the other kernels, and the noise is instance 0's
-Philox stream.
+The history ring is node-major ([N][nh + 8]) so the K slots an edge reads
+in a block of K steps are contiguous; one kernel launch per block (the
+launch boundary is the grid-wide barrier).  Either K lanes per node (lane k
+gathers step k, one contiguous load per edge across the lanes; the default)
+or one thread per node; both give bit-identical results.  The step is the
+CUDA-order step of the other kernels, and the noise is instance 0's Philox
+stream.
 """
 
 import ctypes
@@ -30,11 +32,12 @@ class SingleNetwork:
     state0 : (N, nsvar);  nparam : (N, npar) or per-node scalar
     block_k : 4 or 8 steps per launch (default: 8 when d_min >= 7)
     threads : CTA width
+    lanes : True (block_k lanes per node) or False (one thread per node)
     """
 
     def __init__(self, model, cfun, scheme, conn, dt, coupling=1.0, speed=None, delays=None,
                  rounding='ceil', state0=None, nparam=None, seed=0, block_k=None, threads=256,
-                 cf_b=None, t0=0):
+                 cf_b=None, t0=0, lanes=True):
         _device_ok()
         torch = _torch()
         self.torch = torch
@@ -90,6 +93,7 @@ class SingleNetwork:
         self.cf_b = np.float32(cf_b if cf_b is not None else
                                (cf_b0 if isinstance(cf_b0, (int, float, np.number)) else 0.0))
         self.threads = int(threads)
+        self.lanes = bool(lanes)
         self.t = int(t0)
         self.status = DeviceStatus()
 
@@ -115,6 +119,7 @@ class SingleNetwork:
         cfg = nat.tvbg_launch()
         cfg.model, cfg.cfun, cfg.threads, cfg.block_k = (self.model_id, self.cfun_id, self.threads,
                                                          self.block_k)
+        cfg.tpn = self.block_k if self.lanes else 1
         cfg.d_status = self.status.t.data_ptr()
         d = self.descriptor()
         nat.check(lib.tvbg_net_run(ctypes.byref(d), self.t, int(nsteps), ctypes.byref(cfg),
