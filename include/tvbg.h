@@ -66,12 +66,17 @@ extern "C" {
 #define TVBG_MODEL_JANSENRIT 6 /* model.py:226-247 Jansen-Rit, state y0..y5,
                                  params v0 r, observable y0 - y1; no noise
                                  (more than 4 state variables) */
+#define TVBG_MODEL_LEMS 64    /* a model generated from LEMS XML
+                                 (dsl/dsl_cuda/LEMS2CUDA.py); only the
+                                 libraries of include/tvbg_lems.h run it */
 
 /* ---- coupling functions (tvb_hpc/coupling.py) --------------------------- */
 #define TVBG_CFUN_LINEAR 0    /* pre = x_j,                  post = a*sum + b */
 #define TVBG_CFUN_DIFF 1      /* pre = x_j - x_i,            post = a*sum + b */
 #define TVBG_CFUN_KURAMOTO 2  /* pre = sin(x_j - x_i),       post = a*mean    */
 #define TVBG_CFUN_SIGMOIDAL 3 /* pre = cmax/(1+exp(r(mid-x_j))), post = a*sum */
+#define TVBG_CFUN_LEMS 64     /* the coupling of a LEMS model: pre(x_j, x_i)
+                                 from its XML, sum passed to the model raw */
 
 /* ---- per-instance flags ------------------------------------------------- */
 #define TVBG_F_NOISE 1u      /* Euler-Maruyama with Philox normals          */

@@ -10,6 +10,7 @@
 
 #include "tvbg_abi_internal.h"
 #include "tvbg_device.cuh"
+#include "tvbg_step_launch.cuh"
 
 namespace tvbg {
 
@@ -55,24 +56,10 @@ uint32_t blocked_aux_bytes(int model, int k, int nmax) {
     return 4u * static_cast<uint32_t>(2 * k * nmax * (2 + ns) + 4 * nmax) + 32u;
 }
 
-// Dynamic shared memory of a step launch: ring capacity + per-warp sums + mbarrier.
-static size_t step_smem_bytes(int threads, int smem_ring) {
-    return static_cast<size_t>(smem_ring) + 4u * static_cast<size_t>(threads) + 16u;
-}
+static const ErrSink kSink{set_error, set_cuda_error};
 
 static int check_launch(const tvbg_launch* cfg, const tvbg_instance* d_inst, int32_t n_inst) {
-    if (!cfg || !d_inst || n_inst < 0) return set_error(TVBG_EINVAL, "null launch config or instances");
-    if (cfg->threads < 32 || cfg->threads > 1024 || (cfg->threads & 31))
-        return set_error(TVBG_EINVAL, "threads must be a multiple of 32 in [32, 1024]");
-    if (cfg->tpn != 1 && cfg->tpn != 2 && cfg->tpn != 4 && cfg->tpn != 8)
-        return set_error(TVBG_EINVAL, "tpn must be 1, 2, 4 or 8");
-    if (cfg->smem_ring < 0 || (cfg->smem_ring & 15))
-        return set_error(TVBG_EINVAL, "smem_ring must be a non-negative multiple of 16");
-    if (cfg->block_k != 0 && cfg->block_k != 1 && cfg->block_k != 4 && cfg->block_k != 8)
-        return set_error(TVBG_EINVAL, "block_k must be 0, 1, 4 or 8");
-    if (cfg->nmax < 0 || cfg->nmax > cfg->threads)
-        return set_error(TVBG_EINVAL, "nmax must be in [0, threads]");
-    return TVBG_OK;
+    return check_step_launch(cfg, d_inst, n_inst, kSink);
 }
 
 static int launch_step(int model, int cfun, const tvbg_instance* d_inst, int32_t n_inst,
@@ -96,29 +83,10 @@ static int launch_step(int model, int cfun, const tvbg_instance* d_inst, int32_t
         kfn = reinterpret_cast<const void*>(k1);
         smem = step_smem_bytes(cfg->threads, cfg->smem_ring);
     }
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return set_cuda_error(e, "cudaGetDevice");
-    int optin = 0;
-    e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    if (e != cudaSuccess) return set_cuda_error(e, "cudaDeviceGetAttribute");
-    // the kernel's static shared memory (instance descriptor, counter) needs ~300 bytes
-    if (smem + 512 > static_cast<size_t>(optin))
-        return set_error(TVBG_EINVAL, "ring capacity exceeds the shared memory of one CTA");
-    e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-    if (e != cudaSuccess) return set_cuda_error(e, "cudaFuncSetAttribute(smem)");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    int grid = n_inst;
-    if (persistent) {
-        if (!cfg->d_counter) return set_error(TVBG_EINVAL, "tvbg_batch_run needs d_counter");
-        int sms = 0;
-        e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (e != cudaSuccess) return set_cuda_error(e, "cudaDeviceGetAttribute(SMs)");
-        grid = cfg->ctas > 0 ? cfg->ctas : sms;
-        if (grid > n_inst) grid = n_inst;
-        e = cudaMemsetAsync(cfg->d_counter, 0, sizeof(int32_t), st);
-        if (e != cudaSuccess) return set_cuda_error(e, "cudaMemsetAsync(counter)");
-    }
+    int grid = 0;
+    int rc = prepare_step_launch(kfn, smem, n_inst, cfg, persistent, st, kSink, &grid);
+    if (rc) return rc;
     if (grid == 0) return TVBG_OK;
     const int32_t* order = persistent ? cfg->d_order : nullptr;
     int32_t* counter = persistent ? cfg->d_counter : nullptr;
@@ -128,7 +96,7 @@ static int launch_step(int model, int cfun, const tvbg_instance* d_inst, int32_t
     else
         k1<<<grid, cfg->threads, smem, st>>>(d_inst, n_inst, order, counter, cfg->d_status,
                                              static_cast<uint32_t>(cfg->smem_ring));
-    e = cudaGetLastError();
+    const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return set_cuda_error(e, "step kernel launch");
     return TVBG_OK;
 }

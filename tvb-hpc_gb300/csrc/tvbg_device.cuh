@@ -88,8 +88,9 @@ __device__ __forceinline__ void box_muller_fast(uint32_t a, uint32_t b, float& z
 }
 
 __device__ __forceinline__ void philox_normals4(uint32_t c0, uint32_t c1, uint32_t c2,
-                                               uint32_t k0, uint32_t k1, float z[4]) {
-    const u32x4 w = philox4x32_10(c0, c1, c2, 0u, k0, k1);
+                                               uint32_t k0, uint32_t k1, float z[4],
+                                               uint32_t c3 = 0u) {
+    const u32x4 w = philox4x32_10(c0, c1, c2, c3, k0, k1);
     box_muller(w.v[0], w.v[1], z[0], z[1]);
     box_muller(w.v[2], w.v[3], z[2], z[3]);
 }
@@ -285,6 +286,18 @@ template <class M>
 struct Noise {
     static constexpr bool kOK = M::NS <= 4;
     static constexpr int SPC = M::NS <= 4 ? 4 / M::NS : 1;
+};
+
+// Models that declare kWideNoise (the LEMS-generated ones) with 5..8 state
+// variables take noise in the per-step kernel: two Philox calls per step
+// (counter word 3 = 0, 1) and one amplitude, sigma[0], for every variable.
+template <class M, class = void>
+struct WideNoise {
+    static constexpr bool value = false;
+};
+template <class M>
+struct WideNoise<M, decltype(void(M::kWideNoise))> {
+    static constexpr bool value = M::kWideNoise && M::NS > 4 && M::NS <= 8;
 };
 
 // ---------------------------------------------------------------------------

@@ -305,6 +305,18 @@ __device__ __forceinline__ void run_steps(const tvbg_instance& d, const Ring<SME
                             x[v] = fmaf(sqrt_dt * zv, d.sigma[v], x[v]);
                         }
                     }
+                } else if constexpr (WideNoise<M>::value) {
+                    if (noise) {
+                        float z8[8];
+                        const uint32_t tt = static_cast<uint32_t>(t);
+                        philox_normals4(static_cast<uint32_t>(my), tt, d.seed_hi, d.seed_lo,
+                                        d.inst_id, z8, 0u);
+                        philox_normals4(static_cast<uint32_t>(my), tt, d.seed_hi, d.seed_lo,
+                                        d.inst_id, z8 + 4, 1u);
+#pragma unroll
+                        for (int v = 0; v < M::NS; ++v)
+                            x[v] = fmaf(sqrt_dt * z8[v], d.sigma[0], x[v]);
+                    }
                 }
                 M::limit(x, flags);
                 obs0 = M::obs(x, 0);
@@ -331,7 +343,8 @@ __device__ __forceinline__ void run_instance(const tvbg_instance& d, const SmemP
     const int my = threadIdx.x;
     const bool own = my < N;
     if (N > static_cast<int>(blockDim.x) || N <= 0 || d.lognh < 2 || d.lognh > 24 ||
-        d.model != M::ID || d.cfun != CF || (!Noise<M>::kOK && (d.flags & TVBG_F_NOISE))) {
+        d.model != M::ID || d.cfun != CF ||
+        (!Noise<M>::kOK && !WideNoise<M>::value && (d.flags & TVBG_F_NOISE))) {
         if (threadIdx.x == 0) report(status, TVBG_EINVAL);
         return;
     }

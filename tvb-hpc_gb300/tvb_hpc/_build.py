@@ -5,7 +5,9 @@ In-tree build of the engine library (nvcc, sm_103a) and of the checker.
 
 compiles tvb-hpc_gb300/csrc/*.cu in parallel (one nvcc per translation
 unit, objects under tvb-hpc_gb300/_build/) and links
-tvb_hpc/_lib/libtvbg.so with the CUDA runtime linked statically.
+tvb_hpc/_lib/libtvbg.so with the CUDA runtime linked statically; then
+compiles the libraries of the bundled LEMS models (tvb_hpc/lems_models/,
+tvb_hpc/_lib/lems/).
 """
 
 import concurrent.futures as cf
@@ -74,4 +76,6 @@ def build(force=False, extra=(), jobs=None):
         p = subprocess.run(cmd, capture_output=True, text=True)
         if p.returncode != 0:
             raise RuntimeError('link failed:\n' + p.stderr[-4000:])
+    from . import lems
+    lems.prebuild(jobs)
     return LIB

@@ -19,7 +19,7 @@ TPN_CHOICES = (1, 2, 4, 8)
 
 
 def _key(iset):
-    return (iset.model_id, iset.cfun_id, iset.N, iset.nnz,
+    return (iset.model_id, iset.cfun_id, getattr(iset, 'kernel_key', None), iset.N, iset.nnz,
             tuple(sorted(set(int(x) for x in iset.lognh))), bool(iset.bold is not None),
             tuple(sorted(set(int(k) for k in iset.block_k))), iset.warps)
 

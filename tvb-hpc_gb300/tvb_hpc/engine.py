@@ -158,6 +158,8 @@ class InstanceSet:
     state0 : (I, N, nsvar) initial state, or (N, nsvar) shared
     nparam : (I, N, npar) or (N, npar) per-node parameters (default: const)
     delays : optional (nnz,) int delays shared by all instances
+    delay_tables : optional (tables, table_of): a list of (nnz,) int delay
+              arrays and, per instance, the index of its table
     rounding : 'ceil' | 'trunc' | 'dsl' delay rule (see network.delays_f32)
     seed : uint64 Philox seed; inst_ids : (I,) request-local ids (key word 1)
     history : 'zero' (zero history before t0) or 'fill' (state0 everywhere)
@@ -180,7 +182,7 @@ class InstanceSet:
                  history='zero', bold_period=0, bold_len=0, trace_every=0, trace_len=0,
                  trace_nobs=None, flags=0, cf_b=None, nh_extra=0, t0=0, order='cuda',
                  sync_every=None, blocked='auto', warps=None, trace_csum=False,
-                 pipeline=True):
+                 pipeline=True, delay_tables=None):
         _device_ok()
         torch = _torch()
         self.torch = torch
@@ -201,7 +203,13 @@ class InstanceSet:
         self.row_np, self.col_np, self.w_np = row, col, w
         self.nnz = int(col.size)
         # delay tables: one per distinct speed
-        if delays is not None:
+        if delay_tables is not None:
+            tables = [np.asarray(d, np.int64).astype(np.int32) for d in delay_tables[0]]
+            tab_of = np.broadcast_to(np.asarray(delay_tables[1], np.int64), (I, )).copy()
+            if tab_of.min() < 0 or tab_of.max() >= len(tables):
+                raise ValueError('delay table index out of range')
+            self.speeds = None
+        elif delays is not None:
             tables = [np.asarray(delays, np.int64).astype(np.int32)]
             tab_of = np.zeros(I, np.int64)
             self.speeds = None
