@@ -29,6 +29,12 @@ computed).  The workload sizes are those of the benchmark configurations
          CPU-runnable parity case).
   net515k   one network of 515 056 nodes (sparse synthetic connectivity),
          node-parallel, 1000 steps.
+  adjoint  the FC fit: MPR, N = 84, 256 instances, 2000 steps, forward +
+         hand-written adjoint with checkpoints every 100 steps; the line
+         carries the gradient error vs the FP64 oracle.
+  lems_epileptor  the CUDA DSL's default 32 x 32 speed x coupling sweep on
+         the Epileptor generated from its LEMS XML file (N = 68, 4000 steps,
+         noise on).
   serve  the serving loop: Poisson arrivals of sweep requests, p50/p99
          latency, served vs plain.
   grid_1k, mixed_small, grid_small: profiling cases.
@@ -171,9 +177,58 @@ def net515k_workload(N=515056, degree=64, nsteps=1000, seed=0):
                 seed=seed)
 
 
+def lems_workload(n_s=32, n_c=32, N=68, nsteps=4000, seed=0):
+    """The CUDA DSL's default sweep (dsl/dsl_cuda/example/cuda_setup.py:55-58,
+    97-101: a 32 x 32 grid of speed x coupling, one work item per point) on a
+    model generated from LEMS XML: the bundled six-variable Epileptor
+    (conditional terms, sine coupling), FP32 literals, noise on (two Philox
+    calls per step); speeds logspace(0, 2) mm/ms, couplings logspace(-2, 0),
+    dt 0.1, 4000 steps; a seeded 68-node synthetic connectome (the config
+    recipe) stands in for the DSL's connectivity_68."""
+    import itertools
+    from tvb_hpc import network
+    w, ln = network.synthetic_connectome(N, 0.3, seed=seed)
+    conn = network.Connectivity.from_dense(w, ln)
+    speeds = np.logspace(0.0, 2.0, n_s)
+    couplings = np.logspace(-2.0, 0.0, n_c)
+    params = np.array(list(itertools.product(speeds, couplings)), np.float32)
+    I = params.shape[0]
+    rng = np.random.default_rng(seed + 1)
+    x0 = np.zeros((I, N, 6), np.float32)
+    for v, (lo, hi) in enumerate([(-1.8, -1.2), (-15, -12), (2.8, 3.2), (-1.2, -0.8), (0, 0.2),
+                                  (-0.1, 0.1)]):
+        x0[:, :, v] = rng.uniform(lo, hi, (I, N))
+    return dict(name='lems_epileptor', conn=conn, couplings=params[:, 1], speeds=params[:, 0],
+                params=params, x0=x0, nsteps=nsteps, dt=0.1, bold_period=0, bold_len=0,
+                target=None, model='Epileptor (generated from LEMS XML, FP32 literals)',
+                cfun='LEMS: c_a sin(x1_j - x1), scaled by global_coupling', noise=True,
+                seed=seed, lems='Epileptor')
+
+
+def adjoint_workload(N=84, I=256, T=2000, C=100, seed=0):
+    """The adjoint fit: Montbrio-Pazo-Roxin + linear coupling, deterministic,
+    N = 84 (config-0 recipe connectome), 256 instances, 2000 steps of 0.1 ms
+    at 4 mm/ms, FC of the rate series vs a seeded target, gradients w.r.t. G
+    and the 84 per-node eta by the hand-written adjoint with checkpoints every
+    100 steps.  One bench step = forward (loss) + backward (gradients)."""
+    from tvb_hpc import network
+    w, ln = network.synthetic_connectome(N, 0.3, seed=seed)
+    conn = network.Connectivity.from_dense(w, ln)
+    rng = np.random.default_rng(seed + 1)
+    x0 = np.stack([rng.uniform(0.05, 0.3, (I, N)), rng.uniform(-1.5, -0.5, (I, N))], -1)
+    eta = rng.uniform(-6, -4, (I, N)).astype(np.float32)
+    G = np.logspace(-2, -0.5, I).astype(np.float32)
+    target = np.corrcoef(rng.normal(size=(N, 60))).astype(np.float32)
+    return dict(name='adjoint', conn=conn, couplings=G, speeds=np.full(I, 4.0, np.float32),
+                x0=x0.astype(np.float32), eta=eta, target_fc=target, nsteps=T, ckpt=C, dt=0.1,
+                bold_period=0, bold_len=0, target=None, model='MPR', cfun='Linear', noise=False,
+                seed=seed)
+
+
 WORKLOADS = {'grid': grid_workload, 'grid_small': grid_small_workload, 'grid_1k': grid_1k_workload,
              'kuramoto': kuramoto_workload, 'mixed': mixed_workload,
-             'mixed_small': mixed_small_workload, 'net515k': net515k_workload}
+             'mixed_small': mixed_small_workload, 'net515k': net515k_workload,
+             'lems_epileptor': lems_workload, 'adjoint': adjoint_workload}
 
 
 def workload_config(wl):
@@ -501,6 +556,183 @@ class NetStep:
         return 1 + -(-self.wl['nsteps'] // self.sw.block_k)
 
 
+class LemsStep:
+    """One bench step of a LEMS-generated model: reset state and ring from
+    resident copies and advance every work item nsteps -- on the
+    lane-interleaved group kernel where the model's coupling and delays allow
+    (LemsGroupSet), else with one per-step launch per ring group (LemsSweep);
+    tables are built once."""
+
+    def __init__(self, wl, torch, tpn=None, path='groups'):
+        from tvb_hpc import lems
+        self.torch = torch
+        self.wl = wl
+        m = lems.load_model(wl['lems'])
+        self.sw = lems.make_set(m, wl['conn'], wl['dt'], wl['params'], state0=wl['x0'],
+                                noise=wl['noise'], single=True, seed=wl['seed'], tpn=tpn,
+                                prefer=path)
+        self.groups = isinstance(self.sw, lems.LemsGroupSet)
+        self.x0 = self.sw.state.clone()
+        self.ring0 = self.sw.ring.clone()
+        if self.groups:
+            self.tpn = None
+            self.sw.t[:] = 0
+            self.launches, _ = self.sw.prepare(wl['nsteps'])
+            self.path = ('generated group kernel (8 work items per group, K = %s steps per '
+                         'block), %d groups' % (sorted(set(self.sw.block_k.tolist())),
+                                                 self.sw.n_groups))
+        else:
+            self.tpn = self.sw.pick_tpn()
+            self.sw.t[:] = 0
+            self.launches = self.sw.prepare(wl['nsteps'])
+            self.path = 'generated per-step kernel (one CTA per work item), tpn %d' % self.tpn
+        self.ns = m.ns
+        self.status = self.sw.status
+
+    def reset(self, x0=None):
+        if self.groups:
+            self.sw.set_state(self.x0 if x0 is None else x0)
+        else:
+            self.sw.state.copy_(self.x0 if x0 is None else x0)
+        self.sw.ring.copy_(self.ring0)
+
+    def _launch(self):
+        if self.groups:
+            self.sw.launch(self.launches)
+        else:
+            self.sw.launch(self.launches, self.tpn)
+
+    def run(self, time_kernels=False):
+        torch = self.torch
+        evs = []
+        if time_kernels:
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            self._launch()
+            e1.record()
+            evs.append((e0, e1))
+        else:
+            self._launch()
+        return evs, None
+
+    def launches_per_step(self):
+        return len(self.launches)
+
+
+class AdjointStep:
+    """One bench step of the adjoint fit: FCFit.forward (checkpointed forward
+    sweep, FP64 FC loss) and FCFit.backward (recomputation + reverse-time
+    kernel per segment, FP64 gradient accumulation)."""
+
+    def __init__(self, wl, torch):
+        from tvb_hpc import adjoint
+        self.torch = torch
+        self.wl = wl
+        self.prob = adjoint.FCFit(wl['conn'], wl['dt'], 4.0, wl['x0'], wl['target_fc'],
+                                  wl['nsteps'], checkpoint_every=wl['ckpt'])
+        self.ns = 2
+        self.tpn = 2
+        self.status = None
+        self.grads = None
+        self.path = ('per-step kernel forward with checkpoints every %d steps; per segment: '
+                     'recomputation + reverse-time kernel; FP64 gradients' % wl['ckpt'])
+        self.x0 = None
+
+    def reset(self, x0=None):
+        pass
+
+    def run(self, time_kernels=False):
+        torch = self.torch
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        loss = self.prob.forward(self.wl['couplings'], self.wl['eta'])
+        self.grads = self.prob.backward()
+        e1.record()
+        self.loss = loss
+        return ([(e0, e1)] if time_kernels else []), None
+
+    def launches_per_step(self):
+        segs = -(-self.wl['nsteps'] // self.wl['ckpt'])
+        return 3 * segs        # forward segment, recomputation, reverse-time kernel
+
+    def grad_error(self, n_check=4):
+        "Max-norm relative error of dL/dG and dL/deta vs the FP64 oracle on a sample."
+        sys.path.insert(0, os.path.join(ROOT, 'oracle'))
+        import pyoracle as orc
+        from tvb_hpc import model as mdl
+        wl = self.wl
+        c = wl['conn']
+        idx = np.linspace(0, wl['couplings'].size - 1, n_check).astype(int)
+        d = c.delays(4.0, wl['dt'], 'ceil')
+        _, consts, _ = mdl.MPR().engine_spec()
+        _, dG_o, deta_o = orc.mpr_adjoint(c.row, c.col, c.wnz, d,
+                                          wl['couplings'][idx].astype(np.float64),
+                                          wl['eta'][idx].astype(np.float64),
+                                          wl['x0'][idx].astype(np.float64), wl['nsteps'], wl['dt'],
+                                          consts, wl['target_fc'])
+        dG = self.grads[0].cpu().numpy()[idx]
+        deta = self.grads[1].cpu().numpy()[idx]
+        e = lambda a, b: float(np.abs(a - b).max() / np.abs(b).max())  # noqa: E731
+        return {'dG': e(dG, dG_o), 'deta': e(deta, deta_o), 'instances_checked': int(n_check),
+                'against': 'FP64 oracle adjoint (C)'}
+
+
+def cpu_baseline_adjoint(wl, budget_s=12.0):
+    "The FP64 oracle's forward + adjoint (C, OpenMP over instances) on a sample."
+    sys.path.insert(0, os.path.join(ROOT, 'oracle'))
+    import pyoracle as orc
+    from tvb_hpc import model as mdl
+    c = wl['conn']
+    cores = os.cpu_count() or 1
+    d = c.delays(4.0, wl['dt'], 'ceil')
+    _, consts, _ = mdl.MPR().engine_spec()
+    I = wl['couplings'].size
+
+    def run(n):
+        idx = np.linspace(0, I - 1, n).astype(int)
+        t = time.perf_counter()
+        orc.mpr_adjoint(c.row, c.col, c.wnz, d, wl['couplings'][idx].astype(np.float64),
+                        wl['eta'][idx].astype(np.float64), wl['x0'][idx].astype(np.float64),
+                        wl['nsteps'], wl['dt'], consts, wl['target_fc'], nthreads=cores)
+        return time.perf_counter() - t
+
+    n = min(I, max(cores, 4))
+    el = run(n)
+    n = int(np.clip(n * budget_s / max(el, 1e-6), n, I))
+    el = run(n)
+    v = n * c.nnode * wl['nsteps'] / el
+    return {'value': round(v, 1), 'unit': UNIT, 'cores': cores, 'kind': 'port',
+            'sample': '%d of %d instances x %d steps, forward + adjoint (%.1f s), FP64 oracle C + '
+                      'OpenMP' % (n, wl['couplings'].size, wl['nsteps'], el)}
+
+
+def cpu_baseline_lems(wl, budget_s=12.0):
+    "The LEMS oracle (numpy, one work item at a time) on a bounded sample."
+    sys.path.insert(0, os.path.join(ROOT, 'oracle'))
+    import lems_oracle as lo
+    from tvb_hpc import lems
+    c = wl['conn']
+    path = lems.lems_file(wl['lems'])
+    idx = np.linspace(0, wl['params'].shape[0] - 1, 4).astype(int)
+
+    def run(nsteps, k):
+        t = time.perf_counter()
+        lo.run(path, wl['lems'], c.row, c.col, c.wnz, c.lnz, wl['params'][idx[k]:idx[k] + 1],
+               wl['dt'], nsteps, wl['x0'][idx[k]])
+        return time.perf_counter() - t
+
+    probe = 20
+    dt_probe = run(probe, 0)
+    nsteps = int(np.clip(probe * budget_s / 4 / max(dt_probe, 1e-6), probe, wl['nsteps']))
+    el = sum(run(nsteps, k) for k in range(4))
+    v = 4 * c.nnode * nsteps / el
+    return {'value': round(v, 1), 'unit': UNIT, 'cores': 1, 'kind': 'port',
+            'sample': '4 of %d work items x %d steps (%.1f s), LEMS oracle (numpy), noise off' % (
+                wl['params'].shape[0], nsteps, el)}
+
+
 def roofline_entry(wl, nsvar, kernel_ms_total, steps):
     """Roofline of the step kernel: algorithmic bytes of the timed steps over
     the step kernels' event-timed duration (for the uneven batch, the graph
@@ -591,6 +823,10 @@ def gpu_arm(args):
         gs = MixedStep(wl, torch, args.path, not args.no_graph)
     elif wl['name'] == 'net515k':
         gs = NetStep(wl, torch)
+    elif wl['name'].startswith('lems'):
+        gs = LemsStep(wl, torch, args.tpn, 'groups' if args.path == 'groups' else 'sweep')
+    elif wl['name'] == 'adjoint':
+        return adjoint_finish(args, wl, AdjointStep(wl, torch), torch, world, rank, barrier_fn=None)
     else:
         gs = GpuStep(wl, torch, args.tpn, args.warps, args.path)
 
@@ -690,7 +926,8 @@ def gpu_arm(args):
             'clocks': clk, 'tpn': gs.tpn}
     line['config']['path'] = gs.path
     if rank == 0 and world == 1 and not args.no_cpu:
-        line['cpu_baseline'] = cpu_baseline(wl)
+        line['cpu_baseline'] = (cpu_baseline_lems(wl) if wl['name'].startswith('lems')
+                                else cpu_baseline(wl))
     if world > 1:
         dist.barrier()
         dist.destroy_process_group()
@@ -735,6 +972,81 @@ def finish_mixed(args, wl, gs, world, rank, value, ms_per_step, clk, kern_ms, n_
             'batched_vs_plain': round(value / plain['value'], 3) if plain else None}
     if rank == 0 and world == 1 and not args.no_cpu:
         line['cpu_baseline'] = cpu_baseline_mixed(wl)
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def adjoint_finish(args, wl, gs, torch, world, rank, barrier_fn=None):
+    "Time the adjoint fit (device-resident and end to end) and print its line."
+    import torch.distributed as dist
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        gs.run()
+    barrier()
+    clocks = ClockSampler(int(os.environ.get('LOCAL_RANK', '0')))
+    clocks.start()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        gs.run()
+    e1.record()
+    barrier()
+    clk = clocks.stop()
+    total_ms = e0.elapsed_time(e1)
+    t = torch.tensor([total_ms], device='cuda')
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    total_ms = float(t.item())
+    ms = total_ms / args.steps
+    value = world * node_steps(wl) * args.steps / (total_ms / 1e3)
+    # end to end: host G, eta in; gradients and loss back on the host
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        loss = gs.prob.forward(wl['couplings'], wl['eta'])
+        dG, deta = gs.prob.backward()
+        out = (loss.cpu(), dG.cpu(), deta.cpu())
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    h2d = wl['couplings'].nbytes + wl['eta'].nbytes
+    d2h = sum(o.numel() * o.element_size() for o in out)
+    err = gs.grad_error()
+    # forward, recomputation and reverse pass each stream the rings and state
+    bpn = 3 * algorithmic_bytes_per_node_step(wl, 2)
+    peaks = {}
+    p = os.path.join(ROOT, 'MEASURED_PEAKS.json')
+    if os.path.exists(p):
+        peaks = json.load(open(p))
+    hbm = peaks.get('hbm_gbs') or 6800.0
+    ach = bpn * node_steps(wl) / (ms / 1e3) / 1e9
+    line = {'metric': METRIC, 'value': round(value, 1), 'unit': UNIT, 'n_gpus': world,
+            'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': round(ms, 3),
+            'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32',
+            'data': 'synthetic (seeded connectome and target FC, config recipe)',
+            'config': dict(workload_config(wl), checkpoint_every=wl['ckpt'],
+                           loss='MSE of FC (r series) vs target', gradients='G [256], eta [256, 84]',
+                           path=gs.path),
+            'e2e': {'value': round(world * node_steps(wl) * args.steps / e2e_s, 1), 'unit': UNIT,
+                    'h2d_bytes_per_step': int(h2d), 'd2h_bytes_per_step': int(d2h)},
+            'gpu_launches': gs.launches_per_step() * args.steps,
+            'roofline': {'bound': 'hbm', 'achieved': round(ach, 1), 'peak': hbm, 'unit': 'GB/s',
+                         'frac': round(ach / hbm, 4), 'traffic': None,
+                         'peak_source': 'measured' if peaks.get('hbm_gbs') else 'fallback',
+                         'algorithmic_bytes_per_node_step': round(bpn, 2),
+                         'note': 'value counts forward node-steps over forward + backward time; '
+                                 'bytes = 3 passes (forward, recomputation, reverse) of 4E + 16'},
+            'gradient_rel_err_vs_fp64': err, 'clocks': clk}
+    if rank == 0 and world == 1 and not args.no_cpu:
+        line['cpu_baseline'] = cpu_baseline_adjoint(wl)
     if world > 1:
         dist.barrier()
         dist.destroy_process_group()
@@ -866,7 +1178,9 @@ def reference_arm(args):
         return
     wl = WORKLOADS[args.workload]()
     vals = []
-    base = cpu_baseline_mixed if wl['name'].startswith('mixed') else cpu_baseline
+    base = (cpu_baseline_mixed if wl['name'].startswith('mixed') else
+            cpu_baseline_lems if wl['name'].startswith('lems') else
+            cpu_baseline_adjoint if wl['name'] == 'adjoint' else cpu_baseline)
     for i in range(args.warmup + args.steps):
         cb = base(wl, budget_s=args.ref_seconds)
         if i >= args.warmup:

@@ -76,7 +76,11 @@ extern "C" {
 #define TVBG_CFUN_KURAMOTO 2  /* pre = sin(x_j - x_i),       post = a*mean    */
 #define TVBG_CFUN_SIGMOIDAL 3 /* pre = cmax/(1+exp(r(mid-x_j))), post = a*sum */
 #define TVBG_CFUN_LEMS 64     /* the coupling of a LEMS model: pre(x_j, x_i)
-                                 from its XML, sum passed to the model raw */
+                                 from its XML, sum passed to the model raw
+                                 (group kernel: pre(x_j) applied when the
+                                 ring slot is written) */
+#define TVBG_CFUN_LEMS_SC 65  /* a LEMS coupling post * sin(x_j - x_i) on the
+                                 group kernel: sin and cos ring channels */
 
 /* ---- per-instance flags ------------------------------------------------- */
 #define TVBG_F_NOISE 1u      /* Euler-Maruyama with Philox normals          */

@@ -11,9 +11,12 @@
  * tvbg_instance / tvbg_launch descriptors as tvbg_sweep (include/tvbg.h),
  * with model = TVBG_MODEL_LEMS and cfun = TVBG_CFUN_LEMS.
  *
- * Per work item, tvbg_instance.consts holds the swept parameters (the
- * model's <Parameter> elements, in file order) followed by its derived
- * parameters (<DerivedParameter>, in file order): TVBG_LEMS_MAX_K floats.
+ * Per work item, the slots are the swept parameters (the model's
+ * <Parameter> elements, in file order) followed by its derived parameters
+ * (<DerivedParameter>, in file order): at most TVBG_LEMS_MAX_K floats.  The
+ * per-step kernel reads them from tvbg_instance.consts (the coupling) and
+ * from the per-node parameter array nparam ([N][NP], replicated over
+ * nodes, NP = max(1, slots); the model).
  * Noise ("noise" component "on") takes sigma[v] = nsig / sqrt(dt); models
  * with 5..8 state variables take sigma[0] for every variable.
  *
@@ -42,7 +45,10 @@ enum {
     TVBG_LEMS_INFO_REC_SPEED_DT = 6, /* consts index of rec_speed_dt, -1 = none  */
     TVBG_LEMS_INFO_NSIG = 7,         /* consts index of nsig, -1 = none          */
     TVBG_LEMS_INFO_ABI = 8,          /* 1                                        */
-    TVBG_LEMS_INFO_LEN = 9
+    TVBG_LEMS_INFO_GROUP = 9,        /* group kernel coupling: 1 = separable     */
+                                     /* (TVBG_CFUN_LEMS), 2 = sine difference    */
+                                     /* (TVBG_CFUN_LEMS_SC), 0 = per-step only   */
+    TVBG_LEMS_INFO_LEN = 10
 };
 
 int tvbg_lems_info(int32_t *info);
@@ -60,6 +66,20 @@ int tvbg_lems_sweep(const tvbg_instance *d_inst, int32_t n_inst, const tvbg_laun
                     void *stream);
 int tvbg_lems_batch_run(const tvbg_instance *d_inst, int32_t n_inst, const tvbg_launch *cfg,
                         void *stream);
+
+/* Lane-interleaved groups of eight work items sharing a delay table
+ * (tvbg_group_run's records, model = TVBG_MODEL_LEMS and cfun as
+ * TVBG_LEMS_INFO_GROUP says).  The per-work-item slots travel in
+ * tvbg_group.nparam ([N][NP][8], replicated over nodes); sigma[0..3] =
+ * nsig / sqrt(dt) shared by the group.  TVBG_EUNSUPPORTED when the coupling
+ * needs the per-step kernel. */
+int tvbg_lems_group_run(const tvbg_group *d_groups, int32_t n_groups, const tvbg_launch *cfg,
+                        void *stream);
+
+/* The value a separable coupling's ring slot holds for observable o, per
+ * work item (slots [n][16] as from tvbg_lems_derived): fills the history
+ * before t0 (o = 0) on the host. */
+int tvbg_lems_ring_value(const float *slots, int32_t n, float o, float *out);
 
 /* Exposures of n node states: d_state [n][ns] -> d_out [n][nexpo]
  * (tmpl8_CUDA.py:244-249 writes them after the last step of a launch). */

@@ -50,15 +50,19 @@ def state0_of(name, N, seed=0):
 PARAMS = np.array([[2.0, 0.05], [5.0, 0.4], [12.0, 1.5]], np.float32)
 
 
-@pytest.mark.parametrize('name,steps,single', [('Kuramoto', 400, False), ('Oscillator', 400, False),
-                                               ('Rwongwang', 400, False), ('Epileptor', 300, False),
-                                               ('Oscillator', 400, True), ('Epileptor', 300, True)])
-def test_lems_matches_oracle(cuda, name, steps, single):
+@pytest.mark.parametrize('name,steps,single,kind', [
+    ('Kuramoto', 400, False, 'sweep'), ('Oscillator', 400, False, 'sweep'),
+    ('Rwongwang', 400, False, 'sweep'), ('Epileptor', 300, False, 'sweep'),
+    ('Oscillator', 400, True, 'sweep'), ('Epileptor', 300, True, 'sweep'),
+    ('Kuramoto', 400, False, 'groups'), ('Oscillator', 400, False, 'groups'),
+    ('Epileptor', 300, False, 'groups'), ('Epileptor', 300, True, 'groups')])
+def test_lems_matches_oracle(cuda, name, steps, single, kind):
     conn = conn_of()
     N = conn.nnode
     x0 = state0_of(name, N)
     m = lems.load_model(name)
-    sw = lems.LemsSweep(m, conn, 0.1, PARAMS, state0=x0, single=single)
+    Set = lems.LemsSweep if kind == 'sweep' else lems.LemsGroupSet
+    sw = Set(m, conn, 0.1, PARAMS, state0=x0, single=single)
     sw.run(steps)
     got = sw.state.cpu().numpy()
     ref = lo.run(lems.lems_file(name), name, conn.row, conn.col, conn.wnz, conn.lnz, PARAMS, 0.1,
@@ -166,3 +170,59 @@ def test_run_simulation_layout(cuda):
                  PARAMS, 0.1, 150)
     # sin(theta) rows of the last launch
     np.testing.assert_allclose(tavg[-1, 30:, :].T, ref['expo'][:, :, 1], atol=1e-4)
+
+
+def test_lems_groups_take_separable_and_sine_couplings(cuda):
+    """The group kernel runs separable couplings with pre applied at the ring
+    write (here the linear OU coupling with a nonzero per-work-item scale)
+    and falls back to the per-step kernel for zero delays."""
+    conn = conn_of(50, seed=12)
+    N = conn.nnode
+    m = lems.load_model('Ou')
+    x0 = np.random.default_rng(3).uniform(-0.5, 0.5, (N, 1)).astype(np.float32)
+    params = np.array([[4.0, 0.02], [4.0, 0.05], [9.0, 0.1]], np.float32)
+    gs = lems.LemsGroupSet(m, conn, 0.1, params, state0=x0, noise=False)
+    gs.run(500)
+    ref = lo.run(lems.lems_file('Ou'), 'Ou', conn.row, conn.col, conn.wnz, conn.lnz, params, 0.1,
+                 500, x0)
+    assert rel_err(gs.state.cpu().numpy(), ref['state']) < TOL
+    rww = lems.make_set(lems.load_model('Rwongwang'), conn, 0.1, PARAMS)
+    assert isinstance(rww, lems.LemsSweep)          # zero delays: per-step kernel
+    kur = lems.make_set(lems.load_model('Kuramoto'), conn, 0.1, PARAMS)
+    assert isinstance(kur, lems.LemsGroupSet) and kur.channels == 2
+
+
+@pytest.mark.parametrize('name', ['Epileptor', 'Ou6'])
+def test_lems_groups_chunks_bit_exact(cuda, name):
+    conn = conn_of(40, seed=8)
+    N = conn.nnode
+    m = lems.load_model(name)
+    x0 = state0_of(name, N) if name == 'Epileptor' else None
+    a = lems.LemsGroupSet(m, conn, 0.1, PARAMS, state0=x0, seed=11)
+    b = lems.LemsGroupSet(m, conn, 0.1, PARAMS, state0=x0, seed=11)
+    a.run(300)
+    for n in (1, 137, 162):
+        b.run(n)
+    assert np.array_equal(a.state.cpu().numpy(), b.state.cpu().numpy())
+    assert np.array_equal(a.ring.cpu().numpy(), b.ring.cpu().numpy())
+
+
+@pytest.mark.parametrize('name', ['Ou', 'Ou6'])
+def test_lems_groups_noise_statistics(cuda, name):
+    "The group kernel's noise (four and eight normals per step) by its statistics."
+    conn = conn_of(200, seed=9)
+    N = conn.nnode
+    m = lems.load_model(name)
+    params = np.array([[4.0, 0.0]] * 8, np.float32)
+    gs = lems.LemsGroupSet(m, conn, 0.1, params, state0=np.zeros((N, m.ns), np.float32), seed=5)
+    gs.run(2000)
+    x = gs.state.cpu().numpy().reshape(-1, m.ns).astype(np.float64)
+    nsig = np.sqrt(np.float32(0.1)) * np.float32(0.1)
+    var = nsig ** 2 / (1 - (1 - 0.5 * 0.1) ** 2)
+    n = x.shape[0]
+    for v in range(m.ns):
+        assert abs(x[:, v].mean()) < 5 * np.sqrt(var / n)
+        assert abs(x[:, v].var() / var - 1) < 5 * np.sqrt(2.0 / n)
+    if m.ns > 1:
+        c = np.corrcoef(x.T)
+        assert np.abs(c - np.eye(m.ns)).max() < 5 / np.sqrt(n)

@@ -75,6 +75,21 @@ def test_reference_files_parse_and_render(name):
         assert 'struct LemsModel' in lems.render_cuda(m, single)
 
 
+def test_coupling_classes():
+    "Which couplings the group kernel takes: separable or a sine difference."
+    got = {n: lems.load_model(n).coupling_class for n in BUNDLED}
+    assert got == {'Kuramoto': 'sc', 'Oscillator': 'sc', 'Epileptor': 'sc', 'Rwongwang': 'sep',
+                   'Ou': 'sep', 'Ou6': 'sep'}
+    base = open(lems.lems_file('Ou')).read()
+    m = lems.parse(base.replace('expression="x_j"', 'expression="tanh(x_j - x)"'))
+    assert m.coupling_class == 'edge'
+    m = lems.parse(base.replace('expression="x_j"', 'expression="sinf(x_j - x)"'))
+    assert m.coupling_class == 'sc'
+    if os.path.isdir(REF_XML):
+        ref = {n: lems.load_model(n, REF_XML).coupling_class for n in REFERENCE}
+        assert ref == {'Kuramoto': 'sc', 'Oscillator': 'sc', 'Epileptor': 'sc', 'Rwongwang': 'sep'}
+
+
 def test_to_single_and_names():
     assert lems.to_single('2.0 * x + 1e-5 - 3 + 4.0f') == '2.0f * x + 1e-5f - 3 + 4.0f'
     assert lems.names_in('powf(V, 3) + (float) a * sin(b_j)') == ['V', 'a', 'b_j']
@@ -119,6 +134,7 @@ def test_generated_host_derived_parameters_bit_exact():
             np.testing.assert_array_equal(got[b, :slots.size], slots, err_msg='%s %s' % (kind, n))
             assert np.all(got[b, slots.size:] == 0)
         assert L.info['ns'] == m.ns and L.info['nparams'] == 2
+        assert L.info['group'] == {'sep': 1, 'sc': 2, 'edge': 0}[m.coupling_class]
 
 
 def _conn(N=24, seed=3):

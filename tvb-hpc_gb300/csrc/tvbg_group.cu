@@ -2,7 +2,7 @@
 #include <cstring>
 
 #include "tvbg_abi_internal.h"
-#include "tvbg_lanes.cuh"
+#include "tvbg_group_launch.cuh"
 
 using namespace tvbg;
 
@@ -21,22 +21,17 @@ GroupKernel lookup_group(int model, int cfun, int k) {
     }
 }
 
+const ErrSink kSink{set_error, set_cuda_error};
+
 // Validate a group launch; its dynamic shared memory holds the K coupling
 // sums of every thread.
 int check_group_launch(const tvbg_launch* cfg, GroupKernel* kfn, int* cluster, size_t* smem) {
-    if (!cfg) return set_error(TVBG_EINVAL, "null launch config");
-    if (cfg->threads < 32 || cfg->threads > 1024 || (cfg->threads & 31))
-        return set_error(TVBG_EINVAL, "threads must be a multiple of 32 in [32, 1024]");
-    if (cfg->block_k != 4 && cfg->block_k != 8)
-        return set_error(TVBG_EINVAL, "tvbg_group_run: block_k must be 4 or 8");
-    const int c = cfg->cluster <= 0 ? 1 : cfg->cluster;
-    if (c < 1 || c > 8) return set_error(TVBG_EINVAL, "cluster must be in [1, 8]");
-    if (cfg->tpn > 1) return set_error(TVBG_EINVAL, "tvbg_group_run: tpn must be 0 or 1");
+    int rc = check_group_cfg(cfg, kSink, cluster);
+    if (rc) return rc;
     *kfn = lookup_group(cfg->model, cfg->cfun, cfg->block_k);
     if (!*kfn)
         return set_error(TVBG_EUNSUPPORTED, "group kernel not built for this model/coupling/block_k");
-    *cluster = c;
-    *smem = group_smem_bytes(cfg->block_k, cfg->threads, cfg->cfun == TVBG_CFUN_KURAMOTO ? 2 : 1);
+    *smem = group_smem_bytes(cfg->block_k, cfg->threads, group_channels(cfg->cfun));
     return TVBG_OK;
 }
 
@@ -78,31 +73,7 @@ int tvbg_group_run(const tvbg_group* d_groups, int32_t n_groups, const tvbg_laun
     size_t smem = 0;
     int rc = check_group_launch(cfg, &kfn, &cluster, &smem);
     if (rc) return rc;
-    if (n_groups < 0 || (n_groups > 0 && !d_groups))
-        return set_error(TVBG_EINVAL, "tvbg_group_run: bad group array");
-    if (n_groups == 0) return TVBG_OK;
-    cudaError_t e = cudaSuccess;
-    if (smem + sizeof(tvbg_group) > 48u * 1024u) {  // beyond the default: opt in
-        e = cudaFuncSetAttribute(reinterpret_cast<const void*>(kfn),
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-        if (e != cudaSuccess) return set_cuda_error(e, "tvbg_group_run: smem attribute");
-    }
-    cudaLaunchConfig_t lc;
-    std::memset(&lc, 0, sizeof(lc));
-    lc.gridDim = dim3(static_cast<unsigned>(n_groups) * static_cast<unsigned>(cluster), 1, 1);
-    lc.blockDim = dim3(static_cast<unsigned>(cfg->threads), 1, 1);
-    lc.dynamicSmemBytes = smem;
-    lc.stream = static_cast<cudaStream_t>(stream);
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = static_cast<unsigned>(cluster);
-    attr[0].val.clusterDim.y = 1;
-    attr[0].val.clusterDim.z = 1;
-    lc.attrs = attr;
-    lc.numAttrs = cluster > 1 ? 1 : 0;
-    e = cudaLaunchKernelEx(&lc, kfn, d_groups, n_groups, cfg->d_order, cfg->d_status);
-    if (e != cudaSuccess) return set_cuda_error(e, "group kernel launch");
-    return TVBG_OK;
+    return launch_group_kernel(kfn, d_groups, n_groups, cfg, cluster, smem, stream, kSink);
 }
 
 int tvbg_group_occupancy(const tvbg_launch* cfg, int32_t* ctas_per_sm, int32_t* sms) {

@@ -215,10 +215,23 @@ __device__ __forceinline__ void lane_gather_sc(const tvbg_group& g, int lo, int 
     }
 }
 
-// Ring channels per (node, slot): 2 (sin, cos) for the Kuramoto coupling, else 1.
+// Ring channels per (node, slot): 2 (sin, cos) for the Kuramoto coupling and
+// the LEMS sine coupling, else 1.
 template <int CF>
 __host__ __device__ constexpr int ring_channels() {
-    return CF == TVBG_CFUN_KURAMOTO ? 2 : 1;
+    return (CF == TVBG_CFUN_KURAMOTO || CF == TVBG_CFUN_LEMS_SC) ? 2 : 1;
+}
+
+// Value a one-channel ring slot holds for observable o: o itself, or for a
+// LEMS model its separable pre-synaptic term pre(o), so the gather sums
+// w_e * pre(x_j) without evaluating pre per edge.
+template <class M, int CF>
+__device__ __forceinline__ float ring_val(float o, const float* p) {
+    if constexpr (CF == TVBG_CFUN_LEMS) {
+        return M::ring_value(o, p);
+    } else {
+        return o;
+    }
 }
 
 // Dynamic shared memory of a group CTA: the K coupling sums (per ring
@@ -240,7 +253,7 @@ __device__ __forceinline__ void run_group(const tvbg_group& g, float* csum, int3
     const bool cluster = C > 1;
     if (N <= 0 || N > 65535 || g.lognh < 3 || g.lognh > 16 || g.model != M::ID || g.cfun != CF ||
         g.nsteps < 0 || (g.flags & (TVBG_F_TRACKA | TVBG_F_MIDSYNC | TVBG_F_TRACE_CSUM)) ||
-        (!Noise<M>::kOK && (g.flags & TVBG_F_NOISE))) {
+        (!Noise<M>::kOK && !WideNoise<M>::value && (g.flags & TVBG_F_NOISE))) {
         if (threadIdx.x == 0) report(status, TVBG_EINVAL);
         return;  // every CTA of the cluster reads the same descriptor and leaves here
     }
@@ -276,6 +289,9 @@ __device__ __forceinline__ void run_group(const tvbg_group& g, float* csum, int3
             for (int v = 0; v < NS; ++v) x[v] = state[(n * NS + v) * kLanes + l];
             const size_t idx = (static_cast<size_t>(n) * R + pos) * RL + l;
             const float o = M::obs(x, 0);
+            float p[NP];
+#pragma unroll
+            for (int v = 0; v < NP; ++v) p[v] = __ldg(g.nparam + (n * NP + v) * kLanes + l);
             if constexpr (NC == 2) {
                 float sn, cs;
                 sincosf(o, &sn, &cs);
@@ -286,8 +302,9 @@ __device__ __forceinline__ void run_group(const tvbg_group& g, float* csum, int3
                     ring[idx + static_cast<size_t>(nh) * RL + kLanes] = cs;
                 }
             } else {
-                ring[idx] = o;
-                if (pos < kGhost) ring[idx + static_cast<size_t>(nh) * kLanes] = o;
+                const float rv = ring_val<M, CF>(o, p);
+                ring[idx] = rv;
+                if (pos < kGhost) ring[idx + static_cast<size_t>(nh) * kLanes] = rv;
             }
         }
     }
@@ -361,10 +378,16 @@ __device__ __forceinline__ void run_group(const tvbg_group& g, float* csum, int3
                 const float xbold = bold ? M::obs(x, g.bold_obs) : 0.0f;
                 float c;
                 if constexpr (NC == 2) {
-                    // sum_e w sin(x_j - x_i); post = a * mean (coupling.py:119-121)
+                    // sum_e w sin(x_j - x_i); Kuramoto: post = a * mean (coupling.py:119-121)
                     const float S = cs0 * csum[k * blockDim.x + threadIdx.x] -
                                     sn0 * csum[(K + k) * blockDim.x + threadIdx.x];
-                    c = cf_a * (S / static_cast<float>(N));
+                    if constexpr (CF == TVBG_CFUN_LEMS_SC) {
+                        c = M::coupling(S, x, p);
+                    } else {
+                        c = cf_a * (S / static_cast<float>(N));
+                    }
+                } else if constexpr (CF == TVBG_CFUN_LEMS) {
+                    c = M::coupling(csum[k * blockDim.x + threadIdx.x], x, p);
                 } else {
                     c = lane_post<CF>(csum[k * blockDim.x + threadIdx.x], obs0, wsum, cf_a, g.cf_b);
                 }
@@ -386,6 +409,20 @@ __device__ __forceinline__ void run_group(const tvbg_group& g, float* csum, int3
                         for (int v = 0; v < NS; ++v)
                             x[v] = fmaf(sqrt_dt * pick4(zz, r0 * NS + v), g.sigma[v], x[v]);
                     }
+                } else if constexpr (WideNoise<M>::value) {
+                    if (noise) {
+                        float z8[8];
+#pragma unroll
+                        for (int b = 0; b < 2; ++b) {
+                            const u32x4 w = philox4x32_10(static_cast<uint32_t>(n),
+                                                          static_cast<uint32_t>(t), g.seed_hi,
+                                                          static_cast<uint32_t>(b), g.seed_lo, inst_id);
+                            box_muller_fast(w.v[0], w.v[1], z8[4 * b], z8[4 * b + 1]);
+                            box_muller_fast(w.v[2], w.v[3], z8[4 * b + 2], z8[4 * b + 3]);
+                        }
+#pragma unroll
+                        for (int v = 0; v < NS; ++v) x[v] = fmaf(sqrt_dt * z8[v], g.sigma[0], x[v]);
+                    }
                 }
                 M::limit(x, flags);
                 obs0 = M::obs(x, 0);
@@ -400,8 +437,9 @@ __device__ __forceinline__ void run_group(const tvbg_group& g, float* csum, int3
                         ring[idx + static_cast<size_t>(nh) * RL + kLanes] = cs0;
                     }
                 } else {
-                    ring[idx] = obs0;
-                    if (pos < kGhost) ring[idx + static_cast<size_t>(nh) * kLanes] = obs0;
+                    const float rv = ring_val<M, CF>(obs0, p);
+                    ring[idx] = rv;
+                    if (pos < kGhost) ring[idx + static_cast<size_t>(nh) * kLanes] = rv;
                 }
                 if (bold) {
                     Balloon::step(bs, bF, bV, bQ, xbold, g.dt_bold);

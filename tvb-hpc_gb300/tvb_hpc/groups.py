@@ -98,7 +98,7 @@ class GroupSet:
                  nparam=None, delays=None, rounding='ceil', seed=0, inst_ids=None,
                  bold_period=0, bold_len=0, trace_every=0, trace_len=0, trace_nobs=None,
                  flags=0, cf_b=None, t0=0, nsteps=None, block_k=None, threads=None,
-                 cluster=None, history='zero'):
+                 cluster=None, history='zero', delay_tables=None):
         _device_ok()
         torch = _torch()
         self.torch = torch
@@ -108,11 +108,13 @@ class GroupSet:
         self.cfun_id, cf_a0, cf_b0, self.cf_p = cfun.engine_spec()
         separable = self.cfun_id in (nat.CFUN_LINEAR, nat.CFUN_DIFF, nat.CFUN_SIGMOIDAL)
         kuramoto = (self.model_id, self.cfun_id) == (nat.MODEL_KURAMOTO, nat.CFUN_KURAMOTO)
-        if not (separable or kuramoto):
+        lems = self.model_id == nat.MODEL_LEMS and self.cfun_id in (nat.CFUN_LEMS, nat.CFUN_LEMS_SC)
+        if not (separable or kuramoto or lems):
             raise ValueError('group kernel: a separable coupling (Linear, Diff, Sigmoidal), or the '
                              'Kuramoto model with the Kuramoto coupling')
-        # the Kuramoto coupling keeps sin and cos of the observable in the ring
-        self.channels = 2 if self.cfun_id == nat.CFUN_KURAMOTO else 1
+        # the Kuramoto coupling (and a LEMS sine coupling) keeps sin and cos of
+        # the observable in the ring
+        self.channels = 2 if self.cfun_id in (nat.CFUN_KURAMOTO, nat.CFUN_LEMS_SC) else 1
         self.N = N = int(conn.nnode)
         if N > 65535:
             raise ValueError('group kernel: N < 65536')
@@ -128,7 +130,10 @@ class GroupSet:
         self.nnz = int(col.size)
         self.row_np, self.col_np, self.w_np = row, col, w
         # delay tables, one per distinct speed
-        if delays is not None:
+        if delay_tables is not None:
+            tables = [np.asarray(d, np.int64).astype(np.int32) for d in delay_tables[0]]
+            tab_of = np.broadcast_to(np.asarray(delay_tables[1], np.int64), (I, )).copy()
+        elif delays is not None:
             tables = [np.asarray(delays, np.int64).astype(np.int32)]
             tab_of = np.zeros(I, np.int64)
         else:
@@ -395,20 +400,23 @@ class GroupSet:
         the current one); launches of different block lengths run
         concurrently on forked streams joined back into `stream`."""
         torch = self.torch
-        lib = nat.load()
         launches = launches if launches is not None else self._uploaded[0]
         main = stream if stream is not None else torch.cuda.current_stream()
         if len(launches) == 1:
             dev, order, n, cfg = launches[0]
-            nat.check(lib.tvbg_group_run(dev.data_ptr(), n, ctypes.byref(cfg), main.cuda_stream))
+            self._run_groups(dev.data_ptr(), n, cfg, main.cuda_stream)
             return
         if self._streams is None or len(self._streams) < len(launches):
             self._streams = [torch.cuda.Stream() for _ in launches]
         for (dev, order, n, cfg), st in zip(launches, self._streams):
             st.wait_stream(main)
-            nat.check(lib.tvbg_group_run(dev.data_ptr(), n, ctypes.byref(cfg), st.cuda_stream))
+            self._run_groups(dev.data_ptr(), n, cfg, st.cuda_stream)
         for st in self._streams[:len(launches)]:
             main.wait_stream(st)
+
+    def _run_groups(self, dev_ptr, n, cfg, stream):
+        "One group launch through the engine library."
+        nat.check(nat.load().tvbg_group_run(dev_ptr, n, ctypes.byref(cfg), stream))
 
     def advance(self, gmax):
         "Move the group clocks after a launch of the prepared tables."

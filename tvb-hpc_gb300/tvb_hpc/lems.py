@@ -61,6 +61,7 @@ import numpy as np
 from . import _native as nat
 from . import scheme as sch
 from .engine import Sweep
+from .groups import GroupSet, L as L_GROUP
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 PKG_ROOT = os.path.dirname(HERE)
@@ -75,7 +76,7 @@ MAX_NS = 8
 LEMS_ABI = 1
 
 INFO_FIELDS = ('ns', 'nparams', 'nderived', 'nexpo', 'cvar', 'noise', 'rec_speed_dt', 'nsig',
-               'abi')
+               'abi', 'group')
 
 # functions an expression may call (C / CUDA math)
 FUNCS = set('''sin cos tan asin acos atan atan2 sinh cosh tanh exp exp2 expm1 log log2 log10 log1p
@@ -208,6 +209,27 @@ class LemsModel:
             if n == name:
                 return e
         return None
+
+    @property
+    def coupling_class(self):
+        """How the group kernel can take the coupling: 'sep' (pre reads only
+        x_j: applied when the ring slot is written), 'sc' (pre is
+        sin(x_j - x_i): sin and cos ring channels), or 'edge' (per edge only:
+        the per-step kernel)."""
+        c = self.dyn_coupling
+        if c is None:
+            return 'sep'
+        pj, own = c.param[0], self.state_names[c.param[1]]
+        if c.post is not None and pj in names_in(c.post):
+            return 'edge'
+        if c.pre is None or own not in names_in(c.pre):
+            return 'sep'
+        tk = tokens(c.pre)
+        if (len(tk) == 6 and tk[0][0] == 'id' and tk[0][1] in ('sin', 'sinf') and tk[1] == ('op', '(')
+                and tk[2] == ('id', pj) and tk[3] == ('op', '-') and tk[4] == ('id', own)
+                and tk[5] == ('op', ')')):
+            return 'sc'
+        return 'edge'
 
     @property
     def has_delays(self):
@@ -438,6 +460,7 @@ def render_cuda(m, single=False):
     w('#include <cstdio>')
     w('#include "tvbg_step.cuh"')
     w('#include "tvbg_step_launch.cuh"')
+    w('#include "tvbg_group_launch.cuh"')
     w('')
     w('#define M_PI_F 3.14159265358979323846f')
     w('#define PI_2 (2 * M_PI_F)')
@@ -472,13 +495,13 @@ def render_cuda(m, single=False):
     w('struct LemsModel {')
     w('    static constexpr int ID = TVBG_MODEL_LEMS;')
     w('    static constexpr int NS = kNS;')
-    w('    static constexpr int NP = 1;')
+    w('    static constexpr int NP = %d;  // per-work-item slots, read per node' % max(1, len(kn)))
     w('    static constexpr int NOBS = 1 + kNExpo;')
     w('    static constexpr bool kWideNoise = true;')
-    w('    __device__ static __forceinline__ void drift(const float* x_, float S_, const float*,')
-    w('                                                 const float* K_, float* f_) {')
+    w('    __device__ static __forceinline__ void drift(const float* x_, float S_, const float* p_,')
+    w('                                                 const float*, float* f_) {')
     consts('        ', coupling=True)
-    kvals('K_', '        ')
+    kvals('p_', '        ')
     for v, n in enumerate(m.state_names):
         w('        const float %s = x_[%d];' % (n, v))
     for c in m.couplings:
@@ -506,6 +529,27 @@ def render_cuda(m, single=False):
         w('            case %d: return %s;  // %s' % (k + 1, E(e), n))
     w('            default: return x_[kCVar];')
     w('        }')
+    w('    }')
+    # group-kernel hooks: the ring value of a separable coupling, and the
+    # coupling input from the gathered sum
+    cls = m.coupling_class
+    w('    __host__ __device__ static __forceinline__ float ring_value(float o_, const float* p_) {')
+    if cp is not None and cls == 'sep':
+        consts('        ', coupling=True)
+        kvals('p_', '        ')
+        w('        const float %s = o_;' % cp.param[0])
+        w('        return %s;' % ('1.0f' if _none(cp.pre) else '(%s)' % E(cp.pre)))
+    else:
+        w('        return o_;')
+    w('    }')
+    w('    __device__ static __forceinline__ float coupling(float S_, const float* x_, const float* p_) {')
+    if cp is not None and cls in ('sep', 'sc'):
+        consts('        ', coupling=True)
+        kvals('p_', '        ')
+        w('        const float %s = x_[%d];' % (m.state_names[m.cvar], m.cvar))
+        w('        return %s * S_;' % ('1.0f' if _none(cp.post) else '(%s)' % E(cp.post)))
+    else:
+        w('        return 0.0f;')
     w('    }')
     w('    __device__ static __forceinline__ void limit(float* x_, uint32_t) {')
     for v, (n, b) in enumerate(m.states):
@@ -594,6 +638,18 @@ def render_cuda(m, single=False):
     w('#pragma unroll')
     w('    for (int k = 0; k < kNExpo; ++k) o_[i * kNExpo + k] = LemsModel::obs(x_, 1 + k);')
     w('}')
+    gcf = {'sep': 'TVBG_CFUN_LEMS', 'sc': 'TVBG_CFUN_LEMS_SC'}.get(cls)
+    w('GroupKernelFn lookup_group(int cfun, int k) {')
+    if gcf is not None:
+        w('    if (cfun != %s) return nullptr;' % gcf)
+        w('    switch (k) {')
+        w('        case 4: return group_kernel<LemsModel, %s, 4>;' % gcf)
+        w('        case 8: return group_kernel<LemsModel, %s, 8>;' % gcf)
+        w('        default: return nullptr;')
+        w('    }')
+    else:
+        w('    return nullptr;')
+    w('}')
     w('}  // namespace')
     w('')
     # exports
@@ -601,7 +657,8 @@ def render_cuda(m, single=False):
     w('TVBG_LEMS_EXPORT int tvbg_lems_info(int32_t* info) {')
     w('    if (!info) return lems_error(TVBG_EINVAL, "tvbg_lems_info: null");')
     vals = [m.ns, len(m.params), len(m.derived_params), len(m.exposures), m.cvar, int(m.noise),
-            m.k_index('rec_speed_dt') if m.has_delays else -1, m.k_index('nsig'), LEMS_ABI]
+            m.k_index('rec_speed_dt') if m.has_delays else -1, m.k_index('nsig'), LEMS_ABI,
+            {'sep': 1, 'sc': 2}.get(cls, 0)]
     for k, v in enumerate(vals):
         w('    info[%d] = %d;  // %s' % (k, v, INFO_FIELDS[k]))
     w('    return TVBG_OK;')
@@ -633,6 +690,26 @@ def render_cuda(m, single=False):
     w('                                        const tvbg_launch* cfg, void* stream) {')
     w('    return run(d_inst, n_inst, cfg, true, stream);')
     w('}')
+    w('TVBG_LEMS_EXPORT int tvbg_lems_group_run(const tvbg_group* d_groups, int32_t n_groups,')
+    w('                                        const tvbg_launch* cfg, void* stream) {')
+    w('    int cluster = 1;')
+    w('    int rc = check_group_cfg(cfg, kSink, &cluster);')
+    w('    if (rc) return rc;')
+    w('    if (cfg->model != TVBG_MODEL_LEMS)')
+    w('        return lems_error(TVBG_EINVAL, "tvbg_lems_group_run: model must be TVBG_MODEL_LEMS");')
+    w('    GroupKernelFn k = lookup_group(cfg->cfun, cfg->block_k);')
+    w('    if (!k)')
+    w('        return lems_error(TVBG_EUNSUPPORTED, "tvbg_lems_group_run: this coupling needs the '
+      'per-step kernel, or cfun/block_k do not match");')
+    w('    const size_t smem = group_smem_bytes(cfg->block_k, cfg->threads, group_channels(cfg->cfun));')
+    w('    return launch_group_kernel(k, d_groups, n_groups, cfg, cluster, smem, stream, kSink);')
+    w('}')
+    w('TVBG_LEMS_EXPORT int tvbg_lems_ring_value(const float* slots, int32_t n, float o, float* out) {')
+    w('    if (n < 0 || (n > 0 && (!slots || !out)))')
+    w('        return lems_error(TVBG_EINVAL, "tvbg_lems_ring_value: bad arguments");')
+    w('    for (int32_t b = 0; b < n; ++b) out[b] = LemsModel::ring_value(o, slots + %d * b);' % MAX_K)
+    w('    return TVBG_OK;')
+    w('}')
     w('TVBG_LEMS_EXPORT int tvbg_lems_expose(const float* d_state, int64_t n, float* d_out, void* stream) {')
     w('    if (!d_state || !d_out || n < 0) return lems_error(TVBG_EINVAL, "tvbg_lems_expose: bad arguments");')
     w('    if (n == 0) return TVBG_OK;')
@@ -648,7 +725,8 @@ def render_cuda(m, single=False):
 # ---------------------------------------------------------------------------
 # build and load
 # ---------------------------------------------------------------------------
-_HEADERS = ('tvbg_step.cuh', 'tvbg_device.cuh', 'tvbg_step_launch.cuh')
+_HEADERS = ('tvbg_step.cuh', 'tvbg_device.cuh', 'tvbg_step_launch.cuh', 'tvbg_lanes.cuh',
+            'tvbg_step_blocked.cuh', 'tvbg_group_launch.cuh')
 
 
 def _key(src):
@@ -722,6 +800,8 @@ SIGNATURES = {
     'tvbg_lems_sweep': (ctypes.c_int, [_vp, _i32, ctypes.POINTER(nat.tvbg_launch), _vp]),
     'tvbg_lems_batch_run': (ctypes.c_int, [_vp, _i32, ctypes.POINTER(nat.tvbg_launch), _vp]),
     'tvbg_lems_expose': (ctypes.c_int, [_vp, _i64, _vp, _vp]),
+    'tvbg_lems_group_run': (ctypes.c_int, [_vp, _i32, ctypes.POINTER(nat.tvbg_launch), _vp]),
+    'tvbg_lems_ring_value': (ctypes.c_int, [_vp, _i32, ctypes.c_float, _vp]),
 }
 
 _LIBS = {}
@@ -763,13 +843,14 @@ class LemsLibrary:
 
 
 class _EngineModel:
-    "The engine-facing face of a LEMS model (what InstanceSet reads)."
+    """The engine-facing face of a LEMS model (what InstanceSet and GroupSet
+    read): the per-work-item slots are its per-node parameters."""
 
     def __init__(self, m, noise):
         self.m = m
         self.nsvar = m.ns
         self.nobs = 1 + len(m.exposures)
-        self.param_sym = ['lems_unused']
+        self.param_sym = list(m.k_names) or ['lems_unused']
         self._noise = noise
 
     def engine_spec(self):
@@ -777,12 +858,58 @@ class _EngineModel:
         return nat.MODEL_LEMS, np.zeros(MAX_K, np.float32), sigma
 
     def node_params(self, N):
-        return np.zeros((N, 1), np.float32)
+        return np.zeros((N, len(self.param_sym)), np.float32)
 
 
 class _EngineCoupling:
+    def __init__(self, cfun_id=nat.CFUN_LEMS):
+        self.cfun_id = cfun_id
+
     def engine_spec(self):
-        return nat.CFUN_LEMS, 0.0, 0.0, np.zeros(3, np.float32)
+        return self.cfun_id, 0.0, 0.0, np.zeros(3, np.float32)
+
+
+def _setup(lib, m, conn, dt, params):
+    """Per-work-item slots K (I, 16), the delay tables (one per distinct
+    rec_speed_dt) and each work item's table index."""
+    params = np.asarray(params, np.float32)
+    if params.ndim == 1:
+        params = params.reshape(-1, max(1, len(m.params)))
+    I = params.shape[0]
+    K = lib.derived(params, dt, int(conn.nnode))
+    ki = lib.info['rec_speed_dt']
+    if ki >= 0:
+        recs = K[:, ki]
+        if not np.all(np.isfinite(recs)) or np.any(recs < 0):
+            raise ValueError('rec_speed_dt must be finite and non-negative')
+        uniq, tab_of = np.unique(recs, return_inverse=True)
+        tables = [dsl_delays(conn.lnz, r) for r in uniq]
+        if max((int(t.max()) if t.size else 0) for t in tables) >= 1 << 20:
+            raise ValueError('delays beyond 2^20 steps')
+    else:
+        tables, tab_of = [np.zeros(conn.nnz, np.int64)], np.zeros(I, np.int64)
+    return params, K, tables, tab_of
+
+
+def _state0(m, N, state0):
+    if state0 is None:
+        state0 = np.zeros((N, m.ns), np.float32)
+        state0[:, 0] = 0.001
+    return state0
+
+
+def _slots_per_node(m, K, N):
+    npar = max(1, len(m.k_names))
+    return np.ascontiguousarray(np.broadcast_to(K[:, None, :npar], (K.shape[0], N, npar)))
+
+
+def _sigma(lib, K, dt, noise):
+    "Per work item nsig / sqrt(dt) (4 copies), or zeros without noise."
+    if not noise:
+        return np.zeros((K.shape[0], 4), np.float32)
+    sq = np.sqrt(np.float32(dt)).astype(np.float32)
+    sig = (K[:, lib.info['nsig']] / sq).astype(np.float32)
+    return np.repeat(sig[:, None], 4, axis=1)
 
 
 def dsl_delays(lengths, rec_speed_dt):
@@ -813,39 +940,17 @@ class LemsSweep(Sweep):
         self.lems = LemsLibrary(m, single)
         self.lmodel = m
         noise = m.noise if noise is None else bool(noise)
-        params = np.asarray(params, np.float32)
-        if params.ndim == 1:
-            params = params.reshape(-1, max(1, len(m.params)))
-        I = params.shape[0]
-        N = int(conn.nnode)
-        K = self.lems.derived(params, dt, N)
-        # delay tables, one per distinct rec_speed_dt
-        ki = self.lems.info['rec_speed_dt']
-        if ki >= 0:
-            recs = K[:, ki]
-            if not np.all(np.isfinite(recs)) or np.any(recs < 0):
-                raise ValueError('rec_speed_dt must be finite and non-negative')
-            uniq, tab_of = np.unique(recs, return_inverse=True)
-            tables = [dsl_delays(conn.lnz, r) for r in uniq]
-            if max((int(t.max()) if t.size else 0) for t in tables) >= 1 << 20:
-                raise ValueError('delays beyond 2^20 steps')
-        else:
-            tables, tab_of = [np.zeros(conn.nnz, np.int64)], np.zeros(I, np.int64)
-        if state0 is None:
-            state0 = np.zeros((N, m.ns), np.float32)
-            state0[:, 0] = 0.001
+        params, K, tables, tab_of = _setup(self.lems, m, conn, dt, params)
+        I, N = params.shape[0], int(conn.nnode)
         em = _EngineModel(m, noise)
         scm = sch.EulerMaryuyamaStep(dt) if noise else sch.EulerStep(dt)
         kwargs.setdefault('blocked', False)
         super().__init__(em, _EngineCoupling(), scm, conn, dt, np.zeros(I, np.float32),
-                         state0=state0, delay_tables=(tables, tab_of), tpn=tpn, **kwargs)
+                         state0=_state0(m, N, state0), nparam=_slots_per_node(m, K, N),
+                         delay_tables=(tables, tab_of), tpn=tpn, **kwargs)
         self.kernel_key = self.lems.path
         self.consts = K
-        if noise:
-            kn = self.lems.info['nsig']
-            sq = np.sqrt(np.float32(dt)).astype(np.float32)
-            sig = (K[:, kn] / sq).astype(np.float32)
-            self.sigma = np.repeat(sig[:, None], 4, axis=1)
+        self.sigma = _sigma(self.lems, K, dt, noise)
         self.params = params
 
     def launch(self, launches=None, tpn=None, stream=None):
@@ -867,6 +972,91 @@ class LemsSweep(Sweep):
         return out
 
 
+class LemsGroupSet(GroupSet):
+    """
+    Work items of one LEMS model on the lane-interleaved group kernel: eight
+    work items sharing a delay table per group, time-blocked (K = 4 or 8 <=
+    d_min + 1 steps per block).  Takes models whose coupling is separable
+    (pre reads only x_j: its value is written into the ring) or a sine
+    difference post * sin(x_j - x_i) (sin and cos ring channels); others,
+    and delays shorter than 3 steps, need LemsSweep (ValueError here).
+    Noise needs one nsig for every work item.  Arguments as LemsSweep, plus
+    GroupSet's block_k, threads, cluster, trace_*, bold_*.
+    """
+
+    def __init__(self, m, conn, dt, params, state0=None, noise=None, single=False, **kwargs):
+        self.lems = LemsLibrary(m, single)
+        self.lmodel = m
+        cls = self.lems.info['group']
+        if cls == 0:
+            raise ValueError('LEMS model %s: its coupling needs the per-step kernel' % m.name)
+        if kwargs.get('history', 'zero') != 'zero':
+            raise ValueError('LEMS groups start from zero history')
+        noise = m.noise if noise is None else bool(noise)
+        params, K, tables, tab_of = _setup(self.lems, m, conn, dt, params)
+        I, N = params.shape[0], int(conn.nnode)
+        sig = _sigma(self.lems, K, dt, noise)
+        if noise and not np.all(sig == sig[0]):
+            raise ValueError('LEMS groups need one nsig for every work item')
+        # history before t0: the ring holds pre(0) of each work item
+        self._f0 = None
+        if cls == 1:
+            f0 = np.zeros(I, np.float32)
+            Kc = np.ascontiguousarray(K)
+            self.lems.check(self.lems.lib.tvbg_lems_ring_value(Kc.ctypes.data, I, 0.0,
+                                                               f0.ctypes.data))
+            self._f0 = f0
+        em = _EngineModel(m, noise)
+        ec = _EngineCoupling(nat.CFUN_LEMS if cls == 1 else nat.CFUN_LEMS_SC)
+        scm = sch.EulerMaryuyamaStep(dt) if noise else sch.EulerStep(dt)
+        super().__init__(em, ec, scm, conn, dt, np.zeros(I, np.float32),
+                         state0=_state0(m, N, state0), nparam=_slots_per_node(m, K, N),
+                         delay_tables=(tables, tab_of), **kwargs)
+        self.sigma = sig[0] if I else np.zeros(4, np.float32)
+        self.consts = np.zeros(MAX_K, np.float32)
+        self.params = params
+        self.slots = K
+
+    def clear_history(self):
+        super().clear_history()
+        f0 = getattr(self, '_f0', None)
+        if f0 is None or not np.any(f0 != 0):
+            return
+        torch = self.torch
+        N = self.N
+        for g, mem in enumerate(self.members):
+            R = int(self.R[g])
+            o = int(self.ring_off[g])
+            v = np.zeros(L_GROUP, np.float32)
+            v[:mem.size] = f0[mem]
+            self.ring[o:o + N * R * L_GROUP].view(N, R, L_GROUP)[:] = torch.from_numpy(v).cuda()
+
+    def _run_groups(self, dev_ptr, n, cfg, stream):
+        self.lems.check(self.lems.lib.tvbg_lems_group_run(dev_ptr, n, ctypes.byref(cfg), stream))
+
+    def exposures(self, stream=None):
+        "Exposures of the current state, (n_work, N, nexpo), on the device."
+        torch = self.torch
+        st = self.state.contiguous()
+        ne = len(self.lmodel.exposures)
+        out = torch.empty((self.n, self.N, ne), dtype=torch.float32, device='cuda')
+        self.lems.check(self.lems.lib.tvbg_lems_expose(st.data_ptr(), self.n * self.N,
+                                                       out.data_ptr(), nat.stream_handle(stream)))
+        return out
+
+
+def make_set(m, conn, dt, params, prefer='groups', **kwargs):
+    """The fastest set that takes the model: LemsGroupSet where the coupling
+    and the delays allow it, else LemsSweep."""
+    if prefer == 'groups':
+        try:
+            return LemsGroupSet(m, conn, dt, params, **{k: v for k, v in kwargs.items()
+                                                         if k != 'tpn'})
+        except ValueError:
+            pass
+    return LemsSweep(m, conn, dt, params, **kwargs)
+
+
 def run_simulation(m, weights, lengths, params_matrix, dt, nstep, n_inner_steps, single=False,
                    noise=None, seed=0, tpn=None):
     """
@@ -874,11 +1064,12 @@ def run_simulation(m, weights, lengths, params_matrix, dt, nstep, n_inner_steps,
     `nstep` launches of `n_inner_steps` steps for every work item (a row of
     params_matrix), returning the exposures after each launch as
     (nstep, n_nodes * nexpo, n_work) -- the reference's tavg layout -- and
-    the LemsSweep (final state, ring).  weights and lengths are dense N x N.
+    the set that ran them (LemsGroupSet where the coupling and delays allow,
+    else LemsSweep).  weights and lengths are dense N x N.
     """
     from .network import Connectivity
     conn = Connectivity.from_dense(np.asarray(weights, np.float32), np.asarray(lengths, np.float32))
-    sw = LemsSweep(m, conn, dt, params_matrix, noise=noise, single=single, seed=seed, tpn=tpn)
+    sw = make_set(m, conn, dt, params_matrix, noise=noise, single=single, seed=seed, tpn=tpn)
     out = []
     for _ in range(int(nstep)):
         sw.run(int(n_inner_steps))
