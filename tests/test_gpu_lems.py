@@ -186,10 +186,30 @@ def test_lems_groups_take_separable_and_sine_couplings(cuda):
     ref = lo.run(lems.lems_file('Ou'), 'Ou', conn.row, conn.col, conn.wnz, conn.lnz, params, 0.1,
                  500, x0)
     assert rel_err(gs.state.cpu().numpy(), ref['state']) < TOL
-    rww = lems.make_set(lems.load_model('Rwongwang'), conn, 0.1, PARAMS)
-    assert isinstance(rww, lems.LemsSweep)          # zero delays: per-step kernel
     kur = lems.make_set(lems.load_model('Kuramoto'), conn, 0.1, PARAMS)
     assert isinstance(kur, lems.LemsGroupSet) and kur.channels == 2
+    # a coupling the group kernel cannot take falls back to the per-step kernel
+    edge = lems.parse(open(lems.lems_file('Ou')).read().replace('expression="x_j"',
+                                                               'expression="tanh(x_j - x)"'))
+    assert isinstance(lems.make_set(edge, conn, 0.1, params), lems.LemsSweep)
+
+
+@pytest.mark.parametrize('name,speed,k', [('Rwongwang', 1.0, 1), ('Kuramoto', 60.0, 2),
+                                          ('Epileptor', 60.0, 2)])
+def test_lems_groups_short_blocks(cuda, name, speed, k):
+    "Zero delays (K = 1) and d_min = 1 (K = 2) on the group kernel, against the oracle."
+    conn = conn_of(60, seed=13)
+    N = conn.nnode
+    x0 = state0_of(name, N)
+    m = lems.load_model(name)
+    params = np.array([[speed, 0.05], [speed, 0.4], [speed, 1.5]], np.float32)
+    gs = lems.make_set(m, conn, 0.1, params, state0=x0)
+    assert isinstance(gs, lems.LemsGroupSet) and set(gs.block_k.tolist()) == {k}
+    gs.run(300)
+    ref = lo.run(lems.lems_file(name), name, conn.row, conn.col, conn.wnz, conn.lnz, params, 0.1,
+                 300, x0)
+    err = circ_rel_err if name == 'Kuramoto' else rel_err
+    assert err(gs.state.cpu().numpy(), ref['state']) < TOL
 
 
 @pytest.mark.parametrize('name', ['Epileptor', 'Ou6'])

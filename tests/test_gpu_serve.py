@@ -78,3 +78,31 @@ def test_late_arrivals_join_running_work(cuda):
         t[0] += 1.0
         srv.tick()
     assert all(r.steps_done == r.nsteps for r in srv.done)
+
+
+def test_poll_and_cancel(cuda):
+    "A queued and an active request are cancelled; the rest finish unchanged."
+    reqs = requests(seed=3, n=4)
+    for r in reqs:
+        r.nsteps = max(r.nsteps, 1500)
+    srv = serve.Server(chunk=500)
+    for r in reqs:
+        srv.submit(r)
+    assert srv.poll(reqs[0].rid) == 'queued' and srv.poll(12345) is None
+    srv.tick()
+    assert srv.poll(reqs[1].rid) == 'active'
+    used = srv.used
+    assert srv.cancel(reqs[1].rid)
+    assert srv.used == used - reqs[1].nbytes
+    assert srv.poll(reqs[1].rid) == 'cancelled'
+    assert not srv.cancel(reqs[1].rid)
+    done = {r.rid: r for r in srv.run()}
+    assert reqs[1].rid not in done and len(done) == len(reqs) - 1
+    for r in requests(seed=3, n=4):
+        if r.rid == reqs[1].rid:
+            continue
+        r.nsteps = max(r.nsteps, 1500)
+        solo = serve.Server(chunk=500)
+        solo.submit(r)
+        (a, ) = solo.run()
+        assert np.array_equal(a.state, done[r.rid].state)

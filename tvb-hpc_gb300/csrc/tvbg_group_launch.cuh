@@ -15,12 +15,15 @@ namespace tvbg {
 using GroupKernelFn = void (*)(const tvbg_group*, int32_t, const int32_t*, int32_t*);
 
 // Checks of a group launch configuration; *cluster = CTAs per group.
-inline int check_group_cfg(const tvbg_launch* cfg, const ErrSink& es, int* cluster) {
+// k_mask: the block lengths built (bit K set for K in {1, 2, 4, 8}).
+inline int check_group_cfg(const tvbg_launch* cfg, const ErrSink& es, int* cluster,
+                           unsigned k_mask = (1u << 4) | (1u << 8)) {
     if (!cfg) return es.error(TVBG_EINVAL, "null launch config");
     if (cfg->threads < 32 || cfg->threads > 1024 || (cfg->threads & 31))
         return es.error(TVBG_EINVAL, "threads must be a multiple of 32 in [32, 1024]");
-    if (cfg->block_k != 4 && cfg->block_k != 8)
-        return es.error(TVBG_EINVAL, "tvbg_group_run: block_k must be 4 or 8");
+    if (cfg->block_k < 1 || cfg->block_k > 8 || !((k_mask >> cfg->block_k) & 1u))
+        return es.error(TVBG_EINVAL, "tvbg_group_run: block_k not built (4 or 8; 1, 2, 4 or 8 "
+                                     "for LEMS libraries)");
     const int c = cfg->cluster <= 0 ? 1 : cfg->cluster;
     if (c < 1 || c > 8) return es.error(TVBG_EINVAL, "cluster must be in [1, 8]");
     if (cfg->tpn > 1) return es.error(TVBG_EINVAL, "tvbg_group_run: tpn must be 0 or 1");

@@ -32,13 +32,17 @@ from .utils import next_pow2
 L = nat.GROUP_LANES
 
 
-def plan_group(dmin, dmax, block_k=None):
-    """(K, lognh) for delays in [dmin, dmax]: K = 8 or 4 steps per barrier
-    (K <= dmin + 1), nh the smallest power of two >= dmax + 1 + K."""
+def plan_group(dmin, dmax, block_k=None, ks=(8, 4)):
+    """(K, lognh) for delays in [dmin, dmax]: K steps per barrier, the
+    largest of `ks` with K <= dmin + 1 (the engine library builds K = 8, 4;
+    the generated LEMS libraries also 2, 1), nh the smallest power of two
+    >= dmax + 1 + K."""
     dmin, dmax = int(dmin), int(dmax)
-    k = int(block_k) if block_k else (8 if dmin + 1 >= 8 else (4 if dmin + 1 >= 4 else 0))
-    if k not in (4, 8) or k > dmin + 1:
-        raise ValueError('group kernel needs K in (4, 8) and K <= d_min + 1 (d_min = %d)' % dmin)
+    fits = [k for k in sorted(ks, reverse=True) if k <= dmin + 1]
+    k = int(block_k) if block_k else (fits[0] if fits else 0)
+    if k not in ks or k > dmin + 1:
+        raise ValueError('group kernel needs K in %s and K <= d_min + 1 (d_min = %d)'
+                         % (tuple(ks), dmin))
     nh = max(8, next_pow2(dmax + 1 + k))
     return k, int(np.log2(nh))
 
@@ -94,6 +98,8 @@ class GroupSet:
     the group's clock advances by the longest lane.
     """
 
+    block_ks = (8, 4)     # block lengths the library's group kernels are built for
+
     def __init__(self, model, cfun, scheme, conn, dt, couplings, speeds=None, state0=None,
                  nparam=None, delays=None, rounding='ceil', seed=0, inst_ids=None,
                  bold_period=0, bold_len=0, trace_every=0, trace_len=0, trace_nobs=None,
@@ -141,8 +147,8 @@ class GroupSet:
             uniq, tab_of = np.unique(sp, return_inverse=True)
             tables = [delays_f32(conn.lnz, s, dt, rounding) for s in uniq]
         self.delay_tables = tables
-        plans = [plan_group(d.min() if d.size else 7, d.max() if d.size else 0, block_k)
-                 for d in tables]
+        plans = [plan_group(d.min() if d.size else 7, d.max() if d.size else 0, block_k,
+                            self.block_ks) for d in tables]
         # per-node constants shared by every table: in-edge weight sums and
         # the visiting order (in-degree, descending)
         deg = np.diff(row)

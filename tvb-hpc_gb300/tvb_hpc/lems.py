@@ -643,8 +643,8 @@ def render_cuda(m, single=False):
     if gcf is not None:
         w('    if (cfun != %s) return nullptr;' % gcf)
         w('    switch (k) {')
-        w('        case 4: return group_kernel<LemsModel, %s, 4>;' % gcf)
-        w('        case 8: return group_kernel<LemsModel, %s, 8>;' % gcf)
+        for kk in (1, 2, 4, 8):
+            w('        case %d: return group_kernel<LemsModel, %s, %d>;' % (kk, gcf, kk))
         w('        default: return nullptr;')
         w('    }')
     else:
@@ -693,7 +693,7 @@ def render_cuda(m, single=False):
     w('TVBG_LEMS_EXPORT int tvbg_lems_group_run(const tvbg_group* d_groups, int32_t n_groups,')
     w('                                        const tvbg_launch* cfg, void* stream) {')
     w('    int cluster = 1;')
-    w('    int rc = check_group_cfg(cfg, kSink, &cluster);')
+    w('    int rc = check_group_cfg(cfg, kSink, &cluster, 0x116u);  // K = 1, 2, 4, 8')
     w('    if (rc) return rc;')
     w('    if (cfg->model != TVBG_MODEL_LEMS)')
     w('        return lems_error(TVBG_EINVAL, "tvbg_lems_group_run: model must be TVBG_MODEL_LEMS");')
@@ -978,11 +978,14 @@ class LemsGroupSet(GroupSet):
     work items sharing a delay table per group, time-blocked (K = 4 or 8 <=
     d_min + 1 steps per block).  Takes models whose coupling is separable
     (pre reads only x_j: its value is written into the ring) or a sine
-    difference post * sin(x_j - x_i) (sin and cos ring channels); others,
-    and delays shorter than 3 steps, need LemsSweep (ValueError here).
+    difference post * sin(x_j - x_i) (sin and cos ring channels); others
+    need LemsSweep (ValueError here).  Short delays take short blocks
+    (K = 2 for d_min = 1, K = 1 for zero delays).
     Noise needs one nsig for every work item.  Arguments as LemsSweep, plus
     GroupSet's block_k, threads, cluster, trace_*, bold_*.
     """
+
+    block_ks = (8, 4, 2, 1)   # the generated libraries build every block length
 
     def __init__(self, m, conn, dt, params, state0=None, noise=None, single=False, **kwargs):
         self.lems = LemsLibrary(m, single)

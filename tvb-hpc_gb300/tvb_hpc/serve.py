@@ -121,9 +121,36 @@ class Server:
         self.grad_stream = torch.cuda.Stream()
         self.pool = concurrent.futures.ThreadPoolExecutor(max_workers=1)
         self.pending = []
+        self.cancelled = []
 
     def submit(self, req):
         self.queue.append(req)
+
+    def poll(self, rid):
+        """State of request `rid`: 'queued', 'active' (its steps are running),
+        'gradient' (its FC-fit gradients are being computed), 'done',
+        'cancelled', or None if the server has never seen it."""
+        for name, reqs in (('queued', self.queue), ('active', self.active),
+                           ('gradient', [r for r, _ in self.pending]), ('done', self.done),
+                           ('cancelled', self.cancelled)):
+            if any(r.rid == rid for r in reqs):
+                return name
+        return None
+
+    def cancel(self, rid):
+        """Drop a queued or active request between ticks; an active one gives
+        its device memory back at once.  Returns True if it was dropped (a
+        request already in its gradient phase or done is not)."""
+        for lst in (self.queue, self.active):
+            for r in lst:
+                if r.rid == rid:
+                    lst.remove(r)
+                    if r.iset is not None:
+                        self.used -= r.nbytes
+                        r.iset = None
+                    self.cancelled.append(r)
+                    return True
+        return False
 
     def _admit(self, now, into=None):
         """Admit queued requests that have arrived and fit the budget; their
