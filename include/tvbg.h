@@ -81,6 +81,9 @@ extern "C" {
                                  ring slot is written) */
 #define TVBG_CFUN_LEMS_SC 65  /* a LEMS coupling post * sin(x_j - x_i) on the
                                  group kernel: sin and cos ring channels */
+#define TVBG_CFUN_LEMS_2 66   /* two separable LEMS couplings (two coupled
+                                 inputs) on the group kernel: one ring
+                                 channel each */
 
 /* ---- per-instance flags ------------------------------------------------- */
 #define TVBG_F_NOISE 1u      /* Euler-Maruyama with Philox normals          */

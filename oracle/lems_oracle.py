@@ -15,12 +15,13 @@ truncates) and C++/CUDA overload rules for the math functions (an
 every argument is float, else in double).
 
 Step (tmpl8_CUDA.py:145-243), per work item, node i, step t:
-    S_i  = sum over in-edges e of w_e * post * pre(x_j[dim](t - d_e), x_i[dim](t))
-    c_k  = S_i (0 for a coupling without dynamics), then c_k *= expr
+    S_i  = sum over in-edges e of w_e * post * pre(x_j[dim](t - d_e), x_i[dim](t)),
+           one sum per coupling component with dynamics (the front-end takes two)
+    c_k  = S_i of its component (0 for a coupling without dynamics), then c_k *= expr
     derived variables, conditional derived variables, in file order
     x_v  = float(x_v + dt * f_v)         all f_v from the state at t
     wrap ("PI": fmod to [0, 2 pi)) or clamp (lo, hi)
-    history[t + 1] = x[dim]
+    history[t + 1] = x
 d_e = (unsigned)(length_e * rec_speed_dt) in float32; no rec_speed_dt or
 "0" means zero delays; history before t0 is zero, slot t0 holds x[dim].
 Noise is not restated (its statistics are tested instead).
@@ -359,8 +360,6 @@ def run(path, name, row, col, w, lengths, params, dt, nsteps, state0=None):
         state0[:, 0] = F32(0.001)
     st0 = np.broadcast_to(np.asarray(state0, F32), (I, N, ns))
     dyn = [cp for cp in m['couplings'] if cp['pre'] is not None or cp['post'] is not None]
-    cp = dyn[0] if dyn else None
-    dim = cp['param'][1] if cp is not None else 0
     dst = np.repeat(np.arange(N), np.diff(row))
     out_state = np.zeros((I, N, ns), F32)
     out_expo = np.zeros((I, N, len(m['expos'])), F32)
@@ -370,31 +369,35 @@ def run(path, name, row, col, w, lengths, params, dt, nsteps, state0=None):
         d = delays(m, env0, lengths)
         dl.append(d)
         x = st0[b].copy()
-        hist = np.zeros((nsteps + 1, N), F32)
-        hist[0] = x[:, dim]
+        hist = np.zeros((nsteps + 1, N, ns), F32)     # every state variable, t = 0..T
+        hist[0] = x
+        nz = np.diff(row) > 0
         for t in range(nsteps):
             env = dict(env0)
             for v, n in enumerate(names):
                 env[n] = x[:, v]
-            if cp is not None:
-                src = t - d
-                xj = np.where(src >= 0, hist[np.maximum(src, 0), col], F32(0))
+            sums = []
+            src = t - d
+            for cp in dyn:                    # one sum per coupling with dynamics
+                dim = cp['param'][1]
+                xj = np.where(src >= 0, hist[np.maximum(src, 0), col, dim], F32(0))
                 ee = dict(env0)
                 ee[cp['param'][0]] = xj.astype(F32)
                 ee[names[dim]] = x[dst, dim]
                 pre = F32(1) if _none(cp['pre']) else ceval(cp['pre'], ee)
                 post = F32(1) if _none(cp['post']) else ceval(cp['post'], ee)
-                term = (w * np.asarray(post) * np.asarray(pre)).astype(F32)
+                term = np.broadcast_to(w * np.asarray(post) * np.asarray(pre), w.shape).astype(F32)
                 S = np.zeros(N, F32)
-                nz = np.diff(row) > 0
                 if term.size:
                     S[nz] = np.add.reduceat(term, row[:-1][nz]).astype(F32)
-            else:
-                S = np.zeros(N, F32)
+                sums.append(S)
+            k = 0
             for c in m['couplings']:
                 live = c['pre'] is not None or c['post'] is not None
+                S = sums[k] if live else np.zeros(N, F32)
+                k += 1 if live else 0
                 for n, e in c['derived']:
-                    v = S.copy() if live else np.zeros(N, F32)
+                    v = S.copy()
                     if not _none(e):
                         v = (v * ceval(e, env)).astype(F32)
                     env[n] = v
@@ -418,7 +421,7 @@ def run(path, name, row, col, w, lengths, params, dt, nsteps, state0=None):
                     xn[:, v] = np.where(xn[:, v] < lo, lo,
                                         np.where(xn[:, v] > hi, hi, xn[:, v]))
             x = xn
-            hist[t + 1] = x[:, dim]
+            hist[t + 1] = x
         out_state[b] = x
         env = constants_env(m)
         for v, n in enumerate(names):

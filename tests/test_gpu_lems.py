@@ -246,3 +246,51 @@ def test_lems_groups_noise_statistics(cuda, name):
     if m.ns > 1:
         c = np.corrcoef(x.T)
         assert np.abs(c - np.eye(m.ns)).max() < 5 / np.sqrt(n)
+
+
+def test_lems_hmje_two_inputs_matches_oracle(cuda, tmp_path):
+    """tvb_hpc's HMJE (two coupled inputs: c1 from x1, c2 from x2) from its
+    bundled LEMS file with the coupling constants on: one ring channel per
+    input on the group kernel, against the LEMS oracle (itself pinned on
+    tvb_hpc's model definition); x0, Iext, r swept per work item."""
+    from test_lems import hmje_text, hmje_state0
+    path = tmp_path / 'hmje_CUDA.xml'
+    path.write_text(hmje_text())
+    m = lems.parse(str(path), name='HMJE')
+    assert m.coupling_class == 'sep2'
+    conn = conn_of(60, seed=14)
+    x0 = hmje_state0(conn.nnode)
+    params = np.array([[3.0, 0.3, -1.6, 3.1, 0.00035], [6.0, 0.8, -2.2, 3.0, 0.001],
+                       [6.0, 0.1, -1.9, 3.2, 0.0005]], np.float32)
+    gs = lems.make_set(m, conn, 0.1, params, state0=x0, noise=False)
+    assert isinstance(gs, lems.LemsGroupSet) and gs.channels == 2
+    gs.run(400)
+    ref = lo.run(str(path), 'HMJE', conn.row, conn.col, conn.wnz, conn.lnz, params, 0.1, 400, x0)
+    assert rel_err(gs.state.cpu().numpy(), ref['state']) < TOL
+    assert rel_err(gs.exposures().cpu().numpy(), ref['expo']) < TOL
+    with pytest.raises(ValueError):          # two inputs: the group kernel only
+        lems.LemsSweep(m, conn, 0.1, params, state0=x0)
+
+
+@pytest.mark.parametrize('kind', ['groups', 'sweep'])
+def test_lems_noise_scale_per_variable(cuda, kind):
+    """noise="0" takes a state variable out of the noise: with zero initial
+    state the silent variables of uncoupled OU nodes stay exactly zero
+    (six variables: the wide path with its per-variable factors)."""
+    text = open(lems.lems_file('Ou6')).read()
+    for v in range(1, 6):
+        text = text.replace('<StateVariable name="u%d" default="0" boundaries=""/>' % v,
+                            '<StateVariable name="u%d" default="0" boundaries="" noise="0"/>' % v)
+    m = lems.parse(text, name='Ou6')
+    assert m.scales == [1, 0, 0, 0, 0, 0]
+    conn = conn_of(100, seed=15)
+    N = conn.nnode
+    params = np.array([[4.0, 0.0]] * 8, np.float32)
+    Set = lems.LemsGroupSet if kind == 'groups' else lems.LemsSweep
+    sw = Set(m, conn, 0.1, params, state0=np.zeros((N, 6), np.float32), seed=3)
+    sw.run(1000)
+    x = sw.state.cpu().numpy().reshape(-1, 6)
+    assert np.all(x[:, 1:] == 0)
+    nsig = np.sqrt(np.float32(0.1)) * np.float32(0.1)
+    var = nsig ** 2 / (1 - (1 - 0.5 * 0.1) ** 2)
+    assert abs(x[:, 0].var() / var - 1) < 5 * np.sqrt(2.0 / x.shape[0])

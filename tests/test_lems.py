@@ -20,7 +20,7 @@ import pyoracle as orc
 from tvb_hpc import lems, network, model
 
 REF_XML = '/root/reference/dsl/dsl_cuda/XMLmodels'
-BUNDLED = ['Kuramoto', 'Oscillator', 'Rwongwang', 'Epileptor', 'Ou', 'Ou6']
+BUNDLED = ['Kuramoto', 'Oscillator', 'Rwongwang', 'Epileptor', 'Ou', 'Ou6', 'HMJE']
 REFERENCE = ['Kuramoto', 'Oscillator', 'Rwongwang', 'Epileptor']
 
 
@@ -79,7 +79,9 @@ def test_coupling_classes():
     "Which couplings the group kernel takes: separable or a sine difference."
     got = {n: lems.load_model(n).coupling_class for n in BUNDLED}
     assert got == {'Kuramoto': 'sc', 'Oscillator': 'sc', 'Epileptor': 'sc', 'Rwongwang': 'sep',
-                   'Ou': 'sep', 'Ou6': 'sep'}
+                   'Ou': 'sep', 'Ou6': 'sep', 'HMJE': 'sep2'}
+    h = lems.load_model('HMJE')
+    assert (h.cvar, h.cvar2) == (0, 3) and h.scales == [0, 0, 0, 1, 1, 0]
     base = open(lems.lems_file('Ou')).read()
     m = lems.parse(base.replace('expression="x_j"', 'expression="tanh(x_j - x)"'))
     assert m.coupling_class == 'edge'
@@ -199,3 +201,74 @@ def test_oracle_rww_zero_delay_pinned_on_main_oracle():
                   m.node_params(N)[None], x0[None], consts=consts)
     err = np.abs(got['state'][0] - ref['state'][0]).max() / np.abs(ref['state'][0]).max()
     assert err < 1e-4
+
+
+HMJE_COUPLED = {'Kvf': '0.05f', 'Ks': '-0.1f', 'Kf': '0.02f'}
+
+
+def hmje_text(consts=HMJE_COUPLED):
+    "The bundled HMJE file with the coupling constants switched on."
+    t = open(lems.lems_file('HMJE')).read()
+    for k, v in consts.items():
+        t = t.replace('<Constant name="%s" default="0.0f"/>' % k,
+                      '<Constant name="%s" default="%s"/>' % (k, v))
+    return t
+
+
+def hmje_by_tvb_hpc(conn, x0, params, steps, dt=0.1, consts=HMJE_COUPLED):
+    """The HMJE step from tvb_hpc's own model definition (model.HMJE's drift
+    strings, model.py:185-206, evaluated with numpy in float32) with linear
+    coupling on its two inputs c1 <- x1, c2 <- x2 (coupling.py:68-84,103-112)."""
+    m = model.HMJE()
+    const = {k: np.float32(v) for k, v in m.const.items()}
+    const.update({k: np.float32(float(v.rstrip('f'))) for k, v in consts.items()})
+    G, x0p, Iext, r = (np.float32(v) for v in params[1:5])
+    const.update(x0=x0p, Iext=Iext, r=r)
+    d = network.delays_f32(conn.lnz, params[0], dt, 'dsl').astype(np.int64)
+    row, col, w = np.asarray(conn.row), np.asarray(conn.col), np.asarray(conn.wnz, np.float32)
+    N = row.size - 1
+    nz = np.diff(row) > 0
+    x = np.array(x0, np.float32)
+    hist = np.zeros((steps + 1, N, 6), np.float32)
+    hist[0] = x
+    names = [str(s) for s in m.state_sym]
+    for t in range(steps):
+        src = t - d
+        env = dict(const)
+        for k, (inp, var) in enumerate((('c1', 0), ('c2', 3))):
+            xj = np.where(src >= 0, hist[np.maximum(src, 0), col, var], np.float32(0))
+            S = np.zeros(N, np.float32)
+            S[nz] = np.add.reduceat((w * xj).astype(np.float32), row[:-1][nz])
+            env[inp] = (G * S).astype(np.float32)
+        for v, n in enumerate(names):
+            env[n] = x[:, v]
+        f = [np.asarray(eval(e, {}, env), np.float32) for e in m.drift]
+        x = np.stack([(x[:, v] + np.float32(dt) * f[v]).astype(np.float32) for v in range(6)], -1)
+        hist[t + 1] = x
+    return x
+
+
+def hmje_state0(N, seed=0):
+    rng = np.random.default_rng(seed)
+    x = np.zeros((N, 6), np.float32)
+    for v, (lo, hi) in enumerate([(-1.8, -1.2), (-15, -12), (2.8, 3.2), (-1.2, -0.8), (0, 0.2),
+                                  (-0.1, 0.1)]):
+        x[:, v] = rng.uniform(lo, hi, N)
+    return x
+
+
+def test_oracle_hmje_pinned_on_tvb_hpc_model(tmp_path):
+    """The bundled HMJE file, stepped by the LEMS oracle, against tvb_hpc's
+    own HMJE definition with its two coupled inputs."""
+    path = tmp_path / 'hmje_CUDA.xml'
+    path.write_text(hmje_text())
+    conn = _conn(N=30, seed=11)
+    x0 = hmje_state0(conn.nnode)
+    params = np.array([[3.0, 0.3, -1.6, 3.1, 0.00035], [6.0, 0.8, -2.2, 3.0, 0.001]], np.float32)
+    got = lo.run(str(path), 'HMJE', conn.row, conn.col, conn.wnz, conn.lnz, params, 0.1, 300, x0)
+    for b in range(params.shape[0]):
+        ref = hmje_by_tvb_hpc(conn, x0, params[b], 300)
+        err = np.abs(got['state'][b] - ref).max() / np.abs(ref).max()
+        assert err < 1e-5, err
+    np.testing.assert_allclose(got['expo'][..., 3], got['state'][..., 3] - got['state'][..., 0],
+                               rtol=1e-6, atol=1e-6)

@@ -300,6 +300,17 @@ struct WideNoise<M, decltype(void(M::kWideNoise))> {
     static constexpr bool value = M::kWideNoise && M::NS > 4 && M::NS <= 8;
 };
 
+// Per-variable factor on that amplitude: M::noise_scale(v) where the model
+// defines it (LEMS models, from their state variables), else 1.
+template <class M, class = void>
+struct NoiseScale {
+    __device__ static __forceinline__ float at(int) { return 1.0f; }
+};
+template <class M>
+struct NoiseScale<M, decltype(void(M::noise_scale(0)))> {
+    __device__ static __forceinline__ float at(int v) { return M::noise_scale(v); }
+};
+
 // ---------------------------------------------------------------------------
 // Coupling functions, tvb_hpc/coupling.py:103-121 and network.py:115-136:
 //   input_i = post( sum_e w_e * pre(obsrv_j(t - d_e), obsrv_i(t)) ),

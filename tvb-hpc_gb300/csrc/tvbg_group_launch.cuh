@@ -33,7 +33,8 @@ inline int check_group_cfg(const tvbg_launch* cfg, const ErrSink& es, int* clust
 
 // Ring channels of a coupling id (the group kernel's shared-memory sums scale with it).
 inline int group_channels(int cfun) {
-    return (cfun == TVBG_CFUN_KURAMOTO || cfun == TVBG_CFUN_LEMS_SC) ? 2 : 1;
+    return (cfun == TVBG_CFUN_KURAMOTO || cfun == TVBG_CFUN_LEMS_SC || cfun == TVBG_CFUN_LEMS_2) ? 2
+                                                                                                : 1;
 }
 
 // Launch n_groups groups of kfn: grid = n_groups * cluster CTAs, clusters of

@@ -216,10 +216,10 @@ __device__ __forceinline__ void lane_gather_sc(const tvbg_group& g, int lo, int 
 }
 
 // Ring channels per (node, slot): 2 (sin, cos) for the Kuramoto coupling and
-// the LEMS sine coupling, else 1.
+// the LEMS sine coupling, 2 for a LEMS model's two couplings, else 1.
 template <int CF>
 __host__ __device__ constexpr int ring_channels() {
-    return (CF == TVBG_CFUN_KURAMOTO || CF == TVBG_CFUN_LEMS_SC) ? 2 : 1;
+    return (CF == TVBG_CFUN_KURAMOTO || CF == TVBG_CFUN_LEMS_SC || CF == TVBG_CFUN_LEMS_2) ? 2 : 1;
 }
 
 // Value a one-channel ring slot holds for observable o: o itself, or for a
@@ -294,7 +294,12 @@ __device__ __forceinline__ void run_group(const tvbg_group& g, float* csum, int3
             for (int v = 0; v < NP; ++v) p[v] = __ldg(g.nparam + (n * NP + v) * kLanes + l);
             if constexpr (NC == 2) {
                 float sn, cs;
-                sincosf(o, &sn, &cs);
+                if constexpr (CF == TVBG_CFUN_LEMS_2) {
+                    sn = M::ring_value(o, p);
+                    cs = M::ring_value2(x[M::CVAR2], p);
+                } else {
+                    sincosf(o, &sn, &cs);
+                }
                 ring[idx] = sn;
                 ring[idx + kLanes] = cs;
                 if (pos < kGhost) {
@@ -361,7 +366,7 @@ __device__ __forceinline__ void run_group(const tvbg_group& g, float* csum, int3
             }
             float obs0 = M::obs(x, 0);
             float sn0 = 0.0f, cs0 = 0.0f;  // sin, cos of obs0 (Kuramoto coupling)
-            if constexpr (NC == 2) sincosf(obs0, &sn0, &cs0);
+            if constexpr (NC == 2 && CF != TVBG_CFUN_LEMS_2) sincosf(obs0, &sn0, &cs0);
             float zz[4] = {0.0f, 0.0f, 0.0f, 0.0f};
             int b_next = b_until, tr_next = tr_until;
             int brow = b_row, trow = tr_row;
@@ -376,8 +381,11 @@ __device__ __forceinline__ void run_group(const tvbg_group& g, float* csum, int3
                     trow = trow + 1 == g.trace_len ? 0 : trow + 1;
                 }
                 const float xbold = bold ? M::obs(x, g.bold_obs) : 0.0f;
-                float c;
-                if constexpr (NC == 2) {
+                float c, c2 = 0.0f;
+                if constexpr (CF == TVBG_CFUN_LEMS_2) {
+                    c = M::coupling(csum[k * blockDim.x + threadIdx.x], x, p);
+                    c2 = M::coupling2(csum[(K + k) * blockDim.x + threadIdx.x], x, p);
+                } else if constexpr (NC == 2) {
                     // sum_e w sin(x_j - x_i); Kuramoto: post = a * mean (coupling.py:119-121)
                     const float S = cs0 * csum[k * blockDim.x + threadIdx.x] -
                                     sn0 * csum[(K + k) * blockDim.x + threadIdx.x];
@@ -392,7 +400,11 @@ __device__ __forceinline__ void run_group(const tvbg_group& g, float* csum, int3
                     c = lane_post<CF>(csum[k * blockDim.x + threadIdx.x], obs0, wsum, cf_a, g.cf_b);
                 }
                 float f[NS];
-                M::drift(x, c, p, g.consts, f);
+                if constexpr (CF == TVBG_CFUN_LEMS_2) {
+                    M::drift2(x, c, c2, p, g.consts, f);
+                } else {
+                    M::drift(x, c, p, g.consts, f);
+                }
 #pragma unroll
                 for (int v = 0; v < NS; ++v) x[v] = fmaf(dt, f[v], x[v]);
                 if constexpr (Noise<M>::kOK) {
@@ -421,7 +433,8 @@ __device__ __forceinline__ void run_group(const tvbg_group& g, float* csum, int3
                             box_muller_fast(w.v[2], w.v[3], z8[4 * b + 2], z8[4 * b + 3]);
                         }
 #pragma unroll
-                        for (int v = 0; v < NS; ++v) x[v] = fmaf(sqrt_dt * z8[v], g.sigma[0], x[v]);
+                        for (int v = 0; v < NS; ++v)
+                            x[v] = fmaf(sqrt_dt * z8[v], g.sigma[0] * NoiseScale<M>::at(v), x[v]);
                     }
                 }
                 M::limit(x, flags);
@@ -429,7 +442,12 @@ __device__ __forceinline__ void run_group(const tvbg_group& g, float* csum, int3
                 const uint32_t pos = (static_cast<uint32_t>(t) + 1u) & mask;
                 const size_t idx = (static_cast<size_t>(n) * R + pos) * RL + l;
                 if constexpr (NC == 2) {
-                    sincosf(obs0, &sn0, &cs0);
+                    if constexpr (CF == TVBG_CFUN_LEMS_2) {
+                        sn0 = M::ring_value(obs0, p);
+                        cs0 = M::ring_value2(x[M::CVAR2], p);
+                    } else {
+                        sincosf(obs0, &sn0, &cs0);
+                    }
                     ring[idx] = sn0;
                     ring[idx + kLanes] = cs0;
                     if (pos < kGhost) {

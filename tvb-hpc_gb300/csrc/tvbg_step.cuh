@@ -315,7 +315,7 @@ __device__ __forceinline__ void run_steps(const tvbg_instance& d, const Ring<SME
                                         d.inst_id, z8 + 4, 1u);
 #pragma unroll
                         for (int v = 0; v < M::NS; ++v)
-                            x[v] = fmaf(sqrt_dt * z8[v], d.sigma[0], x[v]);
+                            x[v] = fmaf(sqrt_dt * z8[v], d.sigma[0] * NoiseScale<M>::at(v), x[v]);
                     }
                 }
                 M::limit(x, flags);

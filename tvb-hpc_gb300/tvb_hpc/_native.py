@@ -33,7 +33,7 @@ MODEL_KURAMOTO, MODEL_G2DO, MODEL_MPR, MODEL_LINEAR, MODEL_G2DOSC = 0, 1, 2, 3, 
 MODEL_RWW, MODEL_JANSENRIT = 5, 6
 MODEL_LEMS = 64
 CFUN_LINEAR, CFUN_DIFF, CFUN_KURAMOTO, CFUN_SIGMOIDAL = 0, 1, 2, 3
-CFUN_LEMS, CFUN_LEMS_SC = 64, 65
+CFUN_LEMS, CFUN_LEMS_SC, CFUN_LEMS_2 = 64, 65, 66
 
 F_NOISE = 1
 F_BOLD = 2

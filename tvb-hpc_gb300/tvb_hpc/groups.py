@@ -114,13 +114,15 @@ class GroupSet:
         self.cfun_id, cf_a0, cf_b0, self.cf_p = cfun.engine_spec()
         separable = self.cfun_id in (nat.CFUN_LINEAR, nat.CFUN_DIFF, nat.CFUN_SIGMOIDAL)
         kuramoto = (self.model_id, self.cfun_id) == (nat.MODEL_KURAMOTO, nat.CFUN_KURAMOTO)
-        lems = self.model_id == nat.MODEL_LEMS and self.cfun_id in (nat.CFUN_LEMS, nat.CFUN_LEMS_SC)
+        lems = self.model_id == nat.MODEL_LEMS and self.cfun_id in (nat.CFUN_LEMS, nat.CFUN_LEMS_SC,
+                                                                    nat.CFUN_LEMS_2)
         if not (separable or kuramoto or lems):
             raise ValueError('group kernel: a separable coupling (Linear, Diff, Sigmoidal), or the '
                              'Kuramoto model with the Kuramoto coupling')
         # the Kuramoto coupling (and a LEMS sine coupling) keeps sin and cos of
         # the observable in the ring
-        self.channels = 2 if self.cfun_id in (nat.CFUN_KURAMOTO, nat.CFUN_LEMS_SC) else 1
+        self.channels = 2 if self.cfun_id in (nat.CFUN_KURAMOTO, nat.CFUN_LEMS_SC,
+                                              nat.CFUN_LEMS_2) else 1
         self.N = N = int(conn.nnode)
         if N > 65535:
             raise ValueError('group kernel: N < 65536')

@@ -174,6 +174,7 @@ class LemsModel:
     couplings: list            # Coupling
     noise: bool
     source: str = ''
+    noise_scales: list = None  # per state variable factor on nsig (default 1)
 
     # -- shape ------------------------------------------------------------------
     @property
@@ -185,8 +186,13 @@ class LemsModel:
         return [s for s, _ in self.states]
 
     @property
+    def dyn_couplings(self):
+        "Coupling components with dynamics (pre/post), at most two."
+        return [c for c in self.couplings if c.dynamic]
+
+    @property
     def dyn_coupling(self):
-        dyn = [c for c in self.couplings if c.dynamic]
+        dyn = self.dyn_couplings
         return dyn[0] if dyn else None
 
     @property
@@ -194,6 +200,23 @@ class LemsModel:
         "Index of the coupled state variable (the ring's observable)."
         c = self.dyn_coupling
         return int(c.param[1]) if c is not None and c.param is not None else 0
+
+    @property
+    def cvar2(self):
+        "State variable the second coupling reads (= cvar with one coupling)."
+        dyn = self.dyn_couplings
+        return int(dyn[1].param[1]) if len(dyn) > 1 and dyn[1].param is not None else self.cvar
+
+    @property
+    def scales(self):
+        return list(self.noise_scales) if self.noise_scales else [1.0] * self.ns
+
+    def _separable(self, c):
+        "pre reads only x_j (and constants/parameters), post not x_j."
+        pj, own = c.param[0], self.state_names[c.param[1]]
+        if c.post is not None and pj in names_in(c.post):
+            return False
+        return c.pre is None or own not in names_in(c.pre)
 
     @property
     def k_names(self):
@@ -214,15 +237,19 @@ class LemsModel:
     def coupling_class(self):
         """How the group kernel can take the coupling: 'sep' (pre reads only
         x_j: applied when the ring slot is written), 'sc' (pre is
-        sin(x_j - x_i): sin and cos ring channels), or 'edge' (per edge only:
-        the per-step kernel)."""
+        sin(x_j - x_i): sin and cos ring channels), 'sep2' (two separable
+        couplings, one ring channel each), or 'edge' (per edge only: the
+        per-step kernel)."""
+        dyn = self.dyn_couplings
+        if len(dyn) == 2:
+            return 'sep2' if all(self._separable(c) for c in dyn) else 'edge2'
         c = self.dyn_coupling
         if c is None:
             return 'sep'
         pj, own = c.param[0], self.state_names[c.param[1]]
         if c.post is not None and pj in names_in(c.post):
             return 'edge'
-        if c.pre is None or own not in names_in(c.pre):
+        if self._separable(c):
             return 'sep'
         tk = tokens(c.pre)
         if (len(tk) == 6 and tk[0][0] == 'id' and tk[0][1] in ('sin', 'sinf') and tk[1] == ('op', '(')
@@ -245,9 +272,11 @@ class LemsModel:
                 len(self.time_derivs), self.ns))
         if len(self.k_names) > MAX_K:
             raise NotImplementedError('more than %d swept + derived parameters' % MAX_K)
-        dyn = [c for c in self.couplings if c.dynamic]
-        if len(dyn) > 1:
-            raise NotImplementedError('more than one coupling component with dynamics')
+        dyn = self.dyn_couplings
+        if len(dyn) > 2:
+            raise NotImplementedError('more than two coupling components with dynamics')
+        if self.noise_scales is not None and len(self.noise_scales) != self.ns:
+            raise ValueError('one noise factor per state variable')
         if not self.exposures:
             raise ValueError('no Exposure: the model needs an observable')
         if self.noise and self.derived('nsig') is None:
@@ -290,8 +319,7 @@ class LemsModel:
             need(e, base | seen, 'derived parameter %s' % n)
             seen.add(n)
         kvals = consts | params | derived
-        c = self.dyn_coupling
-        if c is not None:
+        for c in dyn:
             if c.param is None:
                 raise ValueError('coupling %s has dynamics but no <Parameter> for x_j' % c.name)
             if not 0 <= c.param[1] < self.ns:
@@ -305,6 +333,8 @@ class LemsModel:
                                 'coupling reads state %r of the receiving node; only the coupled '
                                 'variable %r is available' % (n, own))
                     need(e, kvals | {c.param[0], own}, 'coupling %s' % c.name)
+        if len(dyn) == 2 and self.coupling_class != 'sep2':
+            raise NotImplementedError('two couplings: both must be separable (pre reads only x_j)')
         avail = kvals | states | cnames
         for cc_ in self.couplings:
             for n, e in cc_.derived:
@@ -381,6 +411,9 @@ def parse(path_or_text, name=None):
     derived = _unique([(d.get('name'), d.get('expression'))
                        for d in model_ct.findall('DerivedParameter')])
     states = [(s.get('name'), _attr(s, 'boundaries', '').strip()) for s in dyn.findall('StateVariable')]
+    # extension: <StateVariable noise="0"/> takes a variable out of the noise
+    # (the DSL's noise acts on every state variable)
+    scales = [float(_attr(s, 'noise', '1')) for s in dyn.findall('StateVariable')]
     dvars = [(d.get('name'), d.get('expression')) for d in dyn.findall('DerivedVariable')]
     cvars = []
     for c in dyn.findall('ConditionalDerivedVariable'):
@@ -420,7 +453,7 @@ def parse(path_or_text, name=None):
         cp.derived = [(x.get('name'), x.get('expression')) for x in el.findall('DerivedParameter')]
         couplings.append(cp)
     m = LemsModel(mname, constants, params, derived, states, dvars, cvars, tders, expos, couplings,
-                  noise, source=src)
+                  noise, source=src, noise_scales=None if all(v == 1.0 for v in scales) else scales)
     return m.validate()
 
 
@@ -498,15 +531,32 @@ def render_cuda(m, single=False):
     w('    static constexpr int NP = %d;  // per-work-item slots, read per node' % max(1, len(kn)))
     w('    static constexpr int NOBS = 1 + kNExpo;')
     w('    static constexpr bool kWideNoise = true;')
+    w('    static constexpr int CVAR2 = %d;  // state variable of the second coupling' % m.cvar2)
+    w('    static constexpr bool kTwoInputs = %s;' % ('true' if len(m.dyn_couplings) == 2 else 'false'))
+    w('    __device__ static __forceinline__ float noise_scale(int v_) {')
+    w('        switch (v_) {')
+    for v, f in enumerate(m.scales):
+        w('            case %d: return %sf;' % (v, repr(float(f))))
+    w('            default: return 1.0f;')
+    w('        }')
+    w('    }')
     w('    __device__ static __forceinline__ void drift(const float* x_, float S_, const float* p_,')
-    w('                                                 const float*, float* f_) {')
+    w('                                                 const float* K_, float* f_) {')
+    w('        drift2(x_, S_, 0.0f, p_, K_, f_);')
+    w('    }')
+    w('    // S_, S2_: the raw sums of the first and second coupling with dynamics')
+    w('    __device__ static __forceinline__ void drift2(const float* x_, float S_, float S2_,')
+    w('                                                  const float* p_, const float*, float* f_) {')
     consts('        ', coupling=True)
     kvals('p_', '        ')
     for v, n in enumerate(m.state_names):
         w('        const float %s = x_[%d];' % (n, v))
+    dyn_ids = [id(c) for c in m.dyn_couplings]
     for c in m.couplings:
+        src = ('S_' if dyn_ids and id(c) == dyn_ids[0] else
+               'S2_' if len(dyn_ids) > 1 and id(c) == dyn_ids[1] else '0.0f')
         for n, e in c.derived:
-            w('        float %s = %s;' % (n, 'S_' if c.dynamic else '0.0f'))
+            w('        float %s = %s;' % (n, src))
             if not _none(e):
                 w('        %s *= %s;' % (n, E(e)))
     for n, e in m.derived_vars:
@@ -533,24 +583,36 @@ def render_cuda(m, single=False):
     # group-kernel hooks: the ring value of a separable coupling, and the
     # coupling input from the gathered sum
     cls = m.coupling_class
-    w('    __host__ __device__ static __forceinline__ float ring_value(float o_, const float* p_) {')
-    if cp is not None and cls == 'sep':
-        consts('        ', coupling=True)
-        kvals('p_', '        ')
-        w('        const float %s = o_;' % cp.param[0])
-        w('        return %s;' % ('1.0f' if _none(cp.pre) else '(%s)' % E(cp.pre)))
-    else:
-        w('        return o_;')
-    w('    }')
-    w('    __device__ static __forceinline__ float coupling(float S_, const float* x_, const float* p_) {')
-    if cp is not None and cls in ('sep', 'sc'):
-        consts('        ', coupling=True)
-        kvals('p_', '        ')
-        w('        const float %s = x_[%d];' % (m.state_names[m.cvar], m.cvar))
-        w('        return %s * S_;' % ('1.0f' if _none(cp.post) else '(%s)' % E(cp.post)))
-    else:
-        w('        return 0.0f;')
-    w('    }')
+    dyn = m.dyn_couplings
+
+    def ring_value_fn(fname, c):
+        w('    __host__ __device__ static __forceinline__ float %s(float o_, const float* p_) {' % fname)
+        if c is not None and cls in ('sep', 'sep2'):
+            consts('        ', coupling=True)
+            kvals('p_', '        ')
+            w('        const float %s = o_;' % c.param[0])
+            w('        return %s;' % ('1.0f' if _none(c.pre) else '(%s)' % E(c.pre)))
+        else:
+            w('        return o_;')
+        w('    }')
+
+    def coupling_fn(fname, c):
+        w('    __device__ static __forceinline__ float %s(float S_, const float* x_, const float* p_) {'
+          % fname)
+        if c is not None and cls in ('sep', 'sc', 'sep2'):
+            consts('        ', coupling=True)
+            kvals('p_', '        ')
+            d = int(c.param[1])
+            w('        const float %s = x_[%d];' % (m.state_names[d], d))
+            w('        return %s * S_;' % ('1.0f' if _none(c.post) else '(%s)' % E(c.post)))
+        else:
+            w('        return 0.0f;')
+        w('    }')
+
+    ring_value_fn('ring_value', dyn[0] if dyn else None)
+    ring_value_fn('ring_value2', dyn[1] if len(dyn) > 1 else None)
+    coupling_fn('coupling', dyn[0] if dyn else None)
+    coupling_fn('coupling2', dyn[1] if len(dyn) > 1 else None)
     w('    __device__ static __forceinline__ void limit(float* x_, uint32_t) {')
     for v, (n, b) in enumerate(m.states):
         if b == 'PI':
@@ -615,6 +677,9 @@ def render_cuda(m, single=False):
     w('    if (rc) return rc;')
     w('    if (cfg->model != TVBG_MODEL_LEMS || cfg->cfun != TVBG_CFUN_LEMS || cfg->block_k > 1)')
     w('        return lems_error(TVBG_EINVAL, "LEMS library: model/cfun must be TVBG_*_LEMS, block_k 0 or 1");')
+    w('    if (LemsModel::kTwoInputs)')
+    w('        return lems_error(TVBG_EUNSUPPORTED, "LEMS library: two coupled inputs run on the group '
+      'kernel only (tvbg_lems_group_run)");')
     w('    if (n_inst == 0) return TVBG_OK;')
     w('    Kernel k = lookup(cfg->tpn);')
     w('    const size_t smem = step_smem_bytes(cfg->threads, cfg->smem_ring);')
@@ -638,7 +703,7 @@ def render_cuda(m, single=False):
     w('#pragma unroll')
     w('    for (int k = 0; k < kNExpo; ++k) o_[i * kNExpo + k] = LemsModel::obs(x_, 1 + k);')
     w('}')
-    gcf = {'sep': 'TVBG_CFUN_LEMS', 'sc': 'TVBG_CFUN_LEMS_SC'}.get(cls)
+    gcf = {'sep': 'TVBG_CFUN_LEMS', 'sc': 'TVBG_CFUN_LEMS_SC', 'sep2': 'TVBG_CFUN_LEMS_2'}.get(cls)
     w('GroupKernelFn lookup_group(int cfun, int k) {')
     if gcf is not None:
         w('    if (cfun != %s) return nullptr;' % gcf)
@@ -658,7 +723,7 @@ def render_cuda(m, single=False):
     w('    if (!info) return lems_error(TVBG_EINVAL, "tvbg_lems_info: null");')
     vals = [m.ns, len(m.params), len(m.derived_params), len(m.exposures), m.cvar, int(m.noise),
             m.k_index('rec_speed_dt') if m.has_delays else -1, m.k_index('nsig'), LEMS_ABI,
-            {'sep': 1, 'sc': 2}.get(cls, 0)]
+            {'sep': 1, 'sc': 2, 'sep2': 3}.get(cls, 0)]
     for k, v in enumerate(vals):
         w('    info[%d] = %d;  // %s' % (k, v, INFO_FIELDS[k]))
     w('    return TVBG_OK;')
@@ -704,10 +769,13 @@ def render_cuda(m, single=False):
     w('    const size_t smem = group_smem_bytes(cfg->block_k, cfg->threads, group_channels(cfg->cfun));')
     w('    return launch_group_kernel(k, d_groups, n_groups, cfg, cluster, smem, stream, kSink);')
     w('}')
-    w('TVBG_LEMS_EXPORT int tvbg_lems_ring_value(const float* slots, int32_t n, float o, float* out) {')
-    w('    if (n < 0 || (n > 0 && (!slots || !out)))')
+    w('TVBG_LEMS_EXPORT int tvbg_lems_ring_value(const float* slots, int32_t n, float o, int32_t which,')
+    w('                                         float* out) {')
+    w('    if (n < 0 || (n > 0 && (!slots || !out)) || which < 0 || which > 1)')
     w('        return lems_error(TVBG_EINVAL, "tvbg_lems_ring_value: bad arguments");')
-    w('    for (int32_t b = 0; b < n; ++b) out[b] = LemsModel::ring_value(o, slots + %d * b);' % MAX_K)
+    w('    for (int32_t b = 0; b < n; ++b)')
+    w('        out[b] = which ? LemsModel::ring_value2(o, slots + %d * b) : LemsModel::ring_value(o, slots + %d * b);'
+      % (MAX_K, MAX_K))
     w('    return TVBG_OK;')
     w('}')
     w('TVBG_LEMS_EXPORT int tvbg_lems_expose(const float* d_state, int64_t n, float* d_out, void* stream) {')
@@ -801,7 +869,7 @@ SIGNATURES = {
     'tvbg_lems_batch_run': (ctypes.c_int, [_vp, _i32, ctypes.POINTER(nat.tvbg_launch), _vp]),
     'tvbg_lems_expose': (ctypes.c_int, [_vp, _i64, _vp, _vp]),
     'tvbg_lems_group_run': (ctypes.c_int, [_vp, _i32, ctypes.POINTER(nat.tvbg_launch), _vp]),
-    'tvbg_lems_ring_value': (ctypes.c_int, [_vp, _i32, ctypes.c_float, _vp]),
+    'tvbg_lems_ring_value': (ctypes.c_int, [_vp, _i32, ctypes.c_float, _i32, _vp]),
 }
 
 _LIBS = {}
@@ -904,12 +972,19 @@ def _slots_per_node(m, K, N):
 
 
 def _sigma(lib, K, dt, noise):
-    "Per work item nsig / sqrt(dt) (4 copies), or zeros without noise."
+    """Per work item nsig / sqrt(dt) times each variable's noise factor (up
+    to 4 state variables; with more, the kernels take sigma[0] times the
+    factor), or zeros without noise."""
     if not noise:
         return np.zeros((K.shape[0], 4), np.float32)
     sq = np.sqrt(np.float32(dt)).astype(np.float32)
     sig = (K[:, lib.info['nsig']] / sq).astype(np.float32)
-    return np.repeat(sig[:, None], 4, axis=1)
+    out = np.repeat(sig[:, None], 4, axis=1)
+    sc = lib.model.scales
+    if len(sc) <= 4:
+        for v in range(len(sc)):
+            out[:, v] = (out[:, v] * np.float32(sc[v])).astype(np.float32)
+    return out
 
 
 def dsl_delays(lengths, rec_speed_dt):
@@ -937,6 +1012,8 @@ class LemsSweep(Sweep):
 
     def __init__(self, m, conn, dt, params, state0=None, noise=None, single=False, tpn=None,
                  **kwargs):
+        if len(m.dyn_couplings) > 1:
+            raise ValueError('LEMS model %s: two coupled inputs run on LemsGroupSet only' % m.name)
         self.lems = LemsLibrary(m, single)
         self.lmodel = m
         noise = m.noise if noise is None else bool(noise)
@@ -1001,16 +1078,20 @@ class LemsGroupSet(GroupSet):
         sig = _sigma(self.lems, K, dt, noise)
         if noise and not np.all(sig == sig[0]):
             raise ValueError('LEMS groups need one nsig for every work item')
-        # history before t0: the ring holds pre(0) of each work item
-        self._f0 = None
-        if cls == 1:
-            f0 = np.zeros(I, np.float32)
+        # history before t0: the ring holds pre(0) of each work item (per
+        # coupling); the sine coupling's channels hold (sin 0, cos 0)
+        self._cls = cls
+        self._f = None
+        if cls in (1, 3):
             Kc = np.ascontiguousarray(K)
-            self.lems.check(self.lems.lib.tvbg_lems_ring_value(Kc.ctypes.data, I, 0.0,
-                                                               f0.ctypes.data))
-            self._f0 = f0
+            self._f = []
+            for which in range(1 if cls == 1 else 2):
+                f = np.zeros(I, np.float32)
+                self.lems.check(self.lems.lib.tvbg_lems_ring_value(Kc.ctypes.data, I, 0.0, which,
+                                                                   f.ctypes.data))
+                self._f.append(f)
         em = _EngineModel(m, noise)
-        ec = _EngineCoupling(nat.CFUN_LEMS if cls == 1 else nat.CFUN_LEMS_SC)
+        ec = _EngineCoupling({1: nat.CFUN_LEMS, 2: nat.CFUN_LEMS_SC, 3: nat.CFUN_LEMS_2}[cls])
         scm = sch.EulerMaryuyamaStep(dt) if noise else sch.EulerStep(dt)
         super().__init__(em, ec, scm, conn, dt, np.zeros(I, np.float32),
                          state0=_state0(m, N, state0), nparam=_slots_per_node(m, K, N),
@@ -1022,17 +1103,18 @@ class LemsGroupSet(GroupSet):
 
     def clear_history(self):
         super().clear_history()
-        f0 = getattr(self, '_f0', None)
-        if f0 is None or not np.any(f0 != 0):
+        fs = getattr(self, '_f', None)
+        if fs is None or (self._cls == 1 and not np.any(fs[0] != 0)):
             return
         torch = self.torch
-        N = self.N
+        N, C = self.N, self.channels
         for g, mem in enumerate(self.members):
             R = int(self.R[g])
             o = int(self.ring_off[g])
-            v = np.zeros(L_GROUP, np.float32)
-            v[:mem.size] = f0[mem]
-            self.ring[o:o + N * R * L_GROUP].view(N, R, L_GROUP)[:] = torch.from_numpy(v).cuda()
+            v = np.zeros((C, L_GROUP), np.float32)
+            for c, f in enumerate(fs):
+                v[c, :mem.size] = f[mem]
+            self.ring[o:o + N * R * C * L_GROUP].view(N, R, C, L_GROUP)[:] = torch.from_numpy(v).cuda()
 
     def _run_groups(self, dev_ptr, n, cfg, stream):
         self.lems.check(self.lems.lib.tvbg_lems_group_run(dev_ptr, n, ctypes.byref(cfg), stream))
