@@ -37,7 +37,7 @@ computed).  The workload sizes are those of the benchmark configurations
          noise on).
   serve  the serving loop: Poisson arrivals of sweep requests, p50/p99
          latency, served vs plain.
-  grid_1k, mixed_small, grid_small: profiling cases.
+  grid_1k, mixed_small, grid_small, net_small: profiling cases.
 
 Metric: node-steps/s (one node x one instance x one time step).  `value`
 is device-resident throughput (CUDA events on the launching stream, max
@@ -177,6 +177,13 @@ def net515k_workload(N=515056, degree=64, nsteps=1000, seed=0):
                 seed=seed)
 
 
+def net_small_workload():
+    "Profiling case of net515k: 100 000 nodes, same degree and delays, 200 steps."
+    wl = net515k_workload(N=100000, nsteps=200)
+    wl['name'] = 'net_small'
+    return wl
+
+
 def lems_workload(n_s=32, n_c=32, N=68, nsteps=4000, seed=0):
     """The CUDA DSL's default sweep (dsl/dsl_cuda/example/cuda_setup.py:55-58,
     97-101: a 32 x 32 grid of speed x coupling, one work item per point) on a
@@ -228,7 +235,8 @@ def adjoint_workload(N=84, I=256, T=2000, C=100, seed=0):
 WORKLOADS = {'grid': grid_workload, 'grid_small': grid_small_workload, 'grid_1k': grid_1k_workload,
              'kuramoto': kuramoto_workload, 'mixed': mixed_workload,
              'mixed_small': mixed_small_workload, 'net515k': net515k_workload,
-             'lems_epileptor': lems_workload, 'adjoint': adjoint_workload}
+             'lems_epileptor': lems_workload, 'adjoint': adjoint_workload,
+             'net_small': net_small_workload}
 
 
 def workload_config(wl):
@@ -821,7 +829,7 @@ def gpu_arm(args):
     wl = WORKLOADS[args.workload]()
     if wl['name'].startswith('mixed'):
         gs = MixedStep(wl, torch, args.path, not args.no_graph)
-    elif wl['name'] == 'net515k':
+    elif wl['name'].startswith('net'):
         gs = NetStep(wl, torch)
     elif wl['name'].startswith('lems'):
         gs = LemsStep(wl, torch, args.tpn, 'groups' if args.path == 'groups' else 'sweep')

@@ -42,10 +42,19 @@ verbatim; `single=True` turns unsuffixed floating literals into float
 literals (the whole step in FP32, as the GPU wants) instead of the C rule
 that makes them double.
 
-Restrictions (checked, ValueError / NotImplementedError): at most one
-coupling component with dynamics; its pre/post read only the coupled
-variable, constants and parameters; at most 8 state variables; swept plus
-derived parameters at most 16; exposures read state and constants.
+Restrictions (checked, ValueError / NotImplementedError): at most two
+coupling components with dynamics (two only when both are separable: a
+model with two coupled inputs, on the group kernel); pre/post read only
+the coupled variable, constants and parameters; at most 8 state variables;
+swept plus derived parameters at most 16; exposures read state and
+constants.
+
+Execution: LemsSweep runs the per-step kernel (one CTA per work item, any
+coupling); LemsGroupSet the lane-interleaved group kernel (eight work items
+per group) for separable couplings (pre(x_j) written into the ring), sine
+differences (sin/cos ring channels) and two separable couplings;
+make_set picks the group kernel where it applies.  A state variable's
+noise="0" attribute (an extension) takes it out of the noise.
 """
 
 import ctypes

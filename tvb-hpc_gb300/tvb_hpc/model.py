@@ -154,7 +154,18 @@ class Kuramoto(BaseModel):
 
 
 class HMJE(BaseModel):
-    "Hindmarsh-Rose-Jirsa Epileptor model of seizure dynamics (model.py:185-206)."
+    """Hindmarsh-Rose-Jirsa Epileptor model of seizure dynamics (model.py:185-206).
+
+    Its two coupled inputs (c1 from x1, c2 from x2) run on the engine
+    through the bundled LEMS file of this model (`HMJE.lems()`, i.e.
+    tvb_hpc.lems.load_model('HMJE'): one ring channel per input on the
+    group kernel); engine_spec() has no hand-written kernel for it."""
+
+    @staticmethod
+    def lems():
+        "The bundled LEMS model of HMJE (two coupled inputs, x0/Iext/r per work item)."
+        from . import lems
+        return lems.load_model('HMJE')
     state = 'x1 y1 z x2 y2 g'
     limit = (-2, 1), (20, 2), (2, 5), (-2, 0), (0, 2), (-1, 1)
     input = 'c1 c2'
