@@ -511,6 +511,76 @@ int tvbg_group_run(const tvbg_group *d_groups, int32_t n_groups,
 int tvbg_group_occupancy(const tvbg_launch *cfg, int32_t *ctas_per_sm,
                          int32_t *sms);
 
+/*
+ * ---- serving pool ---------------------------------------------------------
+ * Continuous batching of sweep requests in native code: requests are copied
+ * in (tvbg_serve_admit), admitted to the device when their footprint fits
+ * the pool's HBM budget, advanced together one chunk of steps per
+ * tvbg_serve_tick (each request's lane-interleaved groups on its own
+ * stream, joined into the pool's), retired when done (final state copied
+ * out, device memory freed), and polled or cancelled by id.  The pool is
+ * the one object that allocates device memory behind its calls: it is
+ * created and destroyed explicitly.  The reference has no serving layer;
+ * its DSL launcher runs one sweep per call
+ * (dsl/dsl_cuda/example/cuda_run.py:124-142).  A request's result is the
+ * group kernel's for the same inputs, alone or in any mix (chunk
+ * boundaries are exact; every request keeps its Philox key: seed, and the
+ * request-local instance index).
+ */
+typedef struct tvbg_serve tvbg_serve;
+
+typedef struct tvbg_serve_request {
+    int32_t model;            /* TVBG_MODEL_* with a group kernel            */
+    int32_t cfun;             /* TVBG_CFUN_* (separable, or Kuramoto pair)   */
+    int32_t N;                /* nodes                                       */
+    int32_t nnz;              /* edges                                       */
+    const int32_t *row;       /* host [N+1] CSR offsets (in-edges)           */
+    const int32_t *col;       /* host [nnz]                                  */
+    const float *weights;     /* host [nnz]                                  */
+    const float *lengths;     /* host [nnz] tract lengths (mm)               */
+    int32_t n_inst;           /* instances (parameter points)                */
+    int32_t npar;             /* per-node parameters of the model            */
+    const float *couplings;   /* host [n_inst] coupling a                    */
+    const float *speeds;      /* host [n_inst] conduction speed (mm/ms)      */
+    const float *state0;      /* host [n_inst][N][nsvar]                     */
+    const float *nparam;      /* host [n_inst][N][npar]                      */
+    int64_t nsteps;           /* steps every instance takes                  */
+    float dt;                 /* ms                                          */
+    int32_t rounding;         /* delay rule: 0 trunc, 1 ceil, 2 DSL          */
+    uint64_t seed;            /* Philox key word 0 (lo) / counter word 2 (hi) */
+    uint32_t flags;           /* TVBG_F_NOISE or 0                           */
+    float cf_b;               /* coupling offset b                           */
+    float cf_p[3];            /* sigmoidal coupling parameters               */
+    float sigma[4];           /* noise amplitude per state variable          */
+    float consts[16];         /* model constants (the model's order)         */
+} tvbg_serve_request;
+
+#define TVBG_SERVE_QUEUED 0
+#define TVBG_SERVE_ACTIVE 1
+#define TVBG_SERVE_DONE 2
+#define TVBG_SERVE_CANCELLED 3
+
+/* A pool with `hbm_budget` bytes for admitted requests, advancing every
+ * active request by up to `chunk` steps per tick on `stream` (NULL: its own
+ * stream). */
+int tvbg_serve_create(int64_t hbm_budget, int32_t chunk, void *stream, tvbg_serve **out);
+int tvbg_serve_destroy(tvbg_serve *pool);
+/* Copy a request in and queue it; *id identifies it.  Rejects requests whose
+ * delays are shorter than the group kernel's blocks (d_min < 3) or whose
+ * footprint exceeds the whole budget. */
+int tvbg_serve_admit(tvbg_serve *pool, const tvbg_serve_request *req, int64_t *id);
+/* Admit queued requests that fit, advance every active one by one chunk,
+ * retire the finished; waits for this tick's device work.  *n_active and
+ * *n_queued (either may be NULL) count what is left. */
+int tvbg_serve_tick(tvbg_serve *pool, int32_t *n_active, int32_t *n_queued);
+/* *status = TVBG_SERVE_*; once done, the final state is copied to
+ * state_out (host [n_inst][N][nsvar]) when it is not NULL. */
+int tvbg_serve_poll(tvbg_serve *pool, int64_t id, int32_t *status, float *state_out);
+/* Drop a queued or active request (its device memory is freed at once). */
+int tvbg_serve_cancel(tvbg_serve *pool, int64_t id);
+/* Device bytes held by admitted requests and the footprint of request id. */
+int tvbg_serve_usage(tvbg_serve *pool, int64_t id, int64_t *used, int64_t *footprint);
+
 #ifdef __cplusplus
 }
 #endif

@@ -106,3 +106,52 @@ def test_poll_and_cancel(cuda):
         solo.submit(r)
         (a, ) = solo.run()
         assert np.array_equal(a.state, done[r.rid].state)
+
+
+def test_native_pool_equals_groups(cuda):
+    """The C++ serving pool (tvbg_serve_*): every request's final state is
+    bit-identical to lane-interleaved groups of the same inputs run alone,
+    with requests of different models and sizes in the mix."""
+    from tvb_hpc import groups, model as mdl, scheme as sch
+    reqs = [r for r in requests(seed=5, n=8)]
+    pool = serve.NativeServer(chunk=600)
+    for r in reqs:
+        pool.submit(r)
+    assert pool.poll(reqs[0].rid) == 'queued'
+    done = {r.rid: r for r in pool.run()}
+    assert len(done) == len(reqs)
+    for r in requests(seed=5, n=8):
+        M, C, noise = serve.MODELS[r.model]
+        m = M()
+        scm = sch.EulerMaryuyamaStep(r.dt) if noise else sch.EulerStep(r.dt)
+        gs = groups.GroupSet(m, C(m), scm, r.conn, r.dt, couplings=r.couplings, speeds=r.speeds,
+                             state0=r.x0, nparam=r.nparam, seed=r.seed)
+        gs.run(r.nsteps)
+        ref = gs.state.cpu().numpy()
+        got = done[r.rid].state
+        if C is serve.cpl.Diff:   # in-edge weight sums: the pool sums sequentially
+            assert np.abs(got - ref).max() <= 1e-5 * np.abs(ref).max(), r.model
+        else:
+            assert np.array_equal(got, ref), r.model
+    assert pool.used() == 0
+
+
+def test_native_pool_budget_cancel(cuda):
+    reqs = requests(seed=6, n=4)
+    for r in reqs:
+        r.nsteps = max(r.nsteps, 1500)
+    probe = serve.NativeServer(chunk=500)
+    for r in reqs:
+        probe.submit(r)
+    fp = [probe.footprint(r.rid) for r in reqs]
+    probe.close()
+    pool = serve.NativeServer(hbm_budget=1.5 * max(fp), chunk=500)   # one or two at a time
+    for r in reqs:
+        pool.submit(r)
+    a, q = pool.tick()
+    assert a >= 1 and a + q == len(reqs) and pool.used() <= 1.5 * max(fp)
+    assert pool.cancel(reqs[-1].rid) and pool.poll(reqs[-1].rid) == 'cancelled'
+    assert not pool.cancel(reqs[-1].rid)
+    rest = pool.run()
+    assert {r.rid for r in rest} == {r.rid for r in reqs[:-1]}
+    assert pool.used() == 0

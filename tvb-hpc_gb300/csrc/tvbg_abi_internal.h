@@ -44,6 +44,8 @@ GroupKernel group_kernel_linear(int cfun, int k);
 GroupKernel group_kernel_g2dosc(int cfun, int k);
 GroupKernel group_kernel_rww(int cfun, int k);
 GroupKernel group_kernel_jansenrit(int cfun, int k);
+// Group kernel of the engine library for (model, cfun, K), nullptr if not built.
+GroupKernel lookup_group_kernel(int model, int cfun, int k);
 // Shared memory of the blocked kernel beyond the ring (floats): K * nmax * (2 + NS) + 4 * nmax.
 uint32_t blocked_aux_bytes(int model, int k, int nmax);
 

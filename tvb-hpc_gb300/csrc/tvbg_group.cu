@@ -37,6 +37,8 @@ int check_group_launch(const tvbg_launch* cfg, GroupKernel* kfn, int* cluster, s
 
 }  // namespace
 
+GroupKernel tvbg::lookup_group_kernel(int model, int cfun, int k) { return lookup_group(model, cfun, k); }
+
 extern "C" {
 
 size_t tvbg_group_size(void) { return sizeof(tvbg_group); }

@@ -1,0 +1,589 @@
+// Native serving pool (tvbg_serve_*): continuous batching of sweep requests
+// on the lane-interleaved group kernel.
+//
+// A request is copied in at tvbg_serve_admit and planned on the host the way
+// tvb_hpc.groups.GroupSet plans it: integer delays per distinct speed
+// (tvbg_delays), per delay table the block length K (8 or 4, K <= d_min + 1)
+// and ring length nh (a power of two >= d_max + 1 + K, >= 8), edges packed
+// per table, nodes visited by in-degree (descending, stable), instances in
+// groups of eight per table (request-local index = Philox key word 1), one
+// CTA or cluster per group (the smallest cluster whose CTAs stay within
+// 1024 threads).  Its device buffers are one allocation made when the
+// request is admitted: when its footprint fits the budget and the device.
+//
+// A tick uploads every active request's group records for its next chunk
+// (t0, steps per lane) and launches its groups -- one launch per block
+// length -- on the request's own stream; the streams join the pool's
+// stream, the pool waits, checks each request's device status word, and
+// retires finished requests (state gathered from the lanes to the host,
+// device memory freed).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <new>
+#include <vector>
+
+#include "tvbg_abi_internal.h"
+#include "tvbg_group_launch.cuh"
+
+using namespace tvbg;
+
+namespace {
+
+constexpr int L = TVBG_GROUP_LANES;
+
+// (state variables, per-node parameters, observables) of each model id
+struct ModelShape {
+    int ns, np, nobs;
+};
+bool model_shape(int model, ModelShape* s) {
+    switch (model) {
+        case TVBG_MODEL_KURAMOTO: *s = {1, 1, 2}; return true;
+        case TVBG_MODEL_G2DO: *s = {2, 1, 2}; return true;
+        case TVBG_MODEL_MPR: *s = {2, 1, 2}; return true;
+        case TVBG_MODEL_LINEAR: *s = {1, 1, 1}; return true;
+        case TVBG_MODEL_G2DOSC: *s = {2, 1, 2}; return true;
+        case TVBG_MODEL_RWW: *s = {1, 2, 1}; return true;
+        case TVBG_MODEL_JANSENRIT: *s = {6, 2, 1}; return true;
+        default: return false;
+    }
+}
+
+size_t align_up(size_t x) { return (x + 255) & ~static_cast<size_t>(255); }
+
+__global__ void fill_cos_channel(float* ring, long long n) {
+    // [..][2][L] layout: channel 1 (cos) of every slot holds cos 0 = 1
+    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<long long>(gridDim.x) * blockDim.x)
+        ring[i] = ((i / L) & 1) ? 1.0f : 0.0f;
+}
+
+struct Request {
+    int64_t id = 0;
+    int status = TVBG_SERVE_QUEUED;
+    // inputs
+    int model = 0, cfun = 0, N = 0, nnz = 0, n_inst = 0, npar = 0;
+    ModelShape shape{};
+    int64_t nsteps = 0, done = 0;
+    float dt = 0.0f;
+    uint64_t seed = 0;
+    uint32_t flags = 0;
+    float cf_b = 0.0f, cf_p[3] = {0, 0, 0}, sigma[4] = {0, 0, 0, 0}, consts[16] = {};
+    std::vector<float> couplings, state0, nparam;
+    // plan
+    int channels = 1, threads = 0, cluster = 1;
+    std::vector<int32_t> row, nodes;
+    std::vector<float> wsum;
+    std::vector<tvbg_edge> edges;     // [tables][nnz]
+    std::vector<int> table_k, table_lognh;
+    std::vector<int> g_table;         // per group
+    std::vector<std::vector<int>> members;
+    size_t off_edges = 0, off_row = 0, off_wsum = 0, off_nodes = 0, off_ring = 0, off_state = 0,
+           off_nparam = 0, off_groups = 0, off_order = 0, off_status = 0, bytes = 0;
+    std::vector<size_t> ring_off;     // per group, floats from off_ring
+    std::vector<int32_t> order;       // per block length, the groups of that length
+    std::vector<int> k_list, k_start, k_count;
+    // device
+    char* dev = nullptr;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t done_ev = nullptr;
+    std::vector<tvbg_group> records;
+    std::vector<float> result;        // [n_inst][N][ns] once done
+};
+
+int next_pow2(int v) {
+    int p = 1;
+    while (p < v) p <<= 1;
+    return p;
+}
+
+// Host plan of a request (no device work); fills the byte layout.
+int plan(Request& r, const tvbg_serve_request& q) {
+    const int N = r.N, nnz = r.nnz;
+    // delay tables, one per distinct speed (sorted, as numpy.unique)
+    std::vector<float> speeds(q.speeds, q.speeds + r.n_inst);
+    std::vector<float> uniq = speeds;
+    std::sort(uniq.begin(), uniq.end());
+    uniq.erase(std::unique(uniq.begin(), uniq.end()), uniq.end());
+    std::vector<int> tab_of(r.n_inst);
+    for (int b = 0; b < r.n_inst; ++b)
+        tab_of[b] = static_cast<int>(std::lower_bound(uniq.begin(), uniq.end(), speeds[b]) - uniq.begin());
+    const int T = static_cast<int>(uniq.size());
+    r.edges.resize(static_cast<size_t>(T) * std::max(1, nnz));
+    std::vector<int32_t> d(std::max(1, nnz));
+    for (int t = 0; t < T; ++t) {
+        if (nnz > 0) {
+            int rc = tvbg_delays(nnz, q.lengths, uniq[t], q.dt, q.rounding, d.data());
+            if (rc) return rc;
+        }
+        int dmin = 7, dmax = 0;
+        if (nnz > 0) {
+            dmin = *std::min_element(d.begin(), d.begin() + nnz);
+            dmax = *std::max_element(d.begin(), d.begin() + nnz);
+        }
+        const int k = dmin + 1 >= 8 ? 8 : (dmin + 1 >= 4 ? 4 : 0);
+        if (k == 0)
+            return set_error(TVBG_EUNSUPPORTED,
+                             "tvbg_serve_admit: delays shorter than the group kernel's blocks (d_min < 3)");
+        const int nh = std::max(8, next_pow2(dmax + 1 + k));
+        int lognh = 0;
+        while ((1 << lognh) < nh) ++lognh;
+        if (lognh > 16) return set_error(TVBG_EINVAL, "tvbg_serve_admit: delays beyond 2^16 - 9 steps");
+        r.table_k.push_back(k);
+        r.table_lognh.push_back(lognh);
+        if (nnz > 0) {
+            int rc = tvbg_pack_edges_group(N, nnz, q.row, q.col, q.weights, d.data(), lognh,
+                                           r.edges.data() + static_cast<size_t>(t) * nnz);
+            if (rc) return rc;
+        }
+    }
+    // per-node constants: in-edge weight sums and the visiting order
+    r.row.assign(q.row, q.row + N + 1);
+    r.wsum.assign(N, 0.0f);
+    std::vector<int> deg(N);
+    for (int i = 0; i < N; ++i) {
+        deg[i] = q.row[i + 1] - q.row[i];
+        float s = 0.0f;
+        for (int e = q.row[i]; e < q.row[i + 1]; ++e) s += q.weights[e];
+        r.wsum[i] = s;
+    }
+    r.nodes.resize(N);
+    for (int i = 0; i < N; ++i) r.nodes[i] = i;
+    std::stable_sort(r.nodes.begin(), r.nodes.end(), [&](int a, int b) { return deg[a] > deg[b]; });
+    // groups: per table, eight instances in index order
+    for (int t = 0; t < T; ++t) {
+        std::vector<int> idx;
+        for (int b = 0; b < r.n_inst; ++b)
+            if (tab_of[b] == t) idx.push_back(b);
+        for (size_t g0 = 0; g0 < idx.size(); g0 += L) {
+            r.members.emplace_back(idx.begin() + g0, idx.begin() + std::min(idx.size(), g0 + L));
+            r.g_table.push_back(t);
+        }
+    }
+    const int G = static_cast<int>(r.members.size());
+    // launch shape: the smallest cluster whose CTAs stay within 1024 threads
+    int c = 1;
+    while (L * ((N + c - 1) / c) > 1024 && c < 8) c *= 2;
+    r.cluster = c;
+    const int per = (N + c - 1) / c;
+    r.threads = std::min(1024, 32 * ((L * per + 31) / 32));
+    // launch order: one launch per block length, groups in index order
+    for (int k : {4, 8}) {
+        int cnt = 0;
+        const int start = static_cast<int>(r.order.size());
+        for (int g = 0; g < G; ++g)
+            if (r.table_k[r.g_table[g]] == k) {
+                r.order.push_back(g);
+                ++cnt;
+            }
+        if (cnt) {
+            r.k_list.push_back(k);
+            r.k_start.push_back(start);
+            r.k_count.push_back(cnt);
+        }
+    }
+    // byte layout of the one device allocation
+    const int ns = r.shape.ns, np = r.npar, C = r.channels;
+    size_t o = 0;
+    r.off_edges = o;
+    o = align_up(o + r.edges.size() * sizeof(tvbg_edge));
+    r.off_row = o;
+    o = align_up(o + (N + 1) * sizeof(int32_t));
+    r.off_wsum = o;
+    o = align_up(o + N * sizeof(float));
+    r.off_nodes = o;
+    o = align_up(o + N * sizeof(int32_t));
+    r.off_ring = o;
+    size_t ring_floats = 0;
+    for (int g = 0; g < G; ++g) {
+        r.ring_off.push_back(ring_floats);
+        const size_t R = (static_cast<size_t>(1) << r.table_lognh[r.g_table[g]]) + 8;
+        ring_floats += static_cast<size_t>(N) * R * L * C;
+    }
+    o = align_up(o + ring_floats * sizeof(float));
+    r.off_state = o;
+    o = align_up(o + static_cast<size_t>(G) * N * ns * L * sizeof(float));
+    r.off_nparam = o;
+    o = align_up(o + static_cast<size_t>(G) * N * np * L * sizeof(float));
+    r.off_groups = o;
+    o = align_up(o + static_cast<size_t>(G) * sizeof(tvbg_group));
+    r.off_order = o;
+    o = align_up(o + std::max<size_t>(1, r.order.size()) * sizeof(int32_t));
+    r.off_status = o;
+    o = align_up(o + sizeof(int32_t));
+    r.bytes = o;
+    return TVBG_OK;
+}
+
+// Allocate, upload and initialise the request's device state.
+int materialise(Request& r) {
+    cudaError_t e = cudaMalloc(&r.dev, r.bytes);
+    if (e != cudaSuccess) {
+        r.dev = nullptr;
+        return set_cuda_error(e, "tvbg_serve: cudaMalloc");
+    }
+    e = cudaStreamCreateWithFlags(&r.stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&r.done_ev, cudaEventDisableTiming);
+    if (e != cudaSuccess) return set_cuda_error(e, "tvbg_serve: stream");
+    const int N = r.N, ns = r.shape.ns, np = r.npar, G = static_cast<int>(r.members.size());
+    // lane-interleaved state and parameters [G][N][*][L]
+    std::vector<float> gstate(static_cast<size_t>(G) * N * ns * L, 0.0f);
+    std::vector<float> gpar(static_cast<size_t>(G) * N * np * L, 0.0f);
+    for (int g = 0; g < G; ++g)
+        for (size_t l = 0; l < r.members[g].size(); ++l) {
+            const int b = r.members[g][l];
+            for (int n = 0; n < N; ++n) {
+                for (int v = 0; v < ns; ++v)
+                    gstate[((static_cast<size_t>(g) * N + n) * ns + v) * L + l] =
+                        r.state0[(static_cast<size_t>(b) * N + n) * ns + v];
+                for (int v = 0; v < np; ++v)
+                    gpar[((static_cast<size_t>(g) * N + n) * np + v) * L + l] =
+                        r.nparam[(static_cast<size_t>(b) * N + n) * np + v];
+            }
+        }
+    struct Up {
+        size_t off;
+        const void* src;
+        size_t n;
+    } ups[] = {{r.off_edges, r.edges.data(), r.edges.size() * sizeof(tvbg_edge)},
+               {r.off_row, r.row.data(), r.row.size() * sizeof(int32_t)},
+               {r.off_wsum, r.wsum.data(), r.wsum.size() * sizeof(float)},
+               {r.off_nodes, r.nodes.data(), r.nodes.size() * sizeof(int32_t)},
+               {r.off_state, gstate.data(), gstate.size() * sizeof(float)},
+               {r.off_nparam, gpar.data(), gpar.size() * sizeof(float)},
+               {r.off_order, r.order.data(), r.order.size() * sizeof(int32_t)}};
+    for (const Up& u : ups) {
+        if (u.n == 0) continue;
+        e = cudaMemcpy(r.dev + u.off, u.src, u.n, cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return set_cuda_error(e, "tvbg_serve: upload");
+    }
+    e = cudaMemset(r.dev + r.off_status, 0, sizeof(int32_t));
+    if (e == cudaSuccess) e = cudaMemset(r.dev + r.off_ring, 0, r.off_state - r.off_ring);
+    if (e != cudaSuccess) return set_cuda_error(e, "tvbg_serve: memset");
+    if (r.channels == 2) {  // zero history of the Kuramoto coupling: (sin 0, cos 0)
+        const long long n = static_cast<long long>((r.off_state - r.off_ring) / sizeof(float));
+        fill_cos_channel<<<1024, 256, 0, r.stream>>>(reinterpret_cast<float*>(r.dev + r.off_ring), n);
+        e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaStreamSynchronize(r.stream);
+        if (e != cudaSuccess) return set_cuda_error(e, "tvbg_serve: ring init");
+    }
+    // group records (t0 and step counts are set per tick)
+    r.records.assign(G, tvbg_group{});
+    const uint64_t seed = r.seed;
+    for (int g = 0; g < G; ++g) {
+        tvbg_group& rec = r.records[g];
+        const int t = r.g_table[g];
+        rec.edges = reinterpret_cast<const tvbg_edge*>(r.dev + r.off_edges) +
+                    static_cast<size_t>(t) * std::max(1, r.nnz);
+        rec.row = reinterpret_cast<const int32_t*>(r.dev + r.off_row);
+        rec.wsum = reinterpret_cast<const float*>(r.dev + r.off_wsum);
+        rec.nodes = reinterpret_cast<const int32_t*>(r.dev + r.off_nodes);
+        rec.ring = reinterpret_cast<float*>(r.dev + r.off_ring) + r.ring_off[g];
+        rec.state = reinterpret_cast<float*>(r.dev + r.off_state) + static_cast<size_t>(g) * N * ns * L;
+        rec.nparam = reinterpret_cast<const float*>(r.dev + r.off_nparam) + static_cast<size_t>(g) * N * np * L;
+        rec.N = N;
+        rec.nnz = r.nnz;
+        rec.lognh = r.table_lognh[t];
+        rec.model = r.model;
+        rec.cfun = r.cfun;
+        rec.flags = r.flags;
+        rec.trace_every = 1;
+        rec.trace_len = 1;
+        rec.trace_nobs = r.shape.nobs;
+        rec.bold_period = 1;
+        rec.bold_len = 0;
+        rec.bold_obs = (r.model == TVBG_MODEL_KURAMOTO || r.model == TVBG_MODEL_G2DO) ? 1 : 0;
+        rec.seed_lo = static_cast<uint32_t>(seed & 0xffffffffu);
+        rec.seed_hi = static_cast<uint32_t>(seed >> 32);
+        rec.dt = r.dt;
+        rec.sqrt_dt = std::sqrt(r.dt);
+        rec.dt_bold = static_cast<float>(static_cast<double>(r.dt) / 1000.0);
+        rec.cf_b = r.cf_b;
+        std::memcpy(rec.cf_p, r.cf_p, sizeof(rec.cf_p));
+        std::memcpy(rec.sigma, r.sigma, sizeof(rec.sigma));
+        std::memcpy(rec.consts, r.consts, sizeof(rec.consts));
+        for (size_t l = 0; l < r.members[g].size(); ++l) {
+            rec.lanes[l].cf_a = r.couplings[r.members[g][l]];
+            rec.lanes[l].inst_id = static_cast<uint32_t>(r.members[g][l]);
+        }
+    }
+    return TVBG_OK;
+}
+
+void release(Request& r) {
+    if (r.stream) cudaStreamSynchronize(r.stream);
+    if (r.dev) cudaFree(r.dev);
+    if (r.done_ev) cudaEventDestroy(r.done_ev);
+    if (r.stream) cudaStreamDestroy(r.stream);
+    r.dev = nullptr;
+    r.stream = nullptr;
+    r.done_ev = nullptr;
+    r.records.clear();
+    r.records.shrink_to_fit();
+}
+
+// Enqueue the next `steps` steps of every group of r on r.stream.
+int launch_chunk(Request& r, int64_t steps) {
+    const int G = static_cast<int>(r.records.size());
+    for (int g = 0; g < G; ++g) {
+        tvbg_group& rec = r.records[g];
+        rec.t0 = r.done;
+        rec.nsteps = static_cast<int32_t>(steps);
+        for (size_t l = 0; l < r.members[g].size(); ++l) rec.lanes[l].nsteps = static_cast<int32_t>(steps);
+    }
+    cudaError_t e = cudaMemcpyAsync(r.dev + r.off_groups, r.records.data(), G * sizeof(tvbg_group),
+                                    cudaMemcpyHostToDevice, r.stream);
+    if (e != cudaSuccess) return set_cuda_error(e, "tvbg_serve: group records");
+    static const ErrSink sink{set_error, set_cuda_error};
+    for (size_t i = 0; i < r.k_list.size(); ++i) {
+        tvbg_launch cfg{};
+        cfg.model = r.model;
+        cfg.cfun = r.cfun;
+        cfg.threads = r.threads;
+        cfg.cluster = r.cluster;
+        cfg.block_k = r.k_list[i];
+        cfg.d_status = reinterpret_cast<int32_t*>(r.dev + r.off_status);
+        cfg.d_order = reinterpret_cast<const int32_t*>(r.dev + r.off_order) + r.k_start[i];
+        GroupKernel k = lookup_group_kernel(r.model, r.cfun, r.k_list[i]);
+        if (!k) return set_error(TVBG_EUNSUPPORTED, "tvbg_serve: group kernel not built");
+        const size_t smem = group_smem_bytes(cfg.block_k, cfg.threads, group_channels(cfg.cfun));
+        int rc = launch_group_kernel(k, reinterpret_cast<const tvbg_group*>(r.dev + r.off_groups),
+                                     r.k_count[i], &cfg, r.cluster, smem, r.stream, sink);
+        if (rc) return rc;
+    }
+    e = cudaEventRecord(r.done_ev, r.stream);
+    if (e != cudaSuccess) return set_cuda_error(e, "tvbg_serve: event");
+    return TVBG_OK;
+}
+
+// Gather the final state [n_inst][N][ns] from the lanes.
+int collect(Request& r) {
+    const int N = r.N, ns = r.shape.ns, G = static_cast<int>(r.members.size());
+    std::vector<float> gstate(static_cast<size_t>(G) * N * ns * L);
+    cudaError_t e = cudaMemcpy(gstate.data(), r.dev + r.off_state, gstate.size() * sizeof(float),
+                               cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return set_cuda_error(e, "tvbg_serve: state download");
+    r.result.assign(static_cast<size_t>(r.n_inst) * N * ns, 0.0f);
+    for (int g = 0; g < G; ++g)
+        for (size_t l = 0; l < r.members[g].size(); ++l) {
+            const int b = r.members[g][l];
+            for (int n = 0; n < N; ++n)
+                for (int v = 0; v < ns; ++v)
+                    r.result[(static_cast<size_t>(b) * N + n) * ns + v] =
+                        gstate[((static_cast<size_t>(g) * N + n) * ns + v) * L + l];
+        }
+    return TVBG_OK;
+}
+
+}  // namespace
+
+struct tvbg_serve {
+    int64_t budget = 0, used = 0;
+    int32_t chunk = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int64_t next_id = 1;
+    std::deque<Request*> queue;
+    std::vector<Request*> active;
+    std::map<int64_t, Request*> all;
+};
+
+extern "C" {
+
+int tvbg_serve_create(int64_t hbm_budget, int32_t chunk, void* stream, tvbg_serve** out) {
+    if (!out || hbm_budget <= 0 || chunk <= 0) return set_error(TVBG_EINVAL, "tvbg_serve_create: bad arguments");
+    tvbg_serve* p = new (std::nothrow) tvbg_serve;
+    if (!p) return set_error(TVBG_EINVAL, "tvbg_serve_create: out of host memory");
+    p->budget = hbm_budget;
+    p->chunk = chunk;
+    if (stream) {
+        p->stream = static_cast<cudaStream_t>(stream);
+    } else {
+        cudaError_t e = cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking);
+        if (e != cudaSuccess) {
+            delete p;
+            return set_cuda_error(e, "tvbg_serve_create: stream");
+        }
+        p->own_stream = true;
+    }
+    *out = p;
+    return TVBG_OK;
+}
+
+int tvbg_serve_destroy(tvbg_serve* p) {
+    if (!p) return TVBG_OK;
+    for (auto& kv : p->all) {
+        release(*kv.second);
+        delete kv.second;
+    }
+    if (p->own_stream) cudaStreamDestroy(p->stream);
+    delete p;
+    return TVBG_OK;
+}
+
+int tvbg_serve_admit(tvbg_serve* p, const tvbg_serve_request* q, int64_t* id) {
+    if (!p || !q || !id) return set_error(TVBG_EINVAL, "tvbg_serve_admit: null");
+    ModelShape sh{};
+    if (!model_shape(q->model, &sh)) return set_error(TVBG_EUNSUPPORTED, "tvbg_serve_admit: unknown model");
+    const bool separable = q->cfun == TVBG_CFUN_LINEAR || q->cfun == TVBG_CFUN_DIFF ||
+                           q->cfun == TVBG_CFUN_SIGMOIDAL;
+    const bool kuramoto = q->model == TVBG_MODEL_KURAMOTO && q->cfun == TVBG_CFUN_KURAMOTO;
+    if (!separable && !kuramoto)
+        return set_error(TVBG_EUNSUPPORTED, "tvbg_serve_admit: coupling not on the group kernel");
+    if (q->N <= 0 || q->N > 65535 || q->nnz < 0 || q->n_inst <= 0 || q->npar != sh.np ||
+        q->nsteps < 0 || q->nsteps > 0x7fffffff || !(q->dt > 0.0f) || !q->row ||
+        (q->nnz > 0 && (!q->col || !q->weights || !q->lengths)) || !q->couplings || !q->speeds ||
+        !q->state0 || !q->nparam || (q->flags & ~TVBG_F_NOISE) || q->rounding < 0 || q->rounding > 2)
+        return set_error(TVBG_EINVAL, "tvbg_serve_admit: bad request");
+    if ((q->flags & TVBG_F_NOISE) && sh.ns > 4)
+        return set_error(TVBG_EUNSUPPORTED, "tvbg_serve_admit: noise on more than 4 state variables");
+    Request* r = new (std::nothrow) Request;
+    if (!r) return set_error(TVBG_EINVAL, "tvbg_serve_admit: out of host memory");
+    r->model = q->model;
+    r->cfun = q->cfun;
+    r->N = q->N;
+    r->nnz = q->nnz;
+    r->n_inst = q->n_inst;
+    r->npar = q->npar;
+    r->shape = sh;
+    r->nsteps = q->nsteps;
+    r->dt = q->dt;
+    r->seed = q->seed;
+    r->flags = q->flags;
+    r->cf_b = q->cf_b;
+    std::memcpy(r->cf_p, q->cf_p, sizeof(r->cf_p));
+    std::memcpy(r->sigma, q->sigma, sizeof(r->sigma));
+    std::memcpy(r->consts, q->consts, sizeof(r->consts));
+    r->channels = kuramoto ? 2 : 1;
+    r->couplings.assign(q->couplings, q->couplings + q->n_inst);
+    r->state0.assign(q->state0, q->state0 + static_cast<size_t>(q->n_inst) * q->N * sh.ns);
+    r->nparam.assign(q->nparam, q->nparam + static_cast<size_t>(q->n_inst) * q->N * sh.np);
+    int rc = plan(*r, *q);
+    if (rc == TVBG_OK && static_cast<int64_t>(r->bytes) > p->budget)
+        rc = set_error(TVBG_EINVAL, "tvbg_serve_admit: the request alone exceeds the budget");
+    if (rc) {
+        delete r;
+        return rc;
+    }
+    r->id = p->next_id++;
+    p->queue.push_back(r);
+    p->all[r->id] = r;
+    *id = r->id;
+    return TVBG_OK;
+}
+
+int tvbg_serve_tick(tvbg_serve* p, int32_t* n_active, int32_t* n_queued) {
+    if (!p) return set_error(TVBG_EINVAL, "tvbg_serve_tick: null");
+    // admit in arrival order while the budget and the device allow
+    while (!p->queue.empty()) {
+        Request* r = p->queue.front();
+        size_t free_b = 0, total_b = 0;
+        cudaError_t e = cudaMemGetInfo(&free_b, &total_b);
+        if (e != cudaSuccess) return set_cuda_error(e, "tvbg_serve_tick: cudaMemGetInfo");
+        if (p->used + static_cast<int64_t>(r->bytes) > p->budget || r->bytes > free_b) break;
+        int rc = materialise(*r);
+        if (rc) {
+            release(*r);
+            return rc;
+        }
+        p->queue.pop_front();
+        p->used += static_cast<int64_t>(r->bytes);
+        r->status = TVBG_SERVE_ACTIVE;
+        p->active.push_back(r);
+    }
+    // one chunk for every active request, each on its stream, joined into the pool's
+    cudaEvent_t start;
+    cudaError_t e = cudaEventCreateWithFlags(&start, cudaEventDisableTiming);
+    if (e != cudaSuccess) return set_cuda_error(e, "tvbg_serve_tick: event");
+    e = cudaEventRecord(start, p->stream);
+    std::vector<int64_t> steps(p->active.size());
+    int rc = e == cudaSuccess ? TVBG_OK : set_cuda_error(e, "tvbg_serve_tick: event");
+    for (size_t i = 0; i < p->active.size() && rc == TVBG_OK; ++i) {
+        Request& r = *p->active[i];
+        steps[i] = std::min<int64_t>(p->chunk, r.nsteps - r.done);
+        e = cudaStreamWaitEvent(r.stream, start, 0);
+        if (e != cudaSuccess) {
+            rc = set_cuda_error(e, "tvbg_serve_tick: wait");
+            break;
+        }
+        if (steps[i] > 0) rc = launch_chunk(r, steps[i]);
+        else if (cudaEventRecord(r.done_ev, r.stream) != cudaSuccess)
+            rc = set_error(TVBG_ECUDA, "tvbg_serve_tick: event");
+        if (rc == TVBG_OK) {
+            e = cudaStreamWaitEvent(p->stream, r.done_ev, 0);
+            if (e != cudaSuccess) rc = set_cuda_error(e, "tvbg_serve_tick: join");
+        }
+    }
+    cudaEventDestroy(start);
+    if (rc) return rc;
+    e = cudaStreamSynchronize(p->stream);
+    if (e != cudaSuccess) return set_cuda_error(e, "tvbg_serve_tick: synchronize");
+    // status words, clocks, retirement
+    std::vector<Request*> keep;
+    for (size_t i = 0; i < p->active.size(); ++i) {
+        Request& r = *p->active[i];
+        int32_t st = 0;
+        e = cudaMemcpy(&st, r.dev + r.off_status, sizeof(st), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return set_cuda_error(e, "tvbg_serve_tick: status");
+        if (st != 0) return set_error(TVBG_EDEVICE, "tvbg_serve_tick: a group kernel reported an error");
+        r.done += steps[i];
+        if (r.done >= r.nsteps) {
+            rc = collect(r);
+            if (rc) return rc;
+            release(r);
+            p->used -= static_cast<int64_t>(r.bytes);
+            r.status = TVBG_SERVE_DONE;
+        } else {
+            keep.push_back(&r);
+        }
+    }
+    p->active.swap(keep);
+    if (n_active) *n_active = static_cast<int32_t>(p->active.size());
+    if (n_queued) *n_queued = static_cast<int32_t>(p->queue.size());
+    return TVBG_OK;
+}
+
+int tvbg_serve_poll(tvbg_serve* p, int64_t id, int32_t* status, float* state_out) {
+    if (!p || !status) return set_error(TVBG_EINVAL, "tvbg_serve_poll: null");
+    auto it = p->all.find(id);
+    if (it == p->all.end()) return set_error(TVBG_EINVAL, "tvbg_serve_poll: unknown id");
+    const Request& r = *it->second;
+    *status = r.status;
+    if (r.status == TVBG_SERVE_DONE && state_out)
+        std::memcpy(state_out, r.result.data(), r.result.size() * sizeof(float));
+    return TVBG_OK;
+}
+
+int tvbg_serve_cancel(tvbg_serve* p, int64_t id) {
+    if (!p) return set_error(TVBG_EINVAL, "tvbg_serve_cancel: null");
+    auto it = p->all.find(id);
+    if (it == p->all.end()) return set_error(TVBG_EINVAL, "tvbg_serve_cancel: unknown id");
+    Request* r = it->second;
+    if (r->status == TVBG_SERVE_QUEUED) {
+        p->queue.erase(std::find(p->queue.begin(), p->queue.end(), r));
+    } else if (r->status == TVBG_SERVE_ACTIVE) {
+        p->active.erase(std::find(p->active.begin(), p->active.end(), r));
+        release(*r);
+        p->used -= static_cast<int64_t>(r->bytes);
+    } else {
+        return set_error(TVBG_EINVAL, "tvbg_serve_cancel: the request is done or cancelled");
+    }
+    r->status = TVBG_SERVE_CANCELLED;
+    return TVBG_OK;
+}
+
+int tvbg_serve_usage(tvbg_serve* p, int64_t id, int64_t* used, int64_t* footprint) {
+    if (!p) return set_error(TVBG_EINVAL, "tvbg_serve_usage: null");
+    if (used) *used = p->used;
+    if (footprint) {
+        auto it = p->all.find(id);
+        *footprint = it == p->all.end() ? -1 : static_cast<int64_t>(it->second->bytes);
+    }
+    return TVBG_OK;
+}
+
+}  // extern "C"

@@ -178,6 +178,23 @@ class tvbg_net(ctypes.Structure):
 GROUP_DTYPE = np.dtype(tvbg_group)
 
 
+class tvbg_serve_request(ctypes.Structure):
+    "include/tvbg.h tvbg_serve_request."
+    _fields_ = [
+        ('model', ctypes.c_int32), ('cfun', ctypes.c_int32), ('N', ctypes.c_int32),
+        ('nnz', ctypes.c_int32), ('row', ctypes.c_void_p), ('col', ctypes.c_void_p),
+        ('weights', ctypes.c_void_p), ('lengths', ctypes.c_void_p), ('n_inst', ctypes.c_int32),
+        ('npar', ctypes.c_int32), ('couplings', ctypes.c_void_p), ('speeds', ctypes.c_void_p),
+        ('state0', ctypes.c_void_p), ('nparam', ctypes.c_void_p), ('nsteps', ctypes.c_int64),
+        ('dt', ctypes.c_float), ('rounding', ctypes.c_int32), ('seed', ctypes.c_uint64),
+        ('flags', ctypes.c_uint32), ('cf_b', ctypes.c_float), ('cf_p', ctypes.c_float * 3),
+        ('sigma', ctypes.c_float * 4), ('consts', ctypes.c_float * 16),
+    ]
+
+
+SERVE_QUEUED, SERVE_ACTIVE, SERVE_DONE, SERVE_CANCELLED = 0, 1, 2, 3
+
+
 class tvbg_adjoint(ctypes.Structure):
     _fields_ = [
         ('edges_t', ctypes.c_void_p), ('row_t', ctypes.c_void_p), ('seg', ctypes.c_void_p),
@@ -228,6 +245,14 @@ SIGNATURES = {
     'tvbg_pack_edges_group': (ctypes.c_int, [_i32, _i32, _vp, _vp, _vp, _vp, _i32, _vp]),
     'tvbg_group_run': (ctypes.c_int, [_vp, _i32, ctypes.POINTER(tvbg_launch), _vp]),
     'tvbg_group_occupancy': (ctypes.c_int, [ctypes.c_void_p, _ip, _ip]),
+    'tvbg_serve_create': (ctypes.c_int, [_i64, _i32, _vp, ctypes.POINTER(_vp)]),
+    'tvbg_serve_destroy': (ctypes.c_int, [_vp]),
+    'tvbg_serve_admit': (ctypes.c_int, [_vp, ctypes.POINTER(tvbg_serve_request),
+                                        ctypes.POINTER(_i64)]),
+    'tvbg_serve_tick': (ctypes.c_int, [_vp, _ip, _ip]),
+    'tvbg_serve_poll': (ctypes.c_int, [_vp, _i64, _ip, _vp]),
+    'tvbg_serve_cancel': (ctypes.c_int, [_vp, _i64]),
+    'tvbg_serve_usage': (ctypes.c_int, [_vp, _i64, ctypes.POINTER(_i64), ctypes.POINTER(_i64)]),
 }
 
 

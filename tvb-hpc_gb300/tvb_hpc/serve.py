@@ -315,6 +315,143 @@ class Server:
         return out
 
 
+class NativeServer:
+    """
+    The serving pool in native code (tvbg_serve_*): the same continuous
+    batching as Server for requests without gradients, run by the C++ pool
+    -- requests copied in, admitted by the HBM budget, advanced one chunk
+    per tick on per-request streams, retired, polled and cancelled by id.
+    Each request's result equals lane-interleaved groups of the same inputs
+    (GroupSet), alone or in any mix.
+    """
+
+    def __init__(self, hbm_budget=180e9, chunk=2000, clock=time.perf_counter):
+        import ctypes
+        from . import _native as nat
+        self.nat = nat
+        self.lib = nat.load()
+        self.clock = clock
+        h = ctypes.c_void_p()
+        nat.check(self.lib.tvbg_serve_create(int(hbm_budget), int(chunk), None, ctypes.byref(h)))
+        self.h = h
+        self.reqs = {}          # rid -> (Request, native id, kept host arrays)
+        self.done = []
+        self.ticks = 0
+
+    def close(self):
+        if self.h is not None:
+            self.lib.tvbg_serve_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def submit(self, req):
+        """Copy a request into the pool (queued until it fits); gradient
+        requests need Server."""
+        import ctypes
+        nat = self.nat
+        if req.want_grad:
+            raise ValueError('gradient requests run on Server (FC-fit adjoint)')
+        M, C, noise = MODELS[req.model]
+        m = M()
+        cf = C(m)
+        kid, consts, sigma = m.engine_spec()
+        cid, _, cf_b, cf_p = cf.engine_spec()
+        conn = req.conn
+        I, N = req.couplings.size, conn.nnode
+        keep = dict(
+            row=np.ascontiguousarray(conn.row, np.int32),
+            col=np.ascontiguousarray(conn.col, np.int32),
+            w=np.ascontiguousarray(conn.wnz, np.float32),
+            ln=np.ascontiguousarray(conn.lnz, np.float32),
+            G=np.ascontiguousarray(req.couplings, np.float32),
+            sp=np.ascontiguousarray(np.broadcast_to(np.asarray(req.speeds, np.float32), (I, ))),
+            x0=np.ascontiguousarray(np.broadcast_to(np.asarray(req.x0, np.float32),
+                                                    (I, N, m.nsvar))),
+        )
+        npar = len(m.param_sym)
+        npm = (np.broadcast_to(m.node_params(N), (I, N, npar)) if req.nparam is None
+               else np.broadcast_to(np.asarray(req.nparam, np.float32).reshape(I, N, -1), (I, N, npar)))
+        keep['np'] = np.ascontiguousarray(npm, np.float32)
+        q = nat.tvbg_serve_request()
+        q.model, q.cfun, q.N, q.nnz = kid, cid, N, conn.nnz
+        q.row, q.col = keep['row'].ctypes.data, keep['col'].ctypes.data
+        q.weights, q.lengths = keep['w'].ctypes.data, keep['ln'].ctypes.data
+        q.n_inst, q.npar = I, npar
+        q.couplings, q.speeds = keep['G'].ctypes.data, keep['sp'].ctypes.data
+        q.state0, q.nparam = keep['x0'].ctypes.data, keep['np'].ctypes.data
+        q.nsteps, q.dt, q.rounding = int(req.nsteps), float(req.dt), 1
+        q.seed = int(req.seed) & ((1 << 64) - 1)
+        q.flags = nat.F_NOISE if (noise and np.any(np.asarray(sigma) != 0)) else 0
+        q.cf_b = float(cf_b) if isinstance(cf_b, (int, float, np.number)) else 0.0
+        q.cf_p[:] = [float(v) for v in np.asarray(cf_p, np.float32)]
+        q.sigma[:] = [float(v) for v in np.asarray(sigma, np.float32)[:4]]
+        q.consts[:] = [float(v) for v in np.asarray(consts, np.float32)]
+        nid = ctypes.c_int64()
+        nat.check(self.lib.tvbg_serve_admit(self.h, ctypes.byref(q), ctypes.byref(nid)))
+        self.reqs[req.rid] = (req, nid.value, m.nsvar)
+        return nid.value
+
+    def tick(self):
+        "Admit what fits, advance every active request one chunk, retire; (active, queued)."
+        import ctypes
+        a, q = ctypes.c_int32(), ctypes.c_int32()
+        self.nat.check(self.lib.tvbg_serve_tick(self.h, ctypes.byref(a), ctypes.byref(q)))
+        self.ticks += 1
+        now = self.clock()
+        for rid, (req, nid, ns) in self.reqs.items():
+            if req.finished is None and self.poll(rid) == 'done':
+                req.finished = now
+                out = np.zeros((req.couplings.size, req.conn.nnode, ns), np.float32)
+                st = ctypes.c_int32()
+                self.nat.check(self.lib.tvbg_serve_poll(self.h, nid, ctypes.byref(st), out.ctypes.data))
+                req.state = out
+                self.done.append(req)
+        return a.value, q.value
+
+    def poll(self, rid):
+        "'queued', 'active', 'done', 'cancelled', or None for an unknown request."
+        import ctypes
+        if rid not in self.reqs:
+            return None
+        st = ctypes.c_int32()
+        self.nat.check(self.lib.tvbg_serve_poll(self.h, self.reqs[rid][1], ctypes.byref(st), None))
+        return {0: 'queued', 1: 'active', 2: 'done', 3: 'cancelled'}[st.value]
+
+    def cancel(self, rid):
+        "Drop a queued or active request; False if it is unknown, done or cancelled."
+        if self.poll(rid) not in ('queued', 'active'):
+            return False
+        self.nat.check(self.lib.tvbg_serve_cancel(self.h, self.reqs[rid][1]))
+        return True
+
+    def footprint(self, rid):
+        "Device bytes request rid takes once admitted."
+        import ctypes
+        u, f = ctypes.c_int64(), ctypes.c_int64()
+        self.nat.check(self.lib.tvbg_serve_usage(self.h, self.reqs[rid][1], ctypes.byref(u),
+                                                 ctypes.byref(f)))
+        return f.value
+
+    def used(self):
+        "Device bytes held by admitted requests."
+        import ctypes
+        u, f = ctypes.c_int64(), ctypes.c_int64()
+        self.nat.check(self.lib.tvbg_serve_usage(self.h, 0, ctypes.byref(u), ctypes.byref(f)))
+        return u.value
+
+    def run(self):
+        "Tick until nothing is queued or active; returns the finished requests."
+        while True:
+            a, q = self.tick()
+            if a == 0 and q == 0:
+                return self.done
+
+
 def random_requests(n, rate, rng, conns, models=('Kuramoto', 'G2DO', 'MPR'), inst=(1, 4096),
                     steps=(1000, 100000), grad_frac=0.1, dt=0.1, t0=0.0):
     """Poisson arrivals at `rate` per second; model uniform, connectome
