@@ -512,6 +512,18 @@ int tvbg_group_occupancy(const tvbg_launch *cfg, int32_t *ctas_per_sm,
                          int32_t *sms);
 
 /*
+ * Region mapping (tvb_hpc/network.py:179-202).  to_avg: d_roi[i][j] = sum
+ * of d_node[k][j] over the nodes k with d_rmap[k] == i (RMapToAvg zeroes roi
+ * and accumulates: a sum), one CTA per region, a fixed reduction tree;
+ * from_avg: d_node[k][j] = d_roi[d_rmap[k]][j] (RMapFromAvg).  rmap entries
+ * outside [0, nroi) map to no region (their node rows are left unchanged).
+ */
+int tvbg_rmap_to_avg(int32_t nroi, int32_t nvar, int32_t nnode, const int32_t *d_rmap,
+                     const float *d_node, float *d_roi, void *stream);
+int tvbg_rmap_from_avg(int32_t nroi, int32_t nvar, int32_t nnode, const int32_t *d_rmap,
+                       const float *d_roi, float *d_node, void *stream);
+
+/*
  * ---- serving pool ---------------------------------------------------------
  * Continuous batching of sweep requests in native code: requests are copied
  * in (tvbg_serve_admit), admitted to the device when their footprint fits

@@ -1,6 +1,7 @@
 """
 The tvb_hpc API mirror (no GPU needed): attribute schema, coupling io and
-post-stat rules (tvb_hpc/tests.py:345-365), region maps (tests.py:453-473),
+post-stat rules (tvb_hpc/tests.py:345-365), region maps failing loudly
+without a device (their values: tests/test_gpu_rmap.py),
 connectivity CSR (network.py:66-78), synthetic connectomes, and the rule
 that models or couplings without a hand-written kernel are rejected.
 """
@@ -100,22 +101,15 @@ def test_synthetic_connectome_recipe():
     assert np.array_equal(w, w2)
 
 
-def test_rmap_to_avg():
+def test_rmap_needs_the_device():
+    "Region mapping runs on the GPU kernels only: without a device it fails loudly."
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip('a CUDA device is present')
     i = np.r_[:16].reshape((-1, 1))
-    rmap = i // 4
-    node = i.astype('f')
-    roi = np.zeros((4, 1), 'f')
-    network.RMapToAvg().kernel()(nroi=4, nvar=1, nnode=16, rmap=rmap, node=node, roi=roi)
-    np.testing.assert_allclose(roi[:, 0], node.reshape((4, 4)).sum(axis=1))
-
-
-def test_rmap_from_avg():
-    i = np.r_[:16].reshape((-1, 1))
-    rmap = i // 4
-    node = np.zeros((16, 1), 'f')
-    roi = np.r_[:4].reshape((4, 1)).astype('f')
-    network.RMapFromAvg().kernel()(nroi=4, nvar=1, nnode=16, rmap=rmap, node=node, roi=roi)
-    np.testing.assert_allclose(rmap, node)
+    with pytest.raises(RuntimeError):
+        network.RMapToAvg().kernel()(nroi=4, nvar=1, nnode=16, rmap=i // 4, node=i.astype('f'),
+                                     roi=np.zeros((4, 1), 'f'))
 
 
 def test_scheme_symbolics():

@@ -178,41 +178,51 @@ class RegionMappingMix:
     dtypes = {'roi,node': 'f', 'rmap,nroi,nvar,nnode': 'i'}
 
 
-def _as_torch(a):
+def _rmap_call(fn, nroi, nvar, nnode, rmap, src, dst):
+    """Run a region-mapping kernel on the device: numpy or CUDA-tensor
+    arguments, the result written into `dst` (numpy or tensor) in place."""
     import torch
-    if isinstance(a, torch.Tensor):
-        return a, False
-    return torch.from_numpy(np.ascontiguousarray(a)), True
+    from . import _native as nat
+    from .engine import _device_ok
+    _device_ok()
+    lib = nat.load()
+
+    np_of = {torch.int32: np.int32, torch.float32: np.float32}
+
+    def dev(a, dtype):
+        if isinstance(a, torch.Tensor):
+            return a.to(device='cuda', dtype=dtype).contiguous()
+        return torch.from_numpy(np.ascontiguousarray(np.asarray(a), dtype=np_of[dtype])).cuda()
+
+    rm = dev(rmap, torch.int32).reshape(-1)[:nnode].contiguous()
+    s = dev(src, torch.float32)
+    if isinstance(dst, torch.Tensor) and dst.is_cuda and dst.dtype == torch.float32 and dst.is_contiguous():
+        d = dst
+    else:
+        d = dev(dst, torch.float32)
+    nat.check(getattr(lib, fn)(int(nroi), int(nvar), int(nnode), rm.data_ptr(), s.data_ptr(),
+                               d.data_ptr(), nat.stream_handle()))
+    if d is not dst:
+        if isinstance(dst, np.ndarray):
+            dst[...] = d.cpu().numpy().reshape(dst.shape)
+        else:
+            dst.copy_(d.reshape(dst.shape))
 
 
 class RMapToAvg(RegionMappingMix):
-    "roi[rmap[k], j] += node[k, j] after zeroing roi (network.py:179-191)."
+    """roi[i, j] = sum of node[k, j] over rmap[k] == i (network.py:179-191:
+    roi is zeroed, then accumulated), on the device (tvbg_rmap_to_avg)."""
 
     def kernel(self, target=None):
         def knl(nroi, nvar, nnode, rmap, node, roi):
-            import torch
-            rm, _ = _as_torch(np.asarray(rmap).reshape(-1)[:nnode] if not hasattr(rmap, 'data_ptr') else rmap.reshape(-1)[:nnode])
-            nd, _ = _as_torch(node)
-            out = torch.zeros((nroi, nvar), dtype=nd.dtype, device=nd.device)
-            out.index_add_(0, rm.to(nd.device).long(), nd.reshape(nnode, nvar))
-            if isinstance(roi, np.ndarray):
-                roi[...] = out.cpu().numpy().reshape(roi.shape)
-            else:
-                roi.copy_(out.reshape(roi.shape))
+            _rmap_call('tvbg_rmap_to_avg', nroi, nvar, nnode, rmap, node, roi)
         return knl
 
 
 class RMapFromAvg(RegionMappingMix):
-    "node[k, j] = roi[rmap[k], j] (network.py:194-202)."
+    "node[k, j] = roi[rmap[k], j] (network.py:194-202), on the device (tvbg_rmap_from_avg)."
 
     def kernel(self, target=None):
         def knl(nroi, nvar, nnode, rmap, node, roi):
-            import torch
-            rm, _ = _as_torch(np.asarray(rmap).reshape(-1)[:nnode] if not hasattr(rmap, 'data_ptr') else rmap.reshape(-1)[:nnode])
-            ro, _ = _as_torch(roi)
-            out = ro.reshape(nroi, nvar)[rm.to(ro.device).long()]
-            if isinstance(node, np.ndarray):
-                node[...] = out.cpu().numpy().reshape(node.shape)
-            else:
-                node.copy_(out.reshape(node.shape))
+            _rmap_call('tvbg_rmap_from_avg', nroi, nvar, nnode, rmap, roi, node)
         return knl
