@@ -1126,6 +1126,7 @@ def serve_arm(args):
     st = srv.stats()
     offered = sum(r.node_steps for r in reqs) / max(args.serve_seconds, 1e-9)
     served = st['node_steps'] / wall
+    native = serve_native(args, conns)
     plain = serve_plain(reqs, budget_s=args.serve_plain_seconds)
     line = {'metric': METRIC, 'value': round(served, 1), 'unit': UNIT, 'n_gpus': 1,
             'steps': 1, 'warmup': 1, 'higher_is_better': True, 'scaling': 'weak',
@@ -1139,9 +1140,45 @@ def serve_arm(args):
                       'wall_s': round(wall, 3), 'ticks': st['ticks'], 'phase_s': st['phase_s'],
                       'offered_node_steps_per_s': round(offered, 1),
                       'queue_kept_up': bool(wall <= args.serve_seconds * 1.25)},
+            'native_pool': native,
             'plain': plain,
             'served_vs_plain': round(served / plain['value'], 3) if plain['value'] else None}
     print(json.dumps(line), flush=True)
+
+
+def serve_native(args, conns):
+    """The same arrival stream without the gradient requests, through the
+    native pool (tvbg_serve_*): requests submitted as they arrive, one tick
+    at a time; p50/p99 latency and node-steps/s over the wall time."""
+    from tvb_hpc import serve
+    reqs = [r for r in serve.random_requests(max(1, int(args.serve_rate * args.serve_seconds)),
+                                             args.serve_rate, np.random.default_rng(7), conns,
+                                             inst=(1, args.serve_max_inst), steps=(1000, 100000))
+            if not r.want_grad]
+    pool = serve.NativeServer(chunk=args.serve_chunk)
+    t0 = time.perf_counter()
+    for r in reqs:
+        r.arrival += t0
+    pending = sorted(reqs, key=lambda r: r.arrival)
+    ticks = 0
+    while True:
+        now = time.perf_counter()
+        while pending and pending[0].arrival <= now:
+            pool.submit(pending.pop(0))
+        a, q = pool.tick()
+        ticks += 1
+        if not pending and a == 0 and q == 0:
+            break
+        if a == 0 and q == 0 and pending:
+            time.sleep(max(0.0, min(0.05, pending[0].arrival - time.perf_counter())))
+    wall = time.perf_counter() - t0
+    pool.close()
+    lat = np.array([r.finished - r.arrival for r in reqs])
+    work = sum(r.node_steps for r in reqs)
+    return {'requests': len(reqs), 'p50_latency_s': round(float(np.percentile(lat, 50)), 3),
+            'p99_latency_s': round(float(np.percentile(lat, 99)), 3), 'wall_s': round(wall, 3),
+            'ticks': ticks, 'value': round(work / wall, 1), 'unit': UNIT,
+            'path': 'C++ pool (tvbg_serve_*), group kernel, requests without gradients'}
 
 
 def serve_plain(reqs, budget_s=20.0):

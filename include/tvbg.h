@@ -289,6 +289,11 @@ typedef struct tvbg_adjoint {
 
 int tvbg_adjoint_mpr(const tvbg_adjoint *d_adj, int32_t n_inst, int32_t threads,
                      void *stream);
+/* The same with the adjoint ring staged in smem_ring bytes of shared memory
+ * per CTA (loaded at the start, stored at the end of the call); an instance
+ * whose ring (N << lognh floats) does not fit uses its global ring. */
+int tvbg_adjoint_mpr_ex(const tvbg_adjoint *d_adj, int32_t n_inst, int32_t threads,
+                        int32_t smem_ring, void *stream);
 
 /*
  * Pearson FC per instance over T samples of N nodes, FP64 reduction.

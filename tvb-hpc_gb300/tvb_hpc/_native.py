@@ -235,6 +235,7 @@ SIGNATURES = {
     'tvbg_fc_noalloc': (ctypes.c_int, [_vp, _i32, _i32, _i32, _i64, _vp, _vp, _vp, _vp]),
     'tvbg_philox_normal': (ctypes.c_int, [_u64, _u32, _vp, _i64, _vp]),
     'tvbg_adjoint_mpr': (ctypes.c_int, [_vp, _i32, _i32, _vp]),
+    'tvbg_adjoint_mpr_ex': (ctypes.c_int, [_vp, _i32, _i32, _i32, _vp]),
     'tvbg_philox_u32': (ctypes.c_int, [_u32, _u32, _u32, _u32, _u32, _vp, _i64, _vp]),
     'tvbg_group_size': (_sz, []),
     'tvbg_net_size': (_sz, []),

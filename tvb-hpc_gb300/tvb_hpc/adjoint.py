@@ -27,7 +27,7 @@ import numpy as np
 
 from . import _native as nat
 from . import model as mdl, coupling as cpl, scheme as sch
-from .engine import InstanceSet, plan_ring
+from .engine import InstanceSet, plan_ring, max_smem
 from .utils import getLogger
 
 LOG = getLogger(__name__)
@@ -87,6 +87,7 @@ class FCFit:
         self.edges_t = torch.from_numpy(e_t.view(np.uint8).copy()).cuda()
         _, consts, _ = self.model.engine_spec()
         self.consts = consts
+        self.tpn = 2          # gather lanes per node of the forward and recomputation sweeps
 
     def _set(self, G, eta, trace_len, trace_nobs, trace_csum):
         return InstanceSet(self.model, self.cfun, self.scheme, self.conn, dt=self.dt,
@@ -129,7 +130,7 @@ class FCFit:
         self.ckpt = []
         for (t0, n), pl in zip(segs, plans):
             self.ckpt.append((t0, n, fw.state.clone(), fw.ring.clone()))
-            sw.launch(pl, 2)
+            sw.launch(pl, self.tpn)
         fw.t[:] = self.T
         torch.cuda.synchronize()
         sw.status.check()
@@ -202,12 +203,15 @@ class FCFit:
         row_bytes = I * nat.ADJOINT_DTYPE.itemsize
         # segments last first: recompute from the checkpoint (bit-identical to
         # the forward), then the reverse-time kernel over it, back to back
+        # the adjoint ring in shared memory when it fits one CTA
+        ring_b = 4 * N * nh
+        smem = ring_b if ring_b + 4096 <= max_smem() else 0
         for k, ((t0, n, st, rg), pl) in enumerate(zip(rev, plans)):
             rec.state.copy_(st)
             rec.ring.copy_(rg)
-            sw.launch(pl, 2)
-            nat.check(lib.tvbg_adjoint_mpr(dev.data_ptr() + k * row_bytes, I, threads,
-                                           nat.stream_handle()))
+            sw.launch(pl, self.tpn)
+            nat.check(lib.tvbg_adjoint_mpr_ex(dev.data_ptr() + k * row_bytes, I, threads, smem,
+                                              nat.stream_handle()))
         torch.cuda.synchronize()
         sw.status.check()
         return dGn.sum(1), deta
