@@ -757,16 +757,22 @@ def roofline_entry(wl, nsvar, kernel_ms_total, steps):
     # DRAM traffic of the step kernel from an ncu capture (profiles/traffic.json:
     # bytes per node-step measured on a capture case of this workload), per
     # bench step
-    traffic, tsrc = None, None
+    traffic, tsrc, compute = None, None, None
     tp = os.path.join(ROOT, 'profiles', 'traffic.json')
     if os.path.exists(tp):
         key = 'mixed' if wl['name'].startswith('mixed') else wl['name'].split('_')[0]
         t = json.load(open(tp)).get(key)
         if t:
-            traffic = round(t['dram_bytes_per_node_step'] * node_steps(wl))
+            if t.get('dram_bytes_per_node_step'):
+                traffic = round(t['dram_bytes_per_node_step'] * node_steps(wl))
             tsrc = t.get('source')
+            if 'issue_active_pct' in t:
+                # the second roof: the SM's issue slots and FP32 FMA pipe, from the same capture
+                compute = {'issue_active_pct': t['issue_active_pct'],
+                           'fma_pipe_pct': t['fma_pipe_pct'], 'binding': t['binding']}
     return {'bound': 'hbm', 'achieved': round(achieved, 1), 'peak': hbm, 'unit': 'GB/s',
             'frac': round(achieved / hbm, 4), 'traffic': traffic, 'traffic_source': tsrc,
+            'compute': compute,
             'peak_source': src, 'algorithmic_bytes_per_node_step': round(bpn, 2),
             'note': 'achieved = algorithmic bytes / event-timed kernel time; traffic = DRAM '
                     'bytes per bench step (part of the ring reads hit L2)'}

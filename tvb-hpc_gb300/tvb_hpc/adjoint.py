@@ -142,7 +142,10 @@ class FCFit:
         return loss
 
     def _fc_loss_grad(self, X):
-        "FP64 loss and dL/dX of the Pearson FC fit (batched GEMMs)."
+        """Loss and dL/dX of the Pearson FC fit (batched GEMMs).  The FC and
+        the loss -- reductions over time -- are FP64; dL/dZ = Z A, a sum
+        over N nodes per sample, is FP32 (the backward's precision), and
+        the per-node reductions over time of the chain rule are FP64."""
         I, T, N = X.shape
         P = N * (N - 1) / 2.0
         Xc = X - X.mean(1, keepdim=True)
@@ -154,7 +157,7 @@ class FCFit:
         loss = (D[:, iu[0], iu[1]] ** 2).sum(1) / P
         A = 2.0 * D / P
         A = A - self.torch.diag_embed(self.torch.diagonal(A, dim1=1, dim2=2))
-        gZ = Z @ A
+        gZ = (Z.float() @ A.float()).double()
         zg = (Z * gZ).sum(1, keepdim=True)
         dXc = (gZ - Z * zg) / nrm
         dX = dXc - dXc.mean(1, keepdim=True)
@@ -203,9 +206,12 @@ class FCFit:
         row_bytes = I * nat.ADJOINT_DTYPE.itemsize
         # segments last first: recompute from the checkpoint (bit-identical to
         # the forward), then the reverse-time kernel over it, back to back
-        # the adjoint ring in shared memory when it fits one CTA
+        # the adjoint ring in shared memory when it fits one CTA and the
+        # instances fit one wave of CTAs (with more, the CTAs the smaller
+        # global-ring footprint keeps resident together win: measured)
         ring_b = 4 * N * nh
-        smem = ring_b if ring_b + 4096 <= max_smem() else 0
+        sms = torch.cuda.get_device_properties(0).multi_processor_count
+        smem = ring_b if (ring_b + 4096 <= max_smem() and I <= sms) else 0
         for k, ((t0, n, st, rg), pl) in enumerate(zip(rev, plans)):
             rec.state.copy_(st)
             rec.ring.copy_(rg)
