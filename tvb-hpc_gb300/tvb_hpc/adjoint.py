@@ -87,7 +87,7 @@ class FCFit:
         self.edges_t = torch.from_numpy(e_t.view(np.uint8).copy()).cuda()
         _, consts, _ = self.model.engine_spec()
         self.consts = consts
-        self.tpn = 2          # gather lanes per node of the forward and recomputation sweeps
+        self.tpn = 1          # gather lanes per node of the forward and recomputation sweeps
 
     def _set(self, G, eta, trace_len, trace_nobs, trace_csum):
         return InstanceSet(self.model, self.cfun, self.scheme, self.conn, dt=self.dt,
