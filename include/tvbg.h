@@ -579,7 +579,8 @@ typedef struct tvbg_serve_request {
 
 /* A pool with `hbm_budget` bytes for admitted requests, advancing every
  * active request by up to `chunk` steps per tick on `stream` (NULL: its own
- * stream). */
+ * stream, created at the first tick).  Creating a pool and admitting
+ * requests (host planning only) touch no device. */
 int tvbg_serve_create(int64_t hbm_budget, int32_t chunk, void *stream, tvbg_serve **out);
 int tvbg_serve_destroy(tvbg_serve *pool);
 /* Copy a request in and queue it; *id identifies it.  Rejects requests whose

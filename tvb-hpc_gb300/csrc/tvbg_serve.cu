@@ -400,16 +400,7 @@ int tvbg_serve_create(int64_t hbm_budget, int32_t chunk, void* stream, tvbg_serv
     if (!p) return set_error(TVBG_EINVAL, "tvbg_serve_create: out of host memory");
     p->budget = hbm_budget;
     p->chunk = chunk;
-    if (stream) {
-        p->stream = static_cast<cudaStream_t>(stream);
-    } else {
-        cudaError_t e = cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking);
-        if (e != cudaSuccess) {
-            delete p;
-            return set_cuda_error(e, "tvbg_serve_create: stream");
-        }
-        p->own_stream = true;
-    }
+    p->stream = static_cast<cudaStream_t>(stream);  // NULL: the pool's own, made at the first tick
     *out = p;
     return TVBG_OK;
 }
@@ -420,7 +411,7 @@ int tvbg_serve_destroy(tvbg_serve* p) {
         release(*kv.second);
         delete kv.second;
     }
-    if (p->own_stream) cudaStreamDestroy(p->stream);
+    if (p->own_stream && p->stream) cudaStreamDestroy(p->stream);
     delete p;
     return TVBG_OK;
 }
@@ -478,6 +469,14 @@ int tvbg_serve_admit(tvbg_serve* p, const tvbg_serve_request* q, int64_t* id) {
 
 int tvbg_serve_tick(tvbg_serve* p, int32_t* n_active, int32_t* n_queued) {
     if (!p) return set_error(TVBG_EINVAL, "tvbg_serve_tick: null");
+    if (!p->stream) {
+        cudaError_t e = cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking);
+        if (e != cudaSuccess) {
+            p->stream = nullptr;
+            return set_cuda_error(e, "tvbg_serve_tick: stream");
+        }
+        p->own_stream = true;
+    }
     // admit in arrival order while the budget and the device allow
     while (!p->queue.empty()) {
         Request* r = p->queue.front();
