@@ -58,7 +58,7 @@ __device__ __forceinline__ void adjoint_segment(const tvbg_adjoint& a, AdjRing<S
             V = x[1];
             S = x[2];
             // the rate update of step t was clamped at 0 where it went negative
-            const float fr = (Delta / (pi * tau) + 2.0f * r * V) / tau;
+            const float fr = (Delta / (pi * tau) + 2.0f * r * V) * (1.0f / tau);  // as MPR::drift
             const float rpre = fmaf(dt, fr, r);
             mr = rpre >= 0.0f ? lr : 0.0f;
             mv = lv;

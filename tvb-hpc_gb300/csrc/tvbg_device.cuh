@@ -70,16 +70,18 @@ __device__ __forceinline__ void box_muller(uint32_t a, uint32_t b, float& z0, fl
 }
 
 // The same transform with CUDA's fast intrinsics (__logf, __sincosf of
-// 2 pi u2): used by the group kernel, where the generator is a sixth of the
-// step's instructions.  Its normals differ from box_muller's by a few units
-// in the last place (the intrinsics' documented error bounds, about 2^-21
-// absolute for __sincosf on [-pi, pi] after the range shift below and
-// relative 2^-21 for __logf), far below the state tolerance; the Philox
-// words, and so the stream, are the same.
+// 2 pi u2, and the radius as m rsqrtf(m)): used by the group kernel, where
+// the generator is a sixth of the step's instructions.  Its normals differ
+// from box_muller's by a few units in the last place (the intrinsics'
+// documented error bounds, about 2^-21 absolute for __sincosf on [-pi, pi]
+// after the range shift below, relative 2^-21 for __logf, 2 ulp for
+// rsqrtf), far below the state tolerance; the Philox words, and so the
+// stream, are the same.
 __device__ __forceinline__ void box_muller_fast(uint32_t a, uint32_t b, float& z0, float& z1) {
     const float u1 = (static_cast<float>(a >> 8) + 0.5f) * 5.9604644775390625e-8f;  // 2^-24
     const float u2 = static_cast<float>(b >> 8) * 5.9604644775390625e-8f;
-    const float r = sqrtf(-2.0f * __logf(u1));
+    const float m = -2.0f * __logf(u1);  // > 0: u1 < 1
+    const float r = m * rsqrtf(m);
     float s, c;
     // angle in [-pi, pi): the intrinsics are most accurate near zero
     __sincosf(kTwoPiBM * (u2 - 0.5f), &s, &c);
@@ -151,7 +153,7 @@ struct G2DO {
         const float V2 = V * V;
         const float V3 = V2 * V;
         fo[0] = d * tau * (alpha * W - f * V3 + e * V2 + g * V + gamma * I + gamma * c0);
-        fo[1] = d * (a + b * V + c * V2 - beta * W) / tau;
+        fo[1] = d * (a + b * V + c * V2 - beta * W) * (1.0f / tau);
     }
     __device__ static __forceinline__ float obs(const float* x, int k) { return k == 0 ? x[0] : x[1]; }
     __device__ static __forceinline__ void limit(float*, uint32_t) {}
@@ -178,7 +180,7 @@ struct G2DOsc {
         const float V2 = V * V;
         const float V3 = V2 * V;
         fo[0] = d * tau * (alpha * W - f * V3 + e * V2 + g * V + gamma * I + gamma * c0);
-        fo[1] = d * (a + b * V + c * V2 - beta * W) / tau;
+        fo[1] = d * (a + b * V + c * V2 - beta * W) * (1.0f / tau);
     }
     __device__ static __forceinline__ float obs(const float* x, int k) { return k == 0 ? x[0] : x[1]; }
     __device__ static __forceinline__ void limit(float*, uint32_t) {}
@@ -200,8 +202,11 @@ struct MPR {
         const float Delta = K[0], J = K[1], tau = K[2], I = K[3];
         const float pi = 3.14159265358979323846f;
         const float ptr = pi * tau * r;
-        f[0] = (Delta / (pi * tau) + 2.0f * r * V) / tau;
-        f[1] = (V * V + p[0] + J * tau * r + I + c - ptr * ptr) / tau;
+        // 1 / tau is loop-invariant: one reciprocal per launch instead of a
+        // division per step
+        const float inv_tau = 1.0f / tau;
+        f[0] = (Delta / (pi * tau) + 2.0f * r * V) * inv_tau;
+        f[1] = (V * V + p[0] + J * tau * r + I + c - ptr * ptr) * inv_tau;
     }
     __device__ static __forceinline__ float obs(const float* x, int k) { return k == 0 ? x[0] : x[1]; }
     __device__ static __forceinline__ void limit(float* x, uint32_t flags) {
@@ -242,7 +247,7 @@ struct RWW {
         const float xx = w * J * S + io + J * c;
         const float y = a * xx - b;
         const float h = y / (1.0f - expf(-d * y));
-        f[0] = -(S / ts) + (1.0f - S) * h * g;
+        f[0] = -(S * (1.0f / ts)) + (1.0f - S) * h * g;
     }
     __device__ static __forceinline__ float obs(const float* x, int) { return x[0]; }
     __device__ static __forceinline__ void limit(float*, uint32_t) {}
