@@ -80,8 +80,9 @@ __device__ __forceinline__ void box_muller(uint32_t a, uint32_t b, float& z0, fl
 __device__ __forceinline__ void box_muller_fast(uint32_t a, uint32_t b, float& z0, float& z1) {
     const float u1 = (static_cast<float>(a >> 8) + 0.5f) * 5.9604644775390625e-8f;  // 2^-24
     const float u2 = static_cast<float>(b >> 8) * 5.9604644775390625e-8f;
-    const float m = -2.0f * __logf(u1);  // > 0: u1 < 1
-    const float r = m * rsqrtf(m);
+    // u1 rounds to 1 for the largest words, where m = 0 and the radius is 0
+    const float m = -2.0f * __logf(u1);
+    const float r = m > 0.0f ? m * rsqrtf(m) : 0.0f;
     float s, c;
     // angle in [-pi, pi): the intrinsics are most accurate near zero
     __sincosf(kTwoPiBM * (u2 - 0.5f), &s, &c);
