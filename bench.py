@@ -1082,18 +1082,36 @@ def cpu_baseline_mixed(wl, budget_s=12.0):
         n_inst = min(p['couplings'].size, cores)
         delays = np.stack([c.delays(s, wl['dt'], 'ceil') for s in p['speeds'][:n_inst]])
         nh = int(2 ** np.ceil(np.log2(delays.max() + 2)))
-        nsteps = int(max(50, budget_s / len(wl['parts']) * 2e7 / (c.nnz * n_inst / cores + 1)))
-        nsteps = min(nsteps, 5000)
-        t = time.perf_counter()
-        orc.run(kid, 0, c.row, c.col, c.wnz, nh, nsteps, wl['dt'], delays,
-                p['couplings'][:n_inst], p['nparam'][:n_inst, :, 0], p['x0'][:n_inst],
-                flags=orc.F_NOISE, sigma=sigma, consts=consts, seed=p['seed'], nthreads=cores)
-        el = time.perf_counter() - t
+        def run(nsteps):
+            t = time.perf_counter()
+            orc.run(kid, 0, c.row, c.col, c.wnz, nh, nsteps, wl['dt'], delays,
+                    p['couplings'][:n_inst], p['nparam'][:n_inst, :, 0], p['x0'][:n_inst],
+                    flags=orc.F_NOISE, sigma=sigma, consts=consts, seed=p['seed'], nthreads=cores)
+            return time.perf_counter() - t
+
+        probe = 100
+        per_step = run(probe) / probe
+        nsteps = int(np.clip(budget_s / len(wl['parts']) / max(per_step, 1e-9), probe, 50000))
+        el = run(nsteps)
         done_ns += n_inst * c.nnode * nsteps
         el_tot += el
         desc.append('N=%d: %d inst x %d steps' % (c.nnode, n_inst, nsteps))
+    # the second shape: one instance per call on one core, as the
+    # reference's examples run their sweeps (hackathon.py:67-69)
+    c = wl['parts'][0]['conn']
+    p = wl['parts'][0]
+    d1 = c.delays(p['speeds'][0], wl['dt'], 'ceil')[None]
+    nh = int(2 ** np.ceil(np.log2(d1.max() + 2)))
+    n1 = 2000
+    t = time.perf_counter()
+    orc.run(kid, 0, c.row, c.col, c.wnz, nh, n1, wl['dt'], d1, p['couplings'][:1],
+            p['nparam'][:1, :, 0], p['x0'][:1], flags=orc.F_NOISE, sigma=sigma, consts=consts,
+            seed=p['seed'], nthreads=1)
+    one = c.nnode * n1 / (time.perf_counter() - t)
     return {'value': round(done_ns / el_tot, 1), 'unit': UNIT, 'cores': cores, 'kind': 'port',
-            'sample': '; '.join(desc) + ' (%.1f s), oracle C + OpenMP, -O3' % el_tot}
+            'sample': '; '.join(desc) + ' (%.1f s), oracle C + OpenMP, -O3' % el_tot,
+            'one_instance_one_core': {'value': round(one, 1), 'unit': UNIT,
+                                      'sample': 'N=%d, 1 instance x %d steps' % (c.nnode, n1)}}
 
 
 def serve_arm(args):
