@@ -272,3 +272,21 @@ def test_oracle_hmje_pinned_on_tvb_hpc_model(tmp_path):
         assert err < 1e-5, err
     np.testing.assert_allclose(got['expo'][..., 3], got['state'][..., 3] - got['state'][..., 0],
                                rtol=1e-6, atol=1e-6)
+
+
+def test_generated_library_exports_every_declared_symbol():
+    "Every entry point include/tvbg_lems.h declares is exported by a generated library."
+    import re
+    import subprocess
+    text = open(os.path.join(os.path.dirname(lems.INCLUDE), 'include', 'tvbg_lems.h')).read()
+    text = re.sub(r'/\*.*?\*/', '', text, flags=re.S)
+    syms = sorted(set(re.findall(r'\b(tvbg_lems_[a-z0-9_]+)\s*\(', text)))
+    assert len(syms) >= 8
+    L = lems.LemsLibrary(lems.load_model('Ou'))
+    out = subprocess.run(['nm', '-D', '--defined-only', L.path], capture_output=True, text=True,
+                         check=True).stdout
+    exported = set(line.split()[-1] for line in out.splitlines() if ' T ' in line)
+    assert not [s for s in syms if s not in exported]
+    assert set(lems.SIGNATURES) == set(syms)
+    # nothing else leaks out of the generated library
+    assert not [s for s in exported if s.startswith('tvbg') and s not in syms]
