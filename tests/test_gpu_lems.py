@@ -294,3 +294,25 @@ def test_lems_noise_scale_per_variable(cuda, kind):
     nsig = np.sqrt(np.float32(0.1)) * np.float32(0.1)
     var = nsig ** 2 / (1 - (1 - 0.5 * 0.1) ** 2)
     assert abs(x[:, 0].var() / var - 1) < 5 * np.sqrt(2.0 / x.shape[0])
+
+
+def test_dsl_launcher_interface(cuda):
+    """tvb_hpc.dsl.CudaRun.run_simulation with the DSL launcher's arguments
+    (cuda_run.py:70-147; parameters from cuda_setup.py:88-101) runs the
+    bundled Kuramoto file and returns its tavg layout."""
+    import types
+    from tvb_hpc import dsl
+    w, ln = network.synthetic_connectome(30, 0.3, seed=6)
+    couplings, speeds = dsl.setup_params(4, 2)
+    params = dsl.expand_params(couplings * 1e-3, speeds * 2.0)
+    args = types.SimpleNamespace(model='Kuramoto')
+    tavg = dsl.CudaRun().run_simulation(w, ln, params, speeds, None, args, 30, 8, 2, 3, 40, 1024, 1,
+                                        0.1, float(speeds.min()))
+    assert tavg.shape == (3, 60, 8)
+    conn = network.Connectivity.from_dense(w, ln)
+    ref = lo.run(lems.lems_file('Kuramoto'), 'Kuramoto', conn.row, conn.col, conn.wnz, conn.lnz,
+                 params, 0.1, 120)
+    np.testing.assert_allclose(tavg[-1, 30:, :].T, ref['expo'][:, :, 1], atol=1e-4)
+    with pytest.raises(ValueError):
+        dsl.CudaRun().run_simulation(w, ln, params, speeds, None, args, 30, 8, 2, 3, 40, 1024, 2,
+                                     0.1, 1.0)
