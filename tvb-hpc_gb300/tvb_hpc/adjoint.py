@@ -88,6 +88,7 @@ class FCFit:
         _, consts, _ = self.model.engine_spec()
         self.consts = consts
         self.tpn = 1          # gather lanes per node of the forward and recomputation sweeps
+        self.adjoint_smem = 'auto'   # adjoint ring in shared memory: 'auto' or False
 
     def _set(self, G, eta, trace_len, trace_nobs, trace_csum):
         return InstanceSet(self.model, self.cfun, self.scheme, self.conn, dt=self.dt,
@@ -211,7 +212,8 @@ class FCFit:
         # global-ring footprint keeps resident together win: measured)
         ring_b = 4 * N * nh
         sms = torch.cuda.get_device_properties(0).multi_processor_count
-        smem = ring_b if (ring_b + 4096 <= max_smem() and I <= sms) else 0
+        smem = ring_b if (self.adjoint_smem == 'auto' and ring_b + 4096 <= max_smem()
+                          and I <= sms) else 0
         for k, ((t0, n, st, rg), pl) in enumerate(zip(rev, plans)):
             rec.state.copy_(st)
             rec.ring.copy_(rg)
