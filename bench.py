@@ -1195,8 +1195,6 @@ def serve_native(args, conns):
             break
         if a == 0 and q == 0 and pending:
             time.sleep(max(0.0, min(0.05, pending[0].arrival - time.perf_counter())))
-        else:
-            time.sleep(2e-4)          # ticks do not wait for the device
     wall = time.perf_counter() - t0
     pool.close()
     lat = np.array([r.finished - r.arrival for r in reqs])
@@ -1204,8 +1202,7 @@ def serve_native(args, conns):
     return {'requests': len(reqs), 'p50_latency_s': round(float(np.percentile(lat, 50)), 3),
             'p99_latency_s': round(float(np.percentile(lat, 99)), 3), 'wall_s': round(wall, 3),
             'ticks': ticks, 'value': round(work / wall, 1), 'unit': UNIT,
-            'path': 'C++ pool (tvbg_serve_*): per-request streams, two chunks in flight, '
-                    'group kernel; requests without gradients'}
+            'path': 'C++ pool (tvbg_serve_*), group kernel, requests without gradients'}
 
 
 def serve_plain(reqs, budget_s=20.0):

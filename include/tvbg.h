@@ -532,10 +532,10 @@ int tvbg_rmap_from_avg(int32_t nroi, int32_t nvar, int32_t nnode, const int32_t 
  * ---- serving pool ---------------------------------------------------------
  * Continuous batching of sweep requests in native code: requests are copied
  * in (tvbg_serve_admit), admitted to the device when their footprint fits
- * the pool's HBM budget, advanced independently -- each request's
- * lane-interleaved groups on its own stream, up to two chunks of steps in
- * flight -- retired when done (final state copied out, device memory
- * freed), and polled or cancelled by id.  The pool is
+ * the pool's HBM budget, advanced together one chunk of steps per
+ * tvbg_serve_tick (each request's lane-interleaved groups on its own
+ * stream, joined into the pool's), retired when done (final state copied
+ * out, device memory freed), and polled or cancelled by id.  The pool is
  * the one object that allocates device memory behind its calls: it is
  * created and destroyed explicitly.  The reference has no serving layer;
  * its DSL launcher runs one sweep per call
@@ -577,26 +577,24 @@ typedef struct tvbg_serve_request {
 #define TVBG_SERVE_DONE 2
 #define TVBG_SERVE_CANCELLED 3
 
-/* A pool with `hbm_budget` bytes for admitted requests, launched in chunks
- * of up to `chunk` steps.  Admitted requests start after the work enqueued
- * on `stream` at their admission (NULL: no ordering).  Creating a pool and
- * admitting requests (host planning only) touch no device. */
+/* A pool with `hbm_budget` bytes for admitted requests, advancing every
+ * active request by up to `chunk` steps per tick on `stream` (NULL: its own
+ * stream, created at the first tick).  Creating a pool and admitting
+ * requests (host planning only) touch no device. */
 int tvbg_serve_create(int64_t hbm_budget, int32_t chunk, void *stream, tvbg_serve **out);
 int tvbg_serve_destroy(tvbg_serve *pool);
 /* Copy a request in and queue it; *id identifies it.  Rejects requests whose
  * delays are shorter than the group kernel's blocks (d_min < 3) or whose
  * footprint exceeds the whole budget. */
 int tvbg_serve_admit(tvbg_serve *pool, const tvbg_serve_request *req, int64_t *id);
-/* Admit queued requests that fit, keep every active one at two chunks in
- * flight, retire those whose last chunk has finished; does not wait for the
- * device (call it again to make progress).  *n_active and *n_queued
- * (either may be NULL) count what is left. */
+/* Admit queued requests that fit, advance every active one by one chunk,
+ * retire the finished; waits for this tick's device work.  *n_active and
+ * *n_queued (either may be NULL) count what is left. */
 int tvbg_serve_tick(tvbg_serve *pool, int32_t *n_active, int32_t *n_queued);
 /* *status = TVBG_SERVE_*; once done, the final state is copied to
  * state_out (host [n_inst][N][nsvar]) when it is not NULL. */
 int tvbg_serve_poll(tvbg_serve *pool, int64_t id, int32_t *status, float *state_out);
-/* Drop a queued or active request (an active one's chunks in flight are
- * waited for, then its device memory is freed). */
+/* Drop a queued or active request (its device memory is freed at once). */
 int tvbg_serve_cancel(tvbg_serve *pool, int64_t id);
 /* Device bytes held by admitted requests and the footprint of request id. */
 int tvbg_serve_usage(tvbg_serve *pool, int64_t id, int64_t *used, int64_t *footprint);

@@ -11,14 +11,12 @@
 // 1024 threads).  Its device buffers are one allocation made when the
 // request is admitted: when its footprint fits the budget and the device.
 //
-// Requests advance independently, with no barrier across them: each keeps
-// up to two chunks in flight on its own stream (a chunk = the group records
-// for its steps, uploaded into one of two record slots, then one group
-// launch per block length, then an event).  A tick admits what fits, takes
-// note of the chunks whose events have completed, tops every request up to
-// two chunks in flight, and retires the requests whose last chunk is done
-// (status word checked, state gathered from the lanes to the host, device
-// memory freed).  A tick does not wait for the device.
+// A tick uploads every active request's group records for its next chunk
+// (t0, steps per lane) and launches its groups -- one launch per block
+// length -- on the request's own stream; the streams join the pool's
+// stream, the pool waits, checks each request's device status word, and
+// retires finished requests (state gathered from the lanes to the host,
+// device memory freed).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -92,11 +90,8 @@ struct Request {
     // device
     char* dev = nullptr;
     cudaStream_t stream = nullptr;
-    cudaEvent_t ev[2] = {nullptr, nullptr};   // per record slot: its chunk is done
-    std::vector<tvbg_group> records;          // host copy of the records, set per chunk
-    int64_t enqueued = 0;                     // steps launched
-    int64_t chunk_steps[2] = {0, 0};          // steps of the chunk in each slot
-    int head = 0, inflight = 0;               // oldest slot in flight, chunks in flight
+    cudaEvent_t done_ev = nullptr;
+    std::vector<tvbg_group> records;
     std::vector<float> result;        // [n_inst][N][ns] once done
 };
 
@@ -214,8 +209,8 @@ int plan(Request& r, const tvbg_serve_request& q) {
     o = align_up(o + static_cast<size_t>(G) * N * ns * L * sizeof(float));
     r.off_nparam = o;
     o = align_up(o + static_cast<size_t>(G) * N * np * L * sizeof(float));
-    r.off_groups = o;                 // two record slots of G records
-    o = align_up(o + 2 * static_cast<size_t>(G) * sizeof(tvbg_group));
+    r.off_groups = o;
+    o = align_up(o + static_cast<size_t>(G) * sizeof(tvbg_group));
     r.off_order = o;
     o = align_up(o + std::max<size_t>(1, r.order.size()) * sizeof(int32_t));
     r.off_status = o;
@@ -232,8 +227,7 @@ int materialise(Request& r) {
         return set_cuda_error(e, "tvbg_serve: cudaMalloc");
     }
     e = cudaStreamCreateWithFlags(&r.stream, cudaStreamNonBlocking);
-    for (int k = 0; k < 2 && e == cudaSuccess; ++k)
-        e = cudaEventCreateWithFlags(&r.ev[k], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&r.done_ev, cudaEventDisableTiming);
     if (e != cudaSuccess) return set_cuda_error(e, "tvbg_serve: stream");
     const int N = r.N, ns = r.shape.ns, np = r.npar, G = static_cast<int>(r.members.size());
     // lane-interleaved state and parameters [G][N][*][L]
@@ -323,30 +317,25 @@ int materialise(Request& r) {
 void release(Request& r) {
     if (r.stream) cudaStreamSynchronize(r.stream);
     if (r.dev) cudaFree(r.dev);
-    for (int k = 0; k < 2; ++k)
-        if (r.ev[k]) cudaEventDestroy(r.ev[k]);
+    if (r.done_ev) cudaEventDestroy(r.done_ev);
     if (r.stream) cudaStreamDestroy(r.stream);
     r.dev = nullptr;
     r.stream = nullptr;
-    r.ev[0] = r.ev[1] = nullptr;
+    r.done_ev = nullptr;
     r.records.clear();
     r.records.shrink_to_fit();
 }
 
-// Enqueue the next `steps` steps (from r.enqueued) of every group of r on
-// r.stream, in record slot `slot`, and record that slot's event.
-int launch_chunk(Request& r, int64_t steps, int slot) {
+// Enqueue the next `steps` steps of every group of r on r.stream.
+int launch_chunk(Request& r, int64_t steps) {
     const int G = static_cast<int>(r.records.size());
     for (int g = 0; g < G; ++g) {
         tvbg_group& rec = r.records[g];
-        rec.t0 = r.enqueued;
+        rec.t0 = r.done;
         rec.nsteps = static_cast<int32_t>(steps);
         for (size_t l = 0; l < r.members[g].size(); ++l) rec.lanes[l].nsteps = static_cast<int32_t>(steps);
     }
-    tvbg_group* d_rec = reinterpret_cast<tvbg_group*>(r.dev + r.off_groups) + static_cast<size_t>(slot) * G;
-    // from pageable memory: the call returns once the records are staged,
-    // so the host copy may change for the next chunk
-    cudaError_t e = cudaMemcpyAsync(d_rec, r.records.data(), G * sizeof(tvbg_group),
+    cudaError_t e = cudaMemcpyAsync(r.dev + r.off_groups, r.records.data(), G * sizeof(tvbg_group),
                                     cudaMemcpyHostToDevice, r.stream);
     if (e != cudaSuccess) return set_cuda_error(e, "tvbg_serve: group records");
     static const ErrSink sink{set_error, set_cuda_error};
@@ -362,13 +351,12 @@ int launch_chunk(Request& r, int64_t steps, int slot) {
         GroupKernel k = lookup_group_kernel(r.model, r.cfun, r.k_list[i]);
         if (!k) return set_error(TVBG_EUNSUPPORTED, "tvbg_serve: group kernel not built");
         const size_t smem = group_smem_bytes(cfg.block_k, cfg.threads, group_channels(cfg.cfun));
-        int rc = launch_group_kernel(k, d_rec, r.k_count[i], &cfg, r.cluster, smem, r.stream, sink);
+        int rc = launch_group_kernel(k, reinterpret_cast<const tvbg_group*>(r.dev + r.off_groups),
+                                     r.k_count[i], &cfg, r.cluster, smem, r.stream, sink);
         if (rc) return rc;
     }
-    e = cudaEventRecord(r.ev[slot], r.stream);
+    e = cudaEventRecord(r.done_ev, r.stream);
     if (e != cudaSuccess) return set_cuda_error(e, "tvbg_serve: event");
-    r.chunk_steps[slot] = steps;
-    r.enqueued += steps;
     return TVBG_OK;
 }
 
@@ -397,6 +385,7 @@ struct tvbg_serve {
     int64_t budget = 0, used = 0;
     int32_t chunk = 0;
     cudaStream_t stream = nullptr;
+    bool own_stream = false;
     int64_t next_id = 1;
     std::deque<Request*> queue;
     std::vector<Request*> active;
@@ -411,7 +400,7 @@ int tvbg_serve_create(int64_t hbm_budget, int32_t chunk, void* stream, tvbg_serv
     if (!p) return set_error(TVBG_EINVAL, "tvbg_serve_create: out of host memory");
     p->budget = hbm_budget;
     p->chunk = chunk;
-    p->stream = static_cast<cudaStream_t>(stream);  // NULL: no ordering with the caller's work
+    p->stream = static_cast<cudaStream_t>(stream);  // NULL: the pool's own, made at the first tick
     *out = p;
     return TVBG_OK;
 }
@@ -422,6 +411,7 @@ int tvbg_serve_destroy(tvbg_serve* p) {
         release(*kv.second);
         delete kv.second;
     }
+    if (p->own_stream && p->stream) cudaStreamDestroy(p->stream);
     delete p;
     return TVBG_OK;
 }
@@ -479,6 +469,14 @@ int tvbg_serve_admit(tvbg_serve* p, const tvbg_serve_request* q, int64_t* id) {
 
 int tvbg_serve_tick(tvbg_serve* p, int32_t* n_active, int32_t* n_queued) {
     if (!p) return set_error(TVBG_EINVAL, "tvbg_serve_tick: null");
+    if (!p->stream) {
+        cudaError_t e = cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking);
+        if (e != cudaSuccess) {
+            p->stream = nullptr;
+            return set_cuda_error(e, "tvbg_serve_tick: stream");
+        }
+        p->own_stream = true;
+    }
     // admit in arrival order while the budget and the device allow
     while (!p->queue.empty()) {
         Request* r = p->queue.front();
@@ -495,48 +493,52 @@ int tvbg_serve_tick(tvbg_serve* p, int32_t* n_active, int32_t* n_queued) {
         p->used += static_cast<int64_t>(r->bytes);
         r->status = TVBG_SERVE_ACTIVE;
         p->active.push_back(r);
-        if (p->stream) {  // the request's work starts after the caller's work on the pool stream
-            cudaEvent_t after;
-            e = cudaEventCreateWithFlags(&after, cudaEventDisableTiming);
-            if (e == cudaSuccess) e = cudaEventRecord(after, p->stream);
-            if (e == cudaSuccess) e = cudaStreamWaitEvent(r->stream, after, 0);
-            cudaEventDestroy(after);
-            if (e != cudaSuccess) return set_cuda_error(e, "tvbg_serve_tick: stream order");
+    }
+    // one chunk for every active request, each on its stream, joined into the pool's
+    cudaEvent_t start;
+    cudaError_t e = cudaEventCreateWithFlags(&start, cudaEventDisableTiming);
+    if (e != cudaSuccess) return set_cuda_error(e, "tvbg_serve_tick: event");
+    e = cudaEventRecord(start, p->stream);
+    std::vector<int64_t> steps(p->active.size());
+    int rc = e == cudaSuccess ? TVBG_OK : set_cuda_error(e, "tvbg_serve_tick: event");
+    for (size_t i = 0; i < p->active.size() && rc == TVBG_OK; ++i) {
+        Request& r = *p->active[i];
+        steps[i] = std::min<int64_t>(p->chunk, r.nsteps - r.done);
+        e = cudaStreamWaitEvent(r.stream, start, 0);
+        if (e != cudaSuccess) {
+            rc = set_cuda_error(e, "tvbg_serve_tick: wait");
+            break;
+        }
+        if (steps[i] > 0) rc = launch_chunk(r, steps[i]);
+        else if (cudaEventRecord(r.done_ev, r.stream) != cudaSuccess)
+            rc = set_error(TVBG_ECUDA, "tvbg_serve_tick: event");
+        if (rc == TVBG_OK) {
+            e = cudaStreamWaitEvent(p->stream, r.done_ev, 0);
+            if (e != cudaSuccess) rc = set_cuda_error(e, "tvbg_serve_tick: join");
         }
     }
+    cudaEventDestroy(start);
+    if (rc) return rc;
+    e = cudaStreamSynchronize(p->stream);
+    if (e != cudaSuccess) return set_cuda_error(e, "tvbg_serve_tick: synchronize");
+    // status words, clocks, retirement
     std::vector<Request*> keep;
-    for (Request* rp : p->active) {
-        Request& r = *rp;
-        // chunks that have finished
-        while (r.inflight > 0) {
-            const cudaError_t q = cudaEventQuery(r.ev[r.head]);
-            if (q == cudaErrorNotReady) break;
-            if (q != cudaSuccess) return set_cuda_error(q, "tvbg_serve_tick: chunk");
-            r.done += r.chunk_steps[r.head];
-            r.head ^= 1;
-            --r.inflight;
-        }
-        // top up to two chunks in flight
-        while (r.inflight < 2 && r.enqueued < r.nsteps) {
-            const int64_t steps = std::min<int64_t>(p->chunk, r.nsteps - r.enqueued);
-            int rc = launch_chunk(r, steps, (r.head + r.inflight) & 1);
-            if (rc) return rc;
-            ++r.inflight;
-        }
-        if (r.done < r.nsteps) {
-            keep.push_back(&r);
-            continue;
-        }
-        // retire: the stream is idle
+    for (size_t i = 0; i < p->active.size(); ++i) {
+        Request& r = *p->active[i];
         int32_t st = 0;
-        cudaError_t e = cudaMemcpy(&st, r.dev + r.off_status, sizeof(st), cudaMemcpyDeviceToHost);
+        e = cudaMemcpy(&st, r.dev + r.off_status, sizeof(st), cudaMemcpyDeviceToHost);
         if (e != cudaSuccess) return set_cuda_error(e, "tvbg_serve_tick: status");
         if (st != 0) return set_error(TVBG_EDEVICE, "tvbg_serve_tick: a group kernel reported an error");
-        int rc = collect(r);
-        if (rc) return rc;
-        release(r);
-        p->used -= static_cast<int64_t>(r.bytes);
-        r.status = TVBG_SERVE_DONE;
+        r.done += steps[i];
+        if (r.done >= r.nsteps) {
+            rc = collect(r);
+            if (rc) return rc;
+            release(r);
+            p->used -= static_cast<int64_t>(r.bytes);
+            r.status = TVBG_SERVE_DONE;
+        } else {
+            keep.push_back(&r);
+        }
     }
     p->active.swap(keep);
     if (n_active) *n_active = static_cast<int32_t>(p->active.size());

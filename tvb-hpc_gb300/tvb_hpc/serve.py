@@ -317,11 +317,10 @@ class Server:
 
 class NativeServer:
     """
-    The serving pool in native code (tvbg_serve_*): continuous batching of
-    requests without gradients in the C++ pool -- requests copied in,
-    admitted by the HBM budget, each advanced on its own stream with two
-    chunks in flight (no barrier across requests), retired, polled and
-    cancelled by id; tick() never waits for the device.
+    The serving pool in native code (tvbg_serve_*): the same continuous
+    batching as Server for requests without gradients, run by the C++ pool
+    -- requests copied in, admitted by the HBM budget, advanced one chunk
+    per tick on per-request streams, retired, polled and cancelled by id.
     Each request's result equals lane-interleaved groups of the same inputs
     (GroupSet), alone or in any mix.
     """
@@ -445,13 +444,12 @@ class NativeServer:
         self.nat.check(self.lib.tvbg_serve_usage(self.h, 0, ctypes.byref(u), ctypes.byref(f)))
         return u.value
 
-    def run(self, poll_s=2e-4):
+    def run(self):
         "Tick until nothing is queued or active; returns the finished requests."
         while True:
             a, q = self.tick()
             if a == 0 and q == 0:
                 return self.done
-            time.sleep(poll_s)      # ticks do not wait for the device
 
 
 def random_requests(n, rate, rng, conns, models=('Kuramoto', 'G2DO', 'MPR'), inst=(1, 4096),
