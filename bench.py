@@ -1133,10 +1133,11 @@ def serve_arm(args):
     n_req = max(1, int(args.serve_rate * args.serve_seconds))
     reqs = serve.random_requests(n_req, args.serve_rate, rng, conns,
                                  inst=(1, args.serve_max_inst), steps=(1000, 100000))
-    # warm-up: load every kernel once
+    # warm-up: load every kernel once, the FC-fit gradient path's library
+    # GEMMs included (their first call on a fresh process is slow)
     warm = serve.Server(chunk=args.serve_chunk)
-    for r in serve.random_requests(6, 1e6, np.random.default_rng(1), conns[:2], inst=(1, 2),
-                                   steps=(200, 300), grad_frac=0.0):
+    for r in serve.random_requests(8, 1e6, np.random.default_rng(1), conns[:2], inst=(1, 2),
+                                   steps=(200, 300), grad_frac=1.0):
         warm.submit(r)
     warm.run()
     torch.cuda.synchronize()
