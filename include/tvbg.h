@@ -517,6 +517,16 @@ int tvbg_group_occupancy(const tvbg_launch *cfg, int32_t *ctas_per_sm,
                          int32_t *sms);
 
 /*
+ * dL/dZ = Z A of the FC-fit loss for n_inst instances: d_z [n_inst][T][N]
+ * (normalised, centred series), d_a [n_inst][N][N], d_out [n_inst][T][N],
+ * FP32 (a sum over the N nodes per sample; the FC and the loss, sums over
+ * time, are FP64 in the caller).  Used by the FC-fit adjoint
+ * (tvb_hpc.adjoint.FCFit); no counterpart in the reference.
+ */
+int tvbg_fcfit_zgrad(const float *d_z, const float *d_a, float *d_out, int32_t n_inst,
+                    int32_t T, int32_t N, void *stream);
+
+/*
  * Region mapping (tvb_hpc/network.py:179-202).  to_avg: d_roi[i][j] = sum
  * of d_node[k][j] over the nodes k with d_rmap[k] == i (RMapToAvg zeroes roi
  * and accumulates: a sum), one CTA per region, a fixed reduction tree;

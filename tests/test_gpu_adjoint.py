@@ -72,3 +72,19 @@ def test_adjoint_autograd_function(cuda):
     dG, deta = prob2.backward()
     np.testing.assert_allclose(Gt.grad.cpu().numpy(), dG.cpu().numpy(), rtol=1e-6)
     np.testing.assert_allclose(et.grad.cpu().numpy(), deta.cpu().numpy(), rtol=1e-6, atol=1e-12)
+
+
+def test_fcfit_zgrad_kernel(cuda):
+    "tvbg_fcfit_zgrad (dL/dZ = Z A, FP32) against an FP64 product, ragged sizes."
+    import ctypes
+    from tvb_hpc import _native as nat
+    torch = cuda
+    lib = nat.load()
+    g = torch.Generator(device='cuda').manual_seed(0)
+    for I, T, N in ((3, 130, 84), (1, 2000, 998), (5, 64, 17)):
+        Z = torch.randn(I, T, N, device='cuda', generator=g) / np.sqrt(T)
+        A = torch.randn(I, N, N, device='cuda', generator=g) / N
+        out = torch.empty_like(Z)
+        nat.check(lib.tvbg_fcfit_zgrad(Z.data_ptr(), A.data_ptr(), out.data_ptr(), I, T, N, None))
+        ref = Z.double() @ A.double()
+        assert rel_err(out.cpu().numpy(), ref.cpu().numpy()) < 1e-5

@@ -158,7 +158,11 @@ class FCFit:
         loss = (D[:, iu[0], iu[1]] ** 2).sum(1) / P
         A = 2.0 * D / P
         A = A - self.torch.diag_embed(self.torch.diagonal(A, dim1=1, dim2=2))
-        gZ = (Z.float() @ A.float()).double()
+        Z32, A32 = Z.float().contiguous(), A.float().contiguous()
+        gZ32 = self.torch.empty_like(Z32)
+        nat.check(nat.load().tvbg_fcfit_zgrad(Z32.data_ptr(), A32.data_ptr(), gZ32.data_ptr(), I, T,
+                                             N, nat.stream_handle()))
+        gZ = gZ32.double()
         zg = (Z * gZ).sum(1, keepdim=True)
         dXc = (gZ - Z * zg) / nrm
         dX = dXc - dXc.mean(1, keepdim=True)
