@@ -214,7 +214,7 @@ def lems_workload(n_s=32, n_c=32, N=68, nsteps=4000, seed=0):
 
 def adjoint_workload(N=84, I=256, T=2000, C=100, seed=0):
     """The adjoint fit: Montbrio-Pazo-Roxin + linear coupling, deterministic,
-    N = 84 (config-0 recipe connectome), 256 instances, 2000 steps of 0.1 ms
+    N = 84 (the seeded synthetic connectome recipe), 256 instances, 2000 steps of 0.1 ms
     at 4 mm/ms, FC of the rate series vs a seeded target, gradients w.r.t. G
     and the 84 per-node eta by the hand-written adjoint with checkpoints every
     100 steps.  One bench step = forward (loss) + backward (gradients)."""
@@ -933,7 +933,7 @@ def gpu_arm(args):
     line = {'metric': METRIC, 'value': round(value, 1), 'unit': UNIT, 'n_gpus': world,
             'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': round(ms_per_step, 3),
             'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32',
-            'data': 'synthetic (seeded connectomes, config recipe)',
+            'data': 'synthetic (seeded connectomes: log-normal weights, uniform lengths)',
             'config': workload_config(wl), 'e2e': e2e,
             'gpu_launches': gs.launches_per_step() * args.steps,
             'roofline': roofline_entry(wl, gs.ns, kern_ms, args.steps),
@@ -974,7 +974,7 @@ def finish_mixed(args, wl, gs, world, rank, value, ms_per_step, clk, kern_ms, n_
     line = {'metric': METRIC, 'value': round(value, 1), 'unit': UNIT, 'n_gpus': world,
             'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': round(ms_per_step, 3),
             'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32',
-            'data': 'synthetic (seeded connectomes, config recipe)',
+            'data': 'synthetic (seeded connectomes: log-normal weights, uniform lengths)',
             'config': dict(workload_config(wl), path=(
                 'lane-interleaved groups (8 instances per lane slice, CTA clusters for N > 128), '
                 if gs.path == 'groups' else 'per-instance persistent kernels, ')
@@ -1045,7 +1045,7 @@ def adjoint_finish(args, wl, gs, torch, world, rank, barrier_fn=None):
     line = {'metric': METRIC, 'value': round(value, 1), 'unit': UNIT, 'n_gpus': world,
             'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': round(ms, 3),
             'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32',
-            'data': 'synthetic (seeded connectome and target FC, config recipe)',
+            'data': 'synthetic (seeded connectome and target FC)',
             'config': dict(workload_config(wl), checkpoint_every=wl['ckpt'],
                            loss='MSE of FC (r series) vs target', gradients='G [256], eta [256, 84]',
                            path=gs.path),
@@ -1115,7 +1115,7 @@ def cpu_baseline_mixed(wl, budget_s=12.0):
 
 
 def serve_arm(args):
-    """Serving loop (config-4 shapes): Poisson arrivals, models Kuramoto /
+    """Serving loop: Poisson arrivals, models Kuramoto /
     2-D oscillator / MPR, N in {68, 84, 192, 400, 998}, instance and step
     counts log-uniform, 10% of MPR requests with FC-fit gradients, admission
     by a 180 GB HBM budget.  The arrival window is bounded (--serve-seconds)
@@ -1260,7 +1260,7 @@ def reference_arm(args):
     line = {'metric': METRIC, 'value': round(v, 1), 'unit': UNIT, 'n_gpus': args.gpus,
             'steps': args.steps, 'warmup': args.warmup, 'higher_is_better': True,
             'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32',
-            'data': 'synthetic (seeded connectomes, config recipe)', 'impl': 'reference',
+            'data': 'synthetic (seeded connectomes: log-normal weights, uniform lengths)', 'impl': 'reference',
             'config': workload_config(wl), 'cpu_baseline': cb,
             'e2e': {'value': round(v, 1), 'unit': UNIT, 'h2d_bytes_per_step': 0,
                     'd2h_bytes_per_step': 0}}

@@ -3,7 +3,7 @@ The hand-written adjoint (tvbg_adjoint_mpr + checkpointed recomputation)
 against the FP64 oracle: the oracle's own adjoint (an independent C
 restatement of the recursion) and central finite differences of the FP64
 oracle loss (h = 1e-4).  Tolerance 1e-3 relative (max-norm), as asked of the
-config-3 gradient.  Also the torch.autograd.Function wrapper.
+FC-fit gradient.  Also the torch.autograd.Function wrapper.
 """
 
 import numpy as np

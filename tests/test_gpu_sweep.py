@@ -1,7 +1,7 @@
 """
 GPU parity of the step kernel against the CPU oracle (same seeded inputs).
 
-Tolerances (the benchmark spec): deterministic runs within 1e-4 relative state
+Tolerances: deterministic runs within 1e-4 relative state
 error of the FP32 restatement over 1000 steps (circular distance for
 Kuramoto phases); the error against the FP64 oracle is reported.  Stochastic
 runs use the same Philox stream as the oracle, so they are compared the same
@@ -22,7 +22,7 @@ pytestmark = pytest.mark.gpu
 TOL = 1e-4
 
 
-def config0(I=32, N=68, seed=0, speed=4.0):
+def kuramoto68(I=32, N=68, seed=0, speed=4.0):
     w, ln = network.synthetic_connectome(N, 0.3, seed=seed)
     conn = network.Connectivity.from_dense(w, ln)
     rng = np.random.default_rng(1)
@@ -51,8 +51,8 @@ def compare_rings(sw, ref, circ=False):
 
 
 @pytest.mark.parametrize('tpn', [1, 2, 4, 8])
-def test_kuramoto_config0_parity(cuda, tpn):
-    conn, theta0, omega, G = config0()
+def test_kuramoto68_parity(cuda, tpn):
+    conn, theta0, omega, G = kuramoto68()
     sw = kuramoto_sweep(conn, theta0, omega, G, tpn=tpn)
     assert np.all(sw.build_table(1)['flags'] & nat.F_SMEM_RING)  # 68 x 512 ring fits
     sw.run(1000)
@@ -62,13 +62,13 @@ def test_kuramoto_config0_parity(cuda, tpn):
     assert compare_rings(sw, ref, circ=True) < TOL
     ref64 = orc.run_sweep_like(sw, theta0, 1000, real='f64')
     err64 = circ_rel_err(got, ref64['state'])
-    print('kuramoto config0 tpn=%d: rel err vs f32 oracle %.2e, vs f64 oracle %.2e'
+    print('kuramoto N=68 tpn=%d: rel err vs f32 oracle %.2e, vs f64 oracle %.2e'
           % (tpn, circ_rel_err(got, ref['state']), err64))
     assert err64 < 1e-3
 
 
 def test_global_ring_equals_smem_ring(cuda):
-    conn, theta0, omega, G = config0(I=8)
+    conn, theta0, omega, G = kuramoto68(I=8)
     a = kuramoto_sweep(conn, theta0, omega, G, tpn=2)
     b = kuramoto_sweep(conn, theta0, omega, G, tpn=2)
     a.run(300)
@@ -84,7 +84,7 @@ def test_global_ring_equals_smem_ring(cuda):
 
 
 def test_chunked_runs_are_bit_exact(cuda):
-    conn, theta0, omega, G = config0(I=8)
+    conn, theta0, omega, G = kuramoto68(I=8)
     a = kuramoto_sweep(conn, theta0, omega, G, tpn=4)
     b = kuramoto_sweep(conn, theta0, omega, G, tpn=4)
     a.run(1000)
@@ -110,7 +110,7 @@ def g2do_set(I=12, N=84, speeds=(1.0, 5.0, 20.0), nsteps=0, **kw):
 
 @pytest.mark.parametrize('tpn', [1, 4])
 def test_g2do_diff_noise_parity(cuda, tpn):
-    "config-1 model: G2DO + Diff coupling + Euler-Maruyama with Philox noise."
+    "G2DO + Diff coupling + Euler-Maruyama with Philox noise (the dense grid's model)."
     sw, x0 = g2do_set(tpn=tpn)
     assert len(set(sw.lognh)) == 3   # rings of 2048, 512 and 128 slots
     flags = sw.build_table(1)['flags']
@@ -126,7 +126,7 @@ def test_g2do_diff_noise_parity(cuda, tpn):
 
 
 def test_generic2d_oscillator_parity(cuda):
-    "The CUDA-DSL form of the 2-D oscillator (config-1 model), per-step kernel."
+    "The CUDA-DSL form of the 2-D oscillator, per-step kernel."
     N, I = 84, 6
     w, ln = network.synthetic_connectome(N, 0.3, seed=12)
     conn = network.Connectivity.from_dense(w, ln)
@@ -142,7 +142,7 @@ def test_generic2d_oscillator_parity(cuda):
 
 
 def test_mpr_linear_noise_parity(cuda):
-    "config-2/3 model: Montbrio-Pazo-Roxin with linear coupling on r."
+    "Montbrio-Pazo-Roxin with linear coupling on r (the uneven batch's and the adjoint fit's model)."
     N, I = 84, 8
     w, ln = network.synthetic_connectome(N, 0.3, seed=5)
     conn = network.Connectivity.from_dense(w, ln)
