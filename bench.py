@@ -1135,13 +1135,15 @@ def serve_arm(args):
                                  inst=(1, args.serve_max_inst), steps=(1000, 100000))
     # warm-up: load every kernel once, the FC-fit gradient path's library
     # GEMMs included (their first call on a fresh process is slow)
-    warm = serve.Server(chunk=args.serve_chunk)
+    warm = serve.Server(chunk=args.serve_chunk, native=True)
     for r in serve.random_requests(8, 1e6, np.random.default_rng(1), conns[:2], inst=(1, 2),
                                    steps=(200, 300), grad_frac=1.0):
         warm.submit(r)
     warm.run()
     torch.cuda.synchronize()
-    srv = serve.Server(chunk=args.serve_chunk)
+    # requests without gradients in the C++ pool, gradient requests on the
+    # Python path (FC-fit adjoint on a worker thread), the same ticks
+    srv = serve.Server(chunk=args.serve_chunk, native=True)
     t_start = time.perf_counter()
     for r in reqs:
         r.arrival += t_start
@@ -1159,7 +1161,9 @@ def serve_arm(args):
             'config': {'workload': 'serve', 'rate_per_s': args.serve_rate,
                        'window_s': args.serve_seconds, 'requests': n_req,
                        'max_instances': args.serve_max_inst, 'chunk_steps': args.serve_chunk,
-                       'hbm_budget_gb': 180},
+                       'hbm_budget_gb': 180,
+                       'path': 'Server(native=True): C++ pool for requests without gradients, '
+                               'Python path + FC-fit adjoint worker for gradient requests'},
             'serve': {'p50_latency_s': round(st.get('p50_s', float('nan')), 3),
                       'p99_latency_s': round(st.get('p99_s', float('nan')), 3),
                       'wall_s': round(wall, 3), 'ticks': st['ticks'], 'phase_s': st['phase_s'],

@@ -155,3 +155,29 @@ def test_native_pool_budget_cancel(cuda):
     rest = pool.run()
     assert {r.rid for r in rest} == {r.rid for r in reqs[:-1]}
     assert pool.used() == 0
+
+
+def test_server_with_native_pool(cuda):
+    """Server(native=True): requests without gradients run in the C++ pool,
+    the gradient requests on the Python path, in the same ticks; every
+    result equals the same request served alone."""
+    rng = np.random.default_rng(9)
+    reqs = serve.random_requests(8, rate=1e6, rng=rng, conns=conns(), inst=(1, 16),
+                                 steps=(300, 1500), grad_frac=1.0)
+    assert any(r.want_grad for r in reqs) and not all(r.want_grad for r in reqs)
+    srv = serve.Server(chunk=500, native=True)
+    for r in reqs:
+        srv.submit(r)
+    done = {r.rid: r for r in srv.run()}
+    assert len(done) == len(reqs) and not srv.busy
+    assert srv.native.used() == 0
+    for r in serve.random_requests(8, rate=1e6, rng=np.random.default_rng(9), conns=conns(),
+                                   inst=(1, 16), steps=(300, 1500), grad_frac=1.0):
+        solo = serve.Server(chunk=500, native=True)
+        solo.submit(r)
+        (a, ) = solo.run()
+        assert np.array_equal(a.state, done[r.rid].state), r.model
+        if r.want_grad:
+            assert all(np.array_equal(x, y) for x, y in zip(a.grad, done[r.rid].grad))
+    st = srv.stats()
+    assert st['requests'] == len(reqs) and st['p99_s'] >= st['p50_s'] > 0

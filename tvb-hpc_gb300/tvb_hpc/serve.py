@@ -99,10 +99,12 @@ class Server:
     """
     Continuous-batching server.  `hbm_budget` bounds the device bytes of the
     admitted requests; `chunk` is the number of steps every active request
-    advances per tick.
+    advances per tick.  With `native=True` the requests without gradients
+    run in the C++ pool (NativeServer, sharing the budget and the ticks)
+    and only the gradient requests take the Python path.
     """
 
-    def __init__(self, hbm_budget=180e9, chunk=2000, clock=time.perf_counter):
+    def __init__(self, hbm_budget=180e9, chunk=2000, clock=time.perf_counter, native=False):
         import torch
         self.torch = torch
         self.budget = float(hbm_budget)
@@ -122,14 +124,56 @@ class Server:
         self.pool = concurrent.futures.ThreadPoolExecutor(max_workers=1)
         self.pending = []
         self.cancelled = []
+        # requests without gradients in the C++ pool: waiting for their
+        # arrival here, then in the pool until done
+        self.native = NativeServer(hbm_budget, chunk, clock) if native else None
+        self.native_wait = []
+        self.native_busy = False
+        self._native_seen = 0
 
     def submit(self, req):
-        self.queue.append(req)
+        if self.native is not None and not req.want_grad:
+            self.native_wait.append(req)
+        else:
+            self.queue.append(req)
+
+    @property
+    def busy(self):
+        "Work is queued, running or computing gradients."
+        return bool(self.queue or self.active or self.pending or self.native_wait
+                    or self.native_busy)
+
+    def _native_tick(self):
+        """Hand arrived requests to the pool and run one pool tick (its
+        chunks overlap this tick's Python-path launches on the device)."""
+        now = self.clock()
+        keep = []
+        for r in sorted(self.native_wait, key=lambda r: r.arrival):
+            if r.arrival > now:
+                keep.append(r)
+                continue
+            try:
+                self.native.submit(r)
+            except RuntimeError:       # e.g. delays too short for the group kernel
+                self.queue.append(r)   # the Python path has the per-step kernel
+        self.native_wait = keep
+        a, q = self.native.tick()
+        self.native_busy = bool(a or q)
+        for r in self.native.done[self._native_seen:]:
+            self.done.append(r)
+            self.node_steps += r.node_steps
+        self._native_seen = len(self.native.done)
 
     def poll(self, rid):
         """State of request `rid`: 'queued', 'active' (its steps are running),
         'gradient' (its FC-fit gradients are being computed), 'done',
         'cancelled', or None if the server has never seen it."""
+        if self.native is not None:
+            if any(r.rid == rid for r in self.native_wait):
+                return 'queued'
+            st = self.native.poll(rid)
+            if st is not None:
+                return st
         for name, reqs in (('queued', self.queue), ('active', self.active),
                            ('gradient', [r for r, _ in self.pending]), ('done', self.done),
                            ('cancelled', self.cancelled)):
@@ -141,6 +185,14 @@ class Server:
         """Drop a queued or active request between ticks; an active one gives
         its device memory back at once.  Returns True if it was dropped (a
         request already in its gradient phase or done is not)."""
+        if self.native is not None:
+            for r in self.native_wait:
+                if r.rid == rid:
+                    self.native_wait.remove(r)
+                    self.cancelled.append(r)
+                    return True
+            if self.native.poll(rid) is not None:
+                return self.native.cancel(rid)
         for lst in (self.queue, self.active):
             for r in lst:
                 if r.rid == rid:
@@ -165,7 +217,8 @@ class Server:
                 continue
             need = footprint(req)
             free = torch.cuda.mem_get_info()[0]
-            if self.used + need > self.budget or need > free:
+            held = self.used + (self.native.used() if self.native is not None else 0)
+            if held + need > self.budget or need > free:
                 keep.append(req)
                 continue
             req.iset = self._make_set(req)
@@ -234,6 +287,11 @@ class Server:
         t_p = time.perf_counter()
         self.phase_s['admit'] += t_p - t_a
         if not self.active:
+            if self.native is not None:
+                self._native_tick()
+                self.phase_s['device'] += time.perf_counter() - t_p
+                self._collect()
+                self.ticks += 1
             return 0.0
         by_model, grouped = {}, []
         for req in self.active:
@@ -268,6 +326,8 @@ class Server:
                 self._admit(self.clock(), into=fresh)
         t_s = time.perf_counter()
         self.phase_s['admit'] += t_s - t_d
+        if self.native is not None:
+            self._native_tick()
         # wait for this tick's launches and the admissions' copies only (a
         # gradient job may be running on its own stream)
         done.synchronize()
@@ -290,14 +350,15 @@ class Server:
         return work
 
     def run(self, until_empty=True, max_ticks=None):
-        while self.queue or self.active or self.pending:
+        while self.busy:
             if max_ticks is not None and self.ticks >= max_ticks:
                 break
-            if not self.active and not self.queue:
+            if not (self.active or self.queue or self.native_wait or self.native_busy):
                 self._collect(wait=True)     # only gradient jobs are left
                 break
-            if not self.active and self.queue:
-                nxt = min(r.arrival for r in self.queue)
+            waiting = self.queue + self.native_wait
+            if not self.active and not self.native_busy and waiting:
+                nxt = min(r.arrival for r in waiting)
                 wait = nxt - self.clock()
                 if wait > 0:
                     time.sleep(min(wait, 0.05))
