@@ -349,7 +349,7 @@ class MixedStep:
     kernels (tvbg_batch_run).  `run_plain` runs the same work as one
     tvbg_sweep per connectome, sequentially (the plain path)."""
 
-    def __init__(self, wl, torch, path='groups', graph=True):
+    def __init__(self, wl, torch, path='groups', graph=True, tune=True):
         from tvb_hpc import model, coupling, scheme, engine, groups
         self.torch = torch
         self.wl = wl
@@ -367,8 +367,12 @@ class MixedStep:
                 self.sets.append(engine.InstanceSet(m, cf, scm, p['conn'], **kw))
         self.x0 = [s.state.clone() for s in self.sets]
         steps = [p['steps'] for p in wl['parts']]
+        self.steps = steps
         if path == 'groups':
-            self.batch = groups.GroupBatch(self.sets, steps)
+            # launch shapes per connectome (plain or pipelined kernel, CTA
+            # width, cluster) and dispatch priorities from the makespan-aware
+            # tuner: whole-batch trials at scaled-down step counts
+            self.batch = groups.GroupBatch(self.sets, steps, shapes='tune' if tune else None)
             self.n_launch = self.batch.n_launches
         else:
             self.batch = engine.Batch(self.sets, steps)
@@ -422,6 +426,58 @@ class MixedStep:
         for sw, chunks, _ in self.plain:
             for launches in chunks:
                 sw.launch(launches, 2)
+
+    def plain_groups(self):
+        """The same group kernels with one connectome per launch set, the
+        connectomes in sequence, each on its fastest shape when run alone
+        (autotune.tune_group_alone).  Returns (ms, shapes)."""
+        from tvb_hpc import autotune, groups
+        torch = self.torch
+        shapes = [autotune.tune_group_alone(s, n)[0] for s, n in zip(self.sets, self.steps)]
+        solo = [groups.GroupBatch([s], [n], shapes=[sh])
+                for s, n, sh in zip(self.sets, self.steps, shapes)]
+        for s, sh in zip(self.sets, self.batch.shapes):
+            s.set_shape(*sh)
+
+        def once():
+            self.reset()
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for b in solo:
+                b.launch()
+            e1.record()
+            torch.cuda.synchronize()
+            return e0.elapsed_time(e1)
+
+        once()  # warm-up
+        ms = once()
+        for b in solo:
+            b.status.check()
+        self.reset()
+        return ms, shapes
+
+    def accuracy_run(self, nsteps=1000, per_set=2):
+        """Every instance of the benchmarked batch run for its first `nsteps`
+        steps -- same sets, launch shapes and priorities, one launch set --
+        and the final states of `per_set` sampled instances per connectome
+        (the longest and a middle one), for the comparison with the oracle."""
+        from tvb_hpc import groups
+        torch = self.torch
+        self.reset()
+        short = [np.minimum(np.asarray(n), nsteps) for n in self.steps]
+        b = groups.GroupBatch(self.sets, short, shapes=self.batch.shapes,
+                              step_ms=self.batch.step_ms)
+        b.run()
+        out = []
+        for s, n in zip(self.sets, self.steps):
+            order = np.argsort(-np.asarray(n), kind='stable')
+            idx = np.unique(order[np.linspace(0, len(order) - 1, per_set).astype(int)])
+            out.append(dict(idx=idx, state=s.state[torch.from_numpy(idx).cuda()].cpu().numpy(),
+                            nsteps=nsteps))
+        self.reset()
+        return out
 
     def reset_plain(self):
         for sw, _, x0 in self.plain:
@@ -834,7 +890,7 @@ def gpu_arm(args):
     _native.load()
     wl = WORKLOADS[args.workload]()
     if wl['name'].startswith('mixed'):
-        gs = MixedStep(wl, torch, args.path, not args.no_graph)
+        gs = MixedStep(wl, torch, args.path, not args.no_graph, not args.no_tune)
     elif wl['name'].startswith('net'):
         gs = NetStep(wl, torch)
     elif wl['name'].startswith('lems'):
@@ -900,6 +956,14 @@ def gpu_arm(args):
                  'ms_per_step': round(pms, 3),
                  'path': 'per-step kernel, one sweep per connectome in %d-step launches, '
                          'connectomes in sequence' % PLAIN_CHUNK}
+        if gs.path == 'groups':
+            gms, gshapes = gs.plain_groups()
+            plain['groups'] = {
+                'value': round(node_steps(wl) / (gms / 1e3), 1), 'unit': UNIT,
+                'ms_per_step': round(gms, 3),
+                'shapes': [[x[0], x[1], 'pipelined' if x[3] == 2 else 'plain'] for x in gshapes],
+                'path': 'the same group kernels, one connectome per launch set, connectomes in '
+                        'sequence, each on its fastest shape alone (threads, cluster, kernel)'}
         return finish_mixed(args, wl, gs, world, rank, value, ms_per_step, clk, kern_ms, n_kern,
                             plain, torch, dist, barrier)
 
@@ -971,21 +1035,43 @@ def finish_mixed(args, wl, gs, world, rank, value, ms_per_step, clk, kern_ms, n_
     nbytes = sum(h.numel() * 4 for h in host_x0)
     e2e = {'value': round(world * node_steps(wl) * args.steps / e2e_s, 1), 'unit': UNIT,
            'h2d_bytes_per_step': int(nbytes), 'd2h_bytes_per_step': int(nbytes)}
+    if gs.path == 'groups':
+        shapes = ', '.join('N=%d: %s %d threads x %d CTAs' % (
+            s.N, 'pipelined' if tp == 2 else 'plain', t, c)
+            for s, (t, c, _, tp) in zip(gs.sets, gs.batch.shapes))
+        if gs.batch.step_ms is not None:
+            shapes += '; groups banded into launch priorities by estimated run time'
+        path = ('lane-interleaved groups (8 instances per lane slice), launch shapes per '
+                'connectome %s[%s], ' % ('from the makespan-aware tuner ' if gs.batch.tuning
+                                         else '', shapes))
+    else:
+        path = 'per-instance persistent kernels, '
+    path += 'one CUDA graph' if gs.batch.graph is not None else 'direct launches'
     line = {'metric': METRIC, 'value': round(value, 1), 'unit': UNIT, 'n_gpus': world,
             'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': round(ms_per_step, 3),
             'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32',
             'data': 'synthetic (seeded connectomes: log-normal weights, uniform lengths)',
-            'config': dict(workload_config(wl), path=(
-                'lane-interleaved groups (8 instances per lane slice, CTA clusters for N > 128), '
-                if gs.path == 'groups' else 'per-instance persistent kernels, ')
-                + ('one CUDA graph' if gs.batch.graph is not None else 'direct launches')),
+            'config': dict(workload_config(wl), path=path),
             'e2e': e2e,
             'gpu_launches': gs.launches_per_step() * args.steps,
             'roofline': roofline_entry(wl, gs.ns, kern_ms, args.steps),
             'clocks': clk, 'plain': plain,
             'batched_vs_plain': round(value / plain['value'], 3) if plain else None}
+    if plain and 'groups' in plain:
+        line['batched_vs_plain_groups'] = round(value / plain['groups']['value'], 3)
+    if gs.path == 'groups' and gs.batch.tuning:
+        tun = gs.batch.tuning
+        line['tuner'] = {k: (round(v, 3) if isinstance(v, float) else v) for k, v in tun.items()
+                         if k in ('ms', 'default_ms', 'full_ms', 'full_default_ms', 'scale',
+                                  'kept_default')}
+        line['tuner']['trials'] = len(tun['trials'])
+        line['tuner']['banded'] = tun['step_ms'] is not None
     if rank == 0 and world == 1 and not args.no_cpu:
-        line['cpu_baseline'] = cpu_baseline_mixed(wl)
+        sample = gs.accuracy_run() if gs.path == 'groups' else None
+        line['cpu_baseline'] = cpu_baseline_mixed(wl, sample, gs.sets if sample else None)
+        acc = line['cpu_baseline'].pop('parity', None)
+        if acc:
+            line.update(acc)
     if world > 1:
         dist.barrier()
         dist.destroy_process_group()
@@ -1068,14 +1154,66 @@ def adjoint_finish(args, wl, gs, torch, world, rank, barrier_fn=None):
         print(json.dumps(line), flush=True)
 
 
-def cpu_baseline_mixed(wl, budget_s=12.0):
-    "The oracle on a bounded sample of the uneven batch (instances of every connectome)."
+def mixed_parity(orc, sample, sets, x0s, cores):
+    """State error of the sampled instances of the benchmarked batch (GPU,
+    first 1000 steps) against the oracle run on the same instances: the
+    FP32 restatement and the FP64 one (max |gpu - oracle| / max |oracle|,
+    worst over the sampled instances)."""
+    e32, e64, desc = 0.0, 0.0, []
+    for smp, gset, x0 in zip(sample, sets, x0s):
+        idx = smp['idx']
+        sub = _SubSet(gset, idx, x0)
+        got = smp['state'].astype(np.float64)
+        for real in ('f32', 'f64'):
+            r = orc.run_groups_like(sub, sub.x0, smp['nsteps'], real=real, nthreads=cores)['state']
+            r = np.asarray(r, np.float64)
+            err = float(np.abs(got - r).max() / max(np.abs(r).max(), 1e-30))
+            if real == 'f32':
+                e32 = max(e32, err)
+            else:
+                e64 = max(e64, err)
+        desc.append('N=%d: instances %s' % (gset.N, [int(i) for i in idx]))
+    return {'state_rel_err_vs_oracle': float('%.3g' % e32),
+            'state_rel_err_vs_fp64': float('%.3g' % e64),
+            'parity_sample': '%d steps from the initial state, %s; tolerance 1e-4' % (
+                sample[0]['nsteps'], '; '.join(desc))}
+
+
+class _SubSet:
+    """The view of a GroupSet that the oracle's run_groups_like reads,
+    restricted to some instances (same delays, parameters, seeds, ids)."""
+
+    def __init__(self, gs, idx, x0):
+        import torch
+        self.n = len(idx)
+        for a in ('N', 'ns', 'flags', 'model_id', 'cfun_id', 'row_np', 'col_np', 'w_np', 'dt',
+                  'sigma', 'consts', 'cf_b', 'cf_p', 'seed', 'trace_every', 'trace_len',
+                  'trace_nobs', 'bold_period', 'bold_len', 'delay_tables', 'lognh', 'gtab'):
+            setattr(self, a, getattr(gs, a))
+        self.bold_obs = gs.bold_obs
+        ii = torch.from_numpy(np.asarray(idx)).cuda()
+        self._gi = gs._gi[ii]
+        self._li = gs._li[ii]
+        self.gnparam = gs.gnparam
+        self.grp_of = gs.grp_of[idx]
+        self.cf_a = gs.cf_a[idx]
+        self.inst_ids = gs.inst_ids[idx]
+        self.x0 = np.asarray(x0, np.float32)[idx]
+
+
+def cpu_baseline_mixed(wl, sample=None, sets=None, budget_s=12.0):
+    """The oracle on a bounded sample of the uneven batch (instances of every
+    connectome); with `sample` (MixedStep.accuracy_run) it also checks the
+    GPU states of the sampled instances against the oracle ('parity')."""
     sys.path.insert(0, os.path.join(ROOT, 'oracle'))
     import pyoracle as orc
     from tvb_hpc import model as mdl
     m = getattr(mdl, wl['model'])()
     kid, consts, sigma = m.engine_spec()
     cores = os.cpu_count() or 1
+    parity = None
+    if sample is not None:
+        parity = mixed_parity(orc, sample, sets, [p['x0'] for p in wl['parts']], cores)
     done_ns, el_tot, desc = 0.0, 0.0, []
     for p in wl['parts']:
         c = p['conn']
@@ -1108,10 +1246,13 @@ def cpu_baseline_mixed(wl, budget_s=12.0):
             p['nparam'][:1, :, 0], p['x0'][:1], flags=orc.F_NOISE, sigma=sigma, consts=consts,
             seed=p['seed'], nthreads=1)
     one = c.nnode * n1 / (time.perf_counter() - t)
-    return {'value': round(done_ns / el_tot, 1), 'unit': UNIT, 'cores': cores, 'kind': 'port',
-            'sample': '; '.join(desc) + ' (%.1f s), oracle C + OpenMP, -O3' % el_tot,
-            'one_instance_one_core': {'value': round(one, 1), 'unit': UNIT,
-                                      'sample': 'N=%d, 1 instance x %d steps' % (c.nnode, n1)}}
+    out = {'value': round(done_ns / el_tot, 1), 'unit': UNIT, 'cores': cores, 'kind': 'port',
+           'sample': '; '.join(desc) + ' (%.1f s), oracle C + OpenMP, -O3' % el_tot,
+           'one_instance_one_core': {'value': round(one, 1), 'unit': UNIT,
+                                     'sample': 'N=%d, 1 instance x %d steps' % (c.nnode, n1)}}
+    if parity is not None:
+        out['parity'] = parity
+    return out
 
 
 def serve_arm(args):
@@ -1291,6 +1432,8 @@ def main():
                     help='lane-interleaved groups (separable couplings) or per-instance kernels')
     ap.add_argument('--no-graph', action='store_true',
                     help='launch the batch directly instead of replaying a CUDA graph')
+    ap.add_argument('--no-tune', action='store_true',
+                    help='mixed batch: default launch shapes instead of the batch tuner')
     args = ap.parse_args()
     if args.impl == 'reference':
         reference_arm(args)

@@ -174,7 +174,10 @@ typedef struct tvbg_launch {
     int32_t block_k;       /* 0 or 1: per-step kernel; 4 or 8: time-blocked     */
                            /* kernel (K steps per block, padded ring layout)    */
     int32_t nmax;          /* largest N of the call (blocked kernel); 0 = threads */
-    int32_t cluster;       /* tvbg_group_run: CTAs per group (1..8; 0 = 1)        */
+    int32_t cluster;       /* tvbg_group_run: CTAs per group (1..16; 0 = 1; 9..16 */
+                           /* are non-portable cluster sizes)                   */
+    int32_t priority;      /* tvbg_group_run: launch priority (0 = the stream's; */
+                           /* lower numbers are higher priority, as CUDA streams) */
     int32_t *d_status;     /* optional device int: first device error code      */
     int32_t *d_counter;    /* tvbg_batch_run work counter (zeroed by the call)  */
     const int32_t *d_order;/* tvbg_batch_run instance order (cost-descending)   */
@@ -480,7 +483,9 @@ typedef struct tvbg_group {
     int32_t bold_obs;
     uint32_t seed_lo;
     uint32_t seed_hi;
-    int32_t reserved0;
+    int32_t dmin;            /* smallest delay of the group's table; read by  */
+                             /* the pipelined kernel (TVBG_GROUP_PIPELINED),   */
+                             /* which needs dmin >= 2 block_k - 1             */
     float dt;
     float sqrt_dt;
     float dt_bold;
@@ -505,16 +510,39 @@ int tvbg_pack_edges_group(int32_t N, int32_t nnz, const int32_t *row,
 
 /*
  * Run the groups d_groups[0..n_groups): cfg->cluster CTAs of cfg->threads
- * threads per group (a thread-block cluster when > 1), group of cluster c =
- * d_order[c] (or c).  cfg->block_k = 4 or 8; cfg->tpn must be 0 or 1;
- * smem_ring, ctas, nmax and d_counter are not used.  Graph-capturable.
+ * threads per group (a thread-block cluster when > 1; up to 16, sizes above
+ * 8 opt in to non-portable clusters), group of cluster c = d_order[c] (or
+ * c).  cfg->block_k = 4 or 8; cfg->priority, when non-zero, is the launch's
+ * scheduling priority (lower = earlier CTA dispatch, clamped to the
+ * device's range); smem_ring, ctas, nmax and d_counter are not used.
+ * cfg->tpn = threads per (node, instance): 0 or 1, or TVBG_GROUP_PIPELINED
+ * (2): the pipelined kernel, whose CTA is two teams of threads / 2 (a
+ * multiple of 64 threads) on the same (node, instance) pairs -- one sums the
+ * coupling of block b + 1 while the other runs the K steps of block b.  It
+ * needs every group's dmin >= 2 block_k - 1, one node per 8-lane slot
+ * (cluster * threads / 16 >= N) and 16-byte aligned rings, else the device
+ * status reports TVBG_EINVAL; its gather is transposed (lane l of a node
+ * slot loads ring position t + l for the 8 instances, one 32-byte run, and
+ * the sums cross lanes through shared memory); results are identical to
+ * the plain kernel's.
+ * Graph-capturable.
  */
+#define TVBG_GROUP_PIPELINED 2
 int tvbg_group_run(const tvbg_group *d_groups, int32_t n_groups,
                    const tvbg_launch *cfg, void *stream);
 
 /* Resident CTAs per SM of the group kernel of `cfg`, and the SM count. */
 int tvbg_group_occupancy(const tvbg_launch *cfg, int32_t *ctas_per_sm,
                          int32_t *sms);
+
+/*
+ * Clusters of cfg->cluster CTAs of the group kernel of `cfg` that can be
+ * resident at once (cudaOccupancyMaxActiveClusters); 0 when the shape
+ * cannot be launched on the current device.  Used by the batch tuner to
+ * skip shapes; no counterpart in the reference (its launch shape is a
+ * command-line choice, dsl/dsl_cuda/example/cuda_setup.py:53-86).
+ */
+int tvbg_group_max_clusters(const tvbg_launch *cfg, int32_t *max_clusters);
 
 /*
  * dL/dZ = Z A of the FC-fit loss for n_inst instances: d_z [n_inst][T][N]

@@ -37,15 +37,15 @@ BlockedKernel blocked_kernel_linear(int cfun, int tpn, int k);
 BlockedKernel blocked_kernel_g2dosc(int cfun, int tpn, int k);
 // Lane-interleaved group kernel signature and per-model lookup for (cfun, K).
 using GroupKernel = void (*)(const tvbg_group*, int32_t, const int32_t*, int32_t*);
-GroupKernel group_kernel_kuramoto(int cfun, int k);
-GroupKernel group_kernel_g2do(int cfun, int k);
-GroupKernel group_kernel_mpr(int cfun, int k);
-GroupKernel group_kernel_linear(int cfun, int k);
-GroupKernel group_kernel_g2dosc(int cfun, int k);
-GroupKernel group_kernel_rww(int cfun, int k);
-GroupKernel group_kernel_jansenrit(int cfun, int k);
+GroupKernel group_kernel_kuramoto(int cfun, int k, bool pipe);
+GroupKernel group_kernel_g2do(int cfun, int k, bool pipe);
+GroupKernel group_kernel_mpr(int cfun, int k, bool pipe);
+GroupKernel group_kernel_linear(int cfun, int k, bool pipe);
+GroupKernel group_kernel_g2dosc(int cfun, int k, bool pipe);
+GroupKernel group_kernel_rww(int cfun, int k, bool pipe);
+GroupKernel group_kernel_jansenrit(int cfun, int k, bool pipe);
 // Group kernel of the engine library for (model, cfun, K), nullptr if not built.
-GroupKernel lookup_group_kernel(int model, int cfun, int k);
+GroupKernel lookup_group_kernel(int model, int cfun, int k, bool pipe = false);
 // Shared memory of the blocked kernel beyond the ring (floats): K * nmax * (2 + NS) + 4 * nmax.
 uint32_t blocked_aux_bytes(int model, int k, int nmax);
 

@@ -8,15 +8,15 @@ using namespace tvbg;
 
 namespace {
 
-GroupKernel lookup_group(int model, int cfun, int k) {
+GroupKernel lookup_group(int model, int cfun, int k, bool pipe) {
     switch (model) {
-        case TVBG_MODEL_KURAMOTO: return group_kernel_kuramoto(cfun, k);
-        case TVBG_MODEL_G2DO: return group_kernel_g2do(cfun, k);
-        case TVBG_MODEL_MPR: return group_kernel_mpr(cfun, k);
-        case TVBG_MODEL_LINEAR: return group_kernel_linear(cfun, k);
-        case TVBG_MODEL_G2DOSC: return group_kernel_g2dosc(cfun, k);
-        case TVBG_MODEL_RWW: return group_kernel_rww(cfun, k);
-        case TVBG_MODEL_JANSENRIT: return group_kernel_jansenrit(cfun, k);
+        case TVBG_MODEL_KURAMOTO: return group_kernel_kuramoto(cfun, k, pipe);
+        case TVBG_MODEL_G2DO: return group_kernel_g2do(cfun, k, pipe);
+        case TVBG_MODEL_MPR: return group_kernel_mpr(cfun, k, pipe);
+        case TVBG_MODEL_LINEAR: return group_kernel_linear(cfun, k, pipe);
+        case TVBG_MODEL_G2DOSC: return group_kernel_g2dosc(cfun, k, pipe);
+        case TVBG_MODEL_RWW: return group_kernel_rww(cfun, k, pipe);
+        case TVBG_MODEL_JANSENRIT: return group_kernel_jansenrit(cfun, k, pipe);
         default: return nullptr;
     }
 }
@@ -26,18 +26,22 @@ const ErrSink kSink{set_error, set_cuda_error};
 // Validate a group launch; its dynamic shared memory holds the K coupling
 // sums of every thread.
 int check_group_launch(const tvbg_launch* cfg, GroupKernel* kfn, int* cluster, size_t* smem) {
-    int rc = check_group_cfg(cfg, kSink, cluster);
+    int rc = check_group_cfg(cfg, kSink, cluster, (1u << 4) | (1u << 8), true);
     if (rc) return rc;
-    *kfn = lookup_group(cfg->model, cfg->cfun, cfg->block_k);
+    const bool pipe = cfg->tpn == TVBG_GROUP_PIPELINED;
+    *kfn = lookup_group(cfg->model, cfg->cfun, cfg->block_k, pipe);
     if (!*kfn)
         return set_error(TVBG_EUNSUPPORTED, "group kernel not built for this model/coupling/block_k");
-    *smem = group_smem_bytes(cfg->block_k, cfg->threads, group_channels(cfg->cfun));
+    *smem = pipe ? group_pipelined_smem_bytes(cfg->block_k, cfg->threads, group_channels(cfg->cfun))
+                 : group_smem_bytes(cfg->block_k, cfg->threads, group_channels(cfg->cfun));
     return TVBG_OK;
 }
 
 }  // namespace
 
-GroupKernel tvbg::lookup_group_kernel(int model, int cfun, int k) { return lookup_group(model, cfun, k); }
+GroupKernel tvbg::lookup_group_kernel(int model, int cfun, int k, bool pipe) {
+    return lookup_group(model, cfun, k, pipe);
+}
 
 extern "C" {
 
@@ -101,6 +105,46 @@ int tvbg_group_occupancy(const tvbg_launch* cfg, int32_t* ctas_per_sm, int32_t* 
     if (e != cudaSuccess) return set_cuda_error(e, "tvbg_group_occupancy: SM count");
     *ctas_per_sm = n;
     *sms = nsm;
+    return TVBG_OK;
+}
+
+int tvbg_group_max_clusters(const tvbg_launch* cfg, int32_t* max_clusters) {
+    if (!max_clusters) return set_error(TVBG_EINVAL, "tvbg_group_max_clusters: null");
+    GroupKernel kfn = nullptr;
+    int cluster = 1;
+    size_t smem = 0;
+    int rc = check_group_launch(cfg, &kfn, &cluster, &smem);
+    if (rc) return rc;
+    cudaError_t e = cudaSuccess;
+    if (smem + sizeof(tvbg_group) > 48u * 1024u) {
+        e = cudaFuncSetAttribute(reinterpret_cast<const void*>(kfn),
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+        if (e != cudaSuccess) return set_cuda_error(e, "tvbg_group_max_clusters: smem attribute");
+    }
+    if (cluster > 8) {
+        e = cudaFuncSetAttribute(reinterpret_cast<const void*>(kfn),
+                                 cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+        if (e != cudaSuccess) return set_cuda_error(e, "tvbg_group_max_clusters: cluster attribute");
+    }
+    cudaLaunchConfig_t lc;
+    std::memset(&lc, 0, sizeof(lc));
+    lc.gridDim = dim3(static_cast<unsigned>(cluster), 1, 1);
+    lc.blockDim = dim3(static_cast<unsigned>(cfg->threads), 1, 1);
+    lc.dynamicSmemBytes = smem;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = static_cast<unsigned>(cluster);
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    lc.attrs = attr;
+    lc.numAttrs = 1;
+    int n = 0;
+    e = cudaOccupancyMaxActiveClusters(&n, reinterpret_cast<const void*>(kfn), &lc);
+    if (e != cudaSuccess) {
+        cudaGetLastError();  // an unschedulable shape is reported here, before any launch
+        n = 0;
+    }
+    *max_clusters = n;
     return TVBG_OK;
 }
 

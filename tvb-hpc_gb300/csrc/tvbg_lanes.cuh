@@ -498,6 +498,428 @@ __device__ __forceinline__ void run_group(const tvbg_group& g, float* csum, int3
     }
 }
 
+// ---------------------------------------------------------------------------
+// Pipelined group kernel (group_kernel_pipelined).  The per-node pieces of
+// run_group as functions; run_group itself keeps its own inline body (its
+// register allocation and instruction schedule were tuned as written).
+// ---------------------------------------------------------------------------
+
+// Transposed gather of one node for the K steps of the block at ring
+// position tm.  The 8 lanes of a node slot share the edge records; lane l
+// reads, per edge, ring position t + (l mod K) for NI = 64 / K consecutive
+// instances m0 = (l / K) NI .. m0 + NI - 1 -- 4 NI contiguous bytes, two
+// (K = 8) or one (K = 4) 16-byte loads -- and accumulates, in CSR order,
+// acc[i] = sum_e w_e pre(v_e[m0 + i]), the sum of step (l mod K) of
+// instance m0 + i.  Pairs of accumulators take one packed FP32 FMA
+// (__ffma2_rn: each half rounded as fmaf), so every sum equals
+// lane_gather's.  The sums are written transposed: cs_slot[k * stride + m]
+// holds step k of instance m, where the node's lane m reads them.  Needs the
+// ring 16-byte aligned and K in {4, 8}.
+template <int CF, int K>
+__device__ __forceinline__ void lane_gather_t(const tvbg_group& g, int lo, int hi, uint32_t tm,
+                                              uint32_t mask, uint32_t R, int l, float* cs_slot,
+                                              int stride) {
+    static_assert(K == 4 || K == 8, "transposed gather: K = 4 or 8");
+    constexpr int NI = K == 8 ? 8 : 4;   // instances per lane
+    constexpr int NV = NI / 4;           // 16-byte loads per edge
+    constexpr int U = 4 / NV;            // edges per iteration: 4 loads (64 bytes) in flight
+    const int ks = l % K;
+    const int m0 = (l / K) * NI;
+    const float* __restrict__ ring = g.ring + m0;
+    const uint2* __restrict__ edges = reinterpret_cast<const uint2*>(g.edges);
+    float2 acc[NI / 2];
+#pragma unroll
+    for (int i = 0; i < NI / 2; ++i) acc[i] = make_float2(0.0f, 0.0f);
+    auto addr = [&](uint32_t pk) {
+        return ring + (static_cast<size_t>(pk >> 16) * R + (((tm + (pk & 0xffffu)) & mask) + ks)) * kLanes;
+    };
+    for (int e = lo; e < hi; e += U) {
+        float4 v[U][NV];
+        float w[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            if (e + u < hi) {
+                const uint2 ed = __ldg(edges + e + u);
+                const float4* p = reinterpret_cast<const float4*>(addr(ed.x));
+                w[u] = __uint_as_float(ed.y);
+#pragma unroll
+                for (int j = 0; j < NV; ++j) v[u][j] = __ldcg(p + j);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            if (e + u < hi) {
+                const float2 ww = make_float2(w[u], w[u]);
+#pragma unroll
+                for (int j = 0; j < NV; ++j) {
+                    const float2 a = make_float2(lane_pre<CF>(v[u][j].x, g.cf_p), lane_pre<CF>(v[u][j].y, g.cf_p));
+                    const float2 b = make_float2(lane_pre<CF>(v[u][j].z, g.cf_p), lane_pre<CF>(v[u][j].w, g.cf_p));
+                    acc[2 * j] = __ffma2_rn(ww, a, acc[2 * j]);
+                    acc[2 * j + 1] = __ffma2_rn(ww, b, acc[2 * j + 1]);
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < NI / 2; ++i) {
+        cs_slot[ks * stride + m0 + 2 * i] = acc[i].x;
+        cs_slot[ks * stride + m0 + 2 * i + 1] = acc[i].y;
+    }
+}
+
+// Per-thread constants of a group run (lane l of one node slot).
+struct GroupLane {
+    int l;                  // lane = instance of the group
+    uint32_t nh, mask, R;   // ring length, mask, row length (nh + ghost slots)
+    uint32_t flags;
+    bool noise, bold, trace;
+    float cf_a;
+    long long t0, t_end;    // this lane updates while t < t_end
+    uint32_t inst_id;
+};
+
+template <class M, int CF>
+__device__ __forceinline__ bool group_descriptor_ok(const tvbg_group& g) {
+    const int N = g.N;
+    return !(N <= 0 || N > 65535 || g.lognh < 3 || g.lognh > 16 || g.model != M::ID || g.cfun != CF ||
+             g.nsteps < 0 || (g.flags & (TVBG_F_TRACKA | TVBG_F_MIDSYNC | TVBG_F_TRACE_CSUM)) ||
+             (!Noise<M>::kOK && !WideNoise<M>::value && (g.flags & TVBG_F_NOISE)));
+}
+
+template <class M>
+__device__ __forceinline__ GroupLane make_lane(const tvbg_group& g, int l) {
+    GroupLane c;
+    c.l = l;
+    c.nh = 1u << g.lognh;
+    c.mask = c.nh - 1u;
+    c.R = c.nh + kGhost;
+    c.flags = g.flags;
+    c.noise = (g.flags & TVBG_F_NOISE) != 0;
+    c.bold = (g.flags & TVBG_F_BOLD) != 0 && g.bold != nullptr && g.bold_out != nullptr;
+    c.trace = (g.flags & TVBG_F_TRACE) != 0 && g.trace != nullptr;
+    c.cf_a = g.lanes[l].cf_a;
+    const int my_steps = g.lanes[l].nsteps < g.nsteps ? g.lanes[l].nsteps : g.nsteps;
+    c.inst_id = g.lanes[l].inst_id;
+    c.t0 = g.t0;
+    c.t_end = g.t0 + my_steps;
+    return c;
+}
+
+// Seed: ring slot t0 of node n holds obs0 (or the ring channels) of the
+// state at t0.
+template <class M, int CF>
+__device__ __forceinline__ void seed_node(const tvbg_group& g, const GroupLane& c, int n) {
+    constexpr int NS = M::NS;
+    constexpr int NP = M::NP;
+    constexpr int NC = ring_channels<CF>();
+    constexpr int RL = kLanes * NC;
+    const int l = c.l;
+    const uint32_t pos = static_cast<uint32_t>(c.t0) & c.mask;
+    float x[NS];
+#pragma unroll
+    for (int v = 0; v < NS; ++v) x[v] = g.state[(n * NS + v) * kLanes + l];
+    const size_t idx = (static_cast<size_t>(n) * c.R + pos) * RL + l;
+    const float o = M::obs(x, 0);
+    float p[NP];
+#pragma unroll
+    for (int v = 0; v < NP; ++v) p[v] = __ldg(g.nparam + (n * NP + v) * kLanes + l);
+    float* __restrict__ ring = g.ring;
+    if constexpr (NC == 2) {
+        float sn, cs;
+        if constexpr (CF == TVBG_CFUN_LEMS_2) {
+            sn = M::ring_value(o, p);
+            cs = M::ring_value2(x[M::CVAR2], p);
+        } else {
+            sincosf(o, &sn, &cs);
+        }
+        ring[idx] = sn;
+        ring[idx + kLanes] = cs;
+        if (pos < kGhost) {
+            ring[idx + static_cast<size_t>(c.nh) * RL] = sn;
+            ring[idx + static_cast<size_t>(c.nh) * RL + kLanes] = cs;
+        }
+    } else {
+        const float rv = ring_val<M, CF>(o, p);
+        ring[idx] = rv;
+        if (pos < kGhost) ring[idx + static_cast<size_t>(c.nh) * kLanes] = rv;
+    }
+}
+
+// Coupling sums of node n (an invalid slot gathers nothing) for the K steps
+// of the block at ring position tm, written to cs[k * stride] (and
+// cs[(K + k) * stride] for the second ring channel); cs points at this
+// thread's own sums.  One-channel couplings take the transposed gather (the
+// caller has checked the ring's 16-byte alignment).
+template <class M, int CF, int K>
+__device__ __forceinline__ void gather_node(const tvbg_group& g, const GroupLane& c, bool valid, int n,
+                                            uint32_t tm, float* cs, int stride) {
+    constexpr int NC = ring_channels<CF>();
+    const int lo = valid ? __ldg(g.row + n) : 0;
+    const int hi = valid ? __ldg(g.row + n + 1) : 0;
+    if constexpr (NC == 2) {
+        float accs[K], accc[K];
+        lane_gather_sc<K>(g, lo, hi, tm, c.mask, c.R, c.l, accs, accc);
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            cs[k * stride] = accs[k];
+            cs[(K + k) * stride] = accc[k];
+        }
+    } else {
+        lane_gather_t<CF, K>(g, lo, hi, tm, c.mask, c.R, c.l, cs - c.l, stride);
+    }
+}
+
+// Monitor schedule as 32-bit counters carried across blocks (the 64-bit
+// divisions run once per kernel): BOLD sample after step t when
+// (t + 1) % bold_period == 0, trace row before step t when
+// t % trace_every == 0.
+struct MonitorClock {
+    int bper, tev;
+    int b_until, b_row, tr_until, tr_row;
+
+    __device__ __forceinline__ void init(const tvbg_group& g, const GroupLane& c) {
+        bper = g.bold_period > 0 ? g.bold_period : 1;
+        tev = g.trace_every > 0 ? g.trace_every : 1;
+        const long long t0 = c.t0;
+        b_until = c.bold ? static_cast<int>((bper - 1) - t0 % bper) : 0;  // steps to the next sample
+        b_row = c.bold ? static_cast<int>((t0 + b_until + 1) / bper - 1) : 0;
+        tr_until = c.trace ? static_cast<int>((tev - t0 % tev) % tev) : 0;
+        tr_row = c.trace ? static_cast<int>(((t0 + tr_until) / tev) % g.trace_len) : 0;
+    }
+    // advance the counters past a block of cnt steps
+    __device__ __forceinline__ void advance(const tvbg_group& g, const GroupLane& c, int cnt) {
+        if (c.bold) {
+            while (b_until < cnt) {
+                b_until += bper;
+                b_row += 1;
+            }
+            b_until -= cnt;
+        }
+        if (c.trace) {
+            while (tr_until < cnt) {
+                tr_until += tev;
+                tr_row = tr_row + 1 == g.trace_len ? 0 : tr_row + 1;
+            }
+            tr_until -= cnt;
+        }
+    }
+};
+
+// The cnt (<= K) updates of node n for the block starting at step tb, from
+// the coupling sums cs[k * stride] (second channel cs[(K + k) * stride]):
+// drift, Euler-Maruyama, limit, ring write, balloon/BOLD and trace -- the
+// update of run_group, in the same order.
+template <class M, int CF, int K>
+__device__ __forceinline__ void update_node(const tvbg_group& g, const GroupLane& c, int n, long long tb,
+                                            int cnt, const float* cs, int stride, const MonitorClock& mc) {
+    constexpr int NS = M::NS;
+    constexpr int NP = M::NP;
+    constexpr int SPC = Noise<M>::SPC;
+    constexpr int NC = ring_channels<CF>();
+    constexpr int RL = kLanes * NC;  // floats per (node, slot)
+    const int N = g.N;
+    const int l = c.l;
+    const uint32_t mask = c.mask, R = c.R, nh = c.nh;
+    const bool noise = c.noise, bold = c.bold, trace = c.trace;
+    const float dt = g.dt, sqrt_dt = g.sqrt_dt;
+    float* __restrict__ ring = g.ring;
+    float* __restrict__ state = g.state;
+    float x[NS], p[NP];
+#pragma unroll
+    for (int v = 0; v < NS; ++v) x[v] = state[(n * NS + v) * kLanes + l];
+#pragma unroll
+    for (int v = 0; v < NP; ++v) p[v] = __ldg(g.nparam + (n * NP + v) * kLanes + l);
+    const float wsum = (CF == TVBG_CFUN_DIFF && g.wsum) ? __ldg(g.wsum + n) : 0.0f;
+    float bs = 0.0f, bF = 0.0f, bV = 0.0f, bQ = 0.0f;
+    if (bold) {
+        bs = g.bold[(0 * N + n) * kLanes + l];
+        bF = g.bold[(1 * N + n) * kLanes + l];
+        bV = g.bold[(2 * N + n) * kLanes + l];
+        bQ = g.bold[(3 * N + n) * kLanes + l];
+    }
+    float obs0 = M::obs(x, 0);
+    float sn0 = 0.0f, cs0 = 0.0f;  // sin, cos of obs0 (Kuramoto coupling)
+    if constexpr (NC == 2 && CF != TVBG_CFUN_LEMS_2) sincosf(obs0, &sn0, &cs0);
+    float zz[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    int b_next = mc.b_until, tr_next = mc.tr_until;
+    int brow = mc.b_row, trow = mc.tr_row;
+#pragma unroll 1
+    for (int k = 0; k < cnt; ++k) {
+        const long long t = tb + k;
+        if (t >= c.t_end) break;
+        if (trace && k == tr_next) {
+            float* dst = g.trace + ((static_cast<size_t>(trow) * N + n) * g.trace_nobs) * kLanes + l;
+            for (int o = 0; o < g.trace_nobs; ++o) dst[o * kLanes] = M::obs(x, o);
+            tr_next += mc.tev;
+            trow = trow + 1 == g.trace_len ? 0 : trow + 1;
+        }
+        const float xbold = bold ? M::obs(x, g.bold_obs) : 0.0f;
+        float cc, c2 = 0.0f;
+        if constexpr (CF == TVBG_CFUN_LEMS_2) {
+            cc = M::coupling(cs[k * stride], x, p);
+            c2 = M::coupling2(cs[(K + k) * stride], x, p);
+        } else if constexpr (NC == 2) {
+            // sum_e w sin(x_j - x_i); Kuramoto: post = a * mean (coupling.py:119-121)
+            const float S = cs0 * cs[k * stride] - sn0 * cs[(K + k) * stride];
+            if constexpr (CF == TVBG_CFUN_LEMS_SC) {
+                cc = M::coupling(S, x, p);
+            } else {
+                cc = c.cf_a * (S / static_cast<float>(N));
+            }
+        } else if constexpr (CF == TVBG_CFUN_LEMS) {
+            cc = M::coupling(cs[k * stride], x, p);
+        } else {
+            cc = lane_post<CF>(cs[k * stride], obs0, wsum, c.cf_a, g.cf_b);
+        }
+        float f[NS];
+        if constexpr (CF == TVBG_CFUN_LEMS_2) {
+            M::drift2(x, cc, c2, p, g.consts, f);
+        } else {
+            M::drift(x, cc, p, g.consts, f);
+        }
+#pragma unroll
+        for (int v = 0; v < NS; ++v) x[v] = fmaf(dt, f[v], x[v]);
+        if constexpr (Noise<M>::kOK) {
+            if (noise) {
+                const int r0 = static_cast<int>(t & (SPC - 1));
+                if (k == 0 || r0 == 0) {
+                    const u32x4 w = philox4x32_10(static_cast<uint32_t>(n), static_cast<uint32_t>(t / SPC),
+                                                  g.seed_hi, 0u, g.seed_lo, c.inst_id);
+                    box_muller_fast(w.v[0], w.v[1], zz[0], zz[1]);
+                    box_muller_fast(w.v[2], w.v[3], zz[2], zz[3]);
+                }
+#pragma unroll
+                for (int v = 0; v < NS; ++v) x[v] = fmaf(sqrt_dt * pick4(zz, r0 * NS + v), g.sigma[v], x[v]);
+            }
+        } else if constexpr (WideNoise<M>::value) {
+            if (noise) {
+                float z8[8];
+#pragma unroll
+                for (int b = 0; b < 2; ++b) {
+                    const u32x4 w = philox4x32_10(static_cast<uint32_t>(n), static_cast<uint32_t>(t), g.seed_hi,
+                                                  static_cast<uint32_t>(b), g.seed_lo, c.inst_id);
+                    box_muller_fast(w.v[0], w.v[1], z8[4 * b], z8[4 * b + 1]);
+                    box_muller_fast(w.v[2], w.v[3], z8[4 * b + 2], z8[4 * b + 3]);
+                }
+#pragma unroll
+                for (int v = 0; v < NS; ++v)
+                    x[v] = fmaf(sqrt_dt * z8[v], g.sigma[0] * NoiseScale<M>::at(v), x[v]);
+            }
+        }
+        M::limit(x, c.flags);
+        obs0 = M::obs(x, 0);
+        const uint32_t pos = (static_cast<uint32_t>(t) + 1u) & mask;
+        const size_t idx = (static_cast<size_t>(n) * R + pos) * RL + l;
+        if constexpr (NC == 2) {
+            if constexpr (CF == TVBG_CFUN_LEMS_2) {
+                sn0 = M::ring_value(obs0, p);
+                cs0 = M::ring_value2(x[M::CVAR2], p);
+            } else {
+                sincosf(obs0, &sn0, &cs0);
+            }
+            ring[idx] = sn0;
+            ring[idx + kLanes] = cs0;
+            if (pos < kGhost) {
+                ring[idx + static_cast<size_t>(nh) * RL] = sn0;
+                ring[idx + static_cast<size_t>(nh) * RL + kLanes] = cs0;
+            }
+        } else {
+            const float rv = ring_val<M, CF>(obs0, p);
+            ring[idx] = rv;
+            if (pos < kGhost) ring[idx + static_cast<size_t>(nh) * kLanes] = rv;
+        }
+        if (bold) {
+            Balloon::step(bs, bF, bV, bQ, xbold, g.dt_bold);
+            if (k == b_next) {
+                if (brow >= 0 && brow < g.bold_len)
+                    g.bold_out[(static_cast<size_t>(brow) * N + n) * kLanes + l] = Balloon::signal(bV, bQ);
+                b_next += mc.bper;
+                brow += 1;
+            }
+        }
+    }
+#pragma unroll
+    for (int v = 0; v < NS; ++v) state[(n * NS + v) * kLanes + l] = x[v];
+    if (bold) {
+        g.bold[(0 * N + n) * kLanes + l] = bs;
+        g.bold[(1 * N + n) * kLanes + l] = bF;
+        g.bold[(2 * N + n) * kLanes + l] = bV;
+        g.bold[(3 * N + n) * kLanes + l] = bQ;
+    }
+}
+
+// Pipelined group run: the CTA's warps form two teams of H = blockDim / 2
+// threads, both mapped onto the same (node, lane) pairs.  While the update
+// team runs the K steps of block b from the coupling sums in one shared
+// buffer, the gather team sums block b + 1 into the other; one (cluster)
+// barrier per block.  Block b + 1 reads ring slots up to
+// tb + 2K - 1 - d_min, so with d_min >= 2K - 1 every slot it reads was
+// written before block b started (ordered by the previous barrier), and
+// the newest slot written in block b (tb + K) is at most d_max < nh slots
+// ahead of the oldest read, so no read aliases a write.  Same arithmetic in
+// the same order as run_group, so the results are identical.  Needs one
+// node per slot (C * H / 8 >= N), K in {4, 8} and a 16-byte aligned ring.
+template <class M, int CF, int K>
+__device__ __forceinline__ void run_group_pipelined(const tvbg_group& g, float* csum, int32_t* status) {
+    constexpr int NC = ring_channels<CF>();
+    const int N = g.N;
+    const uint32_t C = cluster_nranks();
+    const uint32_t rank = cluster_rank();
+    const bool cluster = C > 1;
+    const int H = static_cast<int>(blockDim.x) / 2;
+    const int P = H / kLanes;
+    if (!group_descriptor_ok<M, CF>(g) || g.dmin < 2 * K - 1 || (H & 31) ||
+        static_cast<int>(C) * P < N || (reinterpret_cast<uintptr_t>(g.ring) & 15u) != 0) {
+        if (threadIdx.x == 0) report(status, TVBG_EINVAL);
+        return;  // uniform over the cluster: same descriptor, same launch shape
+    }
+    const bool gather_team = static_cast<int>(threadIdx.x) >= H;
+    const int tid = static_cast<int>(threadIdx.x) - (gather_team ? H : 0);
+    const int l = tid % kLanes;
+    const int q = (tid / kLanes) * static_cast<int>(C) + static_cast<int>(rank);
+    const bool valid = q < N;
+    const int n = valid ? (g.nodes ? __ldg(g.nodes + q) : q) : 0;
+    const GroupLane c = make_lane<M>(g, l);
+    const int bufsz = NC * K * H;  // floats per coupling-sum buffer
+
+    if (!gather_team && valid) seed_node<M, CF>(g, c, n);
+    group_barrier(cluster);
+    // each team runs its own loop (disjoint live ranges); both meet at the
+    // same number of barriers: one after block 0's gather, one per block
+    const long long t_stop = c.t0 + g.nsteps;
+    if (gather_team) {
+        if (g.nsteps > 0)
+            gather_node<M, CF, K>(g, c, valid, n, static_cast<uint32_t>(c.t0) & c.mask, csum + tid, H);
+        group_barrier(cluster);
+        int buf = 1;
+        for (long long tb = c.t0; tb < t_stop; tb += K) {
+            if (tb + K < t_stop)
+                gather_node<M, CF, K>(g, c, valid, n, static_cast<uint32_t>(tb + K) & c.mask,
+                                      csum + buf * bufsz + tid, H);
+            buf ^= 1;
+            group_barrier(cluster);
+        }
+    } else {
+        group_barrier(cluster);
+        MonitorClock mc;
+        mc.init(g, c);
+        int buf = 0;
+        for (long long tb = c.t0; tb < t_stop; tb += K) {
+            const int cnt = (t_stop - tb) < K ? static_cast<int>(t_stop - tb) : K;
+            if (valid) update_node<M, CF, K>(g, c, n, tb, cnt, csum + buf * bufsz + tid, H, mc);
+            mc.advance(g, c, cnt);
+            buf ^= 1;
+            group_barrier(cluster);
+        }
+    }
+}
+
+// Dynamic shared memory of a pipelined group CTA: two coupling-sum buffers
+// of half the CTA each.
+__host__ __device__ constexpr uint32_t group_pipelined_smem_bytes(int K, int threads, int nc) {
+    return static_cast<uint32_t>(4 * 2 * K * (threads / 2) * nc);
+}
+
 // One group per CTA (or per cluster of CTAs): group index = order[cluster id].
 template <class M, int CF, int K>
 __global__ void __launch_bounds__(1024, 1)
@@ -510,6 +932,21 @@ __global__ void __launch_bounds__(1024, 1)
     const int idx = order ? __ldg(order + cid) : cid;
     stage_group(groups + idx, &s_grp);
     run_group<M, CF, K>(s_grp, csum, status);
+}
+
+// Pipelined variant (run_group_pipelined): blockDim = 2 teams x 8 lanes x
+// node slots; same tables and results as group_kernel.
+template <class M, int CF, int K>
+__global__ void __launch_bounds__(1024, 1)
+    group_kernel_pipelined(const tvbg_group* __restrict__ groups, int32_t n_groups,
+                           const int32_t* __restrict__ order, int32_t* __restrict__ status) {
+    __shared__ __align__(16) tvbg_group s_grp;
+    extern __shared__ float csum[];  // [2][channels][K][blockDim / 2]
+    const int cid = static_cast<int>(cluster_id_x());
+    if (cid >= n_groups) return;  // uniform over the cluster
+    const int idx = order ? __ldg(order + cid) : cid;
+    stage_group(groups + idx, &s_grp);
+    run_group_pipelined<M, CF, K>(s_grp, csum, status);
 }
 
 }  // namespace tvbg

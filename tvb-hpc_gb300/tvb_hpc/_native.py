@@ -105,6 +105,7 @@ class tvbg_launch(ctypes.Structure):
         ('block_k', ctypes.c_int32),
         ('nmax', ctypes.c_int32),
         ('cluster', ctypes.c_int32),
+        ('priority', ctypes.c_int32),
         ('d_status', ctypes.c_void_p),
         ('d_counter', ctypes.c_void_p),
         ('d_order', ctypes.c_void_p),
@@ -112,6 +113,7 @@ class tvbg_launch(ctypes.Structure):
 
 
 GROUP_LANES = 8  # instances per lane-interleaved group (TVBG_GROUP_LANES)
+GROUP_PIPELINED = 2  # tvbg_launch.tpn of the pipelined group kernel (TVBG_GROUP_PIPELINED)
 
 
 class tvbg_lane(ctypes.Structure):
@@ -147,7 +149,7 @@ class tvbg_group(ctypes.Structure):
         ('bold_obs', ctypes.c_int32),
         ('seed_lo', ctypes.c_uint32),
         ('seed_hi', ctypes.c_uint32),
-        ('reserved0', ctypes.c_int32),
+        ('dmin', ctypes.c_int32),
         ('dt', ctypes.c_float),
         ('sqrt_dt', ctypes.c_float),
         ('dt_bold', ctypes.c_float),
@@ -246,6 +248,7 @@ SIGNATURES = {
     'tvbg_pack_edges_group': (ctypes.c_int, [_i32, _i32, _vp, _vp, _vp, _vp, _i32, _vp]),
     'tvbg_group_run': (ctypes.c_int, [_vp, _i32, ctypes.POINTER(tvbg_launch), _vp]),
     'tvbg_group_occupancy': (ctypes.c_int, [ctypes.c_void_p, _ip, _ip]),
+    'tvbg_group_max_clusters': (ctypes.c_int, [ctypes.c_void_p, _ip]),
     'tvbg_fcfit_zgrad': (ctypes.c_int, [_vp, _vp, _vp, _i32, _i32, _i32, _vp]),
     'tvbg_rmap_to_avg': (ctypes.c_int, [_i32, _i32, _i32, _vp, _vp, _vp, _vp]),
     'tvbg_rmap_from_avg': (ctypes.c_int, [_i32, _i32, _i32, _vp, _vp, _vp, _vp]),

@@ -7,8 +7,10 @@ to a group, one instance per lane of an 8-lane slice; every per-node array
 of a group is interleaved over its eight instances (include/tvbg.h, "lane-
 interleaved groups"), so a delayed read of one edge is one 32-byte sector
 for the group and the edge record is read once for eight instances.  A
-group runs on one CTA, or on a cluster of 2, 4 or 8 CTAs that split its
-nodes (N > 128), with one barrier every K = 4 or 8 steps.
+group runs on one CTA, or on a cluster of 2 to 16 CTAs that split its
+nodes, with one barrier every K = 4 or 8 steps.  Where every delay is at
+least 2K - 1 steps the pipelined kernel (tpn 2) overlaps the coupling
+gather of block b + 1 with the steps of block b on two thread teams.
 
 The step is the CUDA-order step of the per-instance kernels (same Philox
 streams, same ring semantics); the coupling sums are taken in CSR order.
@@ -47,11 +49,25 @@ def plan_group(dmin, dmax, block_k=None, ks=(8, 4)):
     return k, int(np.log2(nh))
 
 
+MAX_CLUSTER = 16   # CTAs per group; 9..16 are non-portable cluster sizes
+PIPELINED = nat.GROUP_PIPELINED   # tvbg_launch.tpn of the pipelined kernel
+
+
+def pipelined_threads(N, cluster):
+    """CTA width of the pipelined kernel for N nodes on `cluster` CTAs: two
+    teams of one node per 8-lane slot (0 when that exceeds 1024 threads)."""
+    per = -(-N // int(cluster))
+    thr = 2 * 32 * -(-(L * per) // 32)
+    return thr if thr <= 1024 else 0
+
+
 def group_shape(N, threads=None, cluster=None):
-    """(threads, cluster) of a group launch: one node per 8-lane slot, on the
-    smallest cluster (<= 8 CTAs) whose CTAs stay within 1024 threads; beyond
-    8 CTAs the slots take several nodes.  Measured on the uneven batch and
-    the 64 x 64 grid, this beats packing more, smaller CTAs per SM."""
+    """(threads, cluster) of a plain group launch: one node per 8-lane slot,
+    on the smallest cluster (<= 8 CTAs) whose CTAs stay within 1024 threads;
+    beyond 8 CTAs the slots take several nodes.  Measured on the uneven batch
+    and the 64 x 64 grid, this beats packing more, smaller CTAs per SM when
+    every connectome takes the same rule; the batch tuner
+    (autotune.tune_group_batch) picks shapes per connectome by measurement."""
     if cluster is None:
         if threads is not None:
             cluster = min(8, -(-N // (int(threads) // L)))
@@ -59,6 +75,8 @@ def group_shape(N, threads=None, cluster=None):
             cluster = 1
             while L * -(-N // cluster) > 1024 and cluster < 8:
                 cluster *= 2
+    if not 1 <= int(cluster) <= MAX_CLUSTER:
+        raise ValueError('group kernel: cluster in [1, %d]' % MAX_CLUSTER)
     if threads is None:
         per = -(-N // int(cluster))
         threads = min(1024, 32 * -(-(L * per) // 32))
@@ -151,6 +169,9 @@ class GroupSet:
         self.delay_tables = tables
         plans = [plan_group(d.min() if d.size else 7, d.max() if d.size else 0, block_k,
                             self.block_ks) for d in tables]
+        # the pipelined kernel needs d_min >= 2 K - 1 in every table
+        self.dmin_tab = np.array([int(d.min()) if d.size else 1 << 20 for d in tables], np.int64)
+        self.can_pipeline = all(int(dm) >= 2 * k - 1 for dm, (k, _) in zip(self.dmin_tab, plans))
         # per-node constants shared by every table: in-edge weight sums and
         # the visiting order (in-degree, descending)
         deg = np.diff(row)
@@ -204,7 +225,7 @@ class GroupSet:
         self.gstate = torch.zeros((G, N, self.ns, L), dtype=torch.float32, device='cuda')
         if state0 is not None:
             st = np.broadcast_to(np.asarray(state0, np.float32), (I, N, self.ns))
-            self.set_state(torch.from_numpy(np.ascontiguousarray(st)).cuda())
+            self.set_state(torch.from_numpy(np.array(st, np.float32)).cuda())
         if nparam is None:
             npm = np.broadcast_to(model.node_params(N), (I, N, self.npar))
         else:
@@ -216,7 +237,7 @@ class GroupSet:
             npm = np.broadcast_to(npm, (I, N, self.npar))
         self.gnparam = torch.zeros((G, N, self.npar, L), dtype=torch.float32, device='cuda')
         self.gnparam[self._gi, :, :, self._li] = torch.from_numpy(
-            np.ascontiguousarray(npm, np.float32)).cuda()
+            np.array(npm, np.float32)).cuda()
         if history == 'fill':
             self.fill_history()
         elif history != 'zero':
@@ -249,6 +270,8 @@ class GroupSet:
                                (cf_b0 if isinstance(cf_b0, (int, float, np.number)) else 0.0))
         self.t = np.full(G, int(t0), np.int64)
         self.threads, self.cluster = group_shape(N, threads, cluster)
+        self.priority = 0
+        self.tpn = 1
         self.status = DeviceStatus()
         self._uploaded = None
         self._streams = None
@@ -359,6 +382,7 @@ class GroupSet:
         tab['bold_period'] = max(1, self.bold_period)
         tab['bold_len'] = self.bold_len
         tab['bold_obs'] = self.bold_obs()
+        tab['dmin'] = np.minimum(self.dmin_tab[self.gtab], 1 << 30)
         tab['seed_lo'] = self.seed & 0xffffffff
         tab['seed_hi'] = (self.seed >> 32) & 0xffffffff
         tab['dt'] = np.float32(self.dt)
@@ -379,27 +403,65 @@ class GroupSet:
         tab['nsteps'] = gmax
         return tab, gmax
 
-    def launch_cfg(self, block_k, order=None):
+    def set_shape(self, threads=None, cluster=None, priority=0, tpn=1):
+        """Launch shape of the following prepare() calls: CTA width and
+        cluster size (group_shape rules for what is left out), the launch
+        priority (0 = the stream's; lower numbers are dispatched first) and
+        tpn = 2 for the pipelined kernel (threads then count both teams;
+        needs can_pipeline and one node per slot)."""
+        tpn = int(tpn)
+        if tpn == PIPELINED:
+            if not self.can_pipeline:
+                raise ValueError('pipelined group kernel needs d_min >= 2 K - 1')
+            cluster = int(cluster or 1)
+            thr = pipelined_threads(self.N, cluster) if threads is None else int(threads)
+            if not thr or thr % 64 or thr > 1024 or cluster * (thr // (2 * L)) < self.N:
+                raise ValueError('pipelined group kernel: two teams of one node per slot, '
+                                 'a multiple of 64 threads <= 1024')
+            if not 1 <= cluster <= MAX_CLUSTER:
+                raise ValueError('group kernel: cluster in [1, %d]' % MAX_CLUSTER)
+            self.threads, self.cluster = thr, cluster
+        elif tpn in (0, 1):
+            self.threads, self.cluster = group_shape(self.N, threads, cluster)
+        else:
+            raise ValueError('tpn: 1 (plain) or 2 (pipelined)')
+        self.priority = int(priority)
+        self.tpn = max(1, tpn)
+
+    @property
+    def shape(self):
+        "(threads, cluster, priority, tpn) of the next launches."
+        return (self.threads, self.cluster, self.priority, self.tpn)
+
+    def launch_cfg(self, block_k, order=None, priority=None):
         cfg = nat.tvbg_launch()
         cfg.model, cfg.cfun = self.model_id, self.cfun_id
         cfg.threads, cfg.cluster = self.threads, self.cluster
+        cfg.priority = self.priority if priority is None else int(priority)
+        cfg.tpn = self.tpn
         cfg.block_k = int(block_k)
         cfg.d_status = self.status.t.data_ptr()
         cfg.d_order = order.data_ptr() if order is not None else None
         return cfg
 
-    def prepare(self, nsteps):
+    def prepare(self, nsteps, priorities=None):
         """Upload the group tables for the next nsteps: one launch per block
-        length, groups in longest-first order.  Returns the launch list."""
+        length, groups in longest-first order.  With `priorities` (one launch
+        priority per group) the groups of each block length are split into
+        one launch per priority, so that concurrent launches dispatch the
+        CTAs of long groups first.  Returns the launch list."""
         torch = self.torch
         tab, gmax = self.build_table(nsteps)
         dev = torch.from_numpy(tab.view(np.uint8).copy()).cuda()
+        prio = (np.full(self.n_groups, self.priority, np.int64) if priorities is None
+                else np.asarray(priorities, np.int64))
         launches = []
         for k in sorted(set(self.block_k.tolist())):
-            idx = np.nonzero(self.block_k == k)[0]
-            idx = idx[np.argsort(-gmax[idx], kind='stable')].astype(np.int32)
-            order = torch.from_numpy(idx).cuda()
-            launches.append((dev, order, int(idx.size), self.launch_cfg(k, order)))
+            for pr in sorted(set(prio[self.block_k == k].tolist())):
+                idx = np.nonzero((self.block_k == k) & (prio == pr))[0]
+                idx = idx[np.argsort(-gmax[idx], kind='stable')].astype(np.int32)
+                order = torch.from_numpy(idx).cuda()
+                launches.append((dev, order, int(idx.size), self.launch_cfg(k, order, pr)))
         self._uploaded = (launches, gmax)
         return launches, gmax
 
@@ -449,18 +511,48 @@ class GroupBatch:
     Several GroupSets (different connectomes, N and step counts) in one
     launch set: every set's launches go on their own forked stream and the
     whole batch can be captured into one CUDA graph.
+
+    shapes: None (each set's current shape), 'tune' (autotune.tune_group_batch
+    picks a launch shape per set, and whether to band the groups into launch
+    priorities, by the batch's measured makespan), or a list of (threads,
+    cluster[, priority[, tpn]]) per set (GroupSet.set_shape).
+    step_ms: optional per-set time of one step of one group (ms); the groups
+    are then banded by their estimated run time (steps x step_ms) into
+    launch priorities, the longest groups of every set first, so the CTA
+    dispatcher approximates a longest-first schedule over the whole batch
+    instead of within each launch.
     """
 
-    def __init__(self, sets, nsteps):
+    PRIORITY_LEVELS = 6   # CUDA stream priorities 0 (least) .. -5 (greatest)
+
+    def __init__(self, sets, nsteps, shapes=None, step_ms=None):
         torch = _torch()
         self.torch = torch
         self.sets = list(sets)
         self.nsteps = [np.broadcast_to(np.asarray(n, np.int64), (s.n, )).astype(np.int64)
                        for s, n in zip(self.sets, nsteps)]
+        self.tuning = None
+        if isinstance(shapes, str):
+            if shapes != 'tune':
+                raise ValueError("shapes: None, 'tune' or one (threads, cluster[, priority[, tpn]]) "
+                                 "per set")
+            from .autotune import tune_group_batch
+            self.tuning = tune_group_batch(self.sets, self.nsteps)
+            shapes = self.tuning['shapes']
+            if step_ms is None:
+                step_ms = self.tuning.get('step_ms')
+        if shapes is not None:
+            if len(shapes) != len(self.sets):
+                raise ValueError('shapes: one (threads, cluster[, priority[, tpn]]) per set')
+            for s, sh in zip(self.sets, shapes):
+                s.set_shape(*sh)
+        self.shapes = [s.shape for s in self.sets]
+        self.step_ms = step_ms
         self.status = DeviceStatus()
         self.plans = []
-        for s, n in zip(self.sets, self.nsteps):
-            launches, gmax = s.prepare(n)
+        prios = self.group_priorities(step_ms) if step_ms is not None else [None] * len(self.sets)
+        for s, n, pr in zip(self.sets, self.nsteps, prios):
+            launches, gmax = s.prepare(n, pr)
             for _, _, _, cfg in launches:
                 cfg.d_status = self.status.t.data_ptr()
             self.plans.append((s, launches, gmax))
@@ -468,6 +560,24 @@ class GroupBatch:
         self.plans.sort(key=lambda p: -float(p[2].max(initial=0)) * p[0].N)
         self.streams = [torch.cuda.Stream() for _ in self.plans]
         self.graph = None
+
+    def group_priorities(self, step_ms):
+        """Launch priority per group of every set: estimated run time
+        (longest lane's steps x the set's step time) in PRIORITY_LEVELS equal
+        bands of the batch's longest, the longest band at the greatest
+        priority (the most negative number)."""
+        est = []
+        for s, n, tau in zip(self.sets, self.nsteps, step_ms):
+            gmax = np.array([n[m].max(initial=0) for m in s.members], np.float64)
+            est.append(gmax * float(tau))
+        top = max((e.max(initial=0.0) for e in est), default=0.0)
+        levels = self.PRIORITY_LEVELS
+        out = []
+        for e in est:
+            band = np.zeros(e.size, np.int64) if top <= 0 else np.minimum(
+                levels - 1, np.floor(levels * e / top).astype(np.int64))
+            out.append(-band)
+        return out
 
     @property
     def node_steps(self):
