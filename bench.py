@@ -141,6 +141,15 @@ def mixed_workload(seed=0, scale=1.0, steps_lo=5000, steps_hi=50000):
                 bold_period=0, bold_len=0, target=None, seed=seed)
 
 
+def mixed_prof_workload():
+    """Profiling case of the uneven batch's kernels: every connectome of the
+    mixed workload with 1/8 of its instances (128/128/32/8/2) and 500-2000
+    steps, so one launch takes milliseconds under ncu's replays."""
+    wl = mixed_workload(scale=0.125, steps_lo=500, steps_hi=2000)
+    wl['name'] = 'mixed_prof'
+    return wl
+
+
 def grid_1k_workload():
     """Profiling case of the group kernel: the full 64 x 64 grid (same
     instances, rings and BOLD schedule) for 1000 steps; BOLD sampled every
@@ -234,7 +243,8 @@ def adjoint_workload(N=84, I=256, T=2000, C=100, seed=0):
 
 WORKLOADS = {'grid': grid_workload, 'grid_small': grid_small_workload, 'grid_1k': grid_1k_workload,
              'kuramoto': kuramoto_workload, 'mixed': mixed_workload,
-             'mixed_small': mixed_small_workload, 'net515k': net515k_workload,
+             'mixed_small': mixed_small_workload, 'mixed_prof': mixed_prof_workload,
+             'net515k': net515k_workload,
              'lems_epileptor': lems_workload, 'adjoint': adjoint_workload,
              'net_small': net_small_workload}
 
@@ -372,7 +382,11 @@ class MixedStep:
             # launch shapes per connectome (plain or pipelined kernel, CTA
             # width, cluster) and dispatch priorities from the makespan-aware
             # tuner: whole-batch trials at scaled-down step counts
-            self.batch = groups.GroupBatch(self.sets, steps, shapes='tune' if tune else None)
+            if tune == 'pipelined':
+                shapes = [groups.pipelined_shape(s) for s in self.sets]
+            else:
+                shapes = 'tune' if tune else None
+            self.batch = groups.GroupBatch(self.sets, steps, shapes=shapes)
             self.n_launch = self.batch.n_launches
         else:
             self.batch = engine.Batch(self.sets, steps)
@@ -411,6 +425,9 @@ class MixedStep:
         evs = []
         torch = self.torch
         go = self.batch.replay if self.batch.graph is not None else self.batch.launch
+        # NVTX range of one bench step: ncu --nvtx --nvtx-include "mixed_step/"
+        # (with --graph-profiling graph, the concurrent graph as one workload)
+        torch.cuda.nvtx.range_push('mixed_step')
         if time_kernels:
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
@@ -420,6 +437,7 @@ class MixedStep:
             evs.append((e0, e1))
         else:
             go()
+        torch.cuda.nvtx.range_pop()
         return evs, None
 
     def run_plain(self):
@@ -890,7 +908,8 @@ def gpu_arm(args):
     _native.load()
     wl = WORKLOADS[args.workload]()
     if wl['name'].startswith('mixed'):
-        gs = MixedStep(wl, torch, args.path, not args.no_graph, not args.no_tune)
+        gs = MixedStep(wl, torch, args.path, not args.no_graph,
+                       'pipelined' if args.no_tune and args.pipelined else not args.no_tune)
     elif wl['name'].startswith('net'):
         gs = NetStep(wl, torch)
     elif wl['name'].startswith('lems'):
@@ -1433,7 +1452,10 @@ def main():
     ap.add_argument('--no-graph', action='store_true',
                     help='launch the batch directly instead of replaying a CUDA graph')
     ap.add_argument('--no-tune', action='store_true',
-                    help='mixed batch: default launch shapes instead of the batch tuner')
+                    help='mixed batch: rule-based launch shapes instead of the batch tuner')
+    ap.add_argument('--pipelined', action='store_true',
+                    help='with --no-tune: the pipelined kernel on its smallest cluster where it '
+                         'applies (groups.pipelined_shape), else the plain default')
     args = ap.parse_args()
     if args.impl == 'reference':
         reference_arm(args)

@@ -50,6 +50,11 @@ namespace tvbg {
 
 constexpr int kLanes = TVBG_GROUP_LANES;
 
+// 16-byte loads in flight per thread in the transposed gather (lane_gather_t)
+#ifndef TVBG_GATHER_LOADS
+#define TVBG_GATHER_LOADS 8
+#endif
+
 __device__ __forceinline__ uint32_t cluster_nranks() {
     uint32_t n;
     asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(n));
@@ -522,7 +527,7 @@ __device__ __forceinline__ void lane_gather_t(const tvbg_group& g, int lo, int h
     static_assert(K == 4 || K == 8, "transposed gather: K = 4 or 8");
     constexpr int NI = K == 8 ? 8 : 4;   // instances per lane
     constexpr int NV = NI / 4;           // 16-byte loads per edge
-    constexpr int U = 4 / NV;            // edges per iteration: 4 loads (64 bytes) in flight
+    constexpr int U = TVBG_GATHER_LOADS / NV;  // edges per iteration (loads in flight / loads per edge)
     const int ks = l % K;
     const int m0 = (l / K) * NI;
     const float* __restrict__ ring = g.ring + m0;

@@ -61,6 +61,18 @@ def pipelined_threads(N, cluster):
     return thr if thr <= 1024 else 0
 
 
+def pipelined_shape(gset, clusters=(1, 2, 3, 4, 6, 8, 12, 16)):
+    """(threads, cluster, 0, tpn) of gset on the pipelined kernel's smallest
+    cluster that holds one node per slot, or its plain default shape where
+    the pipelined kernel does not apply (short delays, N > 1024)."""
+    if gset.can_pipeline:
+        for c in clusters:
+            thr = pipelined_threads(gset.N, c)
+            if thr:
+                return (thr, c, 0, PIPELINED)
+    return group_shape(gset.N) + (0, 1)
+
+
 def group_shape(N, threads=None, cluster=None):
     """(threads, cluster) of a plain group launch: one node per 8-lane slot,
     on the smallest cluster (<= 8 CTAs) whose CTAs stay within 1024 threads;
