@@ -334,7 +334,10 @@ int tvbg_fc_ex(const float *d_x, int32_t n_inst, int32_t T, int32_t N,
  * that device current; make that first call before any stream capture.  All
  * calls share the one array: every scratch entry a call reads it has written
  * first, but calls that overlap on the GPU (different streams, no ordering)
- * race on it and must be serialised by the caller.
+ * race on it and must be serialised by the caller.  The looked-up address is
+ * kept per device for the life of the process; cudaDeviceReset unloads the
+ * library's device code and invalidates it, so do not call this entry point
+ * on a device after a cudaDeviceReset in the same process.
  */
 #define TVBG_FC_NOALLOC_MAX_DOUBLES 1048576
 int tvbg_fc_noalloc(const float *d_x, int32_t n_inst, int32_t T, int32_t N,

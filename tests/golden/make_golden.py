@@ -117,7 +117,9 @@ def ref_covar(ref):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else '/root/reference'
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get('TVB_HPC_REFERENCE', '')
+    if not ref:
+        sys.exit('usage: make_golden.py <tvb-hpc checkout> (or set TVB_HPC_REFERENCE)')
     import subprocess
     subprocess.run(['make', '-s', '-C', os.path.join(ROOT, 'oracle')], check=True)
     subprocess.run(['make', '-s', '-C', os.path.join(ROOT, 'oracle'), 'ref', 'REF=' + ref],

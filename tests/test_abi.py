@@ -187,6 +187,48 @@ def test_group_plan_and_shape():
     assert groups.group_shape(84, threads=128) == (128, 6)
 
 
+def test_fc_pair_count_is_64_bit():
+    """N (N + 1) overflows 32 bits from N = 46341: the scratch size and the
+    allocation-free entry point's limit check count it in 64 bits (both
+    return before any device call)."""
+    lib = nat.load()
+    out = ctypes.c_int64(0)
+    for n_inst, N in [(1, 46341), (3, 50000), (2, 65535)]:
+        assert lib.tvbg_fc_scratch_bytes(n_inst, N, ctypes.byref(out)) == nat.TVBG_OK
+        assert out.value == n_inst * N * (N + 1) * 8
+    assert lib.tvbg_fc_scratch_bytes(4, 126, ctypes.byref(out)) == nat.TVBG_OK and out.value == 0
+    rc = lib.tvbg_fc_noalloc(None, 1, 16, 46341, 16 * 46341, None, None, None, None)
+    assert rc == nat.TVBG_EINVAL
+    assert b'TVBG_FC_NOALLOC_MAX_DOUBLES' in lib.tvbg_last_error()
+
+
+def test_pipelined_shapes_and_priority_bands():
+    """Host rules of the pipelined group kernel: two teams of one node per
+    8-lane slot in at most 1024 threads; the batch tuner's candidates;
+    priority bands of a batch (no device needed for the rules)."""
+    from tvb_hpc import autotune, groups
+    assert groups.pipelined_threads(998, 16) == 1024 and groups.pipelined_threads(998, 12) == 0
+    assert groups.pipelined_threads(68, 2) == 576 and groups.pipelined_threads(68, 1) == 0
+    for N in (20, 68, 84, 192, 400, 998):
+        for thr, c, pr, tpn in autotune.group_shapes(N, pipelined=True):
+            assert thr % 32 == 0 and thr <= 1024 and 1 <= c <= groups.MAX_CLUSTER and pr == 0
+            per = thr // 8 if tpn == 1 else thr // 16
+            assert c * per >= N
+            if tpn == nat.GROUP_PIPELINED:
+                assert thr % 64 == 0
+
+    class FakeSet:
+        def __init__(self, steps):
+            self.members = [np.arange(i, min(i + 8, len(steps))) for i in range(0, len(steps), 8)]
+
+    b = groups.GroupBatch.__new__(groups.GroupBatch)
+    steps = [np.array([100] * 8 + [50] * 8), np.array([400] * 8)]
+    b.sets = [FakeSet(n) for n in steps]
+    b.nsteps = steps
+    pr = b.group_priorities([1.0, 1.0])
+    assert list(pr[1]) == [-5] and list(pr[0]) == [-1, 0]
+
+
 def test_plan_ring_constraints():
     for order in ('cuda', 'tracka'):
         for dmin, dmax in [(0, 0), (0, 5), (1, 1), (25, 500), (100, 2000), (5, 6), (3, 250)]:

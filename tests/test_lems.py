@@ -19,7 +19,9 @@ import lems_oracle as lo
 import pyoracle as orc
 from tvb_hpc import lems, network, model
 
-REF_XML = '/root/reference/dsl/dsl_cuda/XMLmodels'
+# the reference's own model files, read where TVB_HPC_REFERENCE names a tvb-hpc checkout
+REF_XML = os.path.join(os.environ.get('TVB_HPC_REFERENCE', '') or '/nonexistent',
+                       'dsl', 'dsl_cuda', 'XMLmodels')
 BUNDLED = ['Kuramoto', 'Oscillator', 'Rwongwang', 'Epileptor', 'Ou', 'Ou6', 'HMJE']
 REFERENCE = ['Kuramoto', 'Oscillator', 'Rwongwang', 'Epileptor']
 

@@ -40,7 +40,7 @@ __global__ void __launch_bounds__(kFcThreads)
     }
     __syncthreads();
 
-    const int npairs = N * (N + 1) / 2;
+    const int npairs = N * (N + 1) / 2;  // small path only: N (N + 1) / 2 <= kFcThreads * kMaxPairsPerThread
     double acc[kMaxPairsPerThread];
     int pi[kMaxPairsPerThread], pj[kMaxPairsPerThread];
 #pragma unroll
@@ -186,12 +186,21 @@ __global__ void fc_norm_kernel(const double* __restrict__ gram, int N, float* __
 
 using namespace tvbg;
 
+namespace {
+// Whether N nodes take the one-CTA small path: N (N + 1) / 2 pairs, counted
+// in 64 bits (the product overflows 32 bits from N = 46341).
+bool fc_small_path(int32_t N) {
+    return static_cast<int64_t>(N) * (N + 1) / 2 <= static_cast<int64_t>(kFcThreads) * kMaxPairsPerThread;
+}
+}  // namespace
+
 extern "C" int tvbg_fc_scratch_bytes(int32_t n_inst, int32_t N, int64_t* bytes) {
     if (!bytes || n_inst <= 0 || N <= 0) return set_error(TVBG_EINVAL, "tvbg_fc_scratch_bytes: bad args");
-    if (N * (N + 1) / 2 <= kFcThreads * kMaxPairsPerThread) {
+    if (fc_small_path(N)) {
         *bytes = 0;
     } else {
-        *bytes = static_cast<int64_t>(n_inst) * N * (N + 1) * static_cast<int64_t>(sizeof(double));
+        *bytes = static_cast<int64_t>(n_inst) * N * (static_cast<int64_t>(N) + 1) *
+                 static_cast<int64_t>(sizeof(double));
     }
     return TVBG_OK;
 }
@@ -205,7 +214,7 @@ extern "C" int tvbg_fc_ex(const float* d_x, int32_t n_inst, int32_t T, int32_t N
     if ((d_target == nullptr) != (d_err == nullptr))
         return set_error(TVBG_EINVAL, "tvbg_fc: d_target and d_err go together");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    if (N * (N + 1) / 2 <= kFcThreads * kMaxPairsPerThread) {
+    if (fc_small_path(N)) {
         const size_t smem = sizeof(double) * (static_cast<size_t>(N) + static_cast<size_t>(kTile) * N + kFcThreads);
         if (smem > 200 * 1024) return set_error(TVBG_EINVAL, "tvbg_fc: N too large for the small path");
         if (smem > 48 * 1024) {

@@ -215,7 +215,7 @@ class FCFit:
         # instances fit one wave of CTAs (with more, the CTAs the smaller
         # global-ring footprint keeps resident together win: measured)
         ring_b = 4 * N * nh
-        sms = torch.cuda.get_device_properties(0).multi_processor_count
+        sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
         smem = ring_b if (self.adjoint_smem == 'auto' and ring_b + 4096 <= max_smem()
                           and I <= sms) else 0
         for k, ((t0, n, st, rg), pl) in enumerate(zip(rev, plans)):
