@@ -639,6 +639,13 @@ int tvbg_serve_poll(tvbg_serve *pool, int64_t id, int32_t *status, float *state_
 int tvbg_serve_cancel(tvbg_serve *pool, int64_t id);
 /* Device bytes held by admitted requests and the footprint of request id. */
 int tvbg_serve_usage(tvbg_serve *pool, int64_t id, int64_t *used, int64_t *footprint);
+/* Admission budget of the following ticks, at most the creation budget: a
+ * caller that holds device memory of its own under the same budget (the
+ * Python serving path beside the pool) passes what it leaves free, so the
+ * two together stay within the budget.  Requests already admitted keep
+ * their memory; a request larger than the creation budget is still refused
+ * by tvbg_serve_admit.  No counterpart in the reference (no serving layer). */
+int tvbg_serve_set_budget(tvbg_serve *pool, int64_t budget);
 
 #ifdef __cplusplus
 }

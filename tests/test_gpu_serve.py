@@ -181,3 +181,38 @@ def test_server_with_native_pool(cuda):
             assert all(np.array_equal(x, y) for x, y in zip(a.grad, done[r.rid].grad))
     st = srv.stats()
     assert st['requests'] == len(reqs) and st['p99_s'] >= st['p50_s'] > 0
+
+
+def test_hybrid_server_shares_the_budget(cuda):
+    """Server(native=True): the Python path (gradient requests) and the
+    native pool admit against one budget; at every tick the bytes both hold
+    stay within it.  A request larger than the budget fails instead of
+    waiting forever."""
+    rng = np.random.default_rng(21)
+    reqs = serve.random_requests(10, rate=1e6, rng=rng, conns=conns(), inst=(4, 24),
+                                 steps=(800, 2000), grad_frac=0.5)
+    assert any(r.want_grad for r in reqs) and not all(r.want_grad for r in reqs)
+    need = [serve.footprint(r) for r in reqs]
+    budget = 2.2 * max(need)
+    srv = serve.Server(hbm_budget=budget, chunk=400, native=True)
+    # an MPR gradient request (the Python path, where its footprint is checked)
+    big = serve.random_requests(1, rate=1e6, rng=np.random.default_rng(3), conns=conns()[2:],
+                                models=('MPR', ), inst=(4000, 4000), steps=(500, 500),
+                                grad_frac=1.0)[0]
+    big.rid = 999
+    assert big.want_grad and serve.footprint(big) > budget
+    for r in reqs + [big]:
+        srv.submit(r)
+    peak = 0
+    for _ in range(10000):
+        if not srv.busy:
+            break
+        srv.tick()
+        held = srv.used + srv.native.used()
+        peak = max(peak, held)
+        assert held <= budget
+    srv._collect(wait=True)
+    assert not srv.busy
+    assert srv.poll(999) == 'failed' and 'exceeds the budget' in big.error
+    assert {r.rid for r in srv.done} == {r.rid for r in reqs}
+    assert peak > 0

@@ -92,3 +92,23 @@ def test_admission_rejects():
         assert lib.tvbg_serve_poll(h, 12345, ctypes.byref(st), None) == nat.TVBG_EINVAL
     finally:
         lib.tvbg_serve_destroy(h)
+
+
+def test_set_budget():
+    """tvbg_serve_set_budget lowers the admission budget of the next ticks
+    (clamped to the creation budget); admitting a request is checked against
+    the creation budget, so a request that fits the pool is queued even while
+    the current budget is small."""
+    w, ln = network.synthetic_connectome(30, 0.3, seed=1)
+    conn = network.Connectivity.from_dense(w, ln)
+    lib, h = pool(budget=1 << 24)
+    try:
+        assert lib.tvbg_serve_set_budget(h, -1) == nat.TVBG_EINVAL
+        assert lib.tvbg_serve_set_budget(None, 10) == nat.TVBG_EINVAL
+        nat.check(lib.tvbg_serve_set_budget(h, 16))
+        q, keep = request(conn, I=4)
+        rid = ctypes.c_int64()
+        nat.check(lib.tvbg_serve_admit(h, ctypes.byref(q), ctypes.byref(rid)))
+        nat.check(lib.tvbg_serve_set_budget(h, 1 << 40))   # clamped to the creation budget
+    finally:
+        lib.tvbg_serve_destroy(h)

@@ -382,7 +382,8 @@ int collect(Request& r) {
 }  // namespace
 
 struct tvbg_serve {
-    int64_t budget = 0, used = 0;
+    int64_t cap = 0;               // budget at creation: a request larger never fits
+    int64_t budget = 0, used = 0;  // current admission budget (tvbg_serve_set_budget)
     int32_t chunk = 0;
     cudaStream_t stream = nullptr;
     bool own_stream = false;
@@ -399,6 +400,7 @@ int tvbg_serve_create(int64_t hbm_budget, int32_t chunk, void* stream, tvbg_serv
     tvbg_serve* p = new (std::nothrow) tvbg_serve;
     if (!p) return set_error(TVBG_EINVAL, "tvbg_serve_create: out of host memory");
     p->budget = hbm_budget;
+    p->cap = hbm_budget;
     p->chunk = chunk;
     p->stream = static_cast<cudaStream_t>(stream);  // NULL: the pool's own, made at the first tick
     *out = p;
@@ -454,7 +456,7 @@ int tvbg_serve_admit(tvbg_serve* p, const tvbg_serve_request* q, int64_t* id) {
     r->state0.assign(q->state0, q->state0 + static_cast<size_t>(q->n_inst) * q->N * sh.ns);
     r->nparam.assign(q->nparam, q->nparam + static_cast<size_t>(q->n_inst) * q->N * sh.np);
     int rc = plan(*r, *q);
-    if (rc == TVBG_OK && static_cast<int64_t>(r->bytes) > p->budget)
+    if (rc == TVBG_OK && static_cast<int64_t>(r->bytes) > p->cap)
         rc = set_error(TVBG_EINVAL, "tvbg_serve_admit: the request alone exceeds the budget");
     if (rc) {
         delete r;
@@ -521,26 +523,34 @@ int tvbg_serve_tick(tvbg_serve* p, int32_t* n_active, int32_t* n_queued) {
     if (rc) return rc;
     e = cudaStreamSynchronize(p->stream);
     if (e != cudaSuccess) return set_cuda_error(e, "tvbg_serve_tick: synchronize");
-    // status words, clocks, retirement
-    std::vector<Request*> keep;
+    // status words first: an error here leaves every request as it was
     for (size_t i = 0; i < p->active.size(); ++i) {
-        Request& r = *p->active[i];
+        const Request& r = *p->active[i];
         int32_t st = 0;
         e = cudaMemcpy(&st, r.dev + r.off_status, sizeof(st), cudaMemcpyDeviceToHost);
         if (e != cudaSuccess) return set_cuda_error(e, "tvbg_serve_tick: status");
         if (st != 0) return set_error(TVBG_EDEVICE, "tvbg_serve_tick: a group kernel reported an error");
+    }
+    // clocks and retirement; the active list is rebuilt before any return, so
+    // a retired (released) request never stays in it, and a request whose
+    // result could not be collected stays active and is collected next tick
+    std::vector<Request*> keep;
+    for (size_t i = 0; i < p->active.size(); ++i) {
+        Request& r = *p->active[i];
         r.done += steps[i];
-        if (r.done >= r.nsteps) {
+        if (rc == TVBG_OK && r.done >= r.nsteps) {
             rc = collect(r);
-            if (rc) return rc;
-            release(r);
-            p->used -= static_cast<int64_t>(r.bytes);
-            r.status = TVBG_SERVE_DONE;
-        } else {
-            keep.push_back(&r);
+            if (rc == TVBG_OK) {
+                release(r);
+                p->used -= static_cast<int64_t>(r.bytes);
+                r.status = TVBG_SERVE_DONE;
+                continue;
+            }
         }
+        keep.push_back(&r);
     }
     p->active.swap(keep);
+    if (rc) return rc;
     if (n_active) *n_active = static_cast<int32_t>(p->active.size());
     if (n_queued) *n_queued = static_cast<int32_t>(p->queue.size());
     return TVBG_OK;
@@ -572,6 +582,12 @@ int tvbg_serve_cancel(tvbg_serve* p, int64_t id) {
         return set_error(TVBG_EINVAL, "tvbg_serve_cancel: the request is done or cancelled");
     }
     r->status = TVBG_SERVE_CANCELLED;
+    return TVBG_OK;
+}
+
+int tvbg_serve_set_budget(tvbg_serve* p, int64_t budget) {
+    if (!p || budget < 0) return set_error(TVBG_EINVAL, "tvbg_serve_set_budget: bad arguments");
+    p->budget = budget < p->cap ? budget : p->cap;
     return TVBG_OK;
 }
 

@@ -75,6 +75,7 @@ class Request:
     steps_done: int = 0
     iset: object = field(default=None, repr=False)
     nbytes: int = 0
+    error: str = None       # why the request failed (it can never fit the budget)
 
     @property
     def node_steps(self):
@@ -124,6 +125,7 @@ class Server:
         self.pool = concurrent.futures.ThreadPoolExecutor(max_workers=1)
         self.pending = []
         self.cancelled = []
+        self.failed = []
         # requests without gradients in the C++ pool: waiting for their
         # arrival here, then in the pool until done
         self.native = NativeServer(hbm_budget, chunk, clock) if native else None
@@ -145,7 +147,10 @@ class Server:
 
     def _native_tick(self):
         """Hand arrived requests to the pool and run one pool tick (its
-        chunks overlap this tick's Python-path launches on the device)."""
+        chunks overlap this tick's Python-path launches on the device).  The
+        pool admits within what the Python path leaves of the budget, so the
+        two together never hold more than the budget."""
+        from . import _native as nat
         now = self.clock()
         keep = []
         for r in sorted(self.native_wait, key=lambda r: r.arrival):
@@ -154,9 +159,15 @@ class Server:
                 continue
             try:
                 self.native.submit(r)
-            except RuntimeError:       # e.g. delays too short for the group kernel
-                self.queue.append(r)   # the Python path has the per-step kernel
+            except nat.TvbgError as e:
+                if e.code == nat.TVBG_EUNSUPPORTED:
+                    self.queue.append(r)   # delays too short for the group kernel: per-step kernel
+                elif e.code == nat.TVBG_EINVAL:
+                    self._fail(r, str(e))  # e.g. the request alone exceeds the budget
+                else:
+                    raise
         self.native_wait = keep
+        self.native.set_budget(max(0, int(self.budget - self.used)))
         a, q = self.native.tick()
         self.native_busy = bool(a or q)
         for r in self.native.done[self._native_seen:]:
@@ -167,7 +178,8 @@ class Server:
     def poll(self, rid):
         """State of request `rid`: 'queued', 'active' (its steps are running),
         'gradient' (its FC-fit gradients are being computed), 'done',
-        'cancelled', or None if the server has never seen it."""
+        'cancelled', 'failed' (it can never fit the budget; req.error says why),
+        or None if the server has never seen it."""
         if self.native is not None:
             if any(r.rid == rid for r in self.native_wait):
                 return 'queued'
@@ -176,7 +188,7 @@ class Server:
                 return st
         for name, reqs in (('queued', self.queue), ('active', self.active),
                            ('gradient', [r for r, _ in self.pending]), ('done', self.done),
-                           ('cancelled', self.cancelled)):
+                           ('cancelled', self.cancelled), ('failed', self.failed)):
             if any(r.rid == rid for r in reqs):
                 return name
         return None
@@ -216,6 +228,10 @@ class Server:
                 keep.append(req)
                 continue
             need = footprint(req)
+            if need > self.budget:     # can never fit: fail it rather than queue it forever
+                self._fail(req, 'device footprint %d bytes exceeds the budget %d' % (
+                    need, int(self.budget)))
+                continue
             free = torch.cuda.mem_get_info()[0]
             held = self.used + (self.native.used() if self.native is not None else 0)
             if held + need > self.budget or need > free:
@@ -227,6 +243,11 @@ class Server:
             self.used += need
             into.append(req)
         self.queue = keep
+
+    def _fail(self, req, why):
+        req.error = why
+        req.finished = self.clock()
+        self.failed.append(req)
 
     @staticmethod
     def _make_set(req):
@@ -497,6 +518,10 @@ class NativeServer:
         self.nat.check(self.lib.tvbg_serve_usage(self.h, self.reqs[rid][1], ctypes.byref(u),
                                                  ctypes.byref(f)))
         return f.value
+
+    def set_budget(self, nbytes):
+        "Admission budget of the following ticks (at most the creation budget)."
+        self.nat.check(self.lib.tvbg_serve_set_budget(self.h, int(nbytes)))
 
     def used(self):
         "Device bytes held by admitted requests."
