@@ -1274,13 +1274,73 @@ def cpu_baseline_mixed(wl, sample=None, sets=None, budget_s=12.0):
     return out
 
 
+def serve_window(rate, seconds, max_inst, chunk, conns, seed=7, drain_s=60.0, sample_s=0.5):
+    """One serving run: Poisson arrivals at `rate` per second for `seconds`
+    (models Kuramoto / 2-D oscillator / MPR, N in {68, 84, 192, 400, 998},
+    instances log-uniform in 1..max_inst, steps log-uniform in 1k..100k, 10 %
+    of MPR requests with FC-fit gradients) into Server(native=True) with a
+    180 GB budget; ticks until every request is done or `drain_s` after the
+    window, then cancels what is left.  The requests in the system (arrived,
+    not finished) are sampled every `sample_s`; the queue kept up when that
+    count does not grow over the second half of the window (least-squares
+    slope below 5 % of the arrival rate) and nothing was left at the end."""
+    import torch
+    from tvb_hpc import serve
+    rng = np.random.default_rng(seed)
+    n_req = max(1, int(rate * seconds))
+    reqs = serve.random_requests(n_req, rate, rng, conns, inst=(1, max_inst), steps=(1000, 100000))
+    srv = serve.Server(chunk=chunk, native=True)
+    t_start = time.perf_counter()
+    for r in reqs:
+        r.arrival += t_start
+        srv.submit(r)
+    samples, next_s = [], 0.0
+    stop = t_start + seconds + drain_s
+    while srv.busy and time.perf_counter() < stop:
+        srv.run(until_empty=False)
+        now = time.perf_counter()
+        if now - t_start >= next_s:
+            arrived = sum(1 for r in reqs if r.arrival <= now)
+            finished = sum(1 for r in reqs if r.finished is not None)
+            samples.append((round(now - t_start, 2), arrived - finished))
+            next_s += sample_s
+    left = [r for r in reqs if r.finished is None]
+    for r in left:
+        srv.cancel(r.rid)
+    srv._collect(wait=True)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t_start
+    done = [r for r in reqs if r.finished is not None and r.error is None]
+    failed = [r for r in reqs if r.error is not None]
+    lat = np.array([r.finished - r.arrival for r in done]) if done else np.zeros(1)
+    work = sum(r.node_steps for r in done)
+    t_last = max((r.finished for r in done), default=t_start + 1e-9) - t_start
+    half = [(t, n) for t, n in samples if seconds / 2 <= t <= seconds]
+    slope = float(np.polyfit([t for t, _ in half], [n for _, n in half], 1)[0]) if len(half) > 2 else 0.0
+    offered = sum(r.node_steps for r in reqs) / seconds
+    return {
+        'rate_per_s': rate, 'window_s': seconds, 'requests': n_req, 'completed': len(done),
+        'failed': len(failed), 'left_at_cutoff': len(left),
+        'gradient_requests': sum(1 for r in reqs if r.want_grad),
+        'p50_latency_s': round(float(np.percentile(lat, 50)), 3),
+        'p99_latency_s': round(float(np.percentile(lat, 99)), 3),
+        'offered_node_steps_per_s': round(offered, 1),
+        'served_node_steps_per_s': round(work / max(t_last, 1e-9), 1),
+        'wall_s': round(wall, 2),
+        'in_system_slope_per_s': round(slope, 3),
+        'queue_kept_up': bool(slope < 0.05 * rate and not left),
+        'in_system_samples': samples[::max(1, len(samples) // 60)],
+    }, reqs
+
+
 def serve_arm(args):
-    """Serving loop: Poisson arrivals, models Kuramoto /
-    2-D oscillator / MPR, N in {68, 84, 192, 400, 998}, instance and step
-    counts log-uniform, 10% of MPR requests with FC-fit gradients, admission
-    by a 180 GB HBM budget.  The arrival window is bounded (--serve-seconds)
-    and the instance range capped (--serve-max-inst) so the run ends in
-    minutes; the same requests then run one by one as plain sweeps."""
+    """Serving loop at the configured rate and window (default: 50 requests
+    per second for 60 s, up to 4096 instances, 1k-100k steps, 10 % FC-fit
+    gradient requests, 180 GB budget): p50/p99 latency, offered vs served
+    node-steps/s, requests in the system over time and whether the queue
+    kept up; then a sweep of arrival rates over shorter windows for the
+    largest rate the queue keeps up with; then the plain paths on the same
+    requests (each alone, group kernel and per-step kernel)."""
     import torch
     torch.cuda.set_device(0)
     from tvb_hpc import network, serve, _native
@@ -1289,85 +1349,82 @@ def serve_arm(args):
     for k, (N, dens, _) in enumerate(MIXED_SPEC):
         w, ln = network.synthetic_connectome(N, dens, seed=k)
         conns.append(network.Connectivity.from_dense(w, ln))
-    rng = np.random.default_rng(7)
-    n_req = max(1, int(args.serve_rate * args.serve_seconds))
-    reqs = serve.random_requests(n_req, args.serve_rate, rng, conns,
-                                 inst=(1, args.serve_max_inst), steps=(1000, 100000))
-    # warm-up: load every kernel once, the FC-fit gradient path's library
-    # GEMMs included (their first call on a fresh process is slow)
+    # warm-up: load every kernel once, the FC-fit gradient path included
     warm = serve.Server(chunk=args.serve_chunk, native=True)
     for r in serve.random_requests(8, 1e6, np.random.default_rng(1), conns[:2], inst=(1, 2),
                                    steps=(200, 300), grad_frac=1.0):
         warm.submit(r)
     warm.run()
     torch.cuda.synchronize()
-    # requests without gradients in the C++ pool, gradient requests on the
-    # Python path (FC-fit adjoint on a worker thread), the same ticks
-    srv = serve.Server(chunk=args.serve_chunk, native=True)
-    t_start = time.perf_counter()
-    for r in reqs:
-        r.arrival += t_start
-        srv.submit(r)
-    srv.run()
-    wall = time.perf_counter() - t_start
-    st = srv.stats()
-    offered = sum(r.node_steps for r in reqs) / max(args.serve_seconds, 1e-9)
-    served = st['node_steps'] / wall
-    native = serve_native(args, conns)
+    main, reqs = serve_window(args.serve_rate, args.serve_seconds, args.serve_max_inst,
+                              args.serve_chunk, conns, drain_s=args.serve_drain)
+    sweep = []
+    for rate in [float(x) for x in args.serve_sweep.split(',') if x]:
+        res, _ = serve_window(rate, args.serve_sweep_seconds, args.serve_max_inst, args.serve_chunk,
+                              conns, seed=11, drain_s=args.serve_drain)
+        res.pop('in_system_samples')
+        sweep.append(res)
+    kept = [x['rate_per_s'] for x in sweep if x['queue_kept_up']]
+    plain_groups = serve_plain_groups(reqs, budget_s=args.serve_plain_seconds)
     plain = serve_plain(reqs, budget_s=args.serve_plain_seconds)
-    line = {'metric': METRIC, 'value': round(served, 1), 'unit': UNIT, 'n_gpus': 1,
+    served = main['served_node_steps_per_s']
+    line = {'metric': METRIC, 'value': served, 'unit': UNIT, 'n_gpus': 1,
             'steps': 1, 'warmup': 1, 'higher_is_better': True, 'scaling': 'weak',
             'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic (seeded connectomes)',
             'config': {'workload': 'serve', 'rate_per_s': args.serve_rate,
-                       'window_s': args.serve_seconds, 'requests': n_req,
-                       'max_instances': args.serve_max_inst, 'chunk_steps': args.serve_chunk,
-                       'hbm_budget_gb': 180,
-                       'path': 'Server(native=True): C++ pool for requests without gradients, '
-                               'Python path + FC-fit adjoint worker for gradient requests'},
-            'serve': {'p50_latency_s': round(st.get('p50_s', float('nan')), 3),
-                      'p99_latency_s': round(st.get('p99_s', float('nan')), 3),
-                      'wall_s': round(wall, 3), 'ticks': st['ticks'], 'phase_s': st['phase_s'],
-                      'offered_node_steps_per_s': round(offered, 1),
-                      'queue_kept_up': bool(wall <= args.serve_seconds * 1.25)},
-            'native_pool': native,
+                       'window_s': args.serve_seconds, 'max_instances': args.serve_max_inst,
+                       'steps': '1k-100k log-uniform', 'gradient_fraction_of_mpr': 0.1,
+                       'chunk_steps': args.serve_chunk, 'hbm_budget_gb': 180,
+                       'path': 'Server(native=True): C++ pool (group kernels, pipelined where '
+                               'the delays allow) for requests without gradients, Python path '
+                               '+ FC-fit adjoint worker for gradient requests'},
+            'serve': main,
+            'rate_sweep': sweep,
+            'largest_rate_kept_up': max(kept) if kept else None,
+            'plain_groups': plain_groups,
             'plain': plain,
+            'served_vs_plain_groups': (round(served / plain_groups['value'], 3)
+                                       if plain_groups['value'] else None),
             'served_vs_plain': round(served / plain['value'], 3) if plain['value'] else None}
     print(json.dumps(line), flush=True)
 
 
-def serve_native(args, conns):
-    """The same arrival stream without the gradient requests, through the
-    native pool (tvbg_serve_*): requests submitted as they arrive, one tick
-    at a time; p50/p99 latency and node-steps/s over the wall time."""
-    from tvb_hpc import serve
-    reqs = [r for r in serve.random_requests(max(1, int(args.serve_rate * args.serve_seconds)),
-                                             args.serve_rate, np.random.default_rng(7), conns,
-                                             inst=(1, args.serve_max_inst), steps=(1000, 100000))
-            if not r.want_grad]
-    pool = serve.NativeServer(chunk=args.serve_chunk)
-    t0 = time.perf_counter()
-    for r in reqs:
-        r.arrival += t0
-    pending = sorted(reqs, key=lambda r: r.arrival)
-    ticks = 0
-    while True:
-        now = time.perf_counter()
-        while pending and pending[0].arrival <= now:
-            pool.submit(pending.pop(0))
-        a, q = pool.tick()
-        ticks += 1
-        if not pending and a == 0 and q == 0:
+def serve_plain_groups(reqs, budget_s=20.0):
+    """The best plain path on the same requests: each request alone on the
+    group kernel (GroupSet, pipelined where the delays allow), one launch
+    set per request, requests one after the other in arrival order, until
+    `budget_s` of GPU time is spent (gradient requests run forward only)."""
+    import torch
+    from tvb_hpc import groups, scheme, serve
+    done, el, n_req = 0.0, 0.0, 0
+    for r in sorted(reqs, key=lambda r: r.arrival):
+        if el >= budget_s:
             break
-        if a == 0 and q == 0 and pending:
-            time.sleep(max(0.0, min(0.05, pending[0].arrival - time.perf_counter())))
-    wall = time.perf_counter() - t0
-    pool.close()
-    lat = np.array([r.finished - r.arrival for r in reqs])
-    work = sum(r.node_steps for r in reqs)
-    return {'requests': len(reqs), 'p50_latency_s': round(float(np.percentile(lat, 50)), 3),
-            'p99_latency_s': round(float(np.percentile(lat, 99)), 3), 'wall_s': round(wall, 3),
-            'ticks': ticks, 'value': round(work / wall, 1), 'unit': UNIT,
-            'path': 'C++ pool (tvbg_serve_*), group kernel, requests without gradients'}
+        M, C, noise = serve.MODELS[r.model]
+        m = M()
+        cf = C(m)
+        scm = scheme.EulerMaryuyamaStep(r.dt) if noise else scheme.EulerStep(r.dt)
+        try:
+            gs = groups.GroupSet(m, cf, scm, r.conn, dt=r.dt, couplings=r.couplings,
+                                 speeds=r.speeds, state0=r.x0, nparam=r.nparam, seed=r.seed)
+        except ValueError:
+            continue
+        gs.set_shape(*groups.pipelined_shape(gs))
+        left = int(r.nsteps)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        while left > 0 and el + (time.perf_counter() - t0) < budget_s:
+            n = min(20000, left)
+            gs.run(n)
+            left -= n
+        el += time.perf_counter() - t0
+        done += float(r.couplings.size) * r.conn.nnode * (r.nsteps - left)
+        n_req += 1
+        del gs
+    return {'value': round(done / el, 1) if el > 0 else None, 'unit': UNIT, 'requests': n_req,
+            'seconds': round(el, 3),
+            'path': 'each request alone: group kernel (pipelined where the delays allow), '
+                    'chunks of 20000 steps'}
 
 
 def serve_plain(reqs, budget_s=20.0):
@@ -1438,8 +1495,13 @@ def main():
     ap.add_argument('--warmup', type=int, default=3)
     ap.add_argument('--workload', default='mixed', choices=sorted(WORKLOADS) + ['serve'])
     ap.add_argument('--serve-rate', type=float, default=50.0)
-    ap.add_argument('--serve-seconds', type=float, default=2.0)
-    ap.add_argument('--serve-max-inst', type=int, default=256)
+    ap.add_argument('--serve-seconds', type=float, default=60.0)
+    ap.add_argument('--serve-max-inst', type=int, default=4096)
+    ap.add_argument('--serve-drain', type=float, default=60.0,
+                    help='seconds after the arrival window before unfinished requests are cancelled')
+    ap.add_argument('--serve-sweep', default='4,8,12,16',
+                    help='arrival rates of the stability sweep (comma-separated, empty: none)')
+    ap.add_argument('--serve-sweep-seconds', type=float, default=30.0)
     ap.add_argument('--serve-chunk', type=int, default=5000)
     ap.add_argument('--serve-plain-seconds', type=float, default=20.0)
     ap.add_argument('--impl', default='engine', choices=['engine', 'reference'])

@@ -75,11 +75,11 @@ struct Request {
     float cf_b = 0.0f, cf_p[3] = {0, 0, 0}, sigma[4] = {0, 0, 0, 0}, consts[16] = {};
     std::vector<float> couplings, state0, nparam;
     // plan
-    int channels = 1, threads = 0, cluster = 1;
+    int channels = 1, threads = 0, cluster = 1, tpn = 1;  // tpn 2: pipelined group kernel
     std::vector<int32_t> row, nodes;
     std::vector<float> wsum;
     std::vector<tvbg_edge> edges;     // [tables][nnz]
-    std::vector<int> table_k, table_lognh;
+    std::vector<int> table_k, table_lognh, table_dmin;
     std::vector<int> g_table;         // per group
     std::vector<std::vector<int>> members;
     size_t off_edges = 0, off_row = 0, off_wsum = 0, off_nodes = 0, off_ring = 0, off_state = 0,
@@ -94,6 +94,17 @@ struct Request {
     std::vector<tvbg_group> records;
     std::vector<float> result;        // [n_inst][N][ns] once done
 };
+
+// The plain group kernel's shape: the smallest cluster whose CTAs stay
+// within 1024 threads, one node per 8-lane slot (several beyond 8 CTAs).
+void plain_shape(Request& r) {
+    int c = 1;
+    while (L * ((r.N + c - 1) / c) > 1024 && c < 8) c *= 2;
+    r.tpn = 1;
+    r.cluster = c;
+    const int per = (r.N + c - 1) / c;
+    r.threads = std::min(1024, 32 * ((L * per + 31) / 32));
+}
 
 int next_pow2(int v) {
     int p = 1;
@@ -135,6 +146,7 @@ int plan(Request& r, const tvbg_serve_request& q) {
         if (lognh > 16) return set_error(TVBG_EINVAL, "tvbg_serve_admit: delays beyond 2^16 - 9 steps");
         r.table_k.push_back(k);
         r.table_lognh.push_back(lognh);
+        r.table_dmin.push_back(dmin);
         if (nnz > 0) {
             int rc = tvbg_pack_edges_group(N, nnz, q.row, q.col, q.weights, d.data(), lognh,
                                            r.edges.data() + static_cast<size_t>(t) * nnz);
@@ -165,12 +177,25 @@ int plan(Request& r, const tvbg_serve_request& q) {
         }
     }
     const int G = static_cast<int>(r.members.size());
-    // launch shape: the smallest cluster whose CTAs stay within 1024 threads
-    int c = 1;
-    while (L * ((N + c - 1) / c) > 1024 && c < 8) c *= 2;
-    r.cluster = c;
-    const int per = (N + c - 1) / c;
-    r.threads = std::min(1024, 32 * ((L * per + 31) / 32));
+    // launch shape: the pipelined kernel on its smallest cluster that holds
+    // one node per slot, where every delay is at least 2K - 1 steps (its
+    // results equal the plain kernel's); else the plain kernel on the smallest
+    // cluster whose CTAs stay within 1024 threads
+    bool pipe = true;
+    for (int t = 0; t < T; ++t) pipe = pipe && r.table_dmin[t] >= 2 * r.table_k[t] - 1;
+    r.tpn = 1;
+    if (pipe) {
+        for (int c : {1, 2, 3, 4, 6, 8, 12, 16}) {
+            const int thr = 2 * 32 * ((L * ((N + c - 1) / c) + 31) / 32);
+            if (thr <= 1024) {
+                r.tpn = TVBG_GROUP_PIPELINED;
+                r.cluster = c;
+                r.threads = thr;
+                break;
+            }
+        }
+    }
+    if (r.tpn != TVBG_GROUP_PIPELINED) plain_shape(r);
     // launch order: one launch per block length, groups in index order
     for (int k : {4, 8}) {
         int cnt = 0;
@@ -220,7 +245,44 @@ int plan(Request& r, const tvbg_serve_request& q) {
 }
 
 // Allocate, upload and initialise the request's device state.
+// Whether the device can hold one cluster of the pipelined shape of r
+// (cudaOccupancyMaxActiveClusters); the plain shape is used where not.
+bool pipelined_fits(const Request& r) {
+    for (int k : r.k_list) {
+        GroupKernel kfn = lookup_group_kernel(r.model, r.cfun, k, true);
+        if (!kfn) return false;
+        const size_t smem = group_pipelined_smem_bytes(k, r.threads, group_channels(r.cfun));
+        if (smem + sizeof(tvbg_group) > 48u * 1024u &&
+            cudaFuncSetAttribute(reinterpret_cast<const void*>(kfn),
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 static_cast<int>(smem)) != cudaSuccess)
+            return (cudaGetLastError(), false);
+        if (r.cluster > 8 &&
+            cudaFuncSetAttribute(reinterpret_cast<const void*>(kfn),
+                                 cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess)
+            return (cudaGetLastError(), false);
+        cudaLaunchConfig_t lc;
+        std::memset(&lc, 0, sizeof(lc));
+        lc.gridDim = dim3(static_cast<unsigned>(r.cluster), 1, 1);
+        lc.blockDim = dim3(static_cast<unsigned>(r.threads), 1, 1);
+        lc.dynamicSmemBytes = smem;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = static_cast<unsigned>(r.cluster);
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        lc.attrs = attr;
+        lc.numAttrs = 1;
+        int n = 0;
+        if (cudaOccupancyMaxActiveClusters(&n, reinterpret_cast<const void*>(kfn), &lc) != cudaSuccess)
+            return (cudaGetLastError(), false);
+        if (n < 1) return false;
+    }
+    return true;
+}
+
 int materialise(Request& r) {
+    if (r.tpn == TVBG_GROUP_PIPELINED && !pipelined_fits(r)) plain_shape(r);
     cudaError_t e = cudaMalloc(&r.dev, r.bytes);
     if (e != cudaSuccess) {
         r.dev = nullptr;
@@ -297,6 +359,7 @@ int materialise(Request& r) {
         rec.bold_period = 1;
         rec.bold_len = 0;
         rec.bold_obs = (r.model == TVBG_MODEL_KURAMOTO || r.model == TVBG_MODEL_G2DO) ? 1 : 0;
+        rec.dmin = r.table_dmin[t];
         rec.seed_lo = static_cast<uint32_t>(seed & 0xffffffffu);
         rec.seed_hi = static_cast<uint32_t>(seed >> 32);
         rec.dt = r.dt;
@@ -345,12 +408,16 @@ int launch_chunk(Request& r, int64_t steps) {
         cfg.cfun = r.cfun;
         cfg.threads = r.threads;
         cfg.cluster = r.cluster;
+        cfg.tpn = r.tpn;
         cfg.block_k = r.k_list[i];
         cfg.d_status = reinterpret_cast<int32_t*>(r.dev + r.off_status);
         cfg.d_order = reinterpret_cast<const int32_t*>(r.dev + r.off_order) + r.k_start[i];
-        GroupKernel k = lookup_group_kernel(r.model, r.cfun, r.k_list[i]);
+        const bool pipe = r.tpn == TVBG_GROUP_PIPELINED;
+        GroupKernel k = lookup_group_kernel(r.model, r.cfun, r.k_list[i], pipe);
         if (!k) return set_error(TVBG_EUNSUPPORTED, "tvbg_serve: group kernel not built");
-        const size_t smem = group_smem_bytes(cfg.block_k, cfg.threads, group_channels(cfg.cfun));
+        const size_t smem =
+            pipe ? group_pipelined_smem_bytes(cfg.block_k, cfg.threads, group_channels(cfg.cfun))
+                 : group_smem_bytes(cfg.block_k, cfg.threads, group_channels(cfg.cfun));
         int rc = launch_group_kernel(k, reinterpret_cast<const tvbg_group*>(r.dev + r.off_groups),
                                      r.k_count[i], &cfg, r.cluster, smem, r.stream, sink);
         if (rc) return rc;

@@ -87,13 +87,29 @@ class Request:
 
 
 def footprint(req):
-    "Device bytes a request needs (rings, state, parameters, edges), estimated."
+    """Device bytes a request needs (rings, state, parameters, edges),
+    estimated; a gradient request adds the FC-fit adjoint's memory
+    (adjoint_bytes), which it holds until its gradients are done."""
     from .engine import plan_ring
     N, I = req.conn.nnode, req.couplings.size
     d = req.conn.delays(float(np.min(req.speeds)), req.dt, 'ceil')
     lognh = plan_ring(int(d.min()), int(d.max()), extra=8)[0]
     ring = N * ((1 << lognh) + 8) * 4
-    return I * (ring + N * 4 * 6 + 512) + req.conn.nnz * 8 * len(np.unique(req.speeds))
+    base = I * (ring + N * 4 * 6 + 512) + req.conn.nnz * 8 * len(np.unique(req.speeds))
+    if req.want_grad and req.model == 'MPR' and req.target is not None:
+        base += adjoint_bytes(I, N, int(req.nsteps), 1 << lognh)
+    return base
+
+
+def adjoint_bytes(I, N, T, nh, checkpoint_every=100):
+    """Device bytes of adjoint.FCFit for I instances, N nodes, T steps:
+    the rate series (FP32 trace; FP64 X, its centred and normalised copies
+    and the gradient temporaries of the loss; FP32 copies), dL/dr, one state + ring checkpoint per chunk of
+    checkpoint_every steps, the recomputation trace and the adjoint ring."""
+    series = I * T * N * (4 + 8 * 8 + 4 * 3)   # peak of the loss's FP64/FP32 temporaries
+    ckpt = -(-T // checkpoint_every) * I * N * (nh + 2) * 4
+    chunk = I * checkpoint_every * N * 3 * 4 + I * N * nh * 4
+    return series + ckpt + chunk + I * N * N * 8 * 3
 
 
 class Server:
@@ -271,13 +287,15 @@ class Server:
 
     def _retire(self, req):
         req.state = req.iset.state.cpu().numpy()
-        self.used -= req.nbytes
         req.iset = None
         if req.want_grad and req.model == 'MPR' and req.target is not None:
             # FC-fit gradients (recomputed forward + adjoint) run on a worker
-            # thread with its own stream, so they hold up no tick
+            # thread with its own stream, so they hold up no tick; the
+            # request keeps its bytes (its footprint counts the adjoint)
+            # until they are done
             self.pending.append((req, self.pool.submit(self._gradient, req)))
             return
+        self.used -= req.nbytes
         req.finished = self.clock()
         self.done.append(req)
 
@@ -287,7 +305,10 @@ class Server:
         with torch.cuda.stream(self.grad_stream):
             prob = FCFit(req.conn, req.dt, float(req.speeds[0]), req.x0, req.target, req.nsteps)
             prob.forward(req.couplings, np.asarray(req.nparam).reshape(req.couplings.size, -1))
-            return tuple(t.cpu().numpy() for t in prob.backward())
+            out = tuple(t.cpu().numpy() for t in prob.backward())
+        del prob
+        torch.cuda.empty_cache()   # give the adjoint's memory back for admission
+        return out
 
     def _collect(self, wait=False):
         "Finish the gradient requests whose worker job is done."
@@ -295,6 +316,7 @@ class Server:
         for req, fut in self.pending:
             if wait or fut.done():
                 req.grad = fut.result()
+                self.used -= req.nbytes
                 req.finished = self.clock()
                 self.done.append(req)
             else:
