@@ -1280,10 +1280,13 @@ def serve_window(rate, seconds, max_inst, chunk, conns, seed=7, drain_s=60.0, sa
     instances log-uniform in 1..max_inst, steps log-uniform in 1k..100k, 10 %
     of MPR requests with FC-fit gradients) into Server(native=True) with a
     180 GB budget; ticks until every request is done or `drain_s` after the
-    window, then cancels what is left.  The requests in the system (arrived,
-    not finished) are sampled every `sample_s`; the queue kept up when that
-    count does not grow over the second half of the window (least-squares
-    slope below 5 % of the arrival rate) and nothing was left at the end."""
+    window, then cancels what is left.  Sampled every `sample_s`: the
+    requests in the system (arrived, not finished) and the work backlog
+    (node-steps arrived minus node-steps taken, finished or not).  The queue
+    kept up when the backlog does not grow over the second half of the
+    window (least-squares slope below 5 % of the offered node-steps/s) and
+    no request was left at the cut-off; served node-steps/s count every
+    step taken up to the cut-off."""
     import torch
     from tvb_hpc import serve
     rng = np.random.default_rng(seed)
@@ -1300,10 +1303,13 @@ def serve_window(rate, seconds, max_inst, chunk, conns, seed=7, drain_s=60.0, sa
         srv.run(until_empty=False)
         now = time.perf_counter()
         if now - t_start >= next_s:
-            arrived = sum(1 for r in reqs if r.arrival <= now)
-            finished = sum(1 for r in reqs if r.finished is not None)
-            samples.append((round(now - t_start, 2), arrived - finished))
+            arr = [r for r in reqs if r.arrival <= now]
+            finished = sum(1 for r in arr if r.finished is not None)
+            backlog = sum(r.node_steps for r in arr if r.error is None) - srv.work_done(arr)
+            samples.append((round(now - t_start, 2), len(arr) - finished, float('%.4g' % backlog)))
             next_s += sample_s
+    t_cut = time.perf_counter() - t_start
+    work = srv.work_done(reqs)
     left = [r for r in reqs if r.finished is None]
     for r in left:
         srv.cancel(r.rid)
@@ -1313,10 +1319,12 @@ def serve_window(rate, seconds, max_inst, chunk, conns, seed=7, drain_s=60.0, sa
     done = [r for r in reqs if r.finished is not None and r.error is None]
     failed = [r for r in reqs if r.error is not None]
     lat = np.array([r.finished - r.arrival for r in done]) if done else np.zeros(1)
-    work = sum(r.node_steps for r in done)
-    t_last = max((r.finished for r in done), default=t_start + 1e-9) - t_start
-    half = [(t, n) for t, n in samples if seconds / 2 <= t <= seconds]
-    slope = float(np.polyfit([t for t, _ in half], [n for _, n in half], 1)[0]) if len(half) > 2 else 0.0
+    half = [x for x in samples if seconds / 2 <= x[0] <= seconds]
+
+    def slope(k):
+        return (float(np.polyfit([x[0] for x in half], [x[k] for x in half], 1)[0])
+                if len(half) > 2 else 0.0)
+
     offered = sum(r.node_steps for r in reqs) / seconds
     return {
         'rate_per_s': rate, 'window_s': seconds, 'requests': n_req, 'completed': len(done),
@@ -1324,12 +1332,14 @@ def serve_window(rate, seconds, max_inst, chunk, conns, seed=7, drain_s=60.0, sa
         'gradient_requests': sum(1 for r in reqs if r.want_grad),
         'p50_latency_s': round(float(np.percentile(lat, 50)), 3),
         'p99_latency_s': round(float(np.percentile(lat, 99)), 3),
+        'latency_of': 'completed requests',
         'offered_node_steps_per_s': round(offered, 1),
-        'served_node_steps_per_s': round(work / max(t_last, 1e-9), 1),
+        'served_node_steps_per_s': round(work / max(t_cut, 1e-9), 1),
         'wall_s': round(wall, 2),
-        'in_system_slope_per_s': round(slope, 3),
-        'queue_kept_up': bool(slope < 0.05 * rate and not left),
-        'in_system_samples': samples[::max(1, len(samples) // 60)],
+        'in_system_slope_per_s': round(slope(1), 3),
+        'backlog_slope_node_steps_per_s': float('%.4g' % slope(2)),
+        'queue_kept_up': bool(slope(2) < 0.05 * offered and not left),
+        'samples_t_insystem_backlog': samples[::max(1, len(samples) // 60)],
     }, reqs
 
 
@@ -1362,7 +1372,7 @@ def serve_arm(args):
     for rate in [float(x) for x in args.serve_sweep.split(',') if x]:
         res, _ = serve_window(rate, args.serve_sweep_seconds, args.serve_max_inst, args.serve_chunk,
                               conns, seed=11, drain_s=args.serve_drain)
-        res.pop('in_system_samples')
+        res.pop('samples_t_insystem_backlog')
         sweep.append(res)
     kept = [x['rate_per_s'] for x in sweep if x['queue_kept_up']]
     plain_groups = serve_plain_groups(reqs, budget_s=args.serve_plain_seconds)
@@ -1499,9 +1509,9 @@ def main():
     ap.add_argument('--serve-max-inst', type=int, default=4096)
     ap.add_argument('--serve-drain', type=float, default=60.0,
                     help='seconds after the arrival window before unfinished requests are cancelled')
-    ap.add_argument('--serve-sweep', default='4,8,12,16',
+    ap.add_argument('--serve-sweep', default='4,6,8,10',
                     help='arrival rates of the stability sweep (comma-separated, empty: none)')
-    ap.add_argument('--serve-sweep-seconds', type=float, default=30.0)
+    ap.add_argument('--serve-sweep-seconds', type=float, default=60.0)
     ap.add_argument('--serve-chunk', type=int, default=5000)
     ap.add_argument('--serve-plain-seconds', type=float, default=20.0)
     ap.add_argument('--impl', default='engine', choices=['engine', 'reference'])

@@ -639,6 +639,8 @@ int tvbg_serve_poll(tvbg_serve *pool, int64_t id, int32_t *status, float *state_
 int tvbg_serve_cancel(tvbg_serve *pool, int64_t id);
 /* Device bytes held by admitted requests and the footprint of request id. */
 int tvbg_serve_usage(tvbg_serve *pool, int64_t id, int64_t *used, int64_t *footprint);
+/* Steps request id has taken so far (every instance takes the same). */
+int tvbg_serve_progress(tvbg_serve *pool, int64_t id, int64_t *steps_done);
 /* Admission budget of the following ticks, at most the creation budget: a
  * caller that holds device memory of its own under the same budget (the
  * Python serving path beside the pool) passes what it leaves free, so the

@@ -652,6 +652,14 @@ int tvbg_serve_cancel(tvbg_serve* p, int64_t id) {
     return TVBG_OK;
 }
 
+int tvbg_serve_progress(tvbg_serve* p, int64_t id, int64_t* steps_done) {
+    if (!p || !steps_done) return set_error(TVBG_EINVAL, "tvbg_serve_progress: null");
+    auto it = p->all.find(id);
+    if (it == p->all.end()) return set_error(TVBG_EINVAL, "tvbg_serve_progress: unknown id");
+    *steps_done = it->second->done;
+    return TVBG_OK;
+}
+
 int tvbg_serve_set_budget(tvbg_serve* p, int64_t budget) {
     if (!p || budget < 0) return set_error(TVBG_EINVAL, "tvbg_serve_set_budget: bad arguments");
     p->budget = budget < p->cap ? budget : p->cap;

@@ -410,6 +410,22 @@ class Server:
                 break
         return self.done
 
+    def work_done(self, reqs):
+        """Node-steps taken so far by `reqs` (submitted to this server),
+        finished or not."""
+        total = 0.0
+        for r in reqs:
+            if r.error is not None:
+                continue
+            if r.finished is not None and r.state is not None:
+                steps = r.nsteps
+            elif self.native is not None and r.rid in self.native.reqs:
+                steps = self.native.steps_done(r.rid)
+            else:
+                steps = r.steps_done
+            total += float(r.couplings.size) * r.conn.nnode * steps
+        return total
+
     def stats(self):
         lat = np.array([r.latency for r in self.done if r.latency is not None])
         out = {'requests': len(self.done), 'ticks': self.ticks, 'node_steps': self.node_steps,
@@ -540,6 +556,13 @@ class NativeServer:
         self.nat.check(self.lib.tvbg_serve_usage(self.h, self.reqs[rid][1], ctypes.byref(u),
                                                  ctypes.byref(f)))
         return f.value
+
+    def steps_done(self, rid):
+        "Steps request rid has taken so far."
+        import ctypes
+        d = ctypes.c_int64()
+        self.nat.check(self.lib.tvbg_serve_progress(self.h, self.reqs[rid][1], ctypes.byref(d)))
+        return int(d.value)
 
     def set_budget(self, nbytes):
         "Admission budget of the following ticks (at most the creation budget)."
