@@ -558,6 +558,26 @@ int tvbg_fcfit_zgrad(const float *d_z, const float *d_a, float *d_out, int32_t n
                     int32_t T, int32_t N, void *stream);
 
 /*
+ * The FC-fit loss path of the adjoint in one call (tvb_hpc.adjoint.FCFit),
+ * for n_inst series X_b [T][N]: row s < T - 1 at d_x + b * x_inst_stride +
+ * s * N, row T - 1 at d_last + b * last_inst_stride + i * last_node_stride
+ * (or from d_x too when d_last is NULL).  Computes the Pearson FC in FP64
+ * (two-pass means and norms, a symmetric Gram with FP64 products and sums;
+ * into d_fc [n_inst][N][N] when not NULL), d_loss[b] = mean_{i<j}
+ * (FC_ij - target_ij)^2 (FP64) and, when d_dx is not NULL, dL/dX (FP32) at
+ * d_dx + b * dx_inst_stride + s * N + i.  target [N][N] FP64; d_scratch of
+ * tvbg_fcfit_scratch_bytes().  Restates the Pearson FC of refs/covar.c:70-109
+ * (metric.py:111-139) as an exact two-pass sum; the loss and its gradient
+ * have no counterpart in the reference.
+ */
+int tvbg_fcfit_scratch_bytes(int32_t n_inst, int32_t N, int64_t *bytes);
+int tvbg_fcfit_loss(const float *d_x, int64_t x_inst_stride, const float *d_last,
+                    int64_t last_inst_stride, int64_t last_node_stride, int32_t n_inst,
+                    int32_t T, int32_t N, const double *d_target, double *d_loss,
+                    float *d_dx, int64_t dx_inst_stride, double *d_fc, void *d_scratch,
+                    void *stream);
+
+/*
  * Region mapping (tvb_hpc/network.py:179-202).  to_avg: d_roi[i][j] = sum
  * of d_node[k][j] over the nodes k with d_rmap[k] == i (RMapToAvg zeroes roi
  * and accumulates: a sum), one CTA per region, a fixed reduction tree;

@@ -88,3 +88,92 @@ def test_fcfit_zgrad_kernel(cuda):
         nat.check(lib.tvbg_fcfit_zgrad(Z.data_ptr(), A.data_ptr(), out.data_ptr(), I, T, N, None))
         ref = Z.double() @ A.double()
         assert rel_err(out.cpu().numpy(), ref.cpu().numpy()) < 1e-5
+
+
+def fc_loss_torch(X, target):
+    """The FC-fit loss path in plain torch FP64 (the reference for
+    tvbg_fcfit_loss): Pearson FC, loss mean_{i<j}(FC - F*)^2, dL/dX."""
+    import torch
+    X = X.double().requires_grad_(True)
+    I, T, N = X.shape
+    Xc = X - X.mean(1, keepdim=True)
+    Z = Xc / Xc.norm(dim=1, keepdim=True)
+    FC = Z.transpose(1, 2) @ Z
+    iu = torch.triu_indices(N, N, 1, device=X.device)
+    loss = ((FC - target)[:, iu[0], iu[1]] ** 2).sum(1) / (N * (N - 1) / 2.0)
+    loss.sum().backward()
+    return loss.detach(), FC.detach(), X.grad
+
+
+@pytest.mark.parametrize('I,T,N', [(3, 130, 84), (2, 700, 150), (4, 64, 17)])
+def test_fcfit_loss_kernel(cuda, I, T, N):
+    """tvbg_fcfit_loss (FP64 FC and loss, FP32 dL/dX, the series' last row
+    from a separate array) against torch FP64 autograd of the same loss."""
+    import ctypes
+    from tvb_hpc import _native as nat
+    torch = cuda
+    lib = nat.load()
+    g = torch.Generator(device='cuda').manual_seed(I * T + N)
+    tr = torch.rand(I, T, N, device='cuda', generator=g) + 0.1     # trace rows 0..T-1
+    last = torch.rand(I, N, 2, device='cuda', generator=g) + 0.1   # state (r, V); r is the last row
+    X = torch.cat([tr[:, 1:], last[:, None, :, 0]], 1)
+    target = torch.corrcoef(torch.rand(N, 40, device='cuda', generator=g).double())
+    loss_ref, fc_ref, dx_ref = fc_loss_torch(X, target)
+    nb = ctypes.c_int64()
+    nat.check(lib.tvbg_fcfit_scratch_bytes(I, N, ctypes.byref(nb)))
+    scratch = torch.empty(nb.value, dtype=torch.uint8, device='cuda')
+    loss = torch.empty(I, dtype=torch.float64, device='cuda')
+    fc = torch.empty(I, N, N, dtype=torch.float64, device='cuda')
+    dr = torch.zeros(I, T + 1, N, device='cuda')
+    nat.check(lib.tvbg_fcfit_loss(tr.data_ptr() + 4 * N, T * N, last.data_ptr(), 2 * N, 2, I, T, N,
+                                  target.data_ptr(), loss.data_ptr(), dr.data_ptr() + 4 * N,
+                                  (T + 1) * N, fc.data_ptr(), scratch.data_ptr(), None))
+    torch.cuda.synchronize()
+    assert rel_err(fc.cpu().numpy(), fc_ref.cpu().numpy()) < 1e-12
+    assert rel_err(loss.cpu().numpy(), loss_ref.cpu().numpy()) < 1e-10
+    assert rel_err(dr[:, 1:].cpu().numpy(), dx_ref.cpu().numpy()) < 1e-5
+    assert float(dr[:, 0].abs().max()) == 0.0
+
+
+def test_adjoint_at_benchmark_size(cuda):
+    """The benchmark's adjoint fit: MPR, N = 84, 256 instances, 2000 steps of
+    0.1 ms, checkpoints every 100 steps, deterministic.  Gradients through the
+    torch.autograd.Function wrapper against the FP64 oracle's adjoint on 8
+    sampled instances (1e-3) and against central differences (h = 1e-4) of
+    the FP64 oracle loss for G and 8 eta components of 2 instances (1e-3)."""
+    import os
+    torch = cuda
+    prob, conn, x0, eta, G, target = problem(N=84, I=256, T=2000, C=100, seed=5)
+    Gt = torch.tensor(G, device='cuda', requires_grad=True)
+    et = torch.tensor(eta, device='cuda', requires_grad=True)
+    loss = adjoint.FCFitLoss.apply(Gt, et, prob)
+    loss.sum().backward()
+    loss = loss.detach().cpu().numpy()
+    dG, deta = Gt.grad.cpu().numpy(), et.grad.cpu().numpy()
+    d = conn.delays(4.0, 0.1, 'ceil')
+    _, consts, _ = model.MPR().engine_spec()
+    idx = np.linspace(0, 255, 8).astype(int)
+    loss_o, dG_o, deta_o = orc.mpr_adjoint(conn.row, conn.col, conn.wnz, d,
+                                           G[idx].astype(np.float64), eta[idx].astype(np.float64),
+                                           x0[idx].astype(np.float64), 2000, 0.1, consts, target,
+                                           nthreads=os.cpu_count() or 1)
+    assert rel_err(loss[idx], loss_o) < 1e-4
+    assert rel_err(dG[idx], dG_o) < 1e-3, (dG[idx], dG_o)
+    assert rel_err(deta[idx], deta_o) < 1e-3
+    print('adjoint at N=84, I=256, T=2000: rel err dG %.2e, deta %.2e vs FP64 oracle'
+          % (rel_err(dG[idx], dG_o), rel_err(deta[idx], deta_o)))
+    h = 1e-4
+    for b in (int(idx[1]), int(idx[6])):
+        f = lambda g, e: orc.mpr_loss(conn.row, conn.col, conn.wnz, d, g, e,  # noqa: E731
+                                      x0[b].astype(np.float64), 2000, 0.1, consts, target)
+        eb = eta[b].astype(np.float64)
+        fd_G = (f(G[b] + h, eb) - f(G[b] - h, eb)) / (2 * h)
+        assert abs(dG[b] - fd_G) / abs(fd_G) < 1e-3, (b, dG[b], fd_G)
+        nodes = np.linspace(0, 83, 8).astype(int)
+        fd_eta = []
+        for i in nodes:
+            ep, em = eb.copy(), eb.copy()
+            ep[i] += h
+            em[i] -= h
+            fd_eta.append((f(G[b], ep) - f(G[b], em)) / (2 * h))
+        assert rel_err(deta[b, nodes], np.array(fd_eta)) < 1e-3, b

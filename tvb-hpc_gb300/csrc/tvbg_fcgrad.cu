@@ -1,3 +1,6 @@
+// The FC-fit loss path of the adjoint (tvbg_fcfit_loss, below) and its
+// product dL/dZ = Z A alone (tvbg_fcfit_zgrad).
+//
 // dL/dZ = Z A of the FC-fit loss, per instance: Z [T][N] (the normalised,
 // centred series), A [N][N] (2 (FC - target) / P with a zero diagonal),
 // FP32.  A batched tiled product on the CUDA cores: one CTA per 64 x 64
@@ -75,4 +78,242 @@ extern "C" int tvbg_fcfit_zgrad(const float* d_z, const float* d_a, float* d_out
     fcgrad_kernel<<<grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(d_z, d_a, d_out, T, N);
     const cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? TVBG_OK : tvbg::set_cuda_error(e, "tvbg_fcfit_zgrad launch");
+}
+
+// ---------------------------------------------------------------------------
+// The whole FC-fit loss path (tvbg_fcfit_loss): for instance b, the series
+// X_b [T][N] (rows 0..T-2 from x, row T-1 from `last` when given), its
+// Pearson FC in FP64, the loss mean_{i<j} (FC_ij - F*_ij)^2 and
+// dL/dX = (Z A - Z diag(FC A)) / nrm, Z = (X - mean) / nrm, A = 2 (FC - F*) / P
+// with a zero diagonal (P = N (N - 1) / 2).  The FC is a symmetric FP64
+// Gram (one DFMA per product, upper-triangle tiles only); diag(FC A) is the
+// time reduction sum_t Z_ti (Z A)_ti of the chain rule, taken from FC in
+// FP64; Z A is FP32 (a sum over N nodes per sample), the precision of the
+// backward.  (The Pearson FC restates refs/covar.c:70-109 / metric.py:111-139
+// as an exact two-pass FP64 sum.)
+// ---------------------------------------------------------------------------
+
+namespace {
+
+struct SeriesView {
+    const float* x;      // row s (s < T - 1, or every row without `last`) at x + b * xs + s * N
+    int64_t xs;
+    const float* last;   // row T - 1 at last + b * ls + i * lns, or NULL
+    int64_t ls, lns;
+    int T, N;
+    __device__ __forceinline__ float at(int b, int s, int i) const {
+        if (last && s == T - 1) return __ldg(last + b * ls + static_cast<int64_t>(i) * lns);
+        return __ldg(x + b * xs + static_cast<int64_t>(s) * N + i);
+    }
+};
+
+// mean and norm sqrt(sum (x - mean)^2) of every (instance, node), FP64, two passes
+__global__ void __launch_bounds__(128) fcfit_moments_kernel(SeriesView v, double* mean, double* nrm) {
+    const int b = blockIdx.y;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= v.N) return;
+    double s = 0.0;
+    for (int t = 0; t < v.T; ++t) s += static_cast<double>(v.at(b, t, i));
+    const double m = s / static_cast<double>(v.T);
+    double ss = 0.0;
+    for (int t = 0; t < v.T; ++t) {
+        const double c = static_cast<double>(v.at(b, t, i)) - m;
+        ss = fma(c, c, ss);
+    }
+    mean[static_cast<int64_t>(b) * v.N + i] = m;
+    nrm[static_cast<int64_t>(b) * v.N + i] = sqrt(ss);
+}
+
+constexpr int kGT = 32;   // Gram tile: 32 x 32 node pairs, 32 samples per stage
+
+// FC_ij = sum_t c_ti c_tj / (nrm_i nrm_j), c = x - mean, FP64; one CTA per
+// upper-triangle 32 x 32 tile (blockIdx.x enumerates tiles with jt >= it),
+// 256 threads of 2 x 2 pairs; both triangles written.
+__global__ void __launch_bounds__(256) fcfit_gram_kernel(SeriesView v, const double* __restrict__ mean,
+                                                         const double* __restrict__ nrm, double* fc) {
+    __shared__ double sI[kGT][kGT + 1];
+    __shared__ double sJ[kGT][kGT + 1];
+    const int b = blockIdx.y;
+    const int N = v.N;
+    const int nt = (N + kGT - 1) / kGT;
+    int it = 0, rem = blockIdx.x;
+    while (rem >= nt - it) {
+        rem -= nt - it;
+        ++it;
+    }
+    const int jt = it + rem;
+    const int i0 = it * kGT, j0 = jt * kGT;
+    const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+    const double* mb = mean + static_cast<int64_t>(b) * N;
+    double acc[2][2] = {{0.0, 0.0}, {0.0, 0.0}};
+    for (int t0 = 0; t0 < v.T; t0 += kGT) {
+        for (int k = threadIdx.x; k < kGT * kGT; k += 256) {
+            const int r = k / kGT, c = k % kGT;   // r: sample, c: node within the tile
+            const int t = t0 + r;
+            const int ii = i0 + c, jj = j0 + c;
+            sI[r][c] = (t < v.T && ii < N) ? static_cast<double>(v.at(b, t, ii)) - mb[ii] : 0.0;
+            sJ[r][c] = (t < v.T && jj < N) ? static_cast<double>(v.at(b, t, jj)) - mb[jj] : 0.0;
+        }
+        __syncthreads();
+#pragma unroll 8
+        for (int r = 0; r < kGT; ++r) {
+            const double a0 = sI[r][2 * ty], a1 = sI[r][2 * ty + 1];
+            const double c0 = sJ[r][2 * tx], c1 = sJ[r][2 * tx + 1];
+            acc[0][0] = fma(a0, c0, acc[0][0]);
+            acc[0][1] = fma(a0, c1, acc[0][1]);
+            acc[1][0] = fma(a1, c0, acc[1][0]);
+            acc[1][1] = fma(a1, c1, acc[1][1]);
+        }
+        __syncthreads();
+    }
+    const double* nb = nrm + static_cast<int64_t>(b) * N;
+    double* fb = fc + static_cast<int64_t>(b) * N * N;
+#pragma unroll
+    for (int u = 0; u < 2; ++u)
+#pragma unroll
+        for (int w = 0; w < 2; ++w) {
+            const int i = i0 + 2 * ty + u, j = j0 + 2 * tx + w;
+            if (i < N && j < N && j >= i) {
+                const double r = acc[u][w] / (nb[i] * nb[j]);
+                fb[static_cast<int64_t>(i) * N + j] = r;
+                fb[static_cast<int64_t>(j) * N + i] = r;
+            }
+        }
+}
+
+// loss_b = sum_{i<j} (FC - F*)^2 / P; A = 2 (FC - F*) / P, zero diagonal
+// (FP32 copy for Z A); zg_i = sum_j FC_ij A_ij (FP64).  One CTA per instance.
+__global__ void __launch_bounds__(256) fcfit_loss_kernel(const double* __restrict__ fc,
+                                                         const double* __restrict__ target, int N,
+                                                         double* loss, float* a32, double* zg) {
+    __shared__ double red[256];
+    const int b = blockIdx.x;
+    const double P = 0.5 * static_cast<double>(N) * (N - 1);
+    const double* fb = fc + static_cast<int64_t>(b) * N * N;
+    float* ab = a32 + static_cast<int64_t>(b) * N * N;
+    double part = 0.0;
+    for (int64_t k = threadIdx.x; k < static_cast<int64_t>(N) * N; k += blockDim.x) {
+        const int i = static_cast<int>(k / N), j = static_cast<int>(k % N);
+        const double d = fb[k] - target[k];
+        if (j > i) part = fma(d, d, part);
+        ab[k] = i == j ? 0.0f : static_cast<float>(2.0 * d / P);
+    }
+    red[threadIdx.x] = part;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (static_cast<int>(threadIdx.x) < s) red[threadIdx.x] += red[threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) loss[b] = red[0] / P;
+    for (int i = threadIdx.x; i < N; i += blockDim.x) {
+        double s = 0.0;
+        for (int j = 0; j < N; ++j) {
+            if (j == i) continue;
+            const double d = fb[static_cast<int64_t>(i) * N + j] - target[static_cast<int64_t>(i) * N + j];
+            s = fma(fb[static_cast<int64_t>(i) * N + j], 2.0 * d / P, s);
+        }
+        zg[static_cast<int64_t>(b) * N + i] = s;
+    }
+}
+
+// dL/dX_tj = ((Z A)_tj - Z_tj zg_j) / nrm_j, Z formed on the fly from the
+// series; the tiled FP32 product of fcgrad_kernel with that epilogue.
+__global__ void __launch_bounds__(256)
+    fcfit_dx_kernel(SeriesView v, const double* __restrict__ mean, const double* __restrict__ nrm,
+                    const float* __restrict__ A, const double* __restrict__ zg, float* __restrict__ dx,
+                    int64_t dxs) {
+    __shared__ float sZ[kTK][kTM + 4];  // [k][t]
+    __shared__ float sA[kTK][kTN];      // [k][j]
+    const int b = blockIdx.z;
+    const int T = v.T, N = v.N;
+    const int t0 = blockIdx.y * kTM, j0 = blockIdx.x * kTN;
+    const double* mb = mean + static_cast<int64_t>(b) * N;
+    const double* nb = nrm + static_cast<int64_t>(b) * N;
+    const float* Ab = A + static_cast<size_t>(b) * N * N;
+    const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+    float acc[4][4] = {};
+    for (int k0 = 0; k0 < N; k0 += kTK) {
+        for (int i = threadIdx.x; i < kTM * kTK; i += 256) {
+            const int r = i / kTK, c = i % kTK;
+            const int t = t0 + r, k = k0 + c;
+            sZ[c][r] = (t < T && k < N)
+                           ? static_cast<float>((static_cast<double>(v.at(b, t, k)) - mb[k]) / nb[k])
+                           : 0.0f;
+        }
+        for (int i = threadIdx.x; i < kTK * kTN; i += 256) {
+            const int r = i / kTN, c = i % kTN;
+            const int k = k0 + r, j = j0 + c;
+            sA[r][c] = (k < N && j < N) ? __ldg(Ab + static_cast<size_t>(k) * N + j) : 0.0f;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < kTK; ++k) {
+            float z[4], a[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                z[u] = sZ[k][ty * 4 + u];
+                a[u] = sA[k][tx * 4 + u];
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+#pragma unroll
+                for (int w = 0; w < 4; ++w) acc[u][w] = fmaf(z[u], a[w], acc[u][w]);
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+        const int t = t0 + ty * 4 + u;
+        if (t >= T) continue;
+#pragma unroll
+        for (int w = 0; w < 4; ++w) {
+            const int j = j0 + tx * 4 + w;
+            if (j >= N) continue;
+            const double z = (static_cast<double>(v.at(b, t, j)) - mb[j]) / nb[j];
+            const double g = (static_cast<double>(acc[u][w]) - z * zg[static_cast<int64_t>(b) * N + j]) / nb[j];
+            dx[b * dxs + static_cast<int64_t>(t) * N + j] = static_cast<float>(g);
+        }
+    }
+}
+
+}  // namespace
+
+extern "C" int tvbg_fcfit_scratch_bytes(int32_t n_inst, int32_t N, int64_t* bytes) {
+    if (!bytes || n_inst <= 0 || N <= 0) return tvbg::set_error(TVBG_EINVAL, "tvbg_fcfit_scratch_bytes: bad args");
+    const int64_t nn = static_cast<int64_t>(N) * N, in = static_cast<int64_t>(n_inst);
+    // mean, nrm, zg [I][N] FP64; FC [I][N][N] FP64; A [I][N][N] FP32 (each 256-byte aligned)
+    auto al = [](int64_t x) { return (x + 255) & ~static_cast<int64_t>(255); };
+    *bytes = 3 * al(in * N * 8) + al(in * nn * 8) + al(in * nn * 4);
+    return TVBG_OK;
+}
+
+extern "C" int tvbg_fcfit_loss(const float* d_x, int64_t x_inst_stride, const float* d_last,
+                               int64_t last_inst_stride, int64_t last_node_stride, int32_t n_inst,
+                               int32_t T, int32_t N, const double* d_target, double* d_loss,
+                               float* d_dx, int64_t dx_inst_stride, double* d_fc, void* d_scratch,
+                               void* stream) {
+    if (!d_x || !d_target || !d_loss || !d_scratch || n_inst <= 0 || n_inst > 65535 || T < 2 ||
+        N < 2 || x_inst_stride < 0 || (d_dx && dx_inst_stride < static_cast<int64_t>(T) * N))
+        return tvbg::set_error(TVBG_EINVAL, "tvbg_fcfit_loss: bad arguments (need T >= 2, N >= 2)");
+    const int64_t nn = static_cast<int64_t>(N) * N, in = static_cast<int64_t>(n_inst);
+    auto al = [](int64_t x) { return (x + 255) & ~static_cast<int64_t>(255); };
+    char* s = static_cast<char*>(d_scratch);
+    double* mean = reinterpret_cast<double*>(s);
+    double* nrm = reinterpret_cast<double*>(s + al(in * N * 8));
+    double* zg = reinterpret_cast<double*>(s + 2 * al(in * N * 8));
+    double* fc = d_fc ? d_fc : reinterpret_cast<double*>(s + 3 * al(in * N * 8));
+    float* a32 = reinterpret_cast<float*>(s + 3 * al(in * N * 8) + al(in * nn * 8));
+    SeriesView v{d_x, x_inst_stride, d_last, last_inst_stride, last_node_stride, T, N};
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    fcfit_moments_kernel<<<dim3((N + 127) / 128, n_inst), 128, 0, st>>>(v, mean, nrm);
+    const int nt = (N + kGT - 1) / kGT;
+    fcfit_gram_kernel<<<dim3(nt * (nt + 1) / 2, n_inst), 256, 0, st>>>(v, mean, nrm, fc);
+    fcfit_loss_kernel<<<n_inst, 256, 0, st>>>(fc, d_target, N, d_loss, a32, zg);
+    if (d_dx) {
+        const dim3 grid((N + kTN - 1) / kTN, (T + kTM - 1) / kTM, n_inst);
+        if (grid.y > 65535u) return tvbg::set_error(TVBG_EINVAL, "tvbg_fcfit_loss: T too large");
+        fcfit_dx_kernel<<<grid, 256, 0, st>>>(v, mean, nrm, a32, zg, d_dx, dx_inst_stride);
+    }
+    const cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? TVBG_OK : tvbg::set_cuda_error(e, "tvbg_fcfit_loss launch");
 }

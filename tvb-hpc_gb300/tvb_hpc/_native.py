@@ -250,6 +250,9 @@ SIGNATURES = {
     'tvbg_group_occupancy': (ctypes.c_int, [ctypes.c_void_p, _ip, _ip]),
     'tvbg_group_max_clusters': (ctypes.c_int, [ctypes.c_void_p, _ip]),
     'tvbg_fcfit_zgrad': (ctypes.c_int, [_vp, _vp, _vp, _i32, _i32, _i32, _vp]),
+    'tvbg_fcfit_scratch_bytes': (ctypes.c_int, [_i32, _i32, ctypes.POINTER(_i64)]),
+    'tvbg_fcfit_loss': (ctypes.c_int, [_vp, _i64, _vp, _i64, _i64, _i32, _i32, _i32, _vp, _vp,
+                                       _vp, _i64, _vp, _vp, _vp]),
     'tvbg_rmap_to_avg': (ctypes.c_int, [_i32, _i32, _i32, _vp, _vp, _vp, _vp]),
     'tvbg_rmap_from_avg': (ctypes.c_int, [_i32, _i32, _i32, _vp, _vp, _vp, _vp]),
     'tvbg_serve_create': (ctypes.c_int, [_i64, _i32, _vp, ctypes.POINTER(_vp)]),

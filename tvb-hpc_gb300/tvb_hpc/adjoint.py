@@ -9,8 +9,9 @@ Problem (one connectome, I instances, T steps, deterministic):
 
 ``FCFit.forward`` runs the step kernel in chunks of `checkpoint_every`
 steps, keeping the state and the history ring at every chunk start
-(checkpoints) and the rate series for the FC.  ``FCFit.backward`` takes the
-FC gradient in FP64 (torch, batched GEMMs), then walks the chunks backwards:
+(checkpoints) and the rate series for the FC; tvbg_fcfit_loss then takes
+the FC (a symmetric FP64 Gram), the loss and dL/dr on the device in one
+call, no library GEMM.  ``FCFit.backward`` walks the chunks backwards:
 each chunk is recomputed from its checkpoint (bit-identical to the forward)
 with the state and coupling sums traced, and tvbg_adjoint_mpr runs the
 reverse-time recursion over it, carrying the adjoint state and an adjoint
@@ -133,41 +134,26 @@ class FCFit:
             self.ckpt.append((t0, n, fw.state.clone(), fw.ring.clone()))
             sw.launch(pl, self.tpn)
         fw.t[:] = self.T
+        self.fw = fw
+        # X[s] = r(s + 1): trace rows 1..T-1 (r(t), one column) and the
+        # final state's r; loss, FC and dL/dr(t) = dL/dX[t-1] into dr[:, 1:]
+        # by tvbg_fcfit_loss (FP64 FC and loss, FP32 dL/dX)
+        I, N, T = self.I, self.N, self.T
+        assert fw.trace.shape[1:] == (T, N, 1)
+        self.dr = torch.zeros((I, T + 1, N), dtype=torch.float32, device='cuda')
+        self.fc = torch.empty((I, N, N), dtype=torch.float64, device='cuda')
+        loss = torch.empty(I, dtype=torch.float64, device='cuda')
+        lib = nat.load()
+        nb = ctypes.c_int64()
+        nat.check(lib.tvbg_fcfit_scratch_bytes(I, N, ctypes.byref(nb)))
+        scratch = torch.empty(int(nb.value), dtype=torch.uint8, device='cuda')
+        nat.check(lib.tvbg_fcfit_loss(fw.trace.data_ptr() + 4 * N, T * N, fw.state.data_ptr(),
+                                      2 * N, 2, I, T, N, self.target.data_ptr(), loss.data_ptr(),
+                                      self.dr.data_ptr() + 4 * N, (T + 1) * N, self.fc.data_ptr(),
+                                      scratch.data_ptr(), nat.stream_handle()))
         torch.cuda.synchronize()
         sw.status.check()
-        r_tr = fw.trace[:, :, :, 0]                     # r(t), t = 0..T-1
-        X = torch.cat([r_tr[:, 1:], fw.state[:, None, :, 0]], 1).double()   # X[s] = r(s+1)
-        self.fw = fw
-        loss, dX = self._fc_loss_grad(X)
-        self.dX = dX
         return loss
-
-    def _fc_loss_grad(self, X):
-        """Loss and dL/dX of the Pearson FC fit (batched GEMMs).  The FC and
-        the loss -- reductions over time -- are FP64; dL/dZ = Z A, a sum
-        over N nodes per sample, is FP32 (the backward's precision), and
-        the per-node reductions over time of the chain rule are FP64."""
-        I, T, N = X.shape
-        P = N * (N - 1) / 2.0
-        Xc = X - X.mean(1, keepdim=True)
-        nrm = Xc.norm(dim=1, keepdim=True)
-        Z = Xc / nrm
-        FC = Z.transpose(1, 2) @ Z
-        iu = self.torch.triu_indices(N, N, 1, device=X.device)
-        D = FC - self.target
-        loss = (D[:, iu[0], iu[1]] ** 2).sum(1) / P
-        A = 2.0 * D / P
-        A = A - self.torch.diag_embed(self.torch.diagonal(A, dim1=1, dim2=2))
-        Z32, A32 = Z.float().contiguous(), A.float().contiguous()
-        gZ32 = self.torch.empty_like(Z32)
-        nat.check(nat.load().tvbg_fcfit_zgrad(Z32.data_ptr(), A32.data_ptr(), gZ32.data_ptr(), I, T,
-                                             N, nat.stream_handle()))
-        gZ = gZ32.double()
-        zg = (Z * gZ).sum(1, keepdim=True)
-        dXc = (gZ - Z * zg) / nrm
-        dX = dXc - dXc.mean(1, keepdim=True)
-        self.fc = FC
-        return loss, dX
 
     def backward(self):
         "(dL/dG [I], dL/deta [I, N]) in FP64, by the adjoint over the checkpoints."
@@ -175,8 +161,7 @@ class FCFit:
         lib = nat.load()
         I, N, T = self.I, self.N, self.T
         nh = 1 << self.lognh
-        dr = torch.zeros((I, T + 1, N), dtype=torch.float32, device='cuda')
-        dr[:, 1:] = self.dX.float()                    # dL/dr(t) = dX[t-1]
+        dr = self.dr                                   # dL/dr(t) = dL/dX[t-1], from forward
         lam = torch.zeros((I, N, 2), dtype=torch.float32, device='cuda')
         lam[:, :, 0] = dr[:, T]
         ring = torch.zeros((I, N * nh), dtype=torch.float32, device='cuda')

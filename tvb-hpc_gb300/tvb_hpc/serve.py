@@ -103,13 +103,12 @@ def footprint(req):
 
 def adjoint_bytes(I, N, T, nh, checkpoint_every=100):
     """Device bytes of adjoint.FCFit for I instances, N nodes, T steps:
-    the rate series (FP32 trace; FP64 X, its centred and normalised copies
-    and the gradient temporaries of the loss; FP32 copies), dL/dr, one state + ring checkpoint per chunk of
+    the rate series (FP32 trace), dL/dr (FP32), the loss scratch (FC and A), one state + ring checkpoint per chunk of
     checkpoint_every steps, the recomputation trace and the adjoint ring."""
-    series = I * T * N * (4 + 8 * 8 + 4 * 3)   # peak of the loss's FP64/FP32 temporaries
+    series = I * T * N * (4 + 4)               # r trace and dL/dr (FP32)
     ckpt = -(-T // checkpoint_every) * I * N * (nh + 2) * 4
     chunk = I * checkpoint_every * N * 3 * 4 + I * N * nh * 4
-    return series + ckpt + chunk + I * N * N * 8 * 3
+    return series + ckpt + chunk + I * N * N * (8 * 2 + 4) + I * N * 8 * 3
 
 
 class Server:
