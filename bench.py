@@ -897,6 +897,123 @@ def cpu_baseline(wl, budget_s=12.0):
                 n_inst, I_all, nsteps, el)}
 
 
+def reference_gpu_kuramoto(wl, n_items, inner=100, reps=3):
+    """The reference's own CUDA DSL Kuramoto kernel (dsl/dsl_cuda/CUDAmodels/
+    kuramoto.c, compiled unchanged for sm_103a by baseline/Makefile) on the
+    workload's connectome: one thread per work item scanning the dense N x N
+    weights, curand noise always on, launched as the reference launcher does
+    (dsl/dsl_cuda/example/cuda_run.py:109-142): `inner` steps per launch,
+    the tavg buffer copied to the host after every launch; blocks of 32 x 1
+    threads (blockDim.y = 1: the kernel's __syncthreads() sits in a node loop
+    whose trip count depends on threadIdx.y).  Returns node-steps/s."""
+    import ctypes
+    import torch
+    path = os.path.join(ROOT, 'baseline', '_ref', 'kuramoto_sm103a.cubin')
+    if not os.path.exists(path):
+        return {'unavailable': 'baseline/_ref/kuramoto_sm103a.cubin not built '
+                               '(make -C baseline gpu REF=<tvb-hpc checkout>)'}
+    cu = ctypes.CDLL('libcuda.so.1')
+
+    def ck(rc, what):
+        if rc != 0:
+            raise RuntimeError('%s failed (CUresult %d)' % (what, rc))
+
+    torch.cuda.synchronize()                   # the primary context is current
+    mod, fn = ctypes.c_void_p(), ctypes.c_void_p()
+    ck(cu.cuModuleLoad(ctypes.byref(mod), path.encode()), 'cuModuleLoad')
+    try:
+        ck(cu.cuModuleGetFunction(ctypes.byref(fn), mod, b'_Z8KuramotojjjjjffPfS_S_S_S_'),
+           'cuModuleGetFunction')
+        conn = wl['conn']
+        N = conn.nnode
+        w = np.zeros((N, N), np.float32)
+        ln = np.zeros((N, N), np.float32)
+        rows = np.repeat(np.arange(N), np.diff(conn.row))
+        w[rows, conn.col] = conn.wnz
+        ln[rows, conn.col] = conn.lnz
+        speed = float(wl['speeds'][0])
+        G = np.resize(np.asarray(wl['couplings'], np.float32), n_items)
+        bx = 32
+        n_items = bx * -(-n_items // bx)
+        G = np.resize(G, n_items)
+        dmax = int(np.max(ln * np.float32(np.float32(1.0) / np.float32(speed) / np.float32(wl['dt']))))
+        nh = 1 << int(np.ceil(np.log2(dmax + 2)))
+        dev = lambda a: torch.from_numpy(np.ascontiguousarray(a, np.float32)).cuda()  # noqa: E731
+        d_w, d_l = dev(w), dev(ln)
+        d_p = dev(np.stack([np.full(n_items, speed, np.float32), G]))    # params [2][items]
+        d_s = torch.zeros(nh * N * n_items, dtype=torch.float32, device='cuda')
+        d_t = torch.zeros(N * n_items, dtype=torch.float32, device='cuda')
+        host_t = torch.empty(N * n_items, dtype=torch.float32).pin_memory()
+        nsteps = int(wl['nsteps'])
+
+        def launch(i_step, n_step):
+            vals = [ctypes.c_uint(i_step), ctypes.c_uint(N), ctypes.c_uint(nh), ctypes.c_uint(n_step),
+                    ctypes.c_uint(2), ctypes.c_float(wl['dt']), ctypes.c_float(speed)] + [
+                ctypes.c_void_p(t.data_ptr()) for t in (d_w, d_l, d_p, d_s, d_t)]
+            ptrs = (ctypes.c_void_p * len(vals))(*[ctypes.cast(ctypes.byref(v), ctypes.c_void_p)
+                                                   for v in vals])
+            ck(cu.cuLaunchKernel(fn, n_items // bx, 1, 1, bx, 1, 1, 0, None, ptrs, None),
+               'cuLaunchKernel')
+
+        def run():
+            for i in range(-(-nsteps // inner)):
+                launch(i * inner, min(inner, nsteps - i * inner))
+                host_t.copy_(d_t)              # the launcher's per-launch tavg download
+            torch.cuda.synchronize()
+
+        run()                                  # warm-up (module load, first launch)
+        best = None
+        for _ in range(reps):
+            d_s.zero_()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            run()
+            el = time.perf_counter() - t0
+            best = el if best is None else min(best, el)
+        return {'value': round(N * n_items * nsteps / best, 1), 'unit': UNIT,
+                'work_items': n_items, 'nodes': N, 'steps': nsteps, 'ms': round(best * 1e3, 3),
+                'path': 'reference CUDA DSL kernel kuramoto.c for sm_103a, %d-step launches, '
+                        'blocks of 32 x 1, noise on (curand, hard-wired)' % inner}
+    finally:
+        cu.cuModuleUnload(mod)
+
+
+def engine_kuramoto_items(wl, n_items, reps=3):
+    """The engine on the same sweep as reference_gpu_kuramoto's: the
+    workload's Kuramoto network with n_items instances (couplings tiled),
+    lane-interleaved groups (sin/cos ring), noise off; node-steps/s."""
+    import torch
+    from tvb_hpc import model, coupling, scheme, groups
+    m = model.Kuramoto()
+    cf = coupling.Kuramoto(m)
+    I = int(n_items)
+    x0 = np.resize(wl['x0'], (I, ) + wl['x0'].shape[1:])
+    om = np.resize(wl['nparam'], (I, ) + wl['nparam'].shape[1:])
+    gs = groups.GroupSet(m, cf, scheme.EulerStep(wl['dt']), wl['conn'], dt=wl['dt'],
+                         couplings=np.resize(wl['couplings'], I), speeds=np.resize(wl['speeds'], I),
+                         state0=x0, nparam=om)
+    gs.set_shape(*groups.pipelined_shape(gs))
+    n = int(wl['nsteps'])
+    gs.run(n)
+    best = None
+    for _ in range(reps):
+        gs.t[:] = 0
+        gs.clear_history()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        gs.run(n, check=False)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        best = ms if best is None else min(best, ms)
+    gs.status.check()
+    return {'value': round(wl['conn'].nnode * I * n / (best / 1e3), 1), 'unit': UNIT,
+            'instances': I, 'ms': round(best, 3),
+            'path': 'lane-interleaved groups, Kuramoto sin/cos ring, %s kernel, noise off'
+                    % ('pipelined' if gs.tpn == 2 else 'plain')}
+
+
 def gpu_arm(args):
     import torch
     import torch.distributed as dist
@@ -1024,6 +1141,13 @@ def gpu_arm(args):
             'roofline': roofline_entry(wl, gs.ns, kern_ms, args.steps),
             'clocks': clk, 'tpn': gs.tpn}
     line['config']['path'] = gs.path
+    if rank == 0 and world == 1 and wl['name'] == 'kuramoto':
+        # the reference's own GPU kernel beside the engine: at this workload's
+        # size and at the DSL's default 32 x 32 sweep (1024 work items)
+        line['reference_gpu'] = {
+            'config_size': reference_gpu_kuramoto(wl, wl['couplings'].size),
+            'sweep_1024': reference_gpu_kuramoto(wl, 1024),
+            'engine_sweep_1024': engine_kuramoto_items(wl, 1024)}
     if rank == 0 and world == 1 and not args.no_cpu:
         line['cpu_baseline'] = (cpu_baseline_lems(wl) if wl['name'].startswith('lems')
                                 else cpu_baseline(wl))
