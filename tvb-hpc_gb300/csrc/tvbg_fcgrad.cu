@@ -88,8 +88,8 @@ extern "C" int tvbg_fcfit_zgrad(const float* d_z, const float* d_a, float* d_out
 // with a zero diagonal (P = N (N - 1) / 2).  The FC is a symmetric FP64
 // Gram (one DFMA per product, upper-triangle tiles only); diag(FC A) is the
 // time reduction sum_t Z_ti (Z A)_ti of the chain rule, taken from FC in
-// FP64; Z A is FP32 (a sum over N nodes per sample), the precision of the
-// backward.  (The Pearson FC restates refs/covar.c:70-109 / metric.py:111-139
+// FP64; Z, Z A and the epilogue are FP32 (Z A is a sum over N nodes per
+// sample), the precision of the backward.  (The Pearson FC restates refs/covar.c:70-109 / metric.py:111-139
 // as an exact two-pass FP64 sum.)
 // ---------------------------------------------------------------------------
 
@@ -216,19 +216,29 @@ __global__ void __launch_bounds__(256) fcfit_loss_kernel(const double* __restric
     }
 }
 
-// dL/dX_tj = ((Z A)_tj - Z_tj zg_j) / nrm_j, Z formed on the fly from the
-// series; the tiled FP32 product of fcgrad_kernel with that epilogue.
+// Per (instance, node) FP32 factors of the dL/dX epilogue: mean, 1 / nrm
+// and zg / nrm (rounded once from FP64).
+__global__ void fcfit_scale_kernel(const double* __restrict__ mean, const double* __restrict__ nrm,
+                                   const double* __restrict__ zg, int64_t n, float* f) {
+    const int64_t k = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+    if (k >= n) return;
+    f[3 * k] = static_cast<float>(mean[k]);
+    f[3 * k + 1] = static_cast<float>(1.0 / nrm[k]);
+    f[3 * k + 2] = static_cast<float>(zg[k] / nrm[k]);
+}
+
+// dL/dX_tj = ((Z A)_tj - Z_tj zg_j) / nrm_j with Z = (x - mean) / nrm formed
+// on the fly in FP32 (the backward's precision); the tiled FP32 product of
+// fcgrad_kernel with that epilogue.
 __global__ void __launch_bounds__(256)
-    fcfit_dx_kernel(SeriesView v, const double* __restrict__ mean, const double* __restrict__ nrm,
-                    const float* __restrict__ A, const double* __restrict__ zg, float* __restrict__ dx,
-                    int64_t dxs) {
+    fcfit_dx_kernel(SeriesView v, const float* __restrict__ fs, const float* __restrict__ A,
+                    float* __restrict__ dx, int64_t dxs) {
     __shared__ float sZ[kTK][kTM + 4];  // [k][t]
     __shared__ float sA[kTK][kTN];      // [k][j]
     const int b = blockIdx.z;
     const int T = v.T, N = v.N;
     const int t0 = blockIdx.y * kTM, j0 = blockIdx.x * kTN;
-    const double* mb = mean + static_cast<int64_t>(b) * N;
-    const double* nb = nrm + static_cast<int64_t>(b) * N;
+    const float* fb = fs + static_cast<int64_t>(b) * N * 3;   // [N][mean, 1/nrm, zg/nrm]
     const float* Ab = A + static_cast<size_t>(b) * N * N;
     const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
     float acc[4][4] = {};
@@ -236,9 +246,7 @@ __global__ void __launch_bounds__(256)
         for (int i = threadIdx.x; i < kTM * kTK; i += 256) {
             const int r = i / kTK, c = i % kTK;
             const int t = t0 + r, k = k0 + c;
-            sZ[c][r] = (t < T && k < N)
-                           ? static_cast<float>((static_cast<double>(v.at(b, t, k)) - mb[k]) / nb[k])
-                           : 0.0f;
+            sZ[c][r] = (t < T && k < N) ? (v.at(b, t, k) - fb[3 * k]) * fb[3 * k + 1] : 0.0f;
         }
         for (int i = threadIdx.x; i < kTK * kTN; i += 256) {
             const int r = i / kTN, c = i % kTN;
@@ -269,9 +277,9 @@ __global__ void __launch_bounds__(256)
         for (int w = 0; w < 4; ++w) {
             const int j = j0 + tx * 4 + w;
             if (j >= N) continue;
-            const double z = (static_cast<double>(v.at(b, t, j)) - mb[j]) / nb[j];
-            const double g = (static_cast<double>(acc[u][w]) - z * zg[static_cast<int64_t>(b) * N + j]) / nb[j];
-            dx[b * dxs + static_cast<int64_t>(t) * N + j] = static_cast<float>(g);
+            const float z = (v.at(b, t, j) - fb[3 * j]) * fb[3 * j + 1];
+            dx[b * dxs + static_cast<int64_t>(t) * N + j] =
+                fmaf(-z, fb[3 * j + 2], acc[u][w] * fb[3 * j + 1]);
         }
     }
 }
@@ -281,9 +289,10 @@ __global__ void __launch_bounds__(256)
 extern "C" int tvbg_fcfit_scratch_bytes(int32_t n_inst, int32_t N, int64_t* bytes) {
     if (!bytes || n_inst <= 0 || N <= 0) return tvbg::set_error(TVBG_EINVAL, "tvbg_fcfit_scratch_bytes: bad args");
     const int64_t nn = static_cast<int64_t>(N) * N, in = static_cast<int64_t>(n_inst);
-    // mean, nrm, zg [I][N] FP64; FC [I][N][N] FP64; A [I][N][N] FP32 (each 256-byte aligned)
+    // mean, nrm, zg [I][N] FP64; FC [I][N][N] FP64; A [I][N][N] FP32; the
+    // epilogue factors [I][N][3] FP32 (each 256-byte aligned)
     auto al = [](int64_t x) { return (x + 255) & ~static_cast<int64_t>(255); };
-    *bytes = 3 * al(in * N * 8) + al(in * nn * 8) + al(in * nn * 4);
+    *bytes = 3 * al(in * N * 8) + al(in * nn * 8) + al(in * nn * 4) + al(in * N * 12);
     return TVBG_OK;
 }
 
@@ -303,6 +312,7 @@ extern "C" int tvbg_fcfit_loss(const float* d_x, int64_t x_inst_stride, const fl
     double* zg = reinterpret_cast<double*>(s + 2 * al(in * N * 8));
     double* fc = d_fc ? d_fc : reinterpret_cast<double*>(s + 3 * al(in * N * 8));
     float* a32 = reinterpret_cast<float*>(s + 3 * al(in * N * 8) + al(in * nn * 8));
+    float* fsc = reinterpret_cast<float*>(s + 3 * al(in * N * 8) + al(in * nn * 8) + al(in * nn * 4));
     SeriesView v{d_x, x_inst_stride, d_last, last_inst_stride, last_node_stride, T, N};
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     fcfit_moments_kernel<<<dim3((N + 127) / 128, n_inst), 128, 0, st>>>(v, mean, nrm);
@@ -312,7 +322,9 @@ extern "C" int tvbg_fcfit_loss(const float* d_x, int64_t x_inst_stride, const fl
     if (d_dx) {
         const dim3 grid((N + kTN - 1) / kTN, (T + kTM - 1) / kTM, n_inst);
         if (grid.y > 65535u) return tvbg::set_error(TVBG_EINVAL, "tvbg_fcfit_loss: T too large");
-        fcfit_dx_kernel<<<grid, 256, 0, st>>>(v, mean, nrm, a32, zg, d_dx, dx_inst_stride);
+        fcfit_scale_kernel<<<static_cast<unsigned>((in * N + 255) / 256), 256, 0, st>>>(mean, nrm, zg,
+                                                                                       in * N, fsc);
+        fcfit_dx_kernel<<<grid, 256, 0, st>>>(v, fsc, a32, d_dx, dx_inst_stride);
     }
     const cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? TVBG_OK : tvbg::set_cuda_error(e, "tvbg_fcfit_loss launch");
