@@ -50,6 +50,12 @@ namespace tvbg {
 
 constexpr int kLanes = TVBG_GROUP_LANES;
 
+// steps of the pipelined kernel's update loop unrolled (update_node)
+#ifndef TVBG_UPDATE_UNROLL
+#define TVBG_UPDATE_UNROLL 1
+#endif
+constexpr int kUpdateUnroll = TVBG_UPDATE_UNROLL;
+
 // 16-byte loads in flight per thread in the transposed gather (lane_gather_t)
 #ifndef TVBG_GATHER_LOADS
 #define TVBG_GATHER_LOADS 8
@@ -748,7 +754,7 @@ __device__ __forceinline__ void update_node(const tvbg_group& g, const GroupLane
     float zz[4] = {0.0f, 0.0f, 0.0f, 0.0f};
     int b_next = mc.b_until, tr_next = mc.tr_until;
     int brow = mc.b_row, trow = mc.tr_row;
-#pragma unroll 1
+#pragma unroll kUpdateUnroll
     for (int k = 0; k < cnt; ++k) {
         const long long t = tb + k;
         if (t >= c.t_end) break;
