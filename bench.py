@@ -518,7 +518,8 @@ def build_groups(wl):
 
 
 def groups_supported(wl):
-    return wl['cfun'] in ('Linear', 'Diff', 'Sigmoidal') and wl['model'] != 'Kuramoto'
+    return ((wl['cfun'] in ('Linear', 'Diff', 'Sigmoidal') and wl['model'] != 'Kuramoto')
+            or (wl['model'], wl['cfun']) == ('Kuramoto', 'Kuramoto'))
 
 
 class GpuStep:
@@ -532,7 +533,12 @@ class GpuStep:
         self.wl = wl
         self.groups = path == 'groups' and groups_supported(wl)
         if self.groups:
+            from tvb_hpc import autotune
             self.sw = build_groups(wl)
+            # the set's fastest launch shape alone (plain or pipelined, CTA
+            # width, cluster), by short trials
+            self.shape = autotune.tune_group_alone(self.sw, wl['nsteps'])[0]
+            self.sw.set_shape(*self.shape)
             self.launches = self.sw.prepare(wl['nsteps'])[0]
             self.tpn = None
         else:
@@ -540,7 +546,9 @@ class GpuStep:
             self.sw.pick_tpn()
             self.launches = self.sw.prepare(wl['nsteps'])
             self.tpn = self.sw.tpn
-        self.path = ('lane-interleaved groups' if self.groups else 'per-instance kernels')
+        self.path = (('lane-interleaved groups, %s kernel where the delays allow, %d threads x %d '
+                      'CTAs' % ('pipelined' if self.shape[3] == 2 else 'plain', self.shape[0],
+                                self.shape[1])) if self.groups else 'per-instance kernels')
         self.x0 = self.sw.state.clone()
         self.ns = self.sw.ns
         self.status = self.sw.status

@@ -58,6 +58,24 @@ def test_pipelined_matches_plain(cuda, model_name, cfun_name):
     same(a, b)
 
 
+def test_pipelined_shape_with_short_delay_tables(cuda):
+    """Speeds whose delays are too short for the pipelined kernel (d_min =
+    5 at 20 mm/ms) keep the plain kernel in their own launches while the
+    others pipeline; the whole set equals the plain run bit for bit."""
+    args, kw, _ = setup(I=20, speeds=(4.0, 20.0, 6.0))
+    a, b = pair(args, kw)
+    assert b.can_pipeline and not b.pipe_tab.all()
+    b.set_shape(*pipelined_shape(b))
+    launches, _ = b.prepare(300)
+    assert {cfg.tpn for *_, cfg in launches} == {1, nat.GROUP_PIPELINED}
+    a.run(300)
+    b.launch(launches)
+    b.advance(np.full(b.n_groups, 300))
+    b.torch.cuda.synchronize()
+    b.status.check()
+    same(a, b)
+
+
 def test_pipelined_kuramoto_sin_cos(cuda):
     args, kw, _ = kuramoto_setup(I=12, speeds=(4.0, ))
     a, b = pair(args, kw)
@@ -102,7 +120,8 @@ def test_pipelined_rejects_short_delays(cuda):
     assert not gs.can_pipeline
     with pytest.raises(ValueError):
         gs.set_shape(*pipelined_shape(gs))
-    gs.can_pipeline = True       # bypass the host check: the kernel checks dmin itself
+    gs.can_pipeline = True       # bypass the host checks: the kernel checks dmin itself
+    gs.pipe_tab[:] = True
     gs.set_shape(*pipelined_shape(gs))
     x = gs.state.clone()
     gs.run(64, check=False)

@@ -181,9 +181,12 @@ class GroupSet:
         self.delay_tables = tables
         plans = [plan_group(d.min() if d.size else 7, d.max() if d.size else 0, block_k,
                             self.block_ks) for d in tables]
-        # the pipelined kernel needs d_min >= 2 K - 1 in every table
+        # the pipelined kernel needs d_min >= 2 K - 1 in a group's table; with
+        # the pipelined shape, groups of tables that do not qualify take the
+        # plain kernel on its default shape (their own launches)
         self.dmin_tab = np.array([int(d.min()) if d.size else 1 << 20 for d in tables], np.int64)
-        self.can_pipeline = all(int(dm) >= 2 * k - 1 for dm, (k, _) in zip(self.dmin_tab, plans))
+        self.pipe_tab = np.array([int(dm) >= 2 * k - 1 for dm, (k, _) in zip(self.dmin_tab, plans)])
+        self.can_pipeline = bool(self.pipe_tab.any())
         # per-node constants shared by every table: in-edge weight sums and
         # the visiting order (in-degree, descending)
         deg = np.diff(row)
@@ -420,7 +423,8 @@ class GroupSet:
         cluster size (group_shape rules for what is left out), the launch
         priority (0 = the stream's; lower numbers are dispatched first) and
         tpn = 2 for the pipelined kernel (threads then count both teams;
-        needs can_pipeline and one node per slot)."""
+        needs one node per slot and a table with d_min >= 2 K - 1; groups of
+        the other tables keep the plain kernel on group_shape)."""
         tpn = int(tpn)
         if tpn == PIPELINED:
             if not self.can_pipeline:
@@ -445,12 +449,18 @@ class GroupSet:
         "(threads, cluster, priority, tpn) of the next launches."
         return (self.threads, self.cluster, self.priority, self.tpn)
 
-    def launch_cfg(self, block_k, order=None, priority=None):
+    def launch_cfg(self, block_k, order=None, priority=None, plain=False):
+        """Launch record of one block length; `plain` forces the plain kernel
+        on its default shape (groups whose delays do not allow pipelining)."""
         cfg = nat.tvbg_launch()
         cfg.model, cfg.cfun = self.model_id, self.cfun_id
-        cfg.threads, cfg.cluster = self.threads, self.cluster
+        if plain and self.tpn == PIPELINED:
+            cfg.threads, cfg.cluster = group_shape(self.N)
+            cfg.tpn = 1
+        else:
+            cfg.threads, cfg.cluster = self.threads, self.cluster
+            cfg.tpn = self.tpn
         cfg.priority = self.priority if priority is None else int(priority)
-        cfg.tpn = self.tpn
         cfg.block_k = int(block_k)
         cfg.d_status = self.status.t.data_ptr()
         cfg.d_order = order.data_ptr() if order is not None else None
@@ -467,13 +477,17 @@ class GroupSet:
         dev = torch.from_numpy(tab.view(np.uint8).copy()).cuda()
         prio = (np.full(self.n_groups, self.priority, np.int64) if priorities is None
                 else np.asarray(priorities, np.int64))
+        pipe = self.pipe_tab[self.gtab] if self.tpn == PIPELINED else np.ones(self.n_groups, bool)
         launches = []
         for k in sorted(set(self.block_k.tolist())):
-            for pr in sorted(set(prio[self.block_k == k].tolist())):
-                idx = np.nonzero((self.block_k == k) & (prio == pr))[0]
-                idx = idx[np.argsort(-gmax[idx], kind='stable')].astype(np.int32)
-                order = torch.from_numpy(idx).cuda()
-                launches.append((dev, order, int(idx.size), self.launch_cfg(k, order, pr)))
+            for pk in (True, False):
+                sel = (self.block_k == k) & (pipe == pk)
+                for pr in sorted(set(prio[sel].tolist())):
+                    idx = np.nonzero(sel & (prio == pr))[0]
+                    idx = idx[np.argsort(-gmax[idx], kind='stable')].astype(np.int32)
+                    order = torch.from_numpy(idx).cuda()
+                    launches.append((dev, order, int(idx.size),
+                                     self.launch_cfg(k, order, pr, plain=not pk)))
         self._uploaded = (launches, gmax)
         return launches, gmax
 
