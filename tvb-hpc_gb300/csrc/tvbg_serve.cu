@@ -92,6 +92,9 @@ struct Request {
     cudaStream_t stream = nullptr;
     cudaEvent_t done_ev = nullptr;
     std::vector<tvbg_group> records;
+    tvbg_group* h_records = nullptr;  // pinned staging of records (asynchronous uploads)
+    int32_t* h_status = nullptr;      // pinned copy of the status word, read after each tick
+    int64_t ctas = 0;                 // CTAs of one chunk: groups x cluster
     std::vector<float> result;        // [n_inst][N][ns] once done
 };
 
@@ -292,6 +295,15 @@ int materialise(Request& r) {
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&r.done_ev, cudaEventDisableTiming);
     if (e != cudaSuccess) return set_cuda_error(e, "tvbg_serve: stream");
     const int N = r.N, ns = r.shape.ns, np = r.npar, G = static_cast<int>(r.members.size());
+    e = cudaMallocHost(&r.h_records, static_cast<size_t>(std::max(1, G)) * sizeof(tvbg_group));
+    if (e == cudaSuccess) e = cudaMallocHost(&r.h_status, sizeof(int32_t));
+    if (e != cudaSuccess) {
+        r.h_records = nullptr;
+        r.h_status = nullptr;
+        return set_cuda_error(e, "tvbg_serve: pinned staging");
+    }
+    *r.h_status = 0;
+    r.ctas = static_cast<int64_t>(G) * r.cluster;
     // lane-interleaved state and parameters [G][N][*][L]
     std::vector<float> gstate(static_cast<size_t>(G) * N * ns * L, 0.0f);
     std::vector<float> gpar(static_cast<size_t>(G) * N * np * L, 0.0f);
@@ -380,6 +392,10 @@ int materialise(Request& r) {
 void release(Request& r) {
     if (r.stream) cudaStreamSynchronize(r.stream);
     if (r.dev) cudaFree(r.dev);
+    if (r.h_records) cudaFreeHost(r.h_records);
+    if (r.h_status) cudaFreeHost(r.h_status);
+    r.h_records = nullptr;
+    r.h_status = nullptr;
     if (r.done_ev) cudaEventDestroy(r.done_ev);
     if (r.stream) cudaStreamDestroy(r.stream);
     r.dev = nullptr;
@@ -398,7 +414,10 @@ int launch_chunk(Request& r, int64_t steps) {
         rec.nsteps = static_cast<int32_t>(steps);
         for (size_t l = 0; l < r.members[g].size(); ++l) rec.lanes[l].nsteps = static_cast<int32_t>(steps);
     }
-    cudaError_t e = cudaMemcpyAsync(r.dev + r.off_groups, r.records.data(), G * sizeof(tvbg_group),
+    // refilling the pinned staging is safe: every tick ends with the pool
+    // stream synchronised, which waited for this request's previous upload
+    std::memcpy(r.h_records, r.records.data(), G * sizeof(tvbg_group));
+    cudaError_t e = cudaMemcpyAsync(r.dev + r.off_groups, r.h_records, G * sizeof(tvbg_group),
                                     cudaMemcpyHostToDevice, r.stream);
     if (e != cudaSuccess) return set_cuda_error(e, "tvbg_serve: group records");
     static const ErrSink sink{set_error, set_cuda_error};
@@ -422,6 +441,10 @@ int launch_chunk(Request& r, int64_t steps) {
                                      r.k_count[i], &cfg, r.cluster, smem, r.stream, sink);
         if (rc) return rc;
     }
+    // the status word comes back with the chunk (read after the tick's sync)
+    e = cudaMemcpyAsync(r.h_status, r.dev + r.off_status, sizeof(int32_t), cudaMemcpyDeviceToHost,
+                        r.stream);
+    if (e != cudaSuccess) return set_cuda_error(e, "tvbg_serve: status copy");
     e = cudaEventRecord(r.done_ev, r.stream);
     if (e != cudaSuccess) return set_cuda_error(e, "tvbg_serve: event");
     return TVBG_OK;
@@ -452,6 +475,8 @@ struct tvbg_serve {
     int64_t cap = 0;               // budget at creation: a request larger never fits
     int64_t budget = 0, used = 0;  // current admission budget (tvbg_serve_set_budget)
     int32_t chunk = 0;
+    int64_t cta_cap = -1;          // admission stops at this many resident CTAs (-1: 3 x SMs)
+    int64_t active_ctas = 0;
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     int64_t next_id = 1;
@@ -546,13 +571,24 @@ int tvbg_serve_tick(tvbg_serve* p, int32_t* n_active, int32_t* n_queued) {
         }
         p->own_stream = true;
     }
-    // admit in arrival order while the budget and the device allow
+    if (p->cta_cap < 0) {  // default: about three waves of CTAs resident at once
+        int dev = 0, sms = 0;
+        cudaError_t e = cudaGetDevice(&dev);
+        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (e != cudaSuccess) return set_cuda_error(e, "tvbg_serve_tick: SM count");
+        p->cta_cap = 3 * static_cast<int64_t>(sms);
+    }
+    // admit in arrival order while the budget, the device and the CTA cap
+    // allow (more resident work than a few waves of CTAs only adds per-tick
+    // host work and latency; an empty pool always admits its next request)
     while (!p->queue.empty()) {
         Request* r = p->queue.front();
         size_t free_b = 0, total_b = 0;
         cudaError_t e = cudaMemGetInfo(&free_b, &total_b);
         if (e != cudaSuccess) return set_cuda_error(e, "tvbg_serve_tick: cudaMemGetInfo");
         if (p->used + static_cast<int64_t>(r->bytes) > p->budget || r->bytes > free_b) break;
+        const int64_t ctas = static_cast<int64_t>(r->members.size()) * r->cluster;
+        if (p->cta_cap > 0 && !p->active.empty() && p->active_ctas + ctas > p->cta_cap) break;
         int rc = materialise(*r);
         if (rc) {
             release(*r);
@@ -560,6 +596,7 @@ int tvbg_serve_tick(tvbg_serve* p, int32_t* n_active, int32_t* n_queued) {
         }
         p->queue.pop_front();
         p->used += static_cast<int64_t>(r->bytes);
+        p->active_ctas += r->ctas;
         r->status = TVBG_SERVE_ACTIVE;
         p->active.push_back(r);
     }
@@ -590,13 +627,11 @@ int tvbg_serve_tick(tvbg_serve* p, int32_t* n_active, int32_t* n_queued) {
     if (rc) return rc;
     e = cudaStreamSynchronize(p->stream);
     if (e != cudaSuccess) return set_cuda_error(e, "tvbg_serve_tick: synchronize");
-    // status words first: an error here leaves every request as it was
+    // status words first (copied back with each chunk): an error here leaves
+    // every request as it was
     for (size_t i = 0; i < p->active.size(); ++i) {
-        const Request& r = *p->active[i];
-        int32_t st = 0;
-        e = cudaMemcpy(&st, r.dev + r.off_status, sizeof(st), cudaMemcpyDeviceToHost);
-        if (e != cudaSuccess) return set_cuda_error(e, "tvbg_serve_tick: status");
-        if (st != 0) return set_error(TVBG_EDEVICE, "tvbg_serve_tick: a group kernel reported an error");
+        if (*p->active[i]->h_status != 0)
+            return set_error(TVBG_EDEVICE, "tvbg_serve_tick: a group kernel reported an error");
     }
     // clocks and retirement; the active list is rebuilt before any return, so
     // a retired (released) request never stays in it, and a request whose
@@ -610,6 +645,7 @@ int tvbg_serve_tick(tvbg_serve* p, int32_t* n_active, int32_t* n_queued) {
             if (rc == TVBG_OK) {
                 release(r);
                 p->used -= static_cast<int64_t>(r.bytes);
+                p->active_ctas -= r.ctas;
                 r.status = TVBG_SERVE_DONE;
                 continue;
             }
@@ -645,6 +681,7 @@ int tvbg_serve_cancel(tvbg_serve* p, int64_t id) {
         p->active.erase(std::find(p->active.begin(), p->active.end(), r));
         release(*r);
         p->used -= static_cast<int64_t>(r->bytes);
+        p->active_ctas -= r->ctas;
     } else {
         return set_error(TVBG_EINVAL, "tvbg_serve_cancel: the request is done or cancelled");
     }
@@ -657,6 +694,12 @@ int tvbg_serve_progress(tvbg_serve* p, int64_t id, int64_t* steps_done) {
     auto it = p->all.find(id);
     if (it == p->all.end()) return set_error(TVBG_EINVAL, "tvbg_serve_progress: unknown id");
     *steps_done = it->second->done;
+    return TVBG_OK;
+}
+
+int tvbg_serve_set_concurrency(tvbg_serve* p, int64_t max_ctas) {
+    if (!p) return set_error(TVBG_EINVAL, "tvbg_serve_set_concurrency: null");
+    p->cta_cap = max_ctas < 0 ? -1 : max_ctas;
     return TVBG_OK;
 }
 

@@ -265,6 +265,7 @@ SIGNATURES = {
     'tvbg_serve_usage': (ctypes.c_int, [_vp, _i64, ctypes.POINTER(_i64), ctypes.POINTER(_i64)]),
     'tvbg_serve_set_budget': (ctypes.c_int, [_vp, _i64]),
     'tvbg_serve_progress': (ctypes.c_int, [_vp, _i64, ctypes.POINTER(_i64)]),
+    'tvbg_serve_set_concurrency': (ctypes.c_int, [_vp, _i64]),
 }
 
 
