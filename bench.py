@@ -725,10 +725,11 @@ class AdjointStep:
         self.tpn = 2
         self.status = None
         self.grads = None
-        self.path = ('per-step kernel forward with checkpoints every %d steps; FC-fit loss '
+        self.path = ('%s forward with checkpoints every %d steps; FC-fit loss '
                      'path on the device (tvbg_fcfit_loss: FP64 FC and loss, no library GEMM); '
                      'per segment: recomputation + reverse-time kernel; FP64 gradients'
-                     % wl['ckpt'])
+                     % ('pipelined group kernel' if self.prob.layout == 'groups'
+                        else 'per-step kernel', wl['ckpt']))
         self.x0 = None
 
     def reset(self, x0=None):

@@ -278,14 +278,18 @@ int tvbg_batch_run(const tvbg_instance *d_inst, int32_t n_inst,
 typedef struct tvbg_adjoint {
     const tvbg_edge *edges_t; /* [nnz] transposed edges (out-edges of node j) */
     const int32_t *row_t;     /* [N+1] out-edge offsets                       */
-    const float *seg;         /* [len][N][3]: r, V, S at the start of each step */
+    const float *seg;         /* [len][N][3]: r, V, S at the start of each step, */
+                              /* element stride seg_lanes                      */
     const float *dr;          /* [len][N]: direct dL/dr(t), row t - t0        */
     float *lam;               /* [N][2]: lambda(t0 + len) in, lambda(t0) out  */
     float *ring;              /* [N << lognh] adjoint ring of mu_V            */
     double *deta;             /* [N] accumulated dL/deta                      */
     double *dG;               /* [N] accumulated per-node part of dL/dG       */
     int64_t t0;
-    int32_t len, N, lognh, reserved0;
+    int32_t len, N, lognh;
+    int32_t seg_lanes;        /* 0 or 1: seg per instance; 8: seg points at one */
+                              /* lane of a lane-interleaved group trace        */
+                              /* [len][N][3][8] (TVBG_F_TRACE_CSUM)            */
     float dt, G;
     float consts[4];          /* MPR: Delta, J, tau, I                        */
 } tvbg_adjoint;
@@ -443,7 +447,9 @@ int tvbg_philox_u32(uint32_t k0, uint32_t k1, uint32_t c1, uint32_t c2,
  *                       sin and cos of the observable, zero history (0, 1)
  *   state    [N][nsvar][L]      nparam  [N][npar][L]
  *   bold     [4][N][L]          bold_out [bold_len][N][L]
- *   trace    [trace_len][N][trace_nobs][L]
+ *   trace    [trace_len][N][trace_nobs][L]; with TVBG_F_TRACE_CSUM (the
+ *            pipelined kernel, one-channel couplings) [trace_len][N]
+ *            [trace_nobs + 1][L], the last column the raw coupling sum
  * A lane with nsteps = 0 is padding (its state and ring are not updated).
  * This layout has no counterpart in tvb-hpc; it serves the sweeps of
  * tvb_hpc/examples/hackathon.py:58-89 (a coupling x speed grid, one delay
@@ -559,9 +565,11 @@ int tvbg_fcfit_zgrad(const float *d_z, const float *d_a, float *d_out, int32_t n
 
 /*
  * The FC-fit loss path of the adjoint in one call (tvb_hpc.adjoint.FCFit),
- * for n_inst series X_b [T][N]: row s < T - 1 at d_x + b * x_inst_stride +
- * s * N, row T - 1 at d_last + b * last_inst_stride + i * last_node_stride
- * (or from d_x too when d_last is NULL).  Computes the Pearson FC in FP64
+ * for n_inst series X_b [T][N], instance b in block g = b / lanes at lane
+ * l = b % lanes (lanes = 1: per-instance arrays; 8: lane-interleaved
+ * groups): row s < T - 1 at d_x + g * x_inst_stride + l + (s * N + i) *
+ * lanes, row T - 1 at d_last + g * last_inst_stride + l + i *
+ * last_node_stride (or from d_x too when d_last is NULL).  Computes the Pearson FC in FP64
  * (two-pass means and norms, a symmetric Gram with FP64 products and sums;
  * into d_fc [n_inst][N][N] when not NULL), d_loss[b] = mean_{i<j}
  * (FC_ij - target_ij)^2 (FP64) and, when d_dx is not NULL, dL/dX (FP32) at
@@ -572,10 +580,10 @@ int tvbg_fcfit_zgrad(const float *d_z, const float *d_a, float *d_out, int32_t n
  */
 int tvbg_fcfit_scratch_bytes(int32_t n_inst, int32_t N, int64_t *bytes);
 int tvbg_fcfit_loss(const float *d_x, int64_t x_inst_stride, const float *d_last,
-                    int64_t last_inst_stride, int64_t last_node_stride, int32_t n_inst,
-                    int32_t T, int32_t N, const double *d_target, double *d_loss,
-                    float *d_dx, int64_t dx_inst_stride, double *d_fc, void *d_scratch,
-                    void *stream);
+                    int64_t last_inst_stride, int64_t last_node_stride, int32_t lanes,
+                    int32_t n_inst, int32_t T, int32_t N, const double *d_target,
+                    double *d_loss, float *d_dx, int64_t dx_inst_stride, double *d_fc,
+                    void *d_scratch, void *stream);
 
 /*
  * Region mapping (tvb_hpc/network.py:179-202).  to_avg: d_roi[i][j] = sum

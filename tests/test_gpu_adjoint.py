@@ -30,8 +30,13 @@ def problem(N=40, I=3, T=350, C=100, seed=2):
     return prob, conn, x0, eta, G, target
 
 
-def test_adjoint_matches_fp64_oracle(cuda):
+@pytest.mark.parametrize('layout', ['groups', 'instances'])
+def test_adjoint_matches_fp64_oracle(cuda, layout):
+    """Both sweep layouts of FCFit: the pipelined group kernel (default where
+    the delays allow) and the per-instance step kernel."""
     prob, conn, x0, eta, G, target = problem()
+    assert prob.layout == 'groups'
+    prob.layout = layout
     loss = prob.forward(G, eta).cpu().numpy()
     dG, deta = (t.cpu().numpy() for t in prob.backward())
     d = conn.delays(4.0, 0.1, 'ceil')
@@ -125,14 +130,30 @@ def test_fcfit_loss_kernel(cuda, I, T, N):
     loss = torch.empty(I, dtype=torch.float64, device='cuda')
     fc = torch.empty(I, N, N, dtype=torch.float64, device='cuda')
     dr = torch.zeros(I, T + 1, N, device='cuda')
-    nat.check(lib.tvbg_fcfit_loss(tr.data_ptr() + 4 * N, T * N, last.data_ptr(), 2 * N, 2, I, T, N,
-                                  target.data_ptr(), loss.data_ptr(), dr.data_ptr() + 4 * N,
+    nat.check(lib.tvbg_fcfit_loss(tr.data_ptr() + 4 * N, T * N, last.data_ptr(), 2 * N, 2, 1, I, T,
+                                  N, target.data_ptr(), loss.data_ptr(), dr.data_ptr() + 4 * N,
                                   (T + 1) * N, fc.data_ptr(), scratch.data_ptr(), None))
     torch.cuda.synchronize()
     assert rel_err(fc.cpu().numpy(), fc_ref.cpu().numpy()) < 1e-12
     assert rel_err(loss.cpu().numpy(), loss_ref.cpu().numpy()) < 1e-10
     assert rel_err(dr[:, 1:].cpu().numpy(), dx_ref.cpu().numpy()) < 1e-5
     assert float(dr[:, 0].abs().max()) == 0.0
+    # the same series lane-interleaved (groups of 8: [G][T][N][8], last [G][N][2][8])
+    G = -(-I // 8)
+    trg = torch.zeros(G * 8, T, N, device='cuda')
+    trg[:I] = tr
+    trg = trg.view(G, 8, T, N).permute(0, 2, 3, 1).contiguous()
+    lg = torch.zeros(G * 8, N, 2, device='cuda')
+    lg[:I] = last
+    lg = lg.view(G, 8, N, 2).permute(0, 2, 3, 1).contiguous()
+    dr2 = torch.zeros_like(dr)
+    nat.check(lib.tvbg_fcfit_loss(trg.data_ptr() + 4 * N * 8, T * N * 8, lg.data_ptr(), N * 2 * 8,
+                                  16, 8, I, T, N, target.data_ptr(), loss.data_ptr(),
+                                  dr2.data_ptr() + 4 * N, (T + 1) * N, fc.data_ptr(),
+                                  scratch.data_ptr(), None))
+    torch.cuda.synchronize()
+    assert torch.equal(dr2, dr)
+    assert rel_err(loss.cpu().numpy(), loss_ref.cpu().numpy()) < 1e-10
 
 
 def test_adjoint_at_benchmark_size(cuda):

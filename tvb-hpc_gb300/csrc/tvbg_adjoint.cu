@@ -53,10 +53,11 @@ __device__ __forceinline__ void adjoint_segment(const tvbg_adjoint& a, AdjRing<S
         const uint32_t tm = static_cast<uint32_t>(t) & mask;
         float r = 0.f, V = 0.f, S = 0.f, mr = 0.f, mv = 0.f;
         if (own) {
-            const float* x = a.seg + (static_cast<long long>(k) * N + j) * 3;
+            const long long sl = a.seg_lanes > 1 ? a.seg_lanes : 1;
+            const float* x = a.seg + (static_cast<long long>(k) * N + j) * 3 * sl;
             r = x[0];
-            V = x[1];
-            S = x[2];
+            V = x[sl];
+            S = x[2 * sl];
             // the rate update of step t was clamped at 0 where it went negative
             const float fr = (Delta / (pi * tau) + 2.0f * r * V) * (1.0f / tau);  // as MPR::drift
             const float rpre = fmaf(dt, fr, r);

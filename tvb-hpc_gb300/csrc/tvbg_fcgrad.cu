@@ -95,15 +95,18 @@ extern "C" int tvbg_fcfit_zgrad(const float* d_z, const float* d_a, float* d_out
 
 namespace {
 
+// Instance b of a series lives in block b / lanes at lane b % lanes:
+// lanes = 1 for per-instance arrays, 8 for lane-interleaved groups.
 struct SeriesView {
-    const float* x;      // row s (s < T - 1, or every row without `last`) at x + b * xs + s * N
-    int64_t xs;
-    const float* last;   // row T - 1 at last + b * ls + i * lns, or NULL
+    const float* x;      // row s (s < T - 1, or every row without `last`):
+    int64_t xs;          //   x + (b / lanes) xs + b % lanes + (s N + i) lanes
+    const float* last;   // row T - 1: last + (b / lanes) ls + b % lanes + i lns, or NULL
     int64_t ls, lns;
-    int T, N;
+    int T, N, lanes;
     __device__ __forceinline__ float at(int b, int s, int i) const {
-        if (last && s == T - 1) return __ldg(last + b * ls + static_cast<int64_t>(i) * lns);
-        return __ldg(x + b * xs + static_cast<int64_t>(s) * N + i);
+        const int g = b / lanes, l = b % lanes;
+        if (last && s == T - 1) return __ldg(last + g * ls + l + static_cast<int64_t>(i) * lns);
+        return __ldg(x + g * xs + l + (static_cast<int64_t>(s) * N + i) * lanes);
     }
 };
 
@@ -297,12 +300,13 @@ extern "C" int tvbg_fcfit_scratch_bytes(int32_t n_inst, int32_t N, int64_t* byte
 }
 
 extern "C" int tvbg_fcfit_loss(const float* d_x, int64_t x_inst_stride, const float* d_last,
-                               int64_t last_inst_stride, int64_t last_node_stride, int32_t n_inst,
-                               int32_t T, int32_t N, const double* d_target, double* d_loss,
-                               float* d_dx, int64_t dx_inst_stride, double* d_fc, void* d_scratch,
-                               void* stream) {
+                               int64_t last_inst_stride, int64_t last_node_stride, int32_t lanes,
+                               int32_t n_inst, int32_t T, int32_t N, const double* d_target,
+                               double* d_loss, float* d_dx, int64_t dx_inst_stride, double* d_fc,
+                               void* d_scratch, void* stream) {
     if (!d_x || !d_target || !d_loss || !d_scratch || n_inst <= 0 || n_inst > 65535 || T < 2 ||
-        N < 2 || x_inst_stride < 0 || (d_dx && dx_inst_stride < static_cast<int64_t>(T) * N))
+        N < 2 || x_inst_stride < 0 || lanes < 1 || lanes > 8 ||
+        (d_dx && dx_inst_stride < static_cast<int64_t>(T) * N))
         return tvbg::set_error(TVBG_EINVAL, "tvbg_fcfit_loss: bad arguments (need T >= 2, N >= 2)");
     const int64_t nn = static_cast<int64_t>(N) * N, in = static_cast<int64_t>(n_inst);
     auto al = [](int64_t x) { return (x + 255) & ~static_cast<int64_t>(255); };
@@ -313,7 +317,7 @@ extern "C" int tvbg_fcfit_loss(const float* d_x, int64_t x_inst_stride, const fl
     double* fc = d_fc ? d_fc : reinterpret_cast<double*>(s + 3 * al(in * N * 8));
     float* a32 = reinterpret_cast<float*>(s + 3 * al(in * N * 8) + al(in * nn * 8));
     float* fsc = reinterpret_cast<float*>(s + 3 * al(in * N * 8) + al(in * nn * 8) + al(in * nn * 4));
-    SeriesView v{d_x, x_inst_stride, d_last, last_inst_stride, last_node_stride, T, N};
+    SeriesView v{d_x, x_inst_stride, d_last, last_inst_stride, last_node_stride, T, N, lanes};
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     fcfit_moments_kernel<<<dim3((N + 127) / 128, n_inst), 128, 0, st>>>(v, mean, nrm);
     const int nt = (N + kGT - 1) / kGT;

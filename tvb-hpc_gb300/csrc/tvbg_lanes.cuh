@@ -589,11 +589,15 @@ struct GroupLane {
     uint32_t inst_id;
 };
 
+// allow_csum: the pipelined kernel's one-channel couplings can write the
+// raw coupling sum into the trace (TVBG_F_TRACE_CSUM).
 template <class M, int CF>
-__device__ __forceinline__ bool group_descriptor_ok(const tvbg_group& g) {
+__device__ __forceinline__ bool group_descriptor_ok(const tvbg_group& g, bool allow_csum = false) {
     const int N = g.N;
+    const uint32_t bad = TVBG_F_TRACKA | TVBG_F_MIDSYNC |
+                         ((allow_csum && ring_channels<CF>() == 1) ? 0u : TVBG_F_TRACE_CSUM);
     return !(N <= 0 || N > 65535 || g.lognh < 3 || g.lognh > 16 || g.model != M::ID || g.cfun != CF ||
-             g.nsteps < 0 || (g.flags & (TVBG_F_TRACKA | TVBG_F_MIDSYNC | TVBG_F_TRACE_CSUM)) ||
+             g.nsteps < 0 || (g.flags & bad) ||
              (!Noise<M>::kOK && !WideNoise<M>::value && (g.flags & TVBG_F_NOISE)));
 }
 
@@ -759,8 +763,15 @@ __device__ __forceinline__ void update_node(const tvbg_group& g, const GroupLane
         const long long t = tb + k;
         if (t >= c.t_end) break;
         if (trace && k == tr_next) {
-            float* dst = g.trace + ((static_cast<size_t>(trow) * N + n) * g.trace_nobs) * kLanes + l;
+            // a trace row holds the observables, then with TVBG_F_TRACE_CSUM
+            // the raw coupling sum of the step (one-channel couplings)
+            const bool csum = (c.flags & TVBG_F_TRACE_CSUM) != 0;
+            const int tw = g.trace_nobs + (csum ? 1 : 0);
+            float* dst = g.trace + ((static_cast<size_t>(trow) * N + n) * tw) * kLanes + l;
             for (int o = 0; o < g.trace_nobs; ++o) dst[o * kLanes] = M::obs(x, o);
+            if constexpr (NC == 1) {
+                if (csum) dst[g.trace_nobs * kLanes] = cs[k * stride];
+            }
             tr_next += mc.tev;
             trow = trow + 1 == g.trace_len ? 0 : trow + 1;
         }
@@ -879,7 +890,7 @@ __device__ __forceinline__ void run_group_pipelined(const tvbg_group& g, float* 
     const bool cluster = C > 1;
     const int H = static_cast<int>(blockDim.x) / 2;
     const int P = H / kLanes;
-    if (!group_descriptor_ok<M, CF>(g) || g.dmin < 2 * K - 1 || (H & 31) ||
+    if (!group_descriptor_ok<M, CF>(g, true) || g.dmin < 2 * K - 1 || (H & 31) ||
         static_cast<int>(C) * P < N || (reinterpret_cast<uintptr_t>(g.ring) & 15u) != 0) {
         if (threadIdx.x == 0) report(status, TVBG_EINVAL);
         return;  // uniform over the cluster: same descriptor, same launch shape

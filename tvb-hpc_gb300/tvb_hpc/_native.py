@@ -203,7 +203,7 @@ class tvbg_adjoint(ctypes.Structure):
         ('dr', ctypes.c_void_p), ('lam', ctypes.c_void_p), ('ring', ctypes.c_void_p),
         ('deta', ctypes.c_void_p), ('dG', ctypes.c_void_p), ('t0', ctypes.c_int64),
         ('len', ctypes.c_int32), ('N', ctypes.c_int32), ('lognh', ctypes.c_int32),
-        ('reserved0', ctypes.c_int32), ('dt', ctypes.c_float), ('G', ctypes.c_float),
+        ('seg_lanes', ctypes.c_int32), ('dt', ctypes.c_float), ('G', ctypes.c_float),
         ('consts', ctypes.c_float * 4),
     ]
 
@@ -251,8 +251,8 @@ SIGNATURES = {
     'tvbg_group_max_clusters': (ctypes.c_int, [ctypes.c_void_p, _ip]),
     'tvbg_fcfit_zgrad': (ctypes.c_int, [_vp, _vp, _vp, _i32, _i32, _i32, _vp]),
     'tvbg_fcfit_scratch_bytes': (ctypes.c_int, [_i32, _i32, ctypes.POINTER(_i64)]),
-    'tvbg_fcfit_loss': (ctypes.c_int, [_vp, _i64, _vp, _i64, _i64, _i32, _i32, _i32, _vp, _vp,
-                                       _vp, _i64, _vp, _vp, _vp]),
+    'tvbg_fcfit_loss': (ctypes.c_int, [_vp, _i64, _vp, _i64, _i64, _i32, _i32, _i32, _i32, _vp,
+                                       _vp, _vp, _i64, _vp, _vp, _vp]),
     'tvbg_rmap_to_avg': (ctypes.c_int, [_i32, _i32, _i32, _vp, _vp, _vp, _vp]),
     'tvbg_rmap_from_avg': (ctypes.c_int, [_i32, _i32, _i32, _vp, _vp, _vp, _vp]),
     'tvbg_serve_create': (ctypes.c_int, [_i64, _i32, _vp, ctypes.POINTER(_vp)]),

@@ -7,13 +7,17 @@ Problem (one connectome, I instances, T steps, deterministic):
   S_i(t) = sum_e w_e r_{j_e}(t - d_e)           (zero history)
   X_b[s] = r_b(s + 1),  FC_b = Pearson(X_b),  loss_b = mean_{i<j}(FC_b,ij - F*_ij)^2
 
-``FCFit.forward`` runs the step kernel in chunks of `checkpoint_every`
-steps, keeping the state and the history ring at every chunk start
-(checkpoints) and the rate series for the FC; tvbg_fcfit_loss then takes
+``FCFit.forward`` runs the sweep in chunks of `checkpoint_every` steps --
+on the pipelined lane-interleaved group kernel where the delays allow
+(every delay >= 2 K - 1), else on the per-instance step kernel -- keeping
+the state and the history ring at every chunk start (checkpoints) and the
+rate series for the FC; tvbg_fcfit_loss then takes
 the FC (a symmetric FP64 Gram), the loss and dL/dr on the device in one
 call, no library GEMM.  ``FCFit.backward`` walks the chunks backwards:
-each chunk is recomputed from its checkpoint (bit-identical to the forward)
-with the state and coupling sums traced, and tvbg_adjoint_mpr runs the
+each chunk is recomputed from its checkpoint on the same kernel
+(bit-identical to the forward) with the state and coupling sums traced
+(the group kernel's TVBG_F_TRACE_CSUM column, read in place by the adjoint
+through tvbg_adjoint.seg_lanes), and tvbg_adjoint_mpr runs the
 reverse-time recursion over it, carrying the adjoint state and an adjoint
 ring of mu_V between chunks; dL/dG and dL/deta accumulate in FP64.
 
@@ -88,8 +92,15 @@ class FCFit:
         self.edges_t = torch.from_numpy(e_t.view(np.uint8).copy()).cuda()
         _, consts, _ = self.model.engine_spec()
         self.consts = consts
-        self.tpn = 1          # gather lanes per node of the forward and recomputation sweeps
+        self.tpn = 1          # gather lanes per node of the per-instance sweeps
         self.adjoint_smem = 'auto'   # adjoint ring in shared memory: 'auto' or False
+        # forward and recomputation sweeps: the pipelined lane-interleaved
+        # group kernel where it applies (delays >= 2 K - 1, N <= 1024), else
+        # the per-instance step kernel
+        from .groups import plan_group, pipelined_threads
+        k, _ = plan_group(int(d.min()), int(d.max()))
+        self.layout = ('groups' if int(d.min()) >= 2 * k - 1 and pipelined_threads(self.N, 16)
+                       else 'instances')
 
     def _set(self, G, eta, trace_len, trace_nobs, trace_csum):
         return InstanceSet(self.model, self.cfun, self.scheme, self.conn, dt=self.dt,
@@ -119,12 +130,73 @@ class FCFit:
             plans.append(sw.prepare(n))
         return plans
 
+    def _groups(self, G, eta, trace_len, trace_nobs, trace_csum):
+        "Lane-interleaved groups of the I instances on the pipelined kernel."
+        from .groups import GroupSet, pipelined_shape, PIPELINED
+        gs = GroupSet(self.model, self.cfun, self.scheme, self.conn, dt=self.dt,
+                      couplings=np.asarray(G, np.float32), speeds=self.speed, state0=self.x0,
+                      nparam=np.asarray(eta, np.float32).reshape(self.I, self.N, 1),
+                      rounding=self.rounding, trace_every=1, trace_len=trace_len,
+                      trace_nobs=trace_nobs, trace_csum=trace_csum)
+        shape = pipelined_shape(gs)
+        assert shape[3] == PIPELINED
+        gs.set_shape(*shape)
+        return gs
+
     def forward(self, G, eta):
         "Loss [I] (FP64); keeps checkpoints and the rate series for backward."
-        torch = self.torch
         G = np.asarray(G, np.float32).reshape(self.I)
         eta = np.asarray(eta, np.float32).reshape(self.I, self.N)
         self.G, self.eta = G, eta
+        if self.layout == 'groups':
+            return self._forward_groups(G, eta)
+        return self._forward_instances(G, eta)
+
+    def _forward_groups(self, G, eta):
+        """Forward on the pipelined group kernel: segments of C steps, the
+        group state and ring cloned at each segment start, the r trace
+        lane-interleaved ([G][T][N][1][8]); the loss path reads it in place."""
+        torch = self.torch
+        fw = self._groups(G, eta, self.T, 1, False)
+        segs = [(t, min(self.C, self.T - t)) for t in range(0, self.T, self.C)]
+        plans = []
+        for t0, n in segs:
+            fw.t[:] = t0
+            plans.append(fw.prepare(n)[0])
+        self.ckpt = []
+        for (t0, n), launches in zip(segs, plans):
+            self.ckpt.append((t0, n, fw.gstate.clone(), fw.ring.clone()))
+            fw.launch(launches)
+        fw.t[:] = self.T
+        self.fw = fw
+        I, N, T = self.I, self.N, self.T
+        L = 8
+        loss = self._loss(fw.gtrace.data_ptr() + 4 * N * L, T * N * L, fw.gstate.data_ptr(),
+                          N * 2 * L, 2 * L, L)
+        torch.cuda.synchronize()
+        fw.status.check()
+        return loss
+
+    def _loss(self, x, xs, last, ls, lns, lanes):
+        """tvbg_fcfit_loss on the series at x (rows 1..T-1) and last (row T):
+        FP64 FC and loss; dL/dr(t) = dL/dX[t-1] into self.dr[:, 1:]."""
+        torch = self.torch
+        I, N, T = self.I, self.N, self.T
+        self.dr = torch.zeros((I, T + 1, N), dtype=torch.float32, device='cuda')
+        self.fc = torch.empty((I, N, N), dtype=torch.float64, device='cuda')
+        loss = torch.empty(I, dtype=torch.float64, device='cuda')
+        lib = nat.load()
+        nb = ctypes.c_int64()
+        nat.check(lib.tvbg_fcfit_scratch_bytes(I, N, ctypes.byref(nb)))
+        scratch = torch.empty(int(nb.value), dtype=torch.uint8, device='cuda')
+        nat.check(lib.tvbg_fcfit_loss(x, xs, last, ls, lns, lanes, I, T, N, self.target.data_ptr(),
+                                      loss.data_ptr(), self.dr.data_ptr() + 4 * N, (T + 1) * N,
+                                      self.fc.data_ptr(), scratch.data_ptr(), nat.stream_handle()))
+        return loss
+
+    def _forward_instances(self, G, eta):
+        "Forward on the per-instance step kernel (delays too short for the groups)."
+        torch = self.torch
         fw = self._set(G, eta, self.T, 1, False)
         sw = self._sweep(fw)
         segs = [(t, min(self.C, self.T - t)) for t in range(0, self.T, self.C)]
@@ -136,27 +208,19 @@ class FCFit:
         fw.t[:] = self.T
         self.fw = fw
         # X[s] = r(s + 1): trace rows 1..T-1 (r(t), one column) and the
-        # final state's r; loss, FC and dL/dr(t) = dL/dX[t-1] into dr[:, 1:]
-        # by tvbg_fcfit_loss (FP64 FC and loss, FP32 dL/dX)
+        # final state's r
         I, N, T = self.I, self.N, self.T
         assert fw.trace.shape[1:] == (T, N, 1)
-        self.dr = torch.zeros((I, T + 1, N), dtype=torch.float32, device='cuda')
-        self.fc = torch.empty((I, N, N), dtype=torch.float64, device='cuda')
-        loss = torch.empty(I, dtype=torch.float64, device='cuda')
-        lib = nat.load()
-        nb = ctypes.c_int64()
-        nat.check(lib.tvbg_fcfit_scratch_bytes(I, N, ctypes.byref(nb)))
-        scratch = torch.empty(int(nb.value), dtype=torch.uint8, device='cuda')
-        nat.check(lib.tvbg_fcfit_loss(fw.trace.data_ptr() + 4 * N, T * N, fw.state.data_ptr(),
-                                      2 * N, 2, I, T, N, self.target.data_ptr(), loss.data_ptr(),
-                                      self.dr.data_ptr() + 4 * N, (T + 1) * N, self.fc.data_ptr(),
-                                      scratch.data_ptr(), nat.stream_handle()))
+        loss = self._loss(fw.trace.data_ptr() + 4 * N, T * N, fw.state.data_ptr(), 2 * N, 2, 1)
         torch.cuda.synchronize()
         sw.status.check()
         return loss
 
     def backward(self):
         "(dL/dG [I], dL/deta [I, N]) in FP64, by the adjoint over the checkpoints."
+        return self._backward(self.layout == 'groups')
+
+    def _backward(self, grouped):
         torch = self.torch
         lib = nat.load()
         I, N, T = self.I, self.N, self.T
@@ -167,19 +231,35 @@ class FCFit:
         ring = torch.zeros((I, N * nh), dtype=torch.float32, device='cuda')
         deta = torch.zeros((I, N), dtype=torch.float64, device='cuda')
         dGn = torch.zeros((I, N), dtype=torch.float64, device='cuda')
-        rec = self._set(self.G, self.eta, self.C, 2, True)
-        sw = self._sweep(rec)
         rev = list(reversed(self.ckpt))
-        plans = self._plan(sw, [(t0, n) for (t0, n, _, _) in rev])
-        threads = 32 * ((N + 31) // 32)
-        seg = rec.trace                                  # [I, C, N, 3]: r, V, S of a segment
-        tab = np.zeros((len(rev), I), dtype=nat.ADJOINT_DTYPE)
         b = np.arange(I, dtype=np.int64)
+        if grouped:
+            # recomputation on the same pipelined group kernel (bit-identical
+            # to the forward) with r, V and the coupling sum S traced,
+            # lane-interleaved [G][C][N][3][8]; the adjoint reads it in place
+            rec = self._groups(self.G, self.eta, self.C, 2, True)
+            plans = []
+            for (t0, n, _, _) in rev:
+                rec.t[:] = t0
+                plans.append(rec.prepare(n)[0])
+            seg = rec.gtrace
+            seg_ptr = seg.data_ptr() + 4 * ((b // 8) * self.C * N * 3 * 8 + b % 8)
+            seg_lanes = 8
+        else:
+            rec = self._set(self.G, self.eta, self.C, 2, True)
+            sw = self._sweep(rec)
+            plans = self._plan(sw, [(t0, n) for (t0, n, _, _) in rev])
+            seg = rec.trace                              # [I, C, N, 3]: r, V, S of a segment
+            seg_ptr = seg.data_ptr() + 4 * b * seg.shape[1] * N * 3
+            seg_lanes = 1
+        threads = 32 * ((N + 31) // 32)
+        tab = np.zeros((len(rev), I), dtype=nat.ADJOINT_DTYPE)
         for k, (t0, n, _, _) in enumerate(rev):
             tk = tab[k]
             tk['edges_t'] = self.edges_t.data_ptr()
             tk['row_t'] = self.row_t.data_ptr()
-            tk['seg'] = seg.data_ptr() + 4 * b * seg.shape[1] * N * 3
+            tk['seg'] = seg_ptr
+            tk['seg_lanes'] = seg_lanes
             tk['dr'] = dr.data_ptr() + 4 * (b * (T + 1) * N + t0 * N)
             tk['lam'] = lam.data_ptr() + 4 * b * N * 2
             tk['ring'] = ring.data_ptr() + 4 * b * N * nh
@@ -204,13 +284,18 @@ class FCFit:
         smem = ring_b if (self.adjoint_smem == 'auto' and ring_b + 4096 <= max_smem()
                           and I <= sms) else 0
         for k, ((t0, n, st, rg), pl) in enumerate(zip(rev, plans)):
-            rec.state.copy_(st)
-            rec.ring.copy_(rg)
-            sw.launch(pl, self.tpn)
+            if grouped:
+                rec.gstate.copy_(st)
+                rec.ring.copy_(rg)
+                rec.launch(pl)
+            else:
+                rec.state.copy_(st)
+                rec.ring.copy_(rg)
+                sw.launch(pl, self.tpn)
             nat.check(lib.tvbg_adjoint_mpr_ex(dev.data_ptr() + k * row_bytes, I, threads, smem,
                                               nat.stream_handle()))
         torch.cuda.synchronize()
-        sw.status.check()
+        (rec if grouped else sw).status.check()
         return dGn.sum(1), deta
 
 

@@ -133,6 +133,7 @@ class GroupSet:
     def __init__(self, model, cfun, scheme, conn, dt, couplings, speeds=None, state0=None,
                  nparam=None, delays=None, rounding='ceil', seed=0, inst_ids=None,
                  bold_period=0, bold_len=0, trace_every=0, trace_len=0, trace_nobs=None,
+                 trace_csum=False,
                  flags=0, cf_b=None, t0=0, nsteps=None, block_k=None, threads=None,
                  cluster=None, history='zero', delay_tables=None):
         _device_ok()
@@ -268,11 +269,17 @@ class GroupSet:
             fl |= nat.F_BOLD
         self.trace_every, self.trace_len = int(trace_every), int(trace_len)
         self.trace_nobs = int(trace_nobs if trace_nobs is not None else self.nobs)
+        # trace_csum: one more trace column, the raw coupling sum of the step
+        # (the adjoint's recomputation; pipelined kernel, one-channel couplings)
+        self.trace_csum = bool(trace_csum)
+        self.trace_cols = self.trace_nobs + (1 if self.trace_csum else 0)
         self.gtrace = None
         if self.trace_every > 0:
-            self.gtrace = torch.zeros((G, max(1, self.trace_len), N, self.trace_nobs, L),
+            self.gtrace = torch.zeros((G, max(1, self.trace_len), N, self.trace_cols, L),
                                       dtype=torch.float32, device='cuda')
             fl |= nat.F_TRACE
+            if self.trace_csum:
+                fl |= nat.F_TRACE_CSUM
         # an Euler-Maruyama scheme on a model whose diffusion is zero is Euler
         if getattr(scheme, 'noise', False) and np.any(self.sigma != 0):
             fl |= nat.F_NOISE
@@ -312,7 +319,7 @@ class GroupSet:
 
     @property
     def trace(self):
-        "(I, trace_len, N, trace_nobs) observable trace."
+        "(I, trace_len, N, trace_cols) observable trace (+ coupling sum with trace_csum)."
         return None if self.gtrace is None else self.gtrace[self._gi, :, :, :, self._li]
 
     def reset(self, state=None):
@@ -383,7 +390,7 @@ class GroupSet:
             tab['bold_out'] = self.gbold_out.data_ptr() + 4 * gi * self.gbold_out.shape[1] * N * L
         if self.gtrace is not None:
             tab['trace'] = (self.gtrace.data_ptr()
-                            + 4 * gi * self.gtrace.shape[1] * N * self.trace_nobs * L)
+                            + 4 * gi * self.gtrace.shape[1] * N * self.trace_cols * L)
         tab['t0'] = self.t
         tab['N'] = N
         tab['nnz'] = self.nnz
@@ -478,6 +485,9 @@ class GroupSet:
         prio = (np.full(self.n_groups, self.priority, np.int64) if priorities is None
                 else np.asarray(priorities, np.int64))
         pipe = self.pipe_tab[self.gtab] if self.tpn == PIPELINED else np.ones(self.n_groups, bool)
+        if self.trace_csum and (self.tpn != PIPELINED or not pipe.all()):
+            raise ValueError('trace_csum: every group on the pipelined kernel (set_shape tpn=2, '
+                             'delays >= 2 K - 1)')
         launches = []
         for k in sorted(set(self.block_k.tolist())):
             for pk in (True, False):
