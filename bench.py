@@ -1409,7 +1409,8 @@ def cpu_baseline_mixed(wl, sample=None, sets=None, budget_s=12.0):
     return out
 
 
-def serve_window(rate, seconds, max_inst, chunk, conns, seed=7, drain_s=60.0, sample_s=0.5):
+def serve_window(rate, seconds, max_inst, chunk, conns, seed=7, drain_s=60.0, sample_s=0.5,
+                 max_ctas=None):
     """One serving run: Poisson arrivals at `rate` per second for `seconds`
     (models Kuramoto / 2-D oscillator / MPR, N in {68, 84, 192, 400, 998},
     instances log-uniform in 1..max_inst, steps log-uniform in 1k..100k, 10 %
@@ -1427,7 +1428,7 @@ def serve_window(rate, seconds, max_inst, chunk, conns, seed=7, drain_s=60.0, sa
     rng = np.random.default_rng(seed)
     n_req = max(1, int(rate * seconds))
     reqs = serve.random_requests(n_req, rate, rng, conns, inst=(1, max_inst), steps=(1000, 100000))
-    srv = serve.Server(chunk=chunk, native=True)
+    srv = serve.Server(chunk=chunk, native=True, max_ctas=max_ctas)
     t_start = time.perf_counter()
     for r in reqs:
         r.arrival += t_start
@@ -1502,21 +1503,27 @@ def serve_arm(args):
     warm.run()
     torch.cuda.synchronize()
     main, reqs = serve_window(args.serve_rate, args.serve_seconds, args.serve_max_inst,
-                              args.serve_chunk, conns, drain_s=args.serve_drain)
+                              args.serve_chunk, conns, drain_s=args.serve_drain,
+                              max_ctas=args.serve_max_ctas)
     sweep = []
     for rate in [float(x) for x in args.serve_sweep.split(',') if x]:
         res, _ = serve_window(rate, args.serve_sweep_seconds, args.serve_max_inst, args.serve_chunk,
-                              conns, seed=11, drain_s=args.serve_drain)
+                              conns, seed=11, drain_s=args.serve_drain,
+                              max_ctas=args.serve_max_ctas)
         res.pop('samples_t_insystem_backlog')
         sweep.append(res)
     kept = [x['rate_per_s'] for x in sweep if x['queue_kept_up']]
-    plain_groups = serve_plain_groups(reqs, budget_s=args.serve_plain_seconds)
-    plain = serve_plain(reqs, budget_s=args.serve_plain_seconds)
+    if args.serve_no_plain:
+        plain_groups = plain = {'value': None}
+    else:
+        plain_groups = serve_plain_groups(reqs, budget_s=args.serve_plain_seconds)
+        plain = serve_plain(reqs, budget_s=args.serve_plain_seconds)
     served = main['served_node_steps_per_s']
     line = {'metric': METRIC, 'value': served, 'unit': UNIT, 'n_gpus': 1,
             'steps': 1, 'warmup': 1, 'higher_is_better': True, 'scaling': 'weak',
             'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic (seeded connectomes)',
             'config': {'workload': 'serve', 'rate_per_s': args.serve_rate,
+                       'admission_cap_ctas': args.serve_max_ctas,
                        'window_s': args.serve_seconds, 'max_instances': args.serve_max_inst,
                        'steps': '1k-100k log-uniform', 'gradient_fraction_of_mpr': 0.1,
                        'chunk_steps': args.serve_chunk, 'hbm_budget_gb': 180,
@@ -1647,6 +1654,9 @@ def main():
     ap.add_argument('--serve-sweep', default='4,6,8,10',
                     help='arrival rates of the stability sweep (comma-separated, empty: none)')
     ap.add_argument('--serve-sweep-seconds', type=float, default=60.0)
+    ap.add_argument('--serve-max-ctas', type=int, default=None,
+                    help='native pool admission cap in resident CTAs (0: none; default: the pool\'s)')
+    ap.add_argument('--serve-no-plain', action='store_true', help='skip the plain denominators')
     ap.add_argument('--serve-chunk', type=int, default=5000)
     ap.add_argument('--serve-plain-seconds', type=float, default=20.0)
     ap.add_argument('--impl', default='engine', choices=['engine', 'reference'])

@@ -120,7 +120,8 @@ class Server:
     and only the gradient requests take the Python path.
     """
 
-    def __init__(self, hbm_budget=180e9, chunk=2000, clock=time.perf_counter, native=False):
+    def __init__(self, hbm_budget=180e9, chunk=2000, clock=time.perf_counter, native=False,
+                 max_ctas=None):
         import torch
         self.torch = torch
         self.budget = float(hbm_budget)
@@ -143,7 +144,7 @@ class Server:
         self.failed = []
         # requests without gradients in the C++ pool: waiting for their
         # arrival here, then in the pool until done
-        self.native = NativeServer(hbm_budget, chunk, clock) if native else None
+        self.native = NativeServer(hbm_budget, chunk, clock, max_ctas) if native else None
         self.native_wait = []
         self.native_busy = False
         self._native_seen = 0
@@ -444,7 +445,7 @@ class NativeServer:
     (GroupSet), alone or in any mix.
     """
 
-    def __init__(self, hbm_budget=180e9, chunk=2000, clock=time.perf_counter):
+    def __init__(self, hbm_budget=180e9, chunk=2000, clock=time.perf_counter, max_ctas=None):
         import ctypes
         from . import _native as nat
         self.nat = nat
@@ -453,6 +454,8 @@ class NativeServer:
         h = ctypes.c_void_p()
         nat.check(self.lib.tvbg_serve_create(int(hbm_budget), int(chunk), None, ctypes.byref(h)))
         self.h = h
+        if max_ctas is not None:    # admission cap in resident CTAs (0: none; -1: the default)
+            nat.check(self.lib.tvbg_serve_set_concurrency(h, int(max_ctas)))
         self.reqs = {}          # rid -> (Request, native id, kept host arrays)
         self.done = []
         self.ticks = 0
