@@ -668,9 +668,11 @@ int tvbg_serve_cancel(tvbg_serve *pool, int64_t id);
 /* Device bytes held by admitted requests and the footprint of request id. */
 int tvbg_serve_usage(tvbg_serve *pool, int64_t id, int64_t *used, int64_t *footprint);
 /* Admission stops while the active requests' chunks hold max_ctas CTAs or
- * more (an empty pool still admits its next request); 0 = no limit, -1 =
- * the default, three times the device's SM count.  Admitting more work than
- * a few waves of CTAs only adds per-tick host work and latency. */
+ * more (an empty pool still admits its next request); 0 = no limit (the
+ * default), -1 = three times the device's SM count.  On the mixed serving
+ * workload at 50 requests/s no limit served the most node-steps/s: many
+ * requests have few instances, so a CTA count underestimates how empty the
+ * GPU is. */
 int tvbg_serve_set_concurrency(tvbg_serve *pool, int64_t max_ctas);
 /* Steps request id has taken so far (every instance takes the same). */
 int tvbg_serve_progress(tvbg_serve *pool, int64_t id, int64_t *steps_done);

@@ -475,7 +475,8 @@ struct tvbg_serve {
     int64_t cap = 0;               // budget at creation: a request larger never fits
     int64_t budget = 0, used = 0;  // current admission budget (tvbg_serve_set_budget)
     int32_t chunk = 0;
-    int64_t cta_cap = -1;          // admission stops at this many resident CTAs (-1: 3 x SMs)
+    int64_t cta_cap = 0;           // admission stops at this many resident CTAs (0: no cap,
+                                   // -1: 3 x SMs)
     int64_t active_ctas = 0;
     cudaStream_t stream = nullptr;
     bool own_stream = false;
@@ -571,7 +572,7 @@ int tvbg_serve_tick(tvbg_serve* p, int32_t* n_active, int32_t* n_queued) {
         }
         p->own_stream = true;
     }
-    if (p->cta_cap < 0) {  // default: about three waves of CTAs resident at once
+    if (p->cta_cap < 0) {  // -1: about three waves of CTAs resident at once
         int dev = 0, sms = 0;
         cudaError_t e = cudaGetDevice(&dev);
         if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -579,8 +580,7 @@ int tvbg_serve_tick(tvbg_serve* p, int32_t* n_active, int32_t* n_queued) {
         p->cta_cap = 3 * static_cast<int64_t>(sms);
     }
     // admit in arrival order while the budget, the device and the CTA cap
-    // allow (more resident work than a few waves of CTAs only adds per-tick
-    // host work and latency; an empty pool always admits its next request)
+    // allow (an empty pool always admits its next request)
     while (!p->queue.empty()) {
         Request* r = p->queue.front();
         size_t free_b = 0, total_b = 0;
