@@ -561,7 +561,7 @@ class GroupBatch:
 
     PRIORITY_LEVELS = 6   # CUDA stream priorities 0 (least) .. -5 (greatest)
 
-    def __init__(self, sets, nsteps, shapes=None, step_ms=None):
+    def __init__(self, sets, nsteps, shapes=None, step_ms=None, rank_priority=False):
         torch = _torch()
         self.torch = torch
         self.sets = list(sets)
@@ -594,6 +594,15 @@ class GroupBatch:
             self.plans.append((s, launches, gmax))
         # longest sets first (their streams are forked first)
         self.plans.sort(key=lambda p: -float(p[2].max(initial=0)) * p[0].N)
+        if rank_priority:
+            # launch priority by that rank (the longest set at the greatest
+            # priority), so every replay of a captured graph dispatches the
+            # CTAs of the long chains first whatever order its branches start in
+            n = len(self.plans)
+            for r, (s, launches, _) in enumerate(self.plans):
+                for _, _, _, cfg in launches:
+                    cfg.priority = -max(0, min(self.PRIORITY_LEVELS - 1, n - 1 - r))
+        self.rank_priority = bool(rank_priority)
         self.streams = [torch.cuda.Stream() for _ in self.plans]
         self.graph = None
 
