@@ -159,10 +159,7 @@ class FCFit:
         torch = self.torch
         fw = self._groups(G, eta, self.T, 1, False)
         segs = [(t, min(self.C, self.T - t)) for t in range(0, self.T, self.C)]
-        plans = []
-        for t0, n in segs:
-            fw.t[:] = t0
-            plans.append(fw.prepare(n)[0])
+        plans = fw.prepare_segments(segs)
         self.ckpt = []
         for (t0, n), launches in zip(segs, plans):
             self.ckpt.append((t0, n, fw.gstate.clone(), fw.ring.clone()))
@@ -238,10 +235,7 @@ class FCFit:
             # to the forward) with r, V and the coupling sum S traced,
             # lane-interleaved [G][C][N][3][8]; the adjoint reads it in place
             rec = self._groups(self.G, self.eta, self.C, 2, True)
-            plans = []
-            for (t0, n, _, _) in rev:
-                rec.t[:] = t0
-                plans.append(rec.prepare(n)[0])
+            plans = rec.prepare_segments([(t0, n) for (t0, n, _, _) in rev])
             seg = rec.gtrace
             seg_ptr = seg.data_ptr() + 4 * ((b // 8) * self.C * N * 3 * 8 + b % 8)
             seg_lanes = 8

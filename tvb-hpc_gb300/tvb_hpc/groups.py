@@ -501,6 +501,42 @@ class GroupSet:
         self._uploaded = (launches, gmax)
         return launches, gmax
 
+    def prepare_segments(self, segs):
+        """Launch lists of consecutive segments [(t0, nsteps), ...] of every
+        instance, built together: one table per segment (t0 and step counts
+        set), uploaded in one copy, and one order array per launch shared by
+        all segments.  Each segment's launch list runs like prepare()'s; the
+        caller runs them in order (the clocks are set from t0)."""
+        torch = self.torch
+        old_t = self.t.copy()
+        tabs = []
+        for t0, n in segs:
+            self.t[:] = t0
+            tab, _ = self.build_table(n)
+            tabs.append(tab)
+        self.t[:] = old_t
+        allt = np.stack(tabs)                            # [S, G]
+        dev = torch.from_numpy(allt.view(np.uint8).reshape(-1).copy()).cuda()
+        G = self.n_groups
+        pipe = self.pipe_tab[self.gtab] if self.tpn == PIPELINED else np.ones(G, bool)
+        if self.trace_csum and (self.tpn != PIPELINED or not pipe.all()):
+            raise ValueError('trace_csum: every group on the pipelined kernel (set_shape tpn=2, '
+                             'delays >= 2 K - 1)')
+        shapes = []
+        for k in sorted(set(self.block_k.tolist())):
+            for pk in (True, False):
+                idx = np.nonzero((self.block_k == k) & (pipe == pk))[0].astype(np.int32)
+                if idx.size:
+                    order = torch.from_numpy(idx).cuda()
+                    shapes.append((order, int(idx.size), self.launch_cfg(k, order, None, plain=not pk)))
+        row = G * nat.GROUP_DTYPE.itemsize
+        out = []
+        for s in range(len(segs)):
+            view = dev[s * row:(s + 1) * row]
+            out.append([(view, order, n, cfg) for order, n, cfg in shapes])
+        self._segments_keep = dev
+        return out
+
     def launch(self, launches=None, stream=None):
         """Enqueue the prepared launches on `stream` (a torch stream, default
         the current one); launches of different block lengths run
