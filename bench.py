@@ -257,14 +257,65 @@ def workload_config(wl):
                 'instances': [int(p['couplings'].size) for p in wl['parts']],
                 'time_steps': 'uniform 5k-50k per instance', 'dt_ms': wl['dt'],
                 'noise': 'philox-em', 'max_delay_steps': 500,
-                'l2': 'inputs larger than L2 (rings+state)', 'parallelism': 'replicas'}
+                'l2': wl.get('l2_note'), 'parallelism': 'replicas'}
     c = wl['conn']
     return {'workload': wl['name'], 'model': wl['model'], 'coupling': wl['cfun'],
             'nodes': int(c.nnode), 'edges': int(c.nnz), 'instances': int(wl['couplings'].size),
             'time_steps': int(wl['nsteps']), 'dt_ms': wl['dt'],
             'noise': 'philox-em' if wl['noise'] else 'off',
             'bold_period_steps': int(wl['bold_period']), 'fc': wl['target'] is not None,
-            'l2': 'inputs larger than L2 (rings+state)', 'parallelism': 'replicas'}
+            'l2': wl.get('l2_note'), 'parallelism': 'replicas'}
+
+
+def l2_policy(torch):
+    """The L2 rule of the timed region: with more than twice L2 resident on
+    the device (rings, state, monitors) the inputs are larger than L2;
+    otherwise a buffer of twice L2 is written between timed steps, outside
+    the steps' event pairs.  Returns (flush buffer or None, config note)."""
+    l2 = int(getattr(torch.cuda.get_device_properties(torch.cuda.current_device()),
+                     'L2_cache_size', 0) or 126 * 2**20)
+    res = torch.cuda.memory_allocated()
+    if res > 2 * l2:
+        return None, 'inputs larger than L2 (%.0f MB resident on the device, L2 %.0f MB)' % (
+            res / 2**20, l2 / 2**20)
+    buf = torch.empty(2 * l2 // 4, dtype=torch.float32, device='cuda')
+    return buf, ('L2 flushed between timed steps: a %.0f MB write outside the steps\' event '
+                 'pairs (%.0f MB resident on the device, L2 %.0f MB)' % (
+                     2 * l2 / 2**20, res / 2**20, l2 / 2**20))
+
+
+class StepTimer:
+    """Times K steps: one event pair around the whole region, or with an L2
+    flush buffer, one pair per step with the flush between them."""
+
+    def __init__(self, torch, flush):
+        self.torch, self.flush, self.pairs = torch, flush, []
+        self.e0 = torch.cuda.Event(enable_timing=True)
+        self.e1 = torch.cuda.Event(enable_timing=True)
+
+    def start(self):
+        self.e0.record()
+
+    def before_step(self):
+        if self.flush is not None:
+            self.flush.zero_()
+            a = self.torch.cuda.Event(enable_timing=True)
+            a.record()
+            self.pairs.append([a, None])
+
+    def after_step(self):
+        if self.flush is not None:
+            b = self.torch.cuda.Event(enable_timing=True)
+            b.record()
+            self.pairs[-1][1] = b
+
+    def stop(self):
+        self.e1.record()
+
+    def ms(self):
+        if self.flush is None:
+            return self.e0.elapsed_time(self.e1)
+        return sum(a.elapsed_time(b) for a, b in self.pairs)
 
 
 def node_steps(wl):
@@ -296,9 +347,13 @@ class ClockSampler:
     def __init__(self, index=0):
         self.index = index
         self.samples = []
+        self.mark = 0
         self.proc = None
+        self.held = 0
 
     def start(self):
+        """Start nvidia-smi and wait (at most 3 s) for its first line, which
+        is taken before the timed region and dropped."""
         try:
             self.proc = subprocess.Popen(
                 ['nvidia-smi', '-i', str(self.index), '--query-gpu=' + self.QUERY,
@@ -308,6 +363,25 @@ class ClockSampler:
             self.thread.start()
         except OSError:
             self.proc = None
+            return
+        t0 = time.time()
+        while not self.samples and time.time() - t0 < 3.0 and self.proc.poll() is None:
+            time.sleep(0.01)
+        self.mark = len(self.samples)
+
+    def hold(self, step, min_samples=3, max_s=3.0):
+        """A timed region shorter than the sample period leaves too few
+        samples: keep running the same step, untimed, until min_samples
+        samples were taken since start() (at most max_s seconds).  The line
+        reports how many steps were added."""
+        import torch
+        if self.proc is None:
+            return
+        t0 = time.time()
+        while len(self.samples) - self.mark < min_samples and time.time() - t0 < max_s:
+            step()
+            torch.cuda.synchronize()
+            self.held += 1
 
     def _read(self):
         for line in self.proc.stdout:
@@ -323,7 +397,7 @@ class ClockSampler:
             self.proc.kill()
         sm, mx, reasons = [], [], set()
         names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
-        for s in self.samples:
+        for s in self.samples[self.mark:]:
             try:
                 sm.append(float(s[0]))
                 mx.append(float(s[1]))
@@ -332,9 +406,14 @@ class ClockSampler:
             for name, v in zip(names, s[3:7]):
                 if v.lower() == 'active':
                     reasons.add(name)
-        return {'sm_mhz': float(np.median(sm)) if sm else None,
-                'sm_max_mhz': float(max(mx)) if mx else None,
-                'reasons': sorted(reasons), 'samples': len(sm)}
+        out = {'sm_mhz': float(np.median(sm)) if sm else None,
+               'sm_max_mhz': float(max(mx)) if mx else None,
+               'reasons': sorted(reasons), 'samples': len(sm)}
+        if self.held:
+            out['window'] = ('timed region + %d untimed steps of the same work after it (fewer '
+                             'than 3 samples of the 200 ms period fell in the timed region)'
+                             % self.held)
+        return out
 
 
 # ---------------------------------------------------------------------------
@@ -1058,22 +1137,29 @@ def gpu_arm(args):
         gs.run()
     torch.cuda.synchronize()
     # device-resident timed region
+    flush, wl['l2_note'] = l2_policy(torch)
+    timer = StepTimer(torch, flush)
     clocks = ClockSampler(local)
     clocks.start()
     barrier()
-    e_start = torch.cuda.Event(enable_timing=True)
-    e_stop = torch.cuda.Event(enable_timing=True)
     kern_ms, n_kern = 0.0, 0
     all_evs = []
-    e_start.record()
+    timer.start()
     for _ in range(args.steps):
+        timer.before_step()
         gs.reset()
         evs, fc = gs.run(time_kernels=True)
+        timer.after_step()
         all_evs.extend(evs)
-    e_stop.record()
+    timer.stop()
     barrier()
+
+    def again():
+        gs.reset()
+        gs.run()
+    clocks.hold(again)
     clk = clocks.stop()
-    total_ms = e_start.elapsed_time(e_stop)
+    total_ms = timer.ms()
     for a, b in all_evs:
         kern_ms += a.elapsed_time(b)
         n_kern += 1
@@ -1245,17 +1331,20 @@ def adjoint_finish(args, wl, gs, torch, world, rank, barrier_fn=None):
     for _ in range(args.warmup):
         gs.run()
     barrier()
+    flush, wl['l2_note'] = l2_policy(torch)
+    timer = StepTimer(torch, flush)
     clocks = ClockSampler(int(os.environ.get('LOCAL_RANK', '0')))
     clocks.start()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    e0.record()
+    timer.start()
     for _ in range(args.steps):
+        timer.before_step()
         gs.run()
-    e1.record()
+        timer.after_step()
+    timer.stop()
     barrier()
+    clocks.hold(gs.run)
     clk = clocks.stop()
-    total_ms = e0.elapsed_time(e1)
+    total_ms = timer.ms()
     t = torch.tensor([total_ms], device='cuda')
     if world > 1:
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -1630,6 +1719,7 @@ def reference_arm(args):
             vals.append(cb['value'])
     v = float(np.median(vals))
     cb['value'] = round(v, 1)
+    wl['l2_note'] = 'host arm: the CPU caches, not timed on the device'
     line = {'metric': METRIC, 'value': round(v, 1), 'unit': UNIT, 'n_gpus': args.gpus,
             'steps': args.steps, 'warmup': args.warmup, 'higher_is_better': True,
             'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32',
