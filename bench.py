@@ -806,9 +806,12 @@ class AdjointStep:
         self.grads = None
         self.path = ('%s forward with checkpoints every %d steps; FC-fit loss '
                      'path on the device (tvbg_fcfit_loss: FP64 FC and loss, no library GEMM); '
-                     'per segment: recomputation + reverse-time kernel; FP64 gradients'
+                     'per segment: recomputation + reverse-time kernel (%s); FP64 gradients'
                      % ('pipelined group kernel' if self.prob.layout == 'groups'
-                        else 'per-step kernel', wl['ckpt']))
+                        else 'per-step kernel', wl['ckpt'],
+                        'lane-interleaved groups, time-blocked, %d threads x %d CTAs'
+                        % self.prob.adjoint_shape if self.prob.adjoint_kernel == 'groups'
+                        else 'per instance'))
         self.x0 = None
 
     def reset(self, x0=None):

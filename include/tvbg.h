@@ -303,6 +303,51 @@ int tvbg_adjoint_mpr_ex(const tvbg_adjoint *d_adj, int32_t n_inst, int32_t threa
                         int32_t smem_ring, void *stream);
 
 /*
+ * The same recursion for lane-interleaved groups of up to 8 instances that
+ * share the connectome and delays (one group per CTA or cluster of CTAs,
+ * thread = node slot x lane, lane l = instance 8 g + l), time-blocked:
+ * with every delay >= block_k, the block_k reverse steps of a block read
+ * only adjoint-ring slots written by earlier blocks, so the CTAs meet at
+ * one barrier per block.  Each thread sums its node's out-edges for the
+ * block's steps with 32-byte loads that carry 8 instances (lane l loads
+ * step l of the block), in out-edge order, as tvbg_adjoint_mpr does: the
+ * results are the same as tvbg_adjoint_mpr's on the same segment.
+ * Adjoint ring: [N][R][8] floats, R = nh + block_k, nh = 1 << lognh >=
+ * d_max + block_k; slot s of node i at (i R + (s & (nh-1))) 8 + lane,
+ * slots < block_k mirrored at + nh; zero before the last segment.
+ * Out-edges packed as in tvbg_group: pk = (i << 16) | d.
+ */
+typedef struct tvbg_adjoint_group {
+    const tvbg_edge *edges_t; /* [nnz] out-edges of node j, pk = (i << 16) | d */
+    const int32_t *row_t;     /* [N+1] out-edge offsets                       */
+    const int32_t *nodes;     /* [N] node of each slot position, or NULL      */
+    const float *seg;         /* [len][N][3][8]: r, V, S of the group's lanes  */
+                              /* (a group trace with TVBG_F_TRACE_CSUM)       */
+    const float *dr;          /* lane l: dr + l dr_stride, [len][N] rows t - t0 */
+    float *lam;               /* lane l: lam + 2 N l, [N][2]                  */
+    float *ring;              /* [N][R][8] adjoint ring of mu_V (16-byte aligned) */
+    double *deta;             /* lane l: deta + N l, [N]                      */
+    double *dG;               /* lane l: dG + N l, [N]                        */
+    int64_t t0;
+    int64_t dr_stride;        /* floats between the dr rows of two lanes       */
+    int32_t len, N, lognh;
+    int32_t lanes;            /* live lanes (1..8); others compute, write nothing */
+    int32_t dmin;             /* smallest delay (>= block_k, checked)         */
+    float dt;
+    float G[8];               /* coupling of each lane                        */
+    float consts[4];          /* MPR: Delta, J, tau, I                        */
+} tvbg_adjoint_group;
+
+size_t tvbg_adjoint_group_size(void);
+/* n_groups records; threads = 8 x node slots per CTA (a multiple of 32, <= 512),
+ * cluster CTAs per group (1..16, N <= cluster x threads / 8), block_k 4 or
+ * 8.  A record that does not match the launch sets *d_status (optional) to
+ * TVBG_EINVAL and its group does nothing. */
+int tvbg_adjoint_mpr_groups(const tvbg_adjoint_group *d_adj, int32_t n_groups,
+                            int32_t threads, int32_t cluster, int32_t block_k,
+                            int32_t *d_status, void *stream);
+
+/*
  * Pearson FC per instance over T samples of N nodes, FP64 reduction.
  * d_x: float [n_inst][T][N] (inst_stride floats between instances).
  * d_fc: float [n_inst][N][N].  If d_target ([N][N]) and d_err ([n_inst])

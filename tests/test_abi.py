@@ -47,6 +47,35 @@ def test_struct_layouts_match():
     assert lib.tvbg_launch_size() == ctypes.sizeof(nat.tvbg_launch)
     assert lib.tvbg_group_size() == ctypes.sizeof(nat.tvbg_group) == nat.GROUP_DTYPE.itemsize
     assert ctypes.sizeof(nat.tvbg_lane) == 16 and nat.GROUP_LANES == 8
+    assert (lib.tvbg_adjoint_group_size() == ctypes.sizeof(nat.tvbg_adjoint_group)
+            == nat.ADJOINT_GROUP_DTYPE.itemsize == 160)
+
+
+def test_adjoint_group_edges_and_shapes():
+    """Group packing of the transposed CSR: same out-edge order as the
+    per-instance packing, pk = (i << 16) | d; launch shapes hold N."""
+    from tvb_hpc import adjoint, network
+    w, ln = network.synthetic_connectome(50, 0.3, seed=3)
+    conn = network.Connectivity.from_dense(w, ln)
+    d = conn.delays(4.0, 0.1, 'ceil')
+    lognh = 9
+    row_t, e = adjoint.transpose_edges(conn.row, conn.col, conn.wnz, d, lognh)
+    row_tg, eg = adjoint.transpose_edges_group(conn.row, conn.col, conn.wnz, d)
+    assert np.array_equal(row_t, row_tg)
+    assert np.array_equal(e['w'], eg['w'])
+    i = eg['pk'] >> 16
+    dd = eg['pk'] & 0xffff
+    assert np.array_equal(e['pk'] >> lognh, i)
+    assert np.array_equal(e['pk'] & ((1 << lognh) - 1), (i + dd + 1) & ((1 << lognh) - 1))
+    # every out-edge (j -> i) of the in-edge CSR appears once, in row j
+    tgt = np.repeat(np.arange(50), np.diff(conn.row))
+    pairs = sorted(zip(conn.col.tolist(), tgt.tolist(), d.tolist()))
+    src = np.repeat(np.arange(50), np.diff(row_tg))
+    assert sorted(zip(src.tolist(), i.tolist(), dd.tolist())) == pairs
+    for N in (1, 17, 84, 400, 998, 1024):
+        th, c = adjoint.adjoint_group_shape(N)
+        assert th % 32 == 0 and th <= 512 and 1 <= c <= 16 and c * th // 8 >= N
+    assert adjoint.adjoint_group_shape(1025) is None
 
 
 @pytest.mark.parametrize('rounding', ['trunc', 'ceil', 'dsl'])

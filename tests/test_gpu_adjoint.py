@@ -30,13 +30,17 @@ def problem(N=40, I=3, T=350, C=100, seed=2):
     return prob, conn, x0, eta, G, target
 
 
-@pytest.mark.parametrize('layout', ['groups', 'instances'])
-def test_adjoint_matches_fp64_oracle(cuda, layout):
-    """Both sweep layouts of FCFit: the pipelined group kernel (default where
-    the delays allow) and the per-instance step kernel."""
+@pytest.mark.parametrize('layout,kernel', [('groups', 'groups'), ('groups', 'instances'),
+                                           ('instances', 'instances')])
+def test_adjoint_matches_fp64_oracle(cuda, layout, kernel):
+    """Both sweep layouts of FCFit (the pipelined group kernel, default
+    where the delays allow, and the per-instance step kernel) and both
+    reverse-time kernels on the grouped layout (lane-interleaved groups,
+    default, and per instance).  3 instances: one group with 5 idle lanes."""
     prob, conn, x0, eta, G, target = problem()
-    assert prob.layout == 'groups'
+    assert prob.layout == 'groups' and prob.adjoint_kernel == 'groups'
     prob.layout = layout
+    prob.adjoint_kernel = kernel
     loss = prob.forward(G, eta).cpu().numpy()
     dG, deta = (t.cpu().numpy() for t in prob.backward())
     d = conn.delays(4.0, 0.1, 'ceil')
@@ -63,6 +67,53 @@ def test_adjoint_matches_fp64_oracle(cuda, layout):
         em[i] -= h
         fd_eta.append((f(G[0], ep) - f(G[0], em)) / (2 * h))
     assert rel_err(deta[0, :4], np.array(fd_eta)) < 1e-3
+
+
+@pytest.mark.parametrize('I,N,K', [(11, 40, 8), (16, 84, 4), (9, 130, 8)])
+def test_adjoint_group_kernel_equals_per_instance(cuda, I, N, K):
+    """tvbg_adjoint_mpr_groups (lane-interleaved, time-blocked, clusters
+    where N needs them) against tvbg_adjoint_mpr on the same recomputed
+    traces: the same per-step code and the same out-edge order, so equal
+    results (checkpoints every 30 steps: partial blocks at every segment
+    edge)."""
+    torch = cuda
+    prob, conn, x0, eta, G, target = problem(N=N, I=I, T=180, C=30, seed=N)
+    assert prob.adjoint_kernel == 'groups' and prob.dmin >= K
+    prob.adj_k = K
+    prob.lognh_g = max(1, int(np.ceil(np.log2(prob.dmax + K))))
+    prob.forward(G, eta)
+    dG_g, deta_g = (t.clone() for t in prob.backward())
+    prob.adjoint_kernel = 'instances'
+    dG_i, deta_i = prob.backward()
+    assert torch.equal(dG_g, dG_i), (dG_g - dG_i).abs().max()
+    assert torch.equal(deta_g, deta_i), (deta_g - deta_i).abs().max()
+
+
+def test_adjoint_group_kernel_refuses_short_delays(cuda):
+    """A record whose smallest delay is below the block length sets the
+    status word (TVBG_EINVAL) and leaves the adjoint state untouched."""
+    import ctypes
+    from tvb_hpc import _native as nat
+    torch = cuda
+    lib = nat.load()
+    tab = np.zeros(1, dtype=nat.ADJOINT_GROUP_DTYPE)
+    lam = torch.ones(8 * 4 * 2, device='cuda')
+    ring = torch.zeros(4 * 32 * 8, device='cuda')
+    seg = torch.zeros(8 * 4 * 3 * 8, device='cuda')
+    row = torch.zeros(5, dtype=torch.int32, device='cuda')
+    edges = torch.zeros(2, dtype=torch.int32, device='cuda')
+    t = tab[0]
+    t['edges_t'], t['row_t'], t['seg'] = edges.data_ptr(), row.data_ptr(), seg.data_ptr()
+    t['lam'], t['ring'] = lam.data_ptr(), ring.data_ptr()
+    t['len'], t['N'], t['lognh'], t['lanes'], t['dmin'] = 8, 4, 4, 8, 3
+    dev = torch.from_numpy(tab.view(np.uint8).copy()).cuda()
+    status = torch.zeros(1, dtype=torch.int32, device='cuda')
+    nat.check(lib.tvbg_adjoint_mpr_groups(dev.data_ptr(), 1, 32, 1, 8, status.data_ptr(), None))
+    torch.cuda.synchronize()
+    assert int(status.item()) == nat.TVBG_EINVAL
+    assert float(lam.min()) == 1.0 and float(lam.max()) == 1.0
+    with pytest.raises(nat.TvbgError):
+        nat.check(lib.tvbg_adjoint_mpr_groups(dev.data_ptr(), 1, 1024, 1, 8, None, None))
 
 
 def test_adjoint_autograd_function(cuda):

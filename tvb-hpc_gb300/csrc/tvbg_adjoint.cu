@@ -1,12 +1,53 @@
 // Reverse-time adjoint of the delayed Euler scheme (Montbrio-Pazo-Roxin,
-// linear coupling), one CTA per instance, one thread per node.  The
-// recursion and its terms are documented at tvbg_adjoint_mpr in tvbg.h.
+// linear coupling): one CTA per instance and one thread per node
+// (adjoint_mpr_kernel), or lane-interleaved groups of 8 instances,
+// time-blocked (adjoint_group_kernel).  The recursion and its terms are
+// documented at tvbg_adjoint_mpr in tvbg.h.
 #include <cuda_runtime.h>
+
+#include <cstring>
 
 #include "tvbg_abi_internal.h"
 #include "tvbg_device.cuh"
+#include "tvbg_lanes.cuh"
 
 namespace tvbg {
+
+// One reverse step of one node, shared by both kernels so that they compute
+// the same numbers.  adj_mu_r: mu_r(t+1) = lambda_r(t+1), masked where the
+// rate update of step t was clamped at 0 (rpre as MPR::drift computes it).
+struct AdjMpr {
+    float Delta, J, tau, dt;
+
+    __device__ __forceinline__ float mu_r(float r, float V, float lr) const {
+        const float pi = 3.14159265358979323846f;
+        const float fr = (Delta / (pi * tau) + 2.0f * r * V) * (1.0f / tau);  // as MPR::drift
+        const float rpre = fmaf(dt, fr, r);
+        return rpre >= 0.0f ? lr : 0.0f;
+    }
+
+    // lambda(t) from mu(t+1) = (mr, mv), the coupling gather and dL/dr(t).
+    // Every rounding is spelled out (no contraction left to the compiler), so
+    // both kernels produce the same bits.
+    __device__ __forceinline__ void update(float r, float V, float S, float mr, float mv, float coup,
+                                           float cG, float drt, float& lr, float& lv, double& deta,
+                                           double& dG) const {
+        const float pi = 3.14159265358979323846f;
+        const float dfr_dr = __fdiv_rn(__fmul_rn(2.0f, V), tau);  // = dfV_dV
+        const float dfr_dV = __fdiv_rn(__fmul_rn(2.0f, r), tau);
+        const float c2 = __fmul_rn(__fmul_rn(__fmul_rn(__fmul_rn(2.0f, pi), pi), tau), tau);
+        const float dfV_dr = __fdiv_rn(__fsub_rn(__fmul_rn(J, tau), __fmul_rn(c2, r)), tau);
+        float nlr = __fmaf_rn(dt, __fmaf_rn(mv, dfV_dr, __fmul_rn(mr, dfr_dr)), mr);
+        nlr = __fmaf_rn(cG, coup, nlr);
+        const float nlv = __fmaf_rn(dt, __fmaf_rn(mv, dfr_dr, __fmul_rn(mr, dfr_dV)), mv);
+        const double c = static_cast<double>(__fdiv_rn(dt, tau));
+        const double cm = __dmul_rn(c, static_cast<double>(mv));
+        deta = __dadd_rn(deta, cm);
+        dG = __fma_rn(cm, static_cast<double>(S), dG);
+        lr = __fadd_rn(nlr, drt);
+        lv = nlv;
+    }
+};
 
 // The adjoint ring of mu_V: global memory, or staged in shared memory for
 // the kernel's run (loaded at the start, stored at the end: it carries mu_V
@@ -33,10 +74,8 @@ __device__ __forceinline__ void adjoint_segment(const tvbg_adjoint& a, AdjRing<S
     const bool own = j < N;
     const uint32_t lognh = static_cast<uint32_t>(a.lognh);
     const uint32_t mask = (1u << lognh) - 1u;
-    const float Delta = a.consts[0], J = a.consts[1], tau = a.consts[2];
-    const float pi = 3.14159265358979323846f;
-    const float dt = a.dt;
-    const float cG = dt * a.G / tau;
+    const AdjMpr m{a.consts[0], a.consts[1], a.consts[2], a.dt};
+    const float cG = a.dt * a.G / a.consts[2];
     float lr = 0.f, lv = 0.f;
     double deta = 0.0, dG = 0.0;
     int lo = 0, hi = 0;
@@ -58,10 +97,7 @@ __device__ __forceinline__ void adjoint_segment(const tvbg_adjoint& a, AdjRing<S
             r = x[0];
             V = x[sl];
             S = x[2 * sl];
-            // the rate update of step t was clamped at 0 where it went negative
-            const float fr = (Delta / (pi * tau) + 2.0f * r * V) * (1.0f / tau);  // as MPR::drift
-            const float rpre = fmaf(dt, fr, r);
-            mr = rpre >= 0.0f ? lr : 0.0f;
+            mr = m.mu_r(r, V, lr);
             mv = lv;
             ring.st(my_row | ((tm + 1u + static_cast<uint32_t>(j)) & mask), mv);
         }
@@ -85,16 +121,8 @@ __device__ __forceinline__ void adjoint_segment(const tvbg_adjoint& a, AdjRing<S
                 const uint2 ew = __ldg(edges + e);
                 coup = fmaf(__uint_as_float(ew.y), ring.ld(((tm + ew.x) & mask) | (ew.x & ~mask)), coup);
             }
-            const float dfr_dr = 2.0f * V / tau, dfr_dV = 2.0f * r / tau;
-            const float dfV_dr = (J * tau - 2.0f * pi * pi * tau * tau * r) / tau;
-            const float dfV_dV = 2.0f * V / tau;
-            float nlr = mr + dt * (mr * dfr_dr + mv * dfV_dr) + cG * coup;
-            const float nlv = mv + dt * (mr * dfr_dV + mv * dfV_dV);
-            nlr += a.dr[static_cast<long long>(k) * N + j];
-            deta += static_cast<double>(dt / tau) * static_cast<double>(mv);
-            dG += static_cast<double>(dt / tau) * static_cast<double>(mv) * static_cast<double>(S);
-            lr = nlr;
-            lv = nlv;
+            m.update(r, V, S, mr, mv, coup, cG, a.dr[static_cast<long long>(k) * N + j], lr, lv, deta,
+                     dG);
         }
         __syncthreads();
     }
@@ -124,9 +152,195 @@ __global__ void __launch_bounds__(1024, 1)
     }
 }
 
+// ---------------------------------------------------------------------------
+// Lane-interleaved groups, time-blocked
+// ---------------------------------------------------------------------------
+
+// Out-edge sums of node slot (lanes l = 0..7) for the K reverse steps of a
+// block: lane l loads ring positions tm + d + (l % K) of NI instances
+// (32 contiguous bytes for K = 8) and accumulates pairs of instances with
+// the packed FMA (each half rounded as fmaf), edges in out-edge order.  The
+// sum of step ks, instance m lands at cs[ks * stride + m] (cs: the slot's
+// first thread).  U edges per iteration: 8 loads of 16 bytes in flight.
+template <int K>
+__device__ __forceinline__ void adj_gather(const float* __restrict__ ring_g,
+                                           const uint2* __restrict__ edges, int lo, int hi,
+                                           uint32_t tm, uint32_t mask, uint32_t R, int l, float* cs,
+                                           int stride) {
+    static_assert(K == 4 || K == 8, "adjoint group gather: K = 4 or 8");
+    constexpr int NI = K == 8 ? 8 : 4;  // instances per lane
+    constexpr int NV = NI / 4;          // 16-byte loads per edge
+    constexpr int U = 8 / NV;
+    const int ks = l % K;
+    const int m0 = (l / K) * NI;
+    const float* __restrict__ ring = ring_g + m0;
+    float2 acc[NI / 2];
+#pragma unroll
+    for (int i = 0; i < NI / 2; ++i) acc[i] = make_float2(0.0f, 0.0f);
+    for (int e = lo; e < hi; e += U) {
+        float4 v[U][NV];
+        float w[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            if (e + u < hi) {
+                const uint2 ed = __ldg(edges + e + u);
+                const float4* p = reinterpret_cast<const float4*>(
+                    ring + (static_cast<size_t>(ed.x >> 16) * R + (((tm + (ed.x & 0xffffu)) & mask) + ks)) * kLanes);
+                w[u] = __uint_as_float(ed.y);
+#pragma unroll
+                for (int j = 0; j < NV; ++j) v[u][j] = __ldcg(p + j);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            if (e + u < hi) {
+                const float2 ww = make_float2(w[u], w[u]);
+#pragma unroll
+                for (int j = 0; j < NV; ++j) {
+                    acc[2 * j] = __ffma2_rn(ww, make_float2(v[u][j].x, v[u][j].y), acc[2 * j]);
+                    acc[2 * j + 1] = __ffma2_rn(ww, make_float2(v[u][j].z, v[u][j].w), acc[2 * j + 1]);
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < NI / 2; ++i) {
+        cs[ks * stride + m0 + 2 * i] = acc[i].x;
+        cs[ks * stride + m0 + 2 * i + 1] = acc[i].y;
+    }
+}
+
+// One group per CTA (or cluster of C CTAs): thread t of CTA r is lane
+// l = t % 8 of node slot q = (t / 8) C + r.  Per block of K reverse steps
+// (tb, tb - 1, ..., tb - K + 1): the gather of all K steps (reads slots
+// t + 1 + d >= tb + 2, written by earlier blocks since d >= K), then the K
+// updates from registers, each writing mu_V(t + 1) to slot t + 1, then one
+// barrier.  A slot written in a block aliases slot + nh, which no read of
+// the block reaches (nh >= d_max + K).
+template <int K>
+__global__ void __launch_bounds__(512, 1)
+    adjoint_group_kernel(const tvbg_adjoint_group* __restrict__ adj, int32_t n_groups,
+                         int32_t* __restrict__ status) {
+    __shared__ __align__(16) tvbg_adjoint_group s;
+    extern __shared__ float csum[];  // [K][blockDim]: the block's out-edge sums
+    const int cid = static_cast<int>(cluster_id_x());
+    if (cid >= n_groups) return;  // uniform over the cluster
+    {
+        static_assert(sizeof(tvbg_adjoint_group) % 4 == 0, "record size");
+        const uint32_t* src = reinterpret_cast<const uint32_t*>(adj + cid);
+        uint32_t* dst = reinterpret_cast<uint32_t*>(&s);
+        for (int i = threadIdx.x; i < static_cast<int>(sizeof(tvbg_adjoint_group) / 4); i += blockDim.x)
+            dst[i] = __ldg(src + i);
+        __syncthreads();
+    }
+    const uint32_t C = cluster_nranks();
+    const uint32_t rank = cluster_rank();
+    const bool cluster = C > 1;
+    const int N = s.N;
+    const int P = static_cast<int>(blockDim.x) / kLanes;
+    if (N < 1 || N > 65535 || static_cast<int>(C) * P < N || s.lognh < 1 || s.lognh > 16 ||
+        (1 << s.lognh) < K || s.dmin < K || s.len < 0 || s.lanes < 1 || s.lanes > kLanes ||
+        !s.ring || !s.seg || !s.edges_t || !s.row_t || (reinterpret_cast<uintptr_t>(s.ring) & 15u) != 0) {
+        if (threadIdx.x == 0) report(status, TVBG_EINVAL);
+        return;  // uniform over the cluster: same record, same launch shape
+    }
+    const int tid = static_cast<int>(threadIdx.x);
+    const int l = tid % kLanes;
+    const int q = (tid / kLanes) * static_cast<int>(C) + static_cast<int>(rank);
+    const bool valid = q < N;
+    const int n = valid ? (s.nodes ? __ldg(s.nodes + q) : q) : 0;
+    const bool live = valid && l < s.lanes;
+    const uint32_t nh = 1u << s.lognh;
+    const uint32_t mask = nh - 1u;
+    const uint32_t R = nh + K;
+    const AdjMpr m{s.consts[0], s.consts[1], s.consts[2], s.dt};
+    const float cG = s.dt * s.G[l] / s.consts[2];
+    const int lo = valid ? __ldg(s.row_t + n) : 0;
+    const int hi = valid ? __ldg(s.row_t + n + 1) : 0;
+    float lr = 0.0f, lv = 0.0f;
+    if (live) {
+        lr = s.lam[2LL * N * l + 2 * n];
+        lv = s.lam[2LL * N * l + 2 * n + 1];
+    }
+    double deta = 0.0, dG = 0.0;
+    float* cs = csum + (tid - l);
+    const int stride = static_cast<int>(blockDim.x);
+    const uint2* __restrict__ edges = reinterpret_cast<const uint2*>(s.edges_t);
+    float* __restrict__ ring_n = s.ring + static_cast<size_t>(n) * R * kLanes + l;
+    const float* __restrict__ seg_n = s.seg + static_cast<size_t>(n) * 3 * kLanes + l;
+    const float* __restrict__ dr_n = s.dr + s.dr_stride * l + n;
+    const long long t0 = s.t0;
+    for (long long tb = t0 + s.len - 1; tb >= t0; tb -= K) {
+        const int cnt = (tb - t0 + 1) < K ? static_cast<int>(tb - t0 + 1) : K;
+        adj_gather<K>(s.ring, edges, lo, hi, static_cast<uint32_t>(tb - K + 2) & mask, mask, R, l, cs,
+                      stride);
+        __syncwarp();
+#pragma unroll
+        for (int i = 0; i < K; ++i) {
+            if (i < cnt) {
+                const long long k = tb - i - t0;
+                const float* x = seg_n + static_cast<size_t>(k) * N * 3 * kLanes;
+                const float r = x[0], V = x[kLanes], S = x[2 * kLanes];
+                const float drt = live ? dr_n[k * N] : 0.0f;
+                const float mr = m.mu_r(r, V, lr);
+                const float mv = lv;
+                if (valid) {
+                    const uint32_t pos = static_cast<uint32_t>(tb - i + 1) & mask;
+                    ring_n[pos * kLanes] = mv;
+                    if (pos < static_cast<uint32_t>(K)) ring_n[(pos + nh) * kLanes] = mv;
+                }
+                m.update(r, V, S, mr, mv, cs[(K - 1 - i) * stride + l], cG, drt, lr, lv, deta, dG);
+            }
+        }
+        group_barrier(cluster);
+    }
+    if (live) {
+        s.lam[2LL * N * l + 2 * n] = lr;
+        s.lam[2LL * N * l + 2 * n + 1] = lv;
+        s.deta[static_cast<long long>(N) * l + n] += deta;
+        s.dG[static_cast<long long>(N) * l + n] += dG;
+    }
+}
+
 }  // namespace tvbg
 
 using namespace tvbg;
+
+extern "C" size_t tvbg_adjoint_group_size(void) { return sizeof(tvbg_adjoint_group); }
+
+extern "C" int tvbg_adjoint_mpr_groups(const tvbg_adjoint_group* d_adj, int32_t n_groups,
+                                       int32_t threads, int32_t cluster, int32_t block_k,
+                                       int32_t* d_status, void* stream) {
+    if (n_groups < 0 || (n_groups > 0 && !d_adj) || threads < 32 || threads > 512 || (threads & 31) ||
+        cluster < 1 || cluster > 16 || (block_k != 4 && block_k != 8))
+        return set_error(TVBG_EINVAL, "tvbg_adjoint_mpr_groups: bad arguments");
+    if (n_groups == 0) return TVBG_OK;
+    using Fn = void (*)(const tvbg_adjoint_group*, int32_t, int32_t*);
+    const Fn kfn = block_k == 8 ? adjoint_group_kernel<8> : adjoint_group_kernel<4>;
+    const size_t smem = 4u * static_cast<size_t>(block_k) * static_cast<size_t>(threads);
+    cudaError_t e = cudaSuccess;
+    if (cluster > 8) {
+        e = cudaFuncSetAttribute(reinterpret_cast<const void*>(kfn),
+                                 cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+        if (e != cudaSuccess) return set_cuda_error(e, "tvbg_adjoint_mpr_groups: cluster attribute");
+    }
+    cudaLaunchConfig_t lc;
+    std::memset(&lc, 0, sizeof(lc));
+    lc.gridDim = dim3(static_cast<unsigned>(n_groups) * static_cast<unsigned>(cluster), 1, 1);
+    lc.blockDim = dim3(static_cast<unsigned>(threads), 1, 1);
+    lc.dynamicSmemBytes = smem;
+    lc.stream = static_cast<cudaStream_t>(stream);
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = static_cast<unsigned>(cluster);
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    lc.attrs = attr;
+    lc.numAttrs = cluster > 1 ? 1 : 0;
+    e = cudaLaunchKernelEx(&lc, kfn, d_adj, n_groups, d_status);
+    if (e != cudaSuccess) return set_cuda_error(e, "tvbg_adjoint_mpr_groups launch");
+    return TVBG_OK;
+}
 
 static int adjoint_launch(const tvbg_adjoint* d_adj, int32_t n_inst, int32_t threads,
                           int32_t smem_ring, void* stream) {

@@ -16,10 +16,13 @@ the FC (a symmetric FP64 Gram), the loss and dL/dr on the device in one
 call, no library GEMM.  ``FCFit.backward`` walks the chunks backwards:
 each chunk is recomputed from its checkpoint on the same kernel
 (bit-identical to the forward) with the state and coupling sums traced
-(the group kernel's TVBG_F_TRACE_CSUM column, read in place by the adjoint
-through tvbg_adjoint.seg_lanes), and tvbg_adjoint_mpr runs the
-reverse-time recursion over it, carrying the adjoint state and an adjoint
-ring of mu_V between chunks; dL/dG and dL/deta accumulate in FP64.
+(the group kernel's TVBG_F_TRACE_CSUM column, read in place by the
+adjoint), and the reverse-time recursion runs over it, carrying the adjoint
+state and an adjoint ring of mu_V between chunks: on lane-interleaved
+groups of 8 instances, time-blocked (tvbg_adjoint_mpr_groups), where every
+delay is at least 4 steps and N <= 1024, else per instance
+(tvbg_adjoint_mpr, through tvbg_adjoint.seg_lanes on a group trace);
+dL/dG and dL/deta accumulate in FP64.
 
 ``FCFitLoss`` wraps it as a torch.autograd.Function of (G [I], eta [I, N]).
 The reference builds only symbolic partials (tvb_hpc/model.py:61-65) and an
@@ -38,26 +41,59 @@ from .utils import getLogger
 LOG = getLogger(__name__)
 
 
-def transpose_edges(row, col, w, delays, lognh):
-    """Out-edges of every source node j: (target i, delay d, weight), packed
-    for the adjoint ring read of mu_V,i(t + d + 1): pk = (i << lognh) |
-    ((i + d + 1) & mask).  Returns (row_t [N+1], packed [nnz])."""
+def _transpose(row, col):
+    """Out-edge order of a CSR of in-edges: by source j, then target i.
+    Returns (order, target of each edge, row_t [N+1])."""
     row = np.asarray(row, np.int64)
     col = np.asarray(col, np.int64)
     N = row.size - 1
     tgt = np.repeat(np.arange(N), np.diff(row))
-    order = np.lexsort((tgt, col))              # by source j, then target i
-    src_sorted = col[order]
+    order = np.lexsort((tgt, col))
     row_t = np.zeros(N + 1, np.int64)
-    np.add.at(row_t, src_sorted + 1, 1)
-    row_t = np.cumsum(row_t).astype(np.int32)
+    np.add.at(row_t, col[order] + 1, 1)
+    return order, tgt, np.cumsum(row_t).astype(np.int32)
+
+
+def transpose_edges(row, col, w, delays, lognh):
+    """Out-edges of every source node j: (target i, delay d, weight), packed
+    for the adjoint ring read of mu_V,i(t + d + 1): pk = (i << lognh) |
+    ((i + d + 1) & mask).  Returns (row_t [N+1], packed [nnz])."""
+    order, tgt, row_t = _transpose(row, col)
     mask = (1 << lognh) - 1
     i = tgt[order].astype(np.uint64)
     d = np.asarray(delays, np.int64)[order].astype(np.uint64)
-    out = np.zeros(col.size, dtype=np.dtype([('pk', '<u4'), ('w', '<f4')]))
+    out = np.zeros(len(order), dtype=np.dtype([('pk', '<u4'), ('w', '<f4')]))
     out['pk'] = ((i << np.uint64(lognh)) | ((i + d + np.uint64(1)) & np.uint64(mask))).astype(np.uint32)
     out['w'] = np.asarray(w, np.float32)[order]
     return row_t, out
+
+
+def transpose_edges_group(row, col, w, delays):
+    """The same out-edges, same order, packed for tvbg_adjoint_mpr_groups:
+    pk = (i << 16) | d.  Returns (row_t [N+1], packed [nnz])."""
+    order, tgt, row_t = _transpose(row, col)
+    d = np.asarray(delays, np.int64)[order]
+    if row_t.size - 1 > 65535 or (d.size and int(d.max()) > 65535):
+        raise ValueError('group adjoint edges: N and delays must be < 65536')
+    out = np.zeros(len(order), dtype=np.dtype([('pk', '<u4'), ('w', '<f4')]))
+    out['pk'] = ((tgt[order].astype(np.uint64) << np.uint64(16)) | d.astype(np.uint64)).astype(np.uint32)
+    out['w'] = np.asarray(w, np.float32)[order]
+    return row_t, out
+
+
+def adjoint_group_shape(N, slots=16, max_threads=512, max_cluster=16):
+    """(threads, cluster) of tvbg_adjoint_mpr_groups for N nodes: about
+    `slots` node slots per CTA (measured at N = 84, 256 instances: 16 slots
+    x 6 CTAs 9.15 ms per backward, 44 x 2 9.5 ms), as many CTAs as that
+    takes up to max_cluster, node slots a multiple of 4 (threads a multiple
+    of 32) and at most max_threads / 8; None when N does not fit."""
+    c0 = min(max_cluster, max(-(-N // slots), -(-N // (max_threads // 8)), 1))
+    for c in range(c0, max_cluster + 1):
+        p = -(-N // c)
+        p = -(-p // 4) * 4
+        if 8 * p <= max_threads:
+            return 8 * p, c
+    return None
 
 
 class FCFit:
@@ -101,6 +137,24 @@ class FCFit:
         k, _ = plan_group(int(d.min()), int(d.max()))
         self.layout = ('groups' if int(d.min()) >= 2 * k - 1 and pipelined_threads(self.N, 16)
                        else 'instances')
+        # the reverse-time kernel on the grouped layout: lane-interleaved and
+        # time-blocked (tvbg_adjoint_mpr_groups, blocks of K <= d_min steps)
+        # where the delays and N allow, else per instance over the group trace
+        self.dmin, self.dmax = int(d.min()), int(d.max())
+        self.adj_k = 8 if self.dmin >= 8 else (4 if self.dmin >= 4 else 0)
+        self.adjoint_shape = adjoint_group_shape(self.N) if self.adj_k else None
+        self.adjoint_kernel = ('groups' if self.layout == 'groups' and self.adjoint_shape
+                               else 'instances')
+        if self.adjoint_kernel == 'groups':
+            self.lognh_g = max(1, int(np.ceil(np.log2(self.dmax + self.adj_k))))
+            row_tg, e_tg = transpose_edges_group(conn.row, conn.col, conn.wnz, d)
+            assert np.array_equal(row_tg, row_t)
+            self.edges_tg = torch.from_numpy(e_tg.view(np.uint8).copy()).cuda()
+            # slot positions by out-degree, largest first: the node slots of
+            # a warp see similar edge counts
+            outdeg = np.diff(row_t)
+            self.nodes_t = torch.from_numpy(
+                np.argsort(-outdeg, kind='stable').astype(np.int32)).cuda()
 
     def _set(self, G, eta, trace_len, trace_nobs, trace_csum):
         return InstanceSet(self.model, self.cfun, self.scheme, self.conn, dt=self.dt,
@@ -230,6 +284,10 @@ class FCFit:
         dGn = torch.zeros((I, N), dtype=torch.float64, device='cuda')
         rev = list(reversed(self.ckpt))
         b = np.arange(I, dtype=np.int64)
+        if grouped and self.adjoint_kernel == 'groups':
+            rec = self._groups(self.G, self.eta, self.C, 2, True)
+            plans = rec.prepare_segments([(t0, n) for (t0, n, _, _) in rev])
+            return self._reverse_groups(rec, plans, rev, lam, deta, dGn)
         if grouped:
             # recomputation on the same pipelined group kernel (bit-identical
             # to the forward) with r, V and the coupling sum S traced,
@@ -290,6 +348,60 @@ class FCFit:
                                               nat.stream_handle()))
         torch.cuda.synchronize()
         (rec if grouped else sw).status.check()
+        return dGn.sum(1), deta
+
+
+    def _reverse_groups(self, rec, plans, rev, lam, deta, dGn):
+        """Segments last first: recompute on the group kernel, then
+        tvbg_adjoint_mpr_groups over the group trace in place (r, V, S
+        lane-interleaved [G][C][N][3][8]), an adjoint ring per group."""
+        from .engine import DeviceStatus
+        torch = self.torch
+        lib = nat.load()
+        I, N, T, K = self.I, self.N, self.T, self.adj_k
+        Gn = (I + 7) // 8
+        R = (1 << self.lognh_g) + K
+        ring = torch.zeros((Gn, N, R, 8), dtype=torch.float32, device='cuda')
+        threads, cluster = self.adjoint_shape
+        g = np.arange(Gn, dtype=np.int64)
+        Gl = np.zeros(Gn * 8, np.float32)
+        Gl[:I] = self.G
+        tab = np.zeros((len(rev), Gn), dtype=nat.ADJOINT_GROUP_DTYPE)
+        seg = rec.gtrace
+        for k, (t0, n, _, _) in enumerate(rev):
+            tk = tab[k]
+            tk['edges_t'] = self.edges_tg.data_ptr()
+            tk['row_t'] = self.row_t.data_ptr()
+            tk['nodes'] = self.nodes_t.data_ptr()
+            tk['seg'] = seg.data_ptr() + 4 * g * self.C * N * 3 * 8
+            tk['dr'] = self.dr.data_ptr() + 4 * (8 * g * (T + 1) * N + t0 * N)
+            tk['lam'] = lam.data_ptr() + 4 * 8 * g * N * 2
+            tk['ring'] = ring.data_ptr() + 4 * g * N * R * 8
+            tk['deta'] = deta.data_ptr() + 8 * 8 * g * N
+            tk['dG'] = dGn.data_ptr() + 8 * 8 * g * N
+            tk['t0'] = t0
+            tk['dr_stride'] = (T + 1) * N
+            tk['len'] = n
+            tk['N'] = N
+            tk['lognh'] = self.lognh_g
+            tk['lanes'] = np.minimum(8, I - 8 * g)
+            tk['dmin'] = self.dmin
+            tk['dt'] = np.float32(self.dt)
+            tk['G'] = Gl.reshape(Gn, 8)
+            tk['consts'] = self.consts[:4]
+        dev = torch.from_numpy(tab.view(np.uint8).reshape(-1).copy()).cuda()
+        row_bytes = Gn * nat.ADJOINT_GROUP_DTYPE.itemsize
+        status = DeviceStatus()
+        for k, ((t0, n, st, rg), pl) in enumerate(zip(rev, plans)):
+            rec.gstate.copy_(st)
+            rec.ring.copy_(rg)
+            rec.launch(pl)
+            nat.check(lib.tvbg_adjoint_mpr_groups(dev.data_ptr() + k * row_bytes, Gn, threads,
+                                                  cluster, K, status.t.data_ptr(),
+                                                  nat.stream_handle()))
+        torch.cuda.synchronize()
+        rec.status.check()
+        status.check()
         return dGn.sum(1), deta
 
 
