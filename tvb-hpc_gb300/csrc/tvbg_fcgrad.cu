@@ -110,36 +110,114 @@ struct SeriesView {
     }
 };
 
-// mean and norm sqrt(sum (x - mean)^2) of every (instance, node), FP64, two passes
-__global__ void __launch_bounds__(128) fcfit_moments_kernel(SeriesView v, double* mean, double* nrm) {
+// FP64 mean of every (instance, node): the samples split into kMS slices
+// of consecutive samples, one thread each, the slices' sums added in slice
+// order.  CTA = 32 nodes x kMS slices of one instance (blockIdx.y).
+constexpr int kMS = 8;
+__global__ void __launch_bounds__(256) fcfit_mean_kernel(SeriesView v, double* mean) {
+    __shared__ double part[kMS][32];
     const int b = blockIdx.y;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= v.N) return;
+    const int i = blockIdx.x * 32 + static_cast<int>(threadIdx.x);
+    const int per = (v.T + kMS - 1) / kMS;
+    const int t0 = static_cast<int>(threadIdx.y) * per;
+    const int t1 = t0 + per < v.T ? t0 + per : v.T;
     double s = 0.0;
-    for (int t = 0; t < v.T; ++t) s += static_cast<double>(v.at(b, t, i));
-    const double m = s / static_cast<double>(v.T);
-    double ss = 0.0;
-    for (int t = 0; t < v.T; ++t) {
-        const double c = static_cast<double>(v.at(b, t, i)) - m;
-        ss = fma(c, c, ss);
+    if (i < v.N)
+        for (int t = t0; t < t1; ++t) s += static_cast<double>(v.at(b, t, i));
+    part[threadIdx.y][threadIdx.x] = s;
+    __syncthreads();
+    if (threadIdx.y == 0 && i < v.N) {
+        double m = 0.0;
+#pragma unroll
+        for (int k = 0; k < kMS; ++k) m += part[k][threadIdx.x];
+        mean[static_cast<int64_t>(b) * v.N + i] = m / static_cast<double>(v.T);
     }
-    mean[static_cast<int64_t>(b) * v.N + i] = m;
-    nrm[static_cast<int64_t>(b) * v.N + i] = sqrt(ss);
+}
+
+// Centred Gram G_ij = sum_t c_ti c_tj, c = x - mean, FP64 (one DFMA per
+// product, samples in order), exact upper triangle for N <= kTriMaxN: the
+// triangle of 2 x 2 pair blocks (ceil(N/2) (ceil(N/2) + 1) / 2 of them,
+// row-major) is cut into parts of blockDim blocks, one block per thread;
+// CTA = (instance blockIdx.x, part blockIdx.y), instances fastest so that
+// the lanes of a lane-interleaved group read the same sectors together.
+// kTriL samples of every node staged per pass, centred in FP64.  Both
+// triangles of G written.  GB300 runs about 2 DFMA per SM per clock, so the
+// products are the cost: 3612 products per sample at N = 84, against 6144
+// in 32 x 32 tiles.
+constexpr int kTriL = 32;
+constexpr int kTriMaxN = 192;   // staging kTriL x N doubles <= 48 KB
+__global__ void __launch_bounds__(256) fcfit_gram_tri_kernel(SeriesView v,
+                                                             const double* __restrict__ mean,
+                                                             double* G) {
+    extern __shared__ double sc[];  // [kTriL][Np]
+    const int b = blockIdx.x;
+    const int N = v.N;
+    const int nb = (N + 1) / 2;
+    const int Np = 2 * nb;
+    const long long nblk = static_cast<long long>(nb) * (nb + 1) / 2;
+    const long long k = static_cast<long long>(blockIdx.y) * blockDim.x + threadIdx.x;
+    const bool active = k < nblk;
+    int bi = 0, bj = 0;
+    if (active) {
+        long long rem = k;
+        while (rem >= nb - bi) {
+            rem -= nb - bi;
+            ++bi;
+        }
+        bj = bi + static_cast<int>(rem);
+    }
+    const int i0 = 2 * bi, j0 = 2 * bj;
+    const double* mb = mean + static_cast<int64_t>(b) * N;
+    double a00 = 0.0, a01 = 0.0, a10 = 0.0, a11 = 0.0;
+    for (int t0 = 0; t0 < v.T; t0 += kTriL) {
+        for (int e = threadIdx.x; e < kTriL * Np; e += blockDim.x) {
+            const int r = e / Np, c = e % Np;
+            const int t = t0 + r;
+            sc[e] = (t < v.T && c < N) ? static_cast<double>(v.at(b, t, c)) - mb[c] : 0.0;
+        }
+        __syncthreads();
+        if (active) {
+#pragma unroll 8
+            for (int r = 0; r < kTriL; ++r) {
+                const double* row = sc + r * Np;
+                const double x0 = row[i0], x1 = row[i0 + 1];
+                const double y0 = row[j0], y1 = row[j0 + 1];
+                a00 = fma(x0, y0, a00);
+                a01 = fma(x0, y1, a01);
+                a10 = fma(x1, y0, a10);
+                a11 = fma(x1, y1, a11);
+            }
+        }
+        __syncthreads();
+    }
+    if (!active) return;
+    double* gb = G + static_cast<int64_t>(b) * N * N;
+    const double acc[2][2] = {{a00, a01}, {a10, a11}};
+#pragma unroll
+    for (int u = 0; u < 2; ++u)
+#pragma unroll
+        for (int w = 0; w < 2; ++w) {
+            const int i = i0 + u, j = j0 + w;
+            if (i < N && j < N && j >= i) {
+                gb[static_cast<int64_t>(i) * N + j] = acc[u][w];
+                gb[static_cast<int64_t>(j) * N + i] = acc[u][w];
+            }
+        }
 }
 
 constexpr int kGT = 32;   // Gram tile: 32 x 32 node pairs, 32 samples per stage
 
-// FC_ij = sum_t c_ti c_tj / (nrm_i nrm_j), c = x - mean, FP64; one CTA per
-// upper-triangle 32 x 32 tile (blockIdx.x enumerates tiles with jt >= it),
-// 256 threads of 2 x 2 pairs; both triangles written.
+// The centred Gram for larger N: one CTA per upper-triangle 32 x 32 tile
+// (blockIdx.y enumerates tiles with jt >= it; instance blockIdx.x), 256
+// threads of 2 x 2 pairs, samples in order; both triangles written.
 __global__ void __launch_bounds__(256) fcfit_gram_kernel(SeriesView v, const double* __restrict__ mean,
-                                                         const double* __restrict__ nrm, double* fc) {
+                                                         double* G) {
     __shared__ double sI[kGT][kGT + 1];
     __shared__ double sJ[kGT][kGT + 1];
-    const int b = blockIdx.y;
+    const int b = blockIdx.x;
     const int N = v.N;
     const int nt = (N + kGT - 1) / kGT;
-    int it = 0, rem = blockIdx.x;
+    int it = 0, rem = blockIdx.y;
     while (rem >= nt - it) {
         rem -= nt - it;
         ++it;
@@ -169,35 +247,42 @@ __global__ void __launch_bounds__(256) fcfit_gram_kernel(SeriesView v, const dou
         }
         __syncthreads();
     }
-    const double* nb = nrm + static_cast<int64_t>(b) * N;
-    double* fb = fc + static_cast<int64_t>(b) * N * N;
+    double* gb = G + static_cast<int64_t>(b) * N * N;
 #pragma unroll
     for (int u = 0; u < 2; ++u)
 #pragma unroll
         for (int w = 0; w < 2; ++w) {
             const int i = i0 + 2 * ty + u, j = j0 + 2 * tx + w;
             if (i < N && j < N && j >= i) {
-                const double r = acc[u][w] / (nb[i] * nb[j]);
-                fb[static_cast<int64_t>(i) * N + j] = r;
-                fb[static_cast<int64_t>(j) * N + i] = r;
+                gb[static_cast<int64_t>(i) * N + j] = acc[u][w];
+                gb[static_cast<int64_t>(j) * N + i] = acc[u][w];
             }
         }
 }
 
-// loss_b = sum_{i<j} (FC - F*)^2 / P; A = 2 (FC - F*) / P, zero diagonal
-// (FP32 copy for Z A); zg_i = sum_j FC_ij A_ij (FP64).  One CTA per instance.
-__global__ void __launch_bounds__(256) fcfit_loss_kernel(const double* __restrict__ fc,
-                                                         const double* __restrict__ target, int N,
-                                                         double* loss, float* a32, double* zg) {
+// Per instance (one CTA): nrm_i = sqrt(G_ii) (the centred sum of squares);
+// FC_ij = G_ij / (nrm_i nrm_j) in place; loss_b = sum_{i<j} (FC - F*)^2 / P;
+// A = 2 (FC - F*) / P with a zero diagonal (FP32 copy for Z A);
+// zg_i = sum_j FC_ij A_ij (FP64); and the FP32 factors of the dL/dX
+// epilogue per node: mean, 1 / nrm, zg / nrm (rounded once from FP64).
+__global__ void __launch_bounds__(256) fcfit_loss_kernel(double* fc, const double* __restrict__ target,
+                                                         int N, const double* __restrict__ mean,
+                                                         double* nrm, double* loss, float* a32,
+                                                         double* zg, float* fs) {
     __shared__ double red[256];
     const int b = blockIdx.x;
     const double P = 0.5 * static_cast<double>(N) * (N - 1);
-    const double* fb = fc + static_cast<int64_t>(b) * N * N;
+    double* fb = fc + static_cast<int64_t>(b) * N * N;
+    double* nb = nrm + static_cast<int64_t>(b) * N;
     float* ab = a32 + static_cast<int64_t>(b) * N * N;
+    for (int i = threadIdx.x; i < N; i += blockDim.x) nb[i] = sqrt(fb[static_cast<int64_t>(i) * N + i]);
+    __syncthreads();
     double part = 0.0;
     for (int64_t k = threadIdx.x; k < static_cast<int64_t>(N) * N; k += blockDim.x) {
         const int i = static_cast<int>(k / N), j = static_cast<int>(k % N);
-        const double d = fb[k] - target[k];
+        const double r = fb[k] / (nb[i] * nb[j]);
+        fb[k] = r;
+        const double d = r - target[k];
         if (j > i) part = fma(d, d, part);
         ab[k] = i == j ? 0.0f : static_cast<float>(2.0 * d / P);
     }
@@ -215,32 +300,26 @@ __global__ void __launch_bounds__(256) fcfit_loss_kernel(const double* __restric
             const double d = fb[static_cast<int64_t>(i) * N + j] - target[static_cast<int64_t>(i) * N + j];
             s = fma(fb[static_cast<int64_t>(i) * N + j], 2.0 * d / P, s);
         }
-        zg[static_cast<int64_t>(b) * N + i] = s;
+        const int64_t bi = static_cast<int64_t>(b) * N + i;
+        zg[bi] = s;
+        fs[3 * bi] = static_cast<float>(mean[bi]);
+        fs[3 * bi + 1] = static_cast<float>(1.0 / nb[i]);
+        fs[3 * bi + 2] = static_cast<float>(s / nb[i]);
     }
-}
-
-// Per (instance, node) FP32 factors of the dL/dX epilogue: mean, 1 / nrm
-// and zg / nrm (rounded once from FP64).
-__global__ void fcfit_scale_kernel(const double* __restrict__ mean, const double* __restrict__ nrm,
-                                   const double* __restrict__ zg, int64_t n, float* f) {
-    const int64_t k = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
-    if (k >= n) return;
-    f[3 * k] = static_cast<float>(mean[k]);
-    f[3 * k + 1] = static_cast<float>(1.0 / nrm[k]);
-    f[3 * k + 2] = static_cast<float>(zg[k] / nrm[k]);
 }
 
 // dL/dX_tj = ((Z A)_tj - Z_tj zg_j) / nrm_j with Z = (x - mean) / nrm formed
 // on the fly in FP32 (the backward's precision); the tiled FP32 product of
 // fcgrad_kernel with that epilogue.
+// Grid (instance, sample tile, node tile), instances fastest.
 __global__ void __launch_bounds__(256)
     fcfit_dx_kernel(SeriesView v, const float* __restrict__ fs, const float* __restrict__ A,
                     float* __restrict__ dx, int64_t dxs) {
     __shared__ float sZ[kTK][kTM + 4];  // [k][t]
     __shared__ float sA[kTK][kTN];      // [k][j]
-    const int b = blockIdx.z;
+    const int b = blockIdx.x;
     const int T = v.T, N = v.N;
-    const int t0 = blockIdx.y * kTM, j0 = blockIdx.x * kTN;
+    const int t0 = blockIdx.y * kTM, j0 = blockIdx.z * kTN;
     const float* fb = fs + static_cast<int64_t>(b) * N * 3;   // [N][mean, 1/nrm, zg/nrm]
     const float* Ab = A + static_cast<size_t>(b) * N * N;
     const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
@@ -287,6 +366,78 @@ __global__ void __launch_bounds__(256)
     }
 }
 
+// The same product for N <= 16 WN, whole rows: CTA = (instance blockIdx.x,
+// 64 samples blockIdx.y), A_b [N][16 WN] and the Z tile [64][N + 1] staged
+// in shared memory once; thread (tx, ty) of 16 x 16 owns samples 4 ty .. +3
+// and nodes tx + 16 w.  Sums over k in order, as fcfit_dx_kernel: the same
+// results.
+template <int WN>
+__global__ void __launch_bounds__(256)
+    fcfit_dx_rows_kernel(SeriesView v, const float* __restrict__ fs, const float* __restrict__ A,
+                         float* __restrict__ dx, int64_t dxs) {
+    extern __shared__ float sm[];
+    constexpr int NP = 16 * WN;
+    const int b = blockIdx.x;
+    const int T = v.T, N = v.N;
+    const int t0 = blockIdx.y * 64;
+    float* sA = sm;             // [N][NP]
+    float* sZ = sm + N * NP;    // [64][N + 1]
+    const int zs = N + 1;
+    const float* fb = fs + static_cast<int64_t>(b) * N * 3;
+    const float* Ab = A + static_cast<size_t>(b) * N * N;
+    for (int e = threadIdx.x; e < N * NP; e += 256) {
+        const int k = e / NP, j = e % NP;
+        sA[e] = j < N ? __ldg(Ab + static_cast<size_t>(k) * N + j) : 0.0f;
+    }
+    for (int e = threadIdx.x; e < 64 * N; e += 256) {
+        const int r = e / N, k = e % N;
+        const int t = t0 + r;
+        sZ[r * zs + k] = t < T ? (v.at(b, t, k) - fb[3 * k]) * fb[3 * k + 1] : 0.0f;
+    }
+    __syncthreads();
+    const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+    float acc[4][WN] = {};
+    for (int k = 0; k < N; ++k) {
+        float z[4], a[WN];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) z[u] = sZ[(ty * 4 + u) * zs + k];
+#pragma unroll
+        for (int w = 0; w < WN; ++w) a[w] = sA[k * NP + tx + 16 * w];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+            for (int w = 0; w < WN; ++w) acc[u][w] = fmaf(z[u], a[w], acc[u][w]);
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+        const int t = t0 + ty * 4 + u;
+        if (t >= T) continue;
+#pragma unroll
+        for (int w = 0; w < WN; ++w) {
+            const int j = tx + 16 * w;
+            if (j >= N) continue;
+            const float z = sZ[(ty * 4 + u) * zs + j];
+            dx[b * dxs + static_cast<int64_t>(t) * N + j] =
+                fmaf(-z, fb[3 * j + 2], acc[u][w] * fb[3 * j + 1]);
+        }
+    }
+}
+
+template <int WN>
+int launch_dx_rows(SeriesView v, const float* fs, const float* A, float* dx, int64_t dxs, int n_inst,
+                   cudaStream_t st) {
+    const size_t smem = 4u * (static_cast<size_t>(v.N) * 16 * WN + 64u * (v.N + 1));
+    if (smem > 48u * 1024u) {
+        const cudaError_t e = cudaFuncSetAttribute(reinterpret_cast<const void*>(fcfit_dx_rows_kernel<WN>),
+                                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                   static_cast<int>(smem));
+        if (e != cudaSuccess) return tvbg::set_cuda_error(e, "tvbg_fcfit_loss: smem attribute");
+    }
+    const dim3 grid(static_cast<unsigned>(n_inst), static_cast<unsigned>((v.T + 63) / 64));
+    fcfit_dx_rows_kernel<WN><<<grid, 256, smem, st>>>(v, fs, A, dx, dxs);
+    return TVBG_OK;
+}
+
 }  // namespace
 
 extern "C" int tvbg_fcfit_scratch_bytes(int32_t n_inst, int32_t N, int64_t* bytes) {
@@ -319,16 +470,33 @@ extern "C" int tvbg_fcfit_loss(const float* d_x, int64_t x_inst_stride, const fl
     float* fsc = reinterpret_cast<float*>(s + 3 * al(in * N * 8) + al(in * nn * 8) + al(in * nn * 4));
     SeriesView v{d_x, x_inst_stride, d_last, last_inst_stride, last_node_stride, T, N, lanes};
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    fcfit_moments_kernel<<<dim3((N + 127) / 128, n_inst), 128, 0, st>>>(v, mean, nrm);
+    if ((T + 63) / 64 > 65535) return tvbg::set_error(TVBG_EINVAL, "tvbg_fcfit_loss: T too large");
     const int nt = (N + kGT - 1) / kGT;
-    fcfit_gram_kernel<<<dim3(nt * (nt + 1) / 2, n_inst), 256, 0, st>>>(v, mean, nrm, fc);
-    fcfit_loss_kernel<<<n_inst, 256, 0, st>>>(fc, d_target, N, d_loss, a32, zg);
+    if (N > kTriMaxN && nt * (nt + 1) / 2 > 65535)
+        return tvbg::set_error(TVBG_EINVAL, "tvbg_fcfit_loss: N too large");
+    fcfit_mean_kernel<<<dim3((N + 31) / 32, n_inst), dim3(32, kMS), 0, st>>>(v, mean);
+    if (N <= kTriMaxN) {
+        const int nb = (N + 1) / 2;
+        const long long nblk = static_cast<long long>(nb) * (nb + 1) / 2;
+        const unsigned parts = static_cast<unsigned>((nblk + 255) / 256);
+        const size_t smem = 8u * kTriL * 2u * static_cast<size_t>(nb);
+        fcfit_gram_tri_kernel<<<dim3(n_inst, parts), 256, smem, st>>>(v, mean, fc);
+    } else {
+        fcfit_gram_kernel<<<dim3(n_inst, nt * (nt + 1) / 2), 256, 0, st>>>(v, mean, fc);
+    }
+    fcfit_loss_kernel<<<n_inst, 256, 0, st>>>(fc, d_target, N, mean, nrm, d_loss, a32, zg, fsc);
     if (d_dx) {
-        const dim3 grid((N + kTN - 1) / kTN, (T + kTM - 1) / kTM, n_inst);
-        if (grid.y > 65535u) return tvbg::set_error(TVBG_EINVAL, "tvbg_fcfit_loss: T too large");
-        fcfit_scale_kernel<<<static_cast<unsigned>((in * N + 255) / 256), 256, 0, st>>>(mean, nrm, zg,
-                                                                                       in * N, fsc);
-        fcfit_dx_kernel<<<grid, 256, 0, st>>>(v, fsc, a32, d_dx, dx_inst_stride);
+        int rc = TVBG_OK;
+        if (N <= 32) rc = launch_dx_rows<2>(v, fsc, a32, d_dx, dx_inst_stride, n_inst, st);
+        else if (N <= 64) rc = launch_dx_rows<4>(v, fsc, a32, d_dx, dx_inst_stride, n_inst, st);
+        else if (N <= 96) rc = launch_dx_rows<6>(v, fsc, a32, d_dx, dx_inst_stride, n_inst, st);
+        else if (N <= 128) rc = launch_dx_rows<8>(v, fsc, a32, d_dx, dx_inst_stride, n_inst, st);
+        else {
+            const dim3 grid(n_inst, (T + kTM - 1) / kTM, (N + kTN - 1) / kTN);
+            if (grid.z > 65535u) return tvbg::set_error(TVBG_EINVAL, "tvbg_fcfit_loss: N too large");
+            fcfit_dx_kernel<<<grid, 256, 0, st>>>(v, fsc, a32, d_dx, dx_inst_stride);
+        }
+        if (rc != TVBG_OK) return rc;
     }
     const cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? TVBG_OK : tvbg::set_cuda_error(e, "tvbg_fcfit_loss launch");
