@@ -116,6 +116,25 @@ def test_adjoint_group_kernel_refuses_short_delays(cuda):
         nat.check(lib.tvbg_adjoint_mpr_groups(dev.data_ptr(), 1, 1024, 1, 8, None, None))
 
 
+def test_fcfit_reuse_matches_fresh(cuda):
+    """FCFit keeps its group sets and buffers across calls: a second
+    forward + backward with other couplings and eta gives the same bits as a
+    fresh problem."""
+    torch = cuda
+    prob, conn, x0, eta, G, target = problem(N=40, I=11, T=250, C=50)
+    prob.forward(G, eta)
+    prob.backward()
+    G2 = (G * 1.3).astype(np.float32)
+    eta2 = (eta + 0.25).astype(np.float32)
+    l1 = prob.forward(G2, eta2).clone()
+    g1 = [t.clone() for t in prob.backward()]
+    fresh, *_ = problem(N=40, I=11, T=250, C=50)
+    l2 = fresh.forward(G2, eta2)
+    g2 = fresh.backward()
+    assert torch.equal(l1, l2)
+    assert all(torch.equal(a, b) for a, b in zip(g1, g2))
+
+
 def test_adjoint_autograd_function(cuda):
     torch = cuda
     prob, conn, x0, eta, G, target = problem(I=2, T=200)

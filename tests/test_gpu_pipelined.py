@@ -174,3 +174,20 @@ def test_batch_tuner_plan_is_exact(cuda):
     for s, r, st in zip(sets, ref, steps):
         r.run(st)
         assert np.array_equal(s.state.cpu().numpy(), r.state.cpu().numpy())
+
+
+def test_prepare_segments_tables(cuda):
+    """prepare_segments builds one table and sets t0 and the step counts of
+    each segment in bulk: byte for byte the tables of build_table per
+    segment (13 instances: one group with idle lanes; two delay tables)."""
+    args, kw, _ = setup('MPR', 'Linear', I=13, N=84, speeds=(4.0, 6.0))
+    gs = groups.GroupSet(*args, **kw)
+    gs.set_shape(*pipelined_shape(gs))
+    segs = [(0, 30), (30, 30), (60, 17), (77, 0)]
+    gs.prepare_segments(segs)
+    G = gs.n_groups
+    got = gs._segments_keep.cpu().numpy().view(nat.GROUP_DTYPE).reshape(len(segs), G)
+    for s, (t0, n) in enumerate(segs):
+        gs.t[:] = t0
+        ref, _ = gs.build_table(n)
+        assert got[s].tobytes() == ref.tobytes(), s

@@ -145,6 +145,11 @@ class FCFit:
         self.adjoint_shape = adjoint_group_shape(self.N) if self.adj_k else None
         self.adjoint_kernel = ('groups' if self.layout == 'groups' and self.adjoint_shape
                                else 'instances')
+        # device buffers and group sets reused across calls (built on first use)
+        self._fw_gs = self._rec_gs = None
+        self._ck = None
+        self._bufs = None
+        self._adj_ring = None
         if self.adjoint_kernel == 'groups':
             self.lognh_g = max(1, int(np.ceil(np.log2(self.dmax + self.adj_k))))
             row_tg, e_tg = transpose_edges_group(conn.row, conn.col, conn.wnz, d)
@@ -192,7 +197,9 @@ class FCFit:
                       nparam=np.asarray(eta, np.float32).reshape(self.I, self.N, 1),
                       rounding=self.rounding, trace_every=1, trace_len=trace_len,
                       trace_nobs=trace_nobs, trace_csum=trace_csum)
-        shape = pipelined_shape(gs)
+        sms = self.torch.cuda.get_device_properties(
+            self.torch.cuda.current_device()).multi_processor_count
+        shape = pipelined_shape(gs, min_ctas=sms)
         assert shape[3] == PIPELINED
         gs.set_shape(*shape)
         return gs
@@ -206,17 +213,43 @@ class FCFit:
             return self._forward_groups(G, eta)
         return self._forward_instances(G, eta)
 
+    def _group_sets(self, G, eta):
+        """The forward's and the recomputation's GroupSets (one-column r
+        trace of T rows; r, V and the coupling sum over one segment), built
+        on the first call and given this call's couplings, eta and initial
+        state after that."""
+        torch = self.torch
+        if self._fw_gs is None:
+            self._fw_gs = self._groups(G, eta, self.T, 1, False)
+            self._rec_gs = self._groups(G, eta, self.C, 2, True)
+            self._x0_dev = torch.from_numpy(self.x0).cuda()
+        else:
+            for gs in (self._fw_gs, self._rec_gs):
+                gs.set_couplings(G)
+                gs.set_nparam(eta)
+            fw = self._fw_gs
+            fw.set_state(self._x0_dev)
+            fw.clear_history()
+            fw.t[:] = 0
+        return self._fw_gs, self._rec_gs
+
     def _forward_groups(self, G, eta):
         """Forward on the pipelined group kernel: segments of C steps, the
-        group state and ring cloned at each segment start, the r trace
+        group state and ring copied at each segment start, the r trace
         lane-interleaved ([G][T][N][1][8]); the loss path reads it in place."""
         torch = self.torch
-        fw = self._groups(G, eta, self.T, 1, False)
+        fw, _ = self._group_sets(G, eta)
         segs = [(t, min(self.C, self.T - t)) for t in range(0, self.T, self.C)]
         plans = fw.prepare_segments(segs)
+        if self._ck is None:
+            self._ck = (torch.empty((len(segs), ) + tuple(fw.gstate.shape), dtype=torch.float32,
+                                    device='cuda'),
+                        torch.empty((len(segs), fw.ring.numel()), dtype=torch.float32, device='cuda'))
         self.ckpt = []
-        for (t0, n), launches in zip(segs, plans):
-            self.ckpt.append((t0, n, fw.gstate.clone(), fw.ring.clone()))
+        for s, ((t0, n), launches) in enumerate(zip(segs, plans)):
+            self._ck[0][s].copy_(fw.gstate)
+            self._ck[1][s].copy_(fw.ring)
+            self.ckpt.append((t0, n, self._ck[0][s], self._ck[1][s]))
             fw.launch(launches)
         fw.t[:] = self.T
         self.fw = fw
@@ -233,13 +266,16 @@ class FCFit:
         FP64 FC and loss; dL/dr(t) = dL/dX[t-1] into self.dr[:, 1:]."""
         torch = self.torch
         I, N, T = self.I, self.N, self.T
-        self.dr = torch.zeros((I, T + 1, N), dtype=torch.float32, device='cuda')
-        self.fc = torch.empty((I, N, N), dtype=torch.float64, device='cuda')
-        loss = torch.empty(I, dtype=torch.float64, device='cuda')
         lib = nat.load()
-        nb = ctypes.c_int64()
-        nat.check(lib.tvbg_fcfit_scratch_bytes(I, N, ctypes.byref(nb)))
-        scratch = torch.empty(int(nb.value), dtype=torch.uint8, device='cuda')
+        if self._bufs is None:
+            nb = ctypes.c_int64()
+            nat.check(lib.tvbg_fcfit_scratch_bytes(I, N, ctypes.byref(nb)))
+            # dr row 0 stays zero; the loss path writes rows 1..T every call
+            self._bufs = (torch.zeros((I, T + 1, N), dtype=torch.float32, device='cuda'),
+                          torch.empty((I, N, N), dtype=torch.float64, device='cuda'),
+                          torch.empty(int(nb.value), dtype=torch.uint8, device='cuda'))
+        self.dr, self.fc, scratch = self._bufs
+        loss = torch.empty(I, dtype=torch.float64, device='cuda')
         nat.check(lib.tvbg_fcfit_loss(x, xs, last, ls, lns, lanes, I, T, N, self.target.data_ptr(),
                                       loss.data_ptr(), self.dr.data_ptr() + 4 * N, (T + 1) * N,
                                       self.fc.data_ptr(), scratch.data_ptr(), nat.stream_handle()))
@@ -285,14 +321,14 @@ class FCFit:
         rev = list(reversed(self.ckpt))
         b = np.arange(I, dtype=np.int64)
         if grouped and self.adjoint_kernel == 'groups':
-            rec = self._groups(self.G, self.eta, self.C, 2, True)
+            rec = self._rec_gs
             plans = rec.prepare_segments([(t0, n) for (t0, n, _, _) in rev])
             return self._reverse_groups(rec, plans, rev, lam, deta, dGn)
         if grouped:
             # recomputation on the same pipelined group kernel (bit-identical
             # to the forward) with r, V and the coupling sum S traced,
             # lane-interleaved [G][C][N][3][8]; the adjoint reads it in place
-            rec = self._groups(self.G, self.eta, self.C, 2, True)
+            rec = self._rec_gs
             plans = rec.prepare_segments([(t0, n) for (t0, n, _, _) in rev])
             seg = rec.gtrace
             seg_ptr = seg.data_ptr() + 4 * ((b // 8) * self.C * N * 3 * 8 + b % 8)
@@ -361,34 +397,37 @@ class FCFit:
         I, N, T, K = self.I, self.N, self.T, self.adj_k
         Gn = (I + 7) // 8
         R = (1 << self.lognh_g) + K
-        ring = torch.zeros((Gn, N, R, 8), dtype=torch.float32, device='cuda')
+        if self._adj_ring is None or tuple(self._adj_ring.shape) != (Gn, N, R, 8):
+            self._adj_ring = torch.zeros((Gn, N, R, 8), dtype=torch.float32, device='cuda')
+        else:
+            self._adj_ring.zero_()
+        ring = self._adj_ring
         threads, cluster = self.adjoint_shape
-        g = np.arange(Gn, dtype=np.int64)
+        g = np.arange(Gn, dtype=np.int64)[None, :]           # [1, Gn]
+        t0s = np.array([r[0] for r in rev], np.int64)[:, None]
+        lens = np.array([r[1] for r in rev], np.int64)[:, None]
         Gl = np.zeros(Gn * 8, np.float32)
         Gl[:I] = self.G
         tab = np.zeros((len(rev), Gn), dtype=nat.ADJOINT_GROUP_DTYPE)
-        seg = rec.gtrace
-        for k, (t0, n, _, _) in enumerate(rev):
-            tk = tab[k]
-            tk['edges_t'] = self.edges_tg.data_ptr()
-            tk['row_t'] = self.row_t.data_ptr()
-            tk['nodes'] = self.nodes_t.data_ptr()
-            tk['seg'] = seg.data_ptr() + 4 * g * self.C * N * 3 * 8
-            tk['dr'] = self.dr.data_ptr() + 4 * (8 * g * (T + 1) * N + t0 * N)
-            tk['lam'] = lam.data_ptr() + 4 * 8 * g * N * 2
-            tk['ring'] = ring.data_ptr() + 4 * g * N * R * 8
-            tk['deta'] = deta.data_ptr() + 8 * 8 * g * N
-            tk['dG'] = dGn.data_ptr() + 8 * 8 * g * N
-            tk['t0'] = t0
-            tk['dr_stride'] = (T + 1) * N
-            tk['len'] = n
-            tk['N'] = N
-            tk['lognh'] = self.lognh_g
-            tk['lanes'] = np.minimum(8, I - 8 * g)
-            tk['dmin'] = self.dmin
-            tk['dt'] = np.float32(self.dt)
-            tk['G'] = Gl.reshape(Gn, 8)
-            tk['consts'] = self.consts[:4]
+        tab['edges_t'] = self.edges_tg.data_ptr()
+        tab['row_t'] = self.row_t.data_ptr()
+        tab['nodes'] = self.nodes_t.data_ptr()
+        tab['seg'] = rec.gtrace.data_ptr() + 4 * g * self.C * N * 3 * 8
+        tab['dr'] = self.dr.data_ptr() + 4 * (8 * g * (T + 1) * N + t0s * N)
+        tab['lam'] = lam.data_ptr() + 4 * 8 * g * N * 2
+        tab['ring'] = ring.data_ptr() + 4 * g * N * R * 8
+        tab['deta'] = deta.data_ptr() + 8 * 8 * g * N
+        tab['dG'] = dGn.data_ptr() + 8 * 8 * g * N
+        tab['t0'] = t0s
+        tab['dr_stride'] = (T + 1) * N
+        tab['len'] = lens
+        tab['N'] = N
+        tab['lognh'] = self.lognh_g
+        tab['lanes'] = np.minimum(8, I - 8 * g)
+        tab['dmin'] = self.dmin
+        tab['dt'] = np.float32(self.dt)
+        tab['G'] = Gl.reshape(1, Gn, 8)
+        tab['consts'] = self.consts[:4]
         dev = torch.from_numpy(tab.view(np.uint8).reshape(-1).copy()).cuda()
         row_bytes = Gn * nat.ADJOINT_GROUP_DTYPE.itemsize
         status = DeviceStatus()
