@@ -221,10 +221,14 @@ class FCFit:
         torch = self.torch
         if self._fw_gs is None:
             self._fw_gs = self._groups(G, eta, self.T, 1, False)
-            self._rec_gs = self._groups(G, eta, self.C, 2, True)
+            # two recomputation sets: segment k - 1 is recomputed into one
+            # while the reverse kernel reads segment k from the other
+            self._rec_sets = [self._groups(G, eta, self.C, 2, True) for _ in range(2)]
+            self._rec_gs = self._rec_sets[0]
             self._x0_dev = torch.from_numpy(self.x0).cuda()
+            self._side = torch.cuda.Stream()
         else:
-            for gs in (self._fw_gs, self._rec_gs):
+            for gs in [self._fw_gs] + self._rec_sets:
                 gs.set_couplings(G)
                 gs.set_nparam(eta)
             fw = self._fw_gs
@@ -321,9 +325,7 @@ class FCFit:
         rev = list(reversed(self.ckpt))
         b = np.arange(I, dtype=np.int64)
         if grouped and self.adjoint_kernel == 'groups':
-            rec = self._rec_gs
-            plans = rec.prepare_segments([(t0, n) for (t0, n, _, _) in rev])
-            return self._reverse_groups(rec, plans, rev, lam, deta, dGn)
+            return self._reverse_groups(rev, lam, deta, dGn)
         if grouped:
             # recomputation on the same pipelined group kernel (bit-identical
             # to the forward) with r, V and the coupling sum S traced,
@@ -387,13 +389,27 @@ class FCFit:
         return dGn.sum(1), deta
 
 
-    def _reverse_groups(self, rec, plans, rev, lam, deta, dGn):
+    def _reverse_groups(self, rev, lam, deta, dGn):
         """Segments last first: recompute on the group kernel, then
         tvbg_adjoint_mpr_groups over the group trace in place (r, V, S
-        lane-interleaved [G][C][N][3][8]), an adjoint ring per group."""
+        lane-interleaved [G][C][N][3][8]), an adjoint ring per group.  The
+        recomputation of segment k + 1 (in the list's order) runs on a side
+        stream, into the other of two recomputation sets, while the reverse
+        kernel works on segment k; events order each recomputation after the
+        reverse kernel that last read its set, and each reverse kernel after
+        its recomputation."""
         from .engine import DeviceStatus
         torch = self.torch
         lib = nat.load()
+        recs = self._rec_sets
+        S = len(rev)
+        segs = [(t0, n) for (t0, n, _, _) in rev]
+        plans = [None] * S
+        for j in range(2):
+            ks = list(range(j, S, 2))
+            if ks:
+                for k, pl in zip(ks, recs[j].prepare_segments([segs[k] for k in ks])):
+                    plans[k] = pl
         I, N, T, K = self.I, self.N, self.T, self.adj_k
         Gn = (I + 7) // 8
         R = (1 << self.lognh_g) + K
@@ -412,7 +428,8 @@ class FCFit:
         tab['edges_t'] = self.edges_tg.data_ptr()
         tab['row_t'] = self.row_t.data_ptr()
         tab['nodes'] = self.nodes_t.data_ptr()
-        tab['seg'] = rec.gtrace.data_ptr() + 4 * g * self.C * N * 3 * 8
+        seg0 = np.array([recs[k % 2].gtrace.data_ptr() for k in range(S)], np.int64)[:, None]
+        tab['seg'] = seg0 + 4 * g * self.C * N * 3 * 8
         tab['dr'] = self.dr.data_ptr() + 4 * (8 * g * (T + 1) * N + t0s * N)
         tab['lam'] = lam.data_ptr() + 4 * 8 * g * N * 2
         tab['ring'] = ring.data_ptr() + 4 * g * N * R * 8
@@ -431,15 +448,29 @@ class FCFit:
         dev = torch.from_numpy(tab.view(np.uint8).reshape(-1).copy()).cuda()
         row_bytes = Gn * nat.ADJOINT_GROUP_DTYPE.itemsize
         status = DeviceStatus()
+        main, side = torch.cuda.current_stream(), self._side
+        side.wait_stream(main)
+        done = []
         for k, ((t0, n, st, rg), pl) in enumerate(zip(rev, plans)):
-            rec.gstate.copy_(st)
-            rec.ring.copy_(rg)
-            rec.launch(pl)
+            rec = recs[k % 2]
+            if k >= 2:
+                side.wait_event(done[k - 2])
+            with torch.cuda.stream(side):
+                rec.gstate.copy_(st)
+                rec.ring.copy_(rg)
+            rec.launch(pl, stream=side)
+            ready = torch.cuda.Event()
+            ready.record(side)
+            main.wait_event(ready)
             nat.check(lib.tvbg_adjoint_mpr_groups(dev.data_ptr() + k * row_bytes, Gn, threads,
                                                   cluster, K, status.t.data_ptr(),
-                                                  nat.stream_handle()))
+                                                  main.cuda_stream))
+            done.append(torch.cuda.Event())
+            done[-1].record(main)
+        main.wait_stream(side)
         torch.cuda.synchronize()
-        rec.status.check()
+        for rec in recs:
+            rec.status.check()
         status.check()
         return dGn.sum(1), deta
 
