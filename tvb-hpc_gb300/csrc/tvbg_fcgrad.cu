@@ -134,75 +134,123 @@ __global__ void __launch_bounds__(256) fcfit_mean_kernel(SeriesView v, double* m
     }
 }
 
-// Centred Gram G_ij = sum_t c_ti c_tj, c = x - mean, FP64 (one DFMA per
-// product, samples in order), exact upper triangle for N <= kTriMaxN: the
-// triangle of 2 x 2 pair blocks (ceil(N/2) (ceil(N/2) + 1) / 2 of them,
-// row-major) is cut into parts of blockDim blocks, one block per thread;
-// CTA = (instance blockIdx.x, part blockIdx.y), instances fastest so that
-// the lanes of a lane-interleaved group read the same sectors together.
-// kTriL samples of every node staged per pass, centred in FP64.  Both
-// triangles of G written.  GB300 runs about 2 DFMA per SM per clock, so the
-// products are the cost: 3612 products per sample at N = 84, against 6144
-// in 32 x 32 tiles.
+// Centred Gram G_ij = sum_t c_ti c_tj, c = x - mean, for N <= kTriMaxN:
+// exact upper triangle of 2 x 2 pair blocks (ceil(N/2) (ceil(N/2) + 1) / 2 of
+// them, row-major), kSplitBPT blocks per thread, CTA = (instance
+// blockIdx.x, part blockIdx.y), instances fastest so that the lanes of a
+// lane-interleaved group read the same sectors together.  kTriL samples of
+// every node are staged per pass, centred in FP64 and split into
+// hi = fl32(c) and lo = fl32(c - hi) (c = hi + lo to 2^-48).
+//
+// The products run in FP32 with error-free transformations (TwoProduct by
+// FMA and TwoSum, as in Ogita, Rump and Oishi, "Accurate sum and dot
+// product", SIAM J. Sci. Comput. 26(6), 2005): per pair and sample,
+// hi_i hi_j = p + e exactly; p is summed by TwoSum (its rounding errors
+// collected in a second FP32 word); e + hi_i lo_j + lo_i hi_j (2^-24 of the
+// product) is summed in FP32; every kTriL samples the three words are added
+// into the pair's FP64 sum.  lo_i lo_j (2^-48) is dropped.  The error of a
+// pass is bounded by about kTriL^2 2^-48 sum_t |c_ti c_tj| (the collected
+// rounding errors summed in FP32), below 4e-12 of ||c_i|| ||c_j||; typical
+// errors are near 1e-14.  FP64 work: the staging split and three additions
+// per pair every kTriL samples, against one DFMA per pair and sample (GB300
+// runs FP32 at about 64 times its FP64 rate).  Both triangles of G written.
 constexpr int kTriL = 32;
-constexpr int kTriMaxN = 192;   // staging kTriL x N doubles <= 48 KB
-__global__ void __launch_bounds__(256) fcfit_gram_tri_kernel(SeriesView v,
-                                                             const double* __restrict__ mean,
-                                                             double* G) {
-    extern __shared__ double sc[];  // [kTriL][Np]
+constexpr int kTriMaxN = 192;   // staging kTriL x N float2 <= 48 KB
+constexpr int kSplitBPT = 2;
+__global__ void __launch_bounds__(256) fcfit_gram_split_kernel(SeriesView v,
+                                                               const double* __restrict__ mean,
+                                                               double* G) {
+    extern __shared__ float2 sh[];  // [kTriL][Np]: (hi, lo)
     const int b = blockIdx.x;
     const int N = v.N;
     const int nb = (N + 1) / 2;
     const int Np = 2 * nb;
     const long long nblk = static_cast<long long>(nb) * (nb + 1) / 2;
-    const long long k = static_cast<long long>(blockIdx.y) * blockDim.x + threadIdx.x;
-    const bool active = k < nblk;
-    int bi = 0, bj = 0;
-    if (active) {
-        long long rem = k;
-        while (rem >= nb - bi) {
-            rem -= nb - bi;
-            ++bi;
+    int i0[kSplitBPT], j0[kSplitBPT];
+    bool act[kSplitBPT];
+#pragma unroll
+    for (int q = 0; q < kSplitBPT; ++q) {
+        const long long k =
+            (static_cast<long long>(blockIdx.y) * kSplitBPT + q) * blockDim.x + threadIdx.x;
+        act[q] = k < nblk;
+        int bi = 0, bj = 0;
+        if (act[q]) {
+            long long rem = k;
+            while (rem >= nb - bi) {
+                rem -= nb - bi;
+                ++bi;
+            }
+            bj = bi + static_cast<int>(rem);
         }
-        bj = bi + static_cast<int>(rem);
+        i0[q] = 2 * bi;
+        j0[q] = 2 * bj;
     }
-    const int i0 = 2 * bi, j0 = 2 * bj;
     const double* mb = mean + static_cast<int64_t>(b) * N;
-    double a00 = 0.0, a01 = 0.0, a10 = 0.0, a11 = 0.0;
+    double acc[kSplitBPT][4];
+#pragma unroll
+    for (int q = 0; q < kSplitBPT; ++q)
+#pragma unroll
+        for (int m = 0; m < 4; ++m) acc[q][m] = 0.0;
     for (int t0 = 0; t0 < v.T; t0 += kTriL) {
         for (int e = threadIdx.x; e < kTriL * Np; e += blockDim.x) {
             const int r = e / Np, c = e % Np;
             const int t = t0 + r;
-            sc[e] = (t < v.T && c < N) ? static_cast<double>(v.at(b, t, c)) - mb[c] : 0.0;
+            float2 hl = make_float2(0.0f, 0.0f);
+            if (t < v.T && c < N) {
+                const double cd = static_cast<double>(v.at(b, t, c)) - mb[c];
+                hl.x = __double2float_rn(cd);
+                hl.y = __double2float_rn(cd - static_cast<double>(hl.x));
+            }
+            sh[e] = hl;
         }
         __syncthreads();
-        if (active) {
-#pragma unroll 8
+#pragma unroll
+        for (int q = 0; q < kSplitBPT; ++q) {
+            if (!act[q]) continue;
+            float s[4] = {0.0f, 0.0f, 0.0f, 0.0f}, cp[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+            float sm[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll 4
             for (int r = 0; r < kTriL; ++r) {
-                const double* row = sc + r * Np;
-                const double x0 = row[i0], x1 = row[i0 + 1];
-                const double y0 = row[j0], y1 = row[j0 + 1];
-                a00 = fma(x0, y0, a00);
-                a01 = fma(x0, y1, a01);
-                a10 = fma(x1, y0, a10);
-                a11 = fma(x1, y1, a11);
+                const float2* row = sh + r * Np;
+                const float2 x[2] = {row[i0[q]], row[i0[q] + 1]};
+                const float2 y[2] = {row[j0[q]], row[j0[q] + 1]};
+#pragma unroll
+                for (int u = 0; u < 2; ++u)
+#pragma unroll
+                    for (int w = 0; w < 2; ++w) {
+                        const int m = 2 * u + w;
+                        const float p = __fmul_rn(x[u].x, y[w].x);
+                        const float e = __fmaf_rn(x[u].x, y[w].x, -p);  // hi hi - p, exact
+                        sm[m] = __fadd_rn(sm[m], __fmaf_rn(x[u].x, y[w].y, __fmaf_rn(x[u].y, y[w].x, e)));
+                        const float t = __fadd_rn(s[m], p);               // TwoSum(s, p)
+                        const float bp = __fsub_rn(t, s[m]);
+                        const float err = __fadd_rn(__fsub_rn(s[m], __fsub_rn(t, bp)), __fsub_rn(p, bp));
+                        s[m] = t;
+                        cp[m] = __fadd_rn(cp[m], err);
+                    }
             }
+#pragma unroll
+            for (int m = 0; m < 4; ++m)
+                acc[q][m] += static_cast<double>(s[m]) +
+                             (static_cast<double>(cp[m]) + static_cast<double>(sm[m]));
         }
         __syncthreads();
     }
-    if (!active) return;
     double* gb = G + static_cast<int64_t>(b) * N * N;
-    const double acc[2][2] = {{a00, a01}, {a10, a11}};
 #pragma unroll
-    for (int u = 0; u < 2; ++u)
+    for (int q = 0; q < kSplitBPT; ++q) {
+        if (!act[q]) continue;
 #pragma unroll
-        for (int w = 0; w < 2; ++w) {
-            const int i = i0 + u, j = j0 + w;
-            if (i < N && j < N && j >= i) {
-                gb[static_cast<int64_t>(i) * N + j] = acc[u][w];
-                gb[static_cast<int64_t>(j) * N + i] = acc[u][w];
+        for (int u = 0; u < 2; ++u)
+#pragma unroll
+            for (int w = 0; w < 2; ++w) {
+                const int i = i0[q] + u, j = j0[q] + w;
+                if (i < N && j < N && j >= i) {
+                    gb[static_cast<int64_t>(i) * N + j] = acc[q][2 * u + w];
+                    gb[static_cast<int64_t>(j) * N + i] = acc[q][2 * u + w];
+                }
             }
-        }
+    }
 }
 
 constexpr int kGT = 32;   // Gram tile: 32 x 32 node pairs, 32 samples per stage
@@ -478,9 +526,9 @@ extern "C" int tvbg_fcfit_loss(const float* d_x, int64_t x_inst_stride, const fl
     if (N <= kTriMaxN) {
         const int nb = (N + 1) / 2;
         const long long nblk = static_cast<long long>(nb) * (nb + 1) / 2;
-        const unsigned parts = static_cast<unsigned>((nblk + 255) / 256);
+        const unsigned parts = static_cast<unsigned>((nblk + 256 * kSplitBPT - 1) / (256 * kSplitBPT));
         const size_t smem = 8u * kTriL * 2u * static_cast<size_t>(nb);
-        fcfit_gram_tri_kernel<<<dim3(n_inst, parts), 256, smem, st>>>(v, mean, fc);
+        fcfit_gram_split_kernel<<<dim3(n_inst, parts), 256, smem, st>>>(v, mean, fc);
     } else {
         fcfit_gram_kernel<<<dim3(n_inst, nt * (nt + 1) / 2), 256, 0, st>>>(v, mean, fc);
     }
