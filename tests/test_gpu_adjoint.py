@@ -180,12 +180,14 @@ def fc_loss_torch(X, target):
     return loss.detach(), FC.detach(), X.grad
 
 
-@pytest.mark.parametrize('I,T,N', [(3, 130, 84), (2, 700, 150), (4, 64, 17), (2, 150, 260)])
+@pytest.mark.parametrize('I,T,N', [(3, 130, 84), (2, 700, 150), (4, 64, 17), (2, 90, 192),
+                                   (2, 150, 260)])
 def test_fcfit_loss_kernel(cuda, I, T, N):
     """tvbg_fcfit_loss (FP64 FC and loss, FP32 dL/dX, the series' last row
     from a separate array) against torch FP64 autograd of the same loss.
-    N = 17, 84, 150: the exact-triangle Gram (N <= 192); 260: the tiled
-    Gram; dL/dX on whole rows for N <= 128, tiles above."""
+    N = 17, 84, 150, 192: the FP32 exact-triangle Gram (N <= 192, 192 with
+    the shared-memory opt-in); 260: the FP64 tiles; dL/dX on whole rows for
+    N <= 128, tiles above."""
     import ctypes
     from tvb_hpc import _native as nat
     torch = cuda

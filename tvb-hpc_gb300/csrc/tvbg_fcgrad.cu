@@ -134,37 +134,52 @@ __global__ void __launch_bounds__(256) fcfit_mean_kernel(SeriesView v, double* m
     }
 }
 
-// Centred Gram G_ij = sum_t c_ti c_tj, c = x - mean, for N <= kTriMaxN:
-// exact upper triangle of 2 x 2 pair blocks (ceil(N/2) (ceil(N/2) + 1) / 2 of
-// them, row-major), kSplitBPT blocks per thread, CTA = (instance
-// blockIdx.x, part blockIdx.y), instances fastest so that the lanes of a
-// lane-interleaved group read the same sectors together.  kTriL samples of
-// every node are staged per pass, centred in FP64 and split into
-// hi = fl32(c) and lo = fl32(c - hi) (c = hi + lo to 2^-48).
+// Error-free transformations in FP32 (Knuth's TwoSum and TwoProduct by FMA,
+// as used in Ogita, Rump and Oishi, "Accurate sum and dot
+// product", SIAM J. Sci. Comput. 26(6), 2005).  Every operation is an
+// explicitly rounded intrinsic: nothing is contracted or reordered.
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// Centred Gram G_ij = sum_t c_ti c_tj, c = x - mean, for N <= kTriMaxN,
+// all in FP32 arithmetic with error-free transformations (GB300 runs FP32
+// at about 64 times its FP64 rate; one DFMA per product took 4.2 ms per
+// adjoint pass at N = 84, 256 instances, 2000 samples).
 //
-// The products run in FP32 with error-free transformations (TwoProduct by
-// FMA and TwoSum, as in Ogita, Rump and Oishi, "Accurate sum and dot
-// product", SIAM J. Sci. Comput. 26(6), 2005): per pair and sample,
-// hi_i hi_j = p + e exactly; p is summed by TwoSum (its rounding errors
-// collected in a second FP32 word); e + hi_i lo_j + lo_i hi_j (2^-24 of the
-// product) is summed in FP32; every kTriL samples the three words are added
-// into the pair's FP64 sum.  lo_i lo_j (2^-48) is dropped.  The error of a
-// pass is bounded by about kTriL^2 2^-48 sum_t |c_ti c_tj| (the collected
-// rounding errors summed in FP32), below 4e-12 of ||c_i|| ||c_j||; typical
-// errors are near 1e-14.  FP64 work: the staging split and three additions
-// per pair every kTriL samples, against one DFMA per pair and sample (GB300
-// runs FP32 at about 64 times its FP64 rate).  Both triangles of G written.
+// Work split: the exact upper triangle of 2 x 2 pair blocks (ceil(N/2)
+// (ceil(N/2) + 1) / 2 of them, row-major), kSplitBPT blocks per thread,
+// CTA = (instance blockIdx.x, part blockIdx.y), instances fastest so that
+// the lanes of a lane-interleaved group read the same sectors together.
+//
+// Centring: each mean (FP64) is split once into mh + ml (FP32 words); a
+// sample x becomes c = (x - mh) - ml as (hi, lo) with hi + lo = c up to
+// about 2^-48 (|c| + 2 |mean|): TwoSum(x, -mh) = (d, de), then
+// TwoSum(d, de - ml).  kTriL samples of every node staged per pass.
+//
+// Products: per pair and sample hi_i hi_j = p + e exactly (TwoProduct);
+// p is summed by TwoSum (rounding errors collected in a second word),
+// e + hi_i lo_j + lo_i hi_j (2^-24 of the product) in a third word; lo_i lo_j
+// (2^-48) is dropped.  Every kTriL samples the three words are added into
+// the pair's double-FP32 sum (TwoSum, then the small words, then TwoSum
+// again), converted to FP64 at the end.  The error is bounded by about kTriL^2 2^-48 sum_t |c_ti c_tj| (the
+// collected rounding errors of a pass summed in FP32), below 4e-12 of
+// ||c_i|| ||c_j||; typical errors are near 1e-14.  Both triangles of G
+// written.
 constexpr int kTriL = 32;
-constexpr int kTriMaxN = 192;   // staging kTriL x N float2 <= 48 KB
+constexpr int kTriMaxN = 192;   // staging (kTriL + 1) x N float2 <= 50.7 KB
 constexpr int kSplitBPT = 2;
 __global__ void __launch_bounds__(256) fcfit_gram_split_kernel(SeriesView v,
                                                                const double* __restrict__ mean,
                                                                double* G) {
-    extern __shared__ float2 sh[];  // [kTriL][Np]: (hi, lo)
+    extern __shared__ float2 sh[];  // [kTriL][Np] (hi, lo); then [Np] (mh, ml)
     const int b = blockIdx.x;
     const int N = v.N;
     const int nb = (N + 1) / 2;
     const int Np = 2 * nb;
+    float2* smean = sh + kTriL * Np;
     const long long nblk = static_cast<long long>(nb) * (nb + 1) / 2;
     int i0[kSplitBPT], j0[kSplitBPT];
     bool act[kSplitBPT];
@@ -186,20 +201,27 @@ __global__ void __launch_bounds__(256) fcfit_gram_split_kernel(SeriesView v,
         j0[q] = 2 * bj;
     }
     const double* mb = mean + static_cast<int64_t>(b) * N;
-    double acc[kSplitBPT][4];
+    for (int c = threadIdx.x; c < N; c += blockDim.x) {
+        const double m = mb[c];
+        const float mh = __double2float_rn(m);
+        smean[c] = make_float2(mh, __double2float_rn(m - static_cast<double>(mh)));
+    }
+    float ah[kSplitBPT][4], al[kSplitBPT][4];  // double-FP32 sums
 #pragma unroll
     for (int q = 0; q < kSplitBPT; ++q)
 #pragma unroll
-        for (int m = 0; m < 4; ++m) acc[q][m] = 0.0;
+        for (int m = 0; m < 4; ++m) ah[q][m] = al[q][m] = 0.0f;
+    __syncthreads();
     for (int t0 = 0; t0 < v.T; t0 += kTriL) {
         for (int e = threadIdx.x; e < kTriL * Np; e += blockDim.x) {
             const int r = e / Np, c = e % Np;
             const int t = t0 + r;
             float2 hl = make_float2(0.0f, 0.0f);
             if (t < v.T && c < N) {
-                const double cd = static_cast<double>(v.at(b, t, c)) - mb[c];
-                hl.x = __double2float_rn(cd);
-                hl.y = __double2float_rn(cd - static_cast<double>(hl.x));
+                const float2 m = smean[c];
+                float d, de;
+                two_sum(v.at(b, t, c), -m.x, d, de);
+                two_sum(d, __fsub_rn(de, m.y), hl.x, hl.y);
             }
             sh[e] = hl;
         }
@@ -222,17 +244,19 @@ __global__ void __launch_bounds__(256) fcfit_gram_split_kernel(SeriesView v,
                         const float p = __fmul_rn(x[u].x, y[w].x);
                         const float e = __fmaf_rn(x[u].x, y[w].x, -p);  // hi hi - p, exact
                         sm[m] = __fadd_rn(sm[m], __fmaf_rn(x[u].x, y[w].y, __fmaf_rn(x[u].y, y[w].x, e)));
-                        const float t = __fadd_rn(s[m], p);               // TwoSum(s, p)
-                        const float bp = __fsub_rn(t, s[m]);
-                        const float err = __fadd_rn(__fsub_rn(s[m], __fsub_rn(t, bp)), __fsub_rn(p, bp));
+                        float t, err;
+                        two_sum(s[m], p, t, err);
                         s[m] = t;
                         cp[m] = __fadd_rn(cp[m], err);
                     }
             }
 #pragma unroll
-            for (int m = 0; m < 4; ++m)
-                acc[q][m] += static_cast<double>(s[m]) +
-                             (static_cast<double>(cp[m]) + static_cast<double>(sm[m]));
+            for (int m = 0; m < 4; ++m) {  // (ah, al) += s + (cp + sm)
+                float hi, lo;
+                two_sum(ah[q][m], s[m], hi, lo);
+                lo = __fadd_rn(lo, __fadd_rn(al[q][m], __fadd_rn(cp[m], sm[m])));
+                two_sum(hi, lo, ah[q][m], al[q][m]);
+            }
         }
         __syncthreads();
     }
@@ -246,8 +270,10 @@ __global__ void __launch_bounds__(256) fcfit_gram_split_kernel(SeriesView v,
             for (int w = 0; w < 2; ++w) {
                 const int i = i0[q] + u, j = j0[q] + w;
                 if (i < N && j < N && j >= i) {
-                    gb[static_cast<int64_t>(i) * N + j] = acc[q][2 * u + w];
-                    gb[static_cast<int64_t>(j) * N + i] = acc[q][2 * u + w];
+                    const double g = static_cast<double>(ah[q][2 * u + w]) +
+                                     static_cast<double>(al[q][2 * u + w]);
+                    gb[static_cast<int64_t>(i) * N + j] = g;
+                    gb[static_cast<int64_t>(j) * N + i] = g;
                 }
             }
     }
@@ -527,7 +553,13 @@ extern "C" int tvbg_fcfit_loss(const float* d_x, int64_t x_inst_stride, const fl
         const int nb = (N + 1) / 2;
         const long long nblk = static_cast<long long>(nb) * (nb + 1) / 2;
         const unsigned parts = static_cast<unsigned>((nblk + 256 * kSplitBPT - 1) / (256 * kSplitBPT));
-        const size_t smem = 8u * kTriL * 2u * static_cast<size_t>(nb);
+        const size_t smem = 8u * (kTriL + 1) * 2u * static_cast<size_t>(nb);
+        if (smem > 48u * 1024u) {
+            const cudaError_t e = cudaFuncSetAttribute(reinterpret_cast<const void*>(fcfit_gram_split_kernel),
+                                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                       static_cast<int>(smem));
+            if (e != cudaSuccess) return tvbg::set_cuda_error(e, "tvbg_fcfit_loss: smem attribute");
+        }
         fcfit_gram_split_kernel<<<dim3(n_inst, parts), 256, smem, st>>>(v, mean, fc);
     } else {
         fcfit_gram_kernel<<<dim3(n_inst, nt * (nt + 1) / 2), 256, 0, st>>>(v, mean, fc);
