@@ -809,9 +809,10 @@ class AdjointStep:
                      'per segment: recomputation + reverse-time kernel (%s); FP64 gradients'
                      % ('pipelined group kernel' if self.prob.layout == 'groups'
                         else 'per-step kernel', wl['ckpt'],
-                        'lane-interleaved groups, time-blocked, %d threads x %d CTAs'
-                        % self.prob.adjoint_shape if self.prob.adjoint_kernel == 'groups'
-                        else 'per instance'))
+                        'lane-interleaved groups, time-blocked%s, %d threads x %d CTAs'
+                        % ((', two thread teams' if self.prob.adjoint_shape[2] else '',)
+                           + tuple(self.prob.adjoint_shape[:2]))
+                        if self.prob.adjoint_kernel == 'groups' else 'per instance'))
         self.x0 = None
 
     def reset(self, x0=None):

@@ -333,6 +333,10 @@ typedef struct tvbg_adjoint_group {
     int32_t len, N, lognh;
     int32_t lanes;            /* live lanes (1..8); others compute, write nothing */
     int32_t dmin;             /* smallest delay (>= block_k, checked)         */
+    int32_t flush_every;      /* > 0: deta and dG partial sums added after each */
+                              /* step t with t % flush_every == 0 (the grouping */
+                              /* of one launch per segment of that length); 0: */
+                              /* once, at the end of the launch                */
     float dt;
     float G[8];               /* coupling of each lane                        */
     float consts[4];          /* MPR: Delta, J, tau, I                        */
@@ -341,11 +345,14 @@ typedef struct tvbg_adjoint_group {
 size_t tvbg_adjoint_group_size(void);
 /* n_groups records; threads = 8 x node slots per CTA (a multiple of 32, <= 512),
  * cluster CTAs per group (1..16, N <= cluster x threads / 8), block_k 4 or
- * 8.  A record that does not match the launch sets *d_status (optional) to
- * TVBG_EINVAL and its group does nothing. */
+ * 8.  pipelined = 1: two thread teams per CTA (threads = 2 x 8 x node slots,
+ * a multiple of 64; N <= cluster x threads / 16), the out-edge sums of block
+ * b + 1 gathered while block b's steps run; needs every delay >= 2 block_k;
+ * the same results.  A record that does not match the launch sets *d_status
+ * (optional) to TVBG_EINVAL and its group does nothing. */
 int tvbg_adjoint_mpr_groups(const tvbg_adjoint_group *d_adj, int32_t n_groups,
                             int32_t threads, int32_t cluster, int32_t block_k,
-                            int32_t *d_status, void *stream);
+                            int32_t pipelined, int32_t *d_status, void *stream);
 
 /*
  * Pearson FC per instance over T samples of N nodes, FP64 reduction.

@@ -48,7 +48,7 @@ def test_struct_layouts_match():
     assert lib.tvbg_group_size() == ctypes.sizeof(nat.tvbg_group) == nat.GROUP_DTYPE.itemsize
     assert ctypes.sizeof(nat.tvbg_lane) == 16 and nat.GROUP_LANES == 8
     assert (lib.tvbg_adjoint_group_size() == ctypes.sizeof(nat.tvbg_adjoint_group)
-            == nat.ADJOINT_GROUP_DTYPE.itemsize == 160)
+            == nat.ADJOINT_GROUP_DTYPE.itemsize == 168)
 
 
 def test_adjoint_group_edges_and_shapes():
@@ -73,9 +73,13 @@ def test_adjoint_group_edges_and_shapes():
     src = np.repeat(np.arange(50), np.diff(row_tg))
     assert sorted(zip(src.tolist(), i.tolist(), dd.tolist())) == pairs
     for N in (1, 17, 84, 400, 998, 1024):
-        th, c = adjoint.adjoint_group_shape(N)
-        assert th % 32 == 0 and th <= 512 and 1 <= c <= 16 and c * th // 8 >= N
+        th, c, pipe = adjoint.adjoint_group_shape(N)
+        assert th % 32 == 0 and th <= 512 and 1 <= c <= 16 and c * th // 8 >= N and pipe == 0
+    for N in (1, 17, 84, 400, 512):
+        th, c, pipe = adjoint.adjoint_group_shape(N, pipelined=True)
+        assert th % 64 == 0 and th <= 512 and 1 <= c <= 16 and c * th // 16 >= N and pipe == 1
     assert adjoint.adjoint_group_shape(1025) is None
+    assert adjoint.adjoint_group_shape(513, pipelined=True) is None
 
 
 @pytest.mark.parametrize('rounding', ['trunc', 'ceil', 'dsl'])

@@ -69,18 +69,21 @@ def test_adjoint_matches_fp64_oracle(cuda, layout, kernel):
     assert rel_err(deta[0, :4], np.array(fd_eta)) < 1e-3
 
 
-@pytest.mark.parametrize('I,N,K', [(11, 40, 8), (16, 84, 4), (9, 130, 8)])
-def test_adjoint_group_kernel_equals_per_instance(cuda, I, N, K):
+@pytest.mark.parametrize('I,N,K,pipe', [(11, 40, 8, False), (16, 84, 4, False), (9, 130, 8, False),
+                                        (11, 40, 8, True), (16, 84, 4, True), (9, 130, 8, True)])
+def test_adjoint_group_kernel_equals_per_instance(cuda, I, N, K, pipe):
     """tvbg_adjoint_mpr_groups (lane-interleaved, time-blocked, clusters
-    where N needs them) against tvbg_adjoint_mpr on the same recomputed
-    traces: the same per-step code and the same out-edge order, so equal
-    results (checkpoints every 30 steps: partial blocks at every segment
-    edge)."""
+    where N needs them; one team or the two pipelined teams) against
+    tvbg_adjoint_mpr on the same recomputed traces: the same per-step code
+    and the same out-edge order, so equal results (checkpoints every 30
+    steps: partial blocks at every segment edge)."""
+    from tvb_hpc import adjoint
     torch = cuda
     prob, conn, x0, eta, G, target = problem(N=N, I=I, T=180, C=30, seed=N)
-    assert prob.adjoint_kernel == 'groups' and prob.dmin >= K
+    assert prob.adjoint_kernel == 'groups' and prob.dmin >= 2 * K
     prob.adj_k = K
     prob.lognh_g = max(1, int(np.ceil(np.log2(prob.dmax + K))))
+    prob.adjoint_shape = adjoint.adjoint_group_shape(N, pipelined=pipe)
     prob.forward(G, eta)
     dG_g, deta_g = (t.clone() for t in prob.backward())
     prob.adjoint_kernel = 'instances'
@@ -108,12 +111,22 @@ def test_adjoint_group_kernel_refuses_short_delays(cuda):
     t['len'], t['N'], t['lognh'], t['lanes'], t['dmin'] = 8, 4, 4, 8, 3
     dev = torch.from_numpy(tab.view(np.uint8).copy()).cuda()
     status = torch.zeros(1, dtype=torch.int32, device='cuda')
-    nat.check(lib.tvbg_adjoint_mpr_groups(dev.data_ptr(), 1, 32, 1, 8, status.data_ptr(), None))
+    nat.check(lib.tvbg_adjoint_mpr_groups(dev.data_ptr(), 1, 32, 1, 8, 0, status.data_ptr(), None))
+    torch.cuda.synchronize()
+    assert int(status.item()) == nat.TVBG_EINVAL
+    assert float(lam.min()) == 1.0 and float(lam.max()) == 1.0
+    # the pipelined teams need every delay >= 2 K: dmin = 10 < 16 is refused
+    status.zero_()
+    t['dmin'] = 10
+    dev = torch.from_numpy(tab.view(np.uint8).copy()).cuda()
+    nat.check(lib.tvbg_adjoint_mpr_groups(dev.data_ptr(), 1, 64, 1, 8, 1, status.data_ptr(), None))
     torch.cuda.synchronize()
     assert int(status.item()) == nat.TVBG_EINVAL
     assert float(lam.min()) == 1.0 and float(lam.max()) == 1.0
     with pytest.raises(nat.TvbgError):
-        nat.check(lib.tvbg_adjoint_mpr_groups(dev.data_ptr(), 1, 1024, 1, 8, None, None))
+        nat.check(lib.tvbg_adjoint_mpr_groups(dev.data_ptr(), 1, 1024, 1, 8, 0, None, None))
+    with pytest.raises(nat.TvbgError):   # pipelined CTAs: a multiple of 64 threads
+        nat.check(lib.tvbg_adjoint_mpr_groups(dev.data_ptr(), 1, 96, 1, 8, 1, None, None))
 
 
 def test_fcfit_reuse_matches_fresh(cuda):
@@ -133,6 +146,28 @@ def test_fcfit_reuse_matches_fresh(cuda):
     g2 = fresh.backward()
     assert torch.equal(l1, l2)
     assert all(torch.equal(a, b) for a, b in zip(g1, g2))
+
+
+def test_adjoint_recompute_windows(cuda):
+    """The recomputation in windows of 1, 2 and 4 segments (several
+    windows: two buffers, the next window recomputed while the reverse
+    kernel reads the current one), with and without the eager start in
+    forward, and a second backward after one forward: the same bits as one
+    window of all segments."""
+    torch = cuda
+    prob, conn, x0, eta, G, target = problem(N=40, I=11, T=250, C=30)
+    prob.forward(G, eta)
+    ref = [t.clone() for t in prob.backward()]
+    again = prob.backward()            # no eager window: from the checkpoints
+    assert all(torch.equal(a, b) for a, b in zip(ref, again))
+    for W, eager in ((1, True), (2, False), (4, True)):
+        p2, *_ = problem(N=40, I=11, T=250, C=30)
+        p2.recompute_window = W
+        p2.eager_recompute = eager
+        p2.forward(G, eta)
+        assert len(p2._windows()[1]) == -(-9 // W)
+        got = p2.backward()
+        assert all(torch.equal(a, b) for a, b in zip(ref, got)), W
 
 
 def test_adjoint_autograd_function(cuda):

@@ -217,12 +217,21 @@ __device__ __forceinline__ void adj_gather(const float* __restrict__ ring_g,
 // updates from registers, each writing mu_V(t + 1) to slot t + 1, then one
 // barrier.  A slot written in a block aliases slot + nh, which no read of
 // the block reaches (nh >= d_max + K).
-template <int K>
+//
+// PIPE: two thread teams of blockDim / 2 on the same (node slot, lane)
+// pairs; the update team runs block b from one coupling-sum buffer while
+// the gather team sums block b + 1 into the other, and the cluster meets at
+// one barrier per block.  Block b + 1 reads slots >= tb - 2K + 2 + d_min,
+// all written before block b started when d_min >= 2K; the slots block b
+// writes ([tb - K + 2, tb + 1]) alias none of them (nh > d_max - 1).  Each
+// team runs its own loop; both meet at the same number of barriers.  Same
+// per-step code and gather order: the same results.
+template <int K, bool PIPE>
 __global__ void __launch_bounds__(512, 1)
     adjoint_group_kernel(const tvbg_adjoint_group* __restrict__ adj, int32_t n_groups,
                          int32_t* __restrict__ status) {
     __shared__ __align__(16) tvbg_adjoint_group s;
-    extern __shared__ float csum[];  // [K][blockDim]: the block's out-edge sums
+    extern __shared__ float csum[];  // [(PIPE ? 2 : 1)][K][team threads]: out-edge sums
     const int cid = static_cast<int>(cluster_id_x());
     if (cid >= n_groups) return;  // uniform over the cluster
     {
@@ -237,14 +246,17 @@ __global__ void __launch_bounds__(512, 1)
     const uint32_t rank = cluster_rank();
     const bool cluster = C > 1;
     const int N = s.N;
-    const int P = static_cast<int>(blockDim.x) / kLanes;
+    const int H = PIPE ? static_cast<int>(blockDim.x) / 2 : static_cast<int>(blockDim.x);
+    const int P = H / kLanes;
     if (N < 1 || N > 65535 || static_cast<int>(C) * P < N || s.lognh < 1 || s.lognh > 16 ||
-        (1 << s.lognh) < K || s.dmin < K || s.len < 0 || s.lanes < 1 || s.lanes > kLanes ||
-        !s.ring || !s.seg || !s.edges_t || !s.row_t || (reinterpret_cast<uintptr_t>(s.ring) & 15u) != 0) {
+        (1 << s.lognh) < K || s.dmin < (PIPE ? 2 * K : K) || (H & 31) || s.len < 0 || s.lanes < 1 ||
+        s.lanes > kLanes || !s.ring || !s.seg || !s.edges_t || !s.row_t ||
+        (reinterpret_cast<uintptr_t>(s.ring) & 15u) != 0) {
         if (threadIdx.x == 0) report(status, TVBG_EINVAL);
         return;  // uniform over the cluster: same record, same launch shape
     }
-    const int tid = static_cast<int>(threadIdx.x);
+    const bool gather_team = PIPE && static_cast<int>(threadIdx.x) >= H;
+    const int tid = static_cast<int>(threadIdx.x) - (gather_team ? H : 0);
     const int l = tid % kLanes;
     const int q = (tid / kLanes) * static_cast<int>(C) + static_cast<int>(rank);
     const bool valid = q < N;
@@ -253,28 +265,57 @@ __global__ void __launch_bounds__(512, 1)
     const uint32_t nh = 1u << s.lognh;
     const uint32_t mask = nh - 1u;
     const uint32_t R = nh + K;
+    float* cs = csum + (tid - l);
+    const int bufsz = K * H;
+    const uint2* __restrict__ edges = reinterpret_cast<const uint2*>(s.edges_t);
+    const long long t0 = s.t0;
+    const long long top = t0 + s.len - 1;
+    int lo = 0, hi = 0;
+    if (!PIPE || gather_team) {
+        lo = valid ? __ldg(s.row_t + n) : 0;
+        hi = valid ? __ldg(s.row_t + n + 1) : 0;
+    }
+    if (gather_team) {
+        if (s.len > 0)
+            adj_gather<K>(s.ring, edges, lo, hi, static_cast<uint32_t>(top - K + 2) & mask, mask, R, l, cs,
+                          H);
+        group_barrier(cluster);
+        int buf = 1;
+        for (long long tb = top; tb >= t0; tb -= K) {
+            if (tb - K >= t0)
+                adj_gather<K>(s.ring, edges, lo, hi, static_cast<uint32_t>(tb - 2 * K + 2) & mask, mask, R,
+                              l, cs + buf * bufsz, H);
+            buf ^= 1;
+            group_barrier(cluster);
+        }
+        return;
+    }
     const AdjMpr m{s.consts[0], s.consts[1], s.consts[2], s.dt};
     const float cG = s.dt * s.G[l] / s.consts[2];
-    const int lo = valid ? __ldg(s.row_t + n) : 0;
-    const int hi = valid ? __ldg(s.row_t + n + 1) : 0;
     float lr = 0.0f, lv = 0.0f;
     if (live) {
         lr = s.lam[2LL * N * l + 2 * n];
         lv = s.lam[2LL * N * l + 2 * n + 1];
     }
     double deta = 0.0, dG = 0.0;
-    float* cs = csum + (tid - l);
-    const int stride = static_cast<int>(blockDim.x);
-    const uint2* __restrict__ edges = reinterpret_cast<const uint2*>(s.edges_t);
     float* __restrict__ ring_n = s.ring + static_cast<size_t>(n) * R * kLanes + l;
     const float* __restrict__ seg_n = s.seg + static_cast<size_t>(n) * 3 * kLanes + l;
     const float* __restrict__ dr_n = s.dr + s.dr_stride * l + n;
-    const long long t0 = s.t0;
-    for (long long tb = t0 + s.len - 1; tb >= t0; tb -= K) {
+    if (PIPE) group_barrier(cluster);  // block 0's sums
+    // partial sums of deta and dG go to memory after each step t with
+    // t % flush_every == 0 (the grouping of one launch per segment)
+    const long long fe = s.flush_every > 0 ? s.flush_every : 0;
+    long long next_flush = fe ? top - (top % fe) : t0 - 1;
+    bool pending = false;
+    int buf = 0;
+    for (long long tb = top; tb >= t0; tb -= K) {
         const int cnt = (tb - t0 + 1) < K ? static_cast<int>(tb - t0 + 1) : K;
-        adj_gather<K>(s.ring, edges, lo, hi, static_cast<uint32_t>(tb - K + 2) & mask, mask, R, l, cs,
-                      stride);
-        __syncwarp();
+        if (!PIPE) {
+            adj_gather<K>(s.ring, edges, lo, hi, static_cast<uint32_t>(tb - K + 2) & mask, mask, R, l, cs,
+                          H);
+            __syncwarp();
+        }
+        const float* csb = cs + buf * bufsz;
 #pragma unroll
         for (int i = 0; i < K; ++i) {
             if (i < cnt) {
@@ -289,16 +330,29 @@ __global__ void __launch_bounds__(512, 1)
                     ring_n[pos * kLanes] = mv;
                     if (pos < static_cast<uint32_t>(K)) ring_n[(pos + nh) * kLanes] = mv;
                 }
-                m.update(r, V, S, mr, mv, cs[(K - 1 - i) * stride + l], cG, drt, lr, lv, deta, dG);
+                m.update(r, V, S, mr, mv, csb[(K - 1 - i) * H + l], cG, drt, lr, lv, deta, dG);
+                pending = true;
+                if (tb - i == next_flush) {
+                    if (live) {
+                        s.deta[static_cast<long long>(N) * l + n] += deta;
+                        s.dG[static_cast<long long>(N) * l + n] += dG;
+                    }
+                    deta = dG = 0.0;
+                    pending = false;
+                    next_flush -= fe;
+                }
             }
         }
+        if (PIPE) buf ^= 1;
         group_barrier(cluster);
     }
     if (live) {
         s.lam[2LL * N * l + 2 * n] = lr;
         s.lam[2LL * N * l + 2 * n + 1] = lv;
-        s.deta[static_cast<long long>(N) * l + n] += deta;
-        s.dG[static_cast<long long>(N) * l + n] += dG;
+        if (pending) {
+            s.deta[static_cast<long long>(N) * l + n] += deta;
+            s.dG[static_cast<long long>(N) * l + n] += dG;
+        }
     }
 }
 
@@ -310,13 +364,15 @@ extern "C" size_t tvbg_adjoint_group_size(void) { return sizeof(tvbg_adjoint_gro
 
 extern "C" int tvbg_adjoint_mpr_groups(const tvbg_adjoint_group* d_adj, int32_t n_groups,
                                        int32_t threads, int32_t cluster, int32_t block_k,
-                                       int32_t* d_status, void* stream) {
+                                       int32_t pipelined, int32_t* d_status, void* stream) {
     if (n_groups < 0 || (n_groups > 0 && !d_adj) || threads < 32 || threads > 512 || (threads & 31) ||
-        cluster < 1 || cluster > 16 || (block_k != 4 && block_k != 8))
+        cluster < 1 || cluster > 16 || (block_k != 4 && block_k != 8) || pipelined < 0 ||
+        pipelined > 1 || (pipelined && (threads & 63)))
         return set_error(TVBG_EINVAL, "tvbg_adjoint_mpr_groups: bad arguments");
     if (n_groups == 0) return TVBG_OK;
     using Fn = void (*)(const tvbg_adjoint_group*, int32_t, int32_t*);
-    const Fn kfn = block_k == 8 ? adjoint_group_kernel<8> : adjoint_group_kernel<4>;
+    const Fn kfn = pipelined ? (block_k == 8 ? adjoint_group_kernel<8, true> : adjoint_group_kernel<4, true>)
+                             : (block_k == 8 ? adjoint_group_kernel<8, false> : adjoint_group_kernel<4, false>);
     const size_t smem = 4u * static_cast<size_t>(block_k) * static_cast<size_t>(threads);
     cudaError_t e = cudaSuccess;
     if (cluster > 8) {

@@ -218,8 +218,8 @@ class tvbg_adjoint_group(ctypes.Structure):
         ('ring', ctypes.c_void_p), ('deta', ctypes.c_void_p), ('dG', ctypes.c_void_p),
         ('t0', ctypes.c_int64), ('dr_stride', ctypes.c_int64),
         ('len', ctypes.c_int32), ('N', ctypes.c_int32), ('lognh', ctypes.c_int32),
-        ('lanes', ctypes.c_int32), ('dmin', ctypes.c_int32), ('dt', ctypes.c_float),
-        ('G', ctypes.c_float * 8), ('consts', ctypes.c_float * 4),
+        ('lanes', ctypes.c_int32), ('dmin', ctypes.c_int32), ('flush_every', ctypes.c_int32),
+        ('dt', ctypes.c_float), ('G', ctypes.c_float * 8), ('consts', ctypes.c_float * 4),
     ]
 
 
@@ -254,7 +254,7 @@ SIGNATURES = {
     'tvbg_adjoint_mpr': (ctypes.c_int, [_vp, _i32, _i32, _vp]),
     'tvbg_adjoint_mpr_ex': (ctypes.c_int, [_vp, _i32, _i32, _i32, _vp]),
     'tvbg_adjoint_group_size': (_sz, []),
-    'tvbg_adjoint_mpr_groups': (ctypes.c_int, [_vp, _i32, _i32, _i32, _i32, _vp, _vp]),
+    'tvbg_adjoint_mpr_groups': (ctypes.c_int, [_vp, _i32, _i32, _i32, _i32, _i32, _vp, _vp]),
     'tvbg_philox_u32': (ctypes.c_int, [_u32, _u32, _u32, _u32, _u32, _vp, _i64, _vp]),
     'tvbg_group_size': (_sz, []),
     'tvbg_net_size': (_sz, []),

@@ -81,18 +81,21 @@ def transpose_edges_group(row, col, w, delays):
     return row_t, out
 
 
-def adjoint_group_shape(N, slots=16, max_threads=512, max_cluster=16):
-    """(threads, cluster) of tvbg_adjoint_mpr_groups for N nodes: about
-    `slots` node slots per CTA (measured at N = 84, 256 instances: 16 slots
-    x 6 CTAs 9.15 ms per backward, 44 x 2 9.5 ms), as many CTAs as that
-    takes up to max_cluster, node slots a multiple of 4 (threads a multiple
-    of 32) and at most max_threads / 8; None when N does not fit."""
-    c0 = min(max_cluster, max(-(-N // slots), -(-N // (max_threads // 8)), 1))
+def adjoint_group_shape(N, pipelined=False, slots=16, max_threads=512, max_cluster=16):
+    """(threads, cluster, pipelined) of tvbg_adjoint_mpr_groups for N
+    nodes: about `slots` node slots per CTA (measured at N = 84, 256
+    instances: 16 slots x 6 CTAs 9.15 ms per backward, 44 x 2 9.5 ms), as
+    many CTAs as that takes up to max_cluster, node slots a multiple of 4
+    (each team's threads a multiple of 32); threads = 8 (16 with the two
+    pipelined teams) per slot, at most max_threads; None when N does not
+    fit."""
+    per = 16 if pipelined else 8
+    c0 = min(max_cluster, max(-(-N // slots), -(-N // (max_threads // per)), 1))
     for c in range(c0, max_cluster + 1):
         p = -(-N // c)
         p = -(-p // 4) * 4
-        if 8 * p <= max_threads:
-            return 8 * p, c
+        if per * p <= max_threads:
+            return per * p, c, int(bool(pipelined))
     return None
 
 
@@ -142,7 +145,12 @@ class FCFit:
         # where the delays and N allow, else per instance over the group trace
         self.dmin, self.dmax = int(d.min()), int(d.max())
         self.adj_k = 8 if self.dmin >= 8 else (4 if self.dmin >= 4 else 0)
-        self.adjoint_shape = adjoint_group_shape(self.N) if self.adj_k else None
+        # the two-team reverse kernel where every delay is >= 2 K
+        self.adjoint_shape = None
+        if self.adj_k:
+            self.adjoint_shape = (adjoint_group_shape(self.N, pipelined=True)
+                                  if self.dmin >= 2 * self.adj_k else None) or \
+                adjoint_group_shape(self.N)
         self.adjoint_kernel = ('groups' if self.layout == 'groups' and self.adjoint_shape
                                else 'instances')
         # device buffers and group sets reused across calls (built on first use)
@@ -150,6 +158,17 @@ class FCFit:
         self._ck = None
         self._bufs = None
         self._adj_ring = None
+        self._win = None
+        self._eager = None
+        self._tables = []
+        # the recomputation on the grouped layout runs in windows of segments,
+        # one launch per window, their traces (r, V, S) and working copies of
+        # the checkpoints within trace_budget bytes; the last window is
+        # recomputed at the end of forward() (side stream, overlapping the
+        # loss path) when eager_recompute
+        self.trace_budget = 2 << 30
+        self.recompute_window = None   # segments per window (None: from trace_budget)
+        self.eager_recompute = True
         if self.adjoint_kernel == 'groups':
             self.lognh_g = max(1, int(np.ceil(np.log2(self.dmax + self.adj_k))))
             row_tg, e_tg = transpose_edges_group(conn.row, conn.col, conn.wnz, d)
@@ -218,17 +237,18 @@ class FCFit:
         trace of T rows; r, V and the coupling sum over one segment), built
         on the first call and given this call's couplings, eta and initial
         state after that."""
+        from .groups import pipelined_shape
         torch = self.torch
         if self._fw_gs is None:
             self._fw_gs = self._groups(G, eta, self.T, 1, False)
-            # two recomputation sets: segment k - 1 is recomputed into one
-            # while the reverse kernel reads segment k from the other
-            self._rec_sets = [self._groups(G, eta, self.C, 2, True) for _ in range(2)]
-            self._rec_gs = self._rec_sets[0]
+            # the recomputation set: its tables, flags and parameters serve the
+            # windows (many groups per launch: the smallest pipelined cluster)
+            self._rec_gs = self._groups(G, eta, self.C, 2, True)
+            self._rec_gs.set_shape(*pipelined_shape(self._rec_gs))
             self._x0_dev = torch.from_numpy(self.x0).cuda()
             self._side = torch.cuda.Stream()
         else:
-            for gs in [self._fw_gs] + self._rec_sets:
+            for gs in (self._fw_gs, self._rec_gs):
                 gs.set_couplings(G)
                 gs.set_nparam(eta)
             fw = self._fw_gs
@@ -243,6 +263,10 @@ class FCFit:
         lane-interleaved ([G][T][N][1][8]); the loss path reads it in place."""
         torch = self.torch
         fw, _ = self._group_sets(G, eta)
+        # an earlier call's recomputation (side stream) may still read the
+        # checkpoints this forward overwrites
+        torch.cuda.current_stream().wait_stream(self._side)
+        self._tables = []
         segs = [(t, min(self.C, self.T - t)) for t in range(0, self.T, self.C)]
         plans = fw.prepare_segments(segs)
         if self._ck is None:
@@ -259,10 +283,16 @@ class FCFit:
         self.fw = fw
         I, N, T = self.I, self.N, self.T
         L = 8
+        self._eager = None
+        if self.adjoint_kernel == 'groups' and self.eager_recompute:
+            # the last window's recomputation overlaps the loss path
+            self._windows()
+            side = self._side
+            side.wait_stream(torch.cuda.current_stream())
+            self._eager = self._recompute_window(0, side)
         loss = self._loss(fw.gtrace.data_ptr() + 4 * N * L, T * N * L, fw.gstate.data_ptr(),
                           N * 2 * L, 2 * L, L)
-        torch.cuda.synchronize()
-        fw.status.check()
+        fw.status.check()   # waits for this stream only
         return loss
 
     def _loss(self, x, xs, last, ls, lns, lanes):
@@ -325,7 +355,7 @@ class FCFit:
         rev = list(reversed(self.ckpt))
         b = np.arange(I, dtype=np.int64)
         if grouped and self.adjoint_kernel == 'groups':
-            return self._reverse_groups(rev, lam, deta, dGn)
+            return self._reverse_windows(lam, deta, dGn)
         if grouped:
             # recomputation on the same pipelined group kernel (bit-identical
             # to the forward) with r, V and the coupling sum S traced,
@@ -389,27 +419,87 @@ class FCFit:
         return dGn.sum(1), deta
 
 
-    def _reverse_groups(self, rev, lam, deta, dGn):
-        """Segments last first: recompute on the group kernel, then
-        tvbg_adjoint_mpr_groups over the group trace in place (r, V, S
-        lane-interleaved [G][C][N][3][8]), an adjoint ring per group.  The
-        recomputation of segment k + 1 (in the list's order) runs on a side
-        stream, into the other of two recomputation sets, while the reverse
-        kernel works on segment k; events order each recomputation after the
-        reverse kernel that last read its set, and each reverse kernel after
-        its recomputation."""
+    def _windows(self):
+        """Windows of segments for the recomputation, last first: (a, b)
+        segment ranges of at most W segments, W set by trace_budget (two
+        buffers when there is more than one window); the buffers, allocated
+        once: traces [G][W C][N][3][8] and working copies of W checkpoints."""
+        torch = self.torch
+        if self._win is not None:
+            return self._win
+        rec = self._rec_gs
+        S = len(self.ckpt)
+        G, N, C = rec.n_groups, self.N, self.C
+        per = 4 * (G * C * N * 3 * 8 + rec.gstate.numel() + rec.ring.numel())
+        W = max(1, min(S, self.trace_budget // per))
+        if W < S:
+            W = max(1, self.trace_budget // (2 * per))
+        if self.recompute_window:
+            W = max(1, min(S, int(self.recompute_window)))
+        wins = []
+        b = S
+        while b > 0:
+            wins.append((max(0, b - W), b))
+            b -= W
+        nbuf = 1 if len(wins) == 1 else 2
+        bufs = [(torch.empty((G, W * C, N, 3, 8), dtype=torch.float32, device='cuda'),
+                 torch.empty((W, ) + tuple(rec.gstate.shape), dtype=torch.float32, device='cuda'),
+                 torch.empty((W, rec.ring.numel()), dtype=torch.float32, device='cuda'))
+                for _ in range(nbuf)]
+        order = torch.arange(W * G, dtype=torch.int32, device='cuda')
+        self._win = (W, wins, bufs, order)
+        return self._win
+
+    def _recompute_window(self, w, stream):
+        """Recompute window w (of _windows) on `stream` in one launch of
+        (segment, group) pairs, each group from a working copy of its
+        segment's checkpoint, traces into the window's buffer (w % 2); the
+        same kernel and tables as the forward's segments, so the same bits.
+        Returns the event recorded after the launch."""
+        torch = self.torch
+        W, wins, bufs, order = self._windows()
+        a, b = wins[w]
+        tr, wst, wrg = bufs[w % len(bufs)]
+        rec = self._rec_gs
+        G, N, C = rec.n_groups, self.N, self.C
+        with torch.cuda.stream(stream):
+            wst[:b - a].copy_(self._ck[0][a:b])
+            wrg[:b - a].copy_(self._ck[1][a:b])
+        base, _ = rec.build_table(C)
+        live = base['lanes']['nsteps'] > 0
+        j = np.arange(b - a, dtype=np.int64)[:, None]        # [J, 1]
+        g = np.arange(G, dtype=np.int64)[None, :]            # [1, G]
+        ns = np.array([self.ckpt[a + k][1] for k in range(b - a)], np.int64)[:, None]
+        tab = np.repeat(base[None], b - a, axis=0)           # [J, G]
+        ns_g = rec.gstate[0].numel()
+        tab['state'] = wst.data_ptr() + 4 * (j * G + g) * ns_g
+        tab['ring'] = wrg.data_ptr() + 4 * (j * rec.ring.numel() + rec.ring_off[None, :])
+        tab['trace'] = tr.data_ptr() + 4 * ((g * W + j) * C * N * 3 * 8)
+        tab['t0'] = (a + j) * C
+        tab['lanes']['nsteps'] = live[None] * ns[:, :, None]
+        tab['nsteps'] = ns
+        with torch.cuda.stream(stream):   # uploaded in the launch's stream order
+            dev = torch.from_numpy(tab.view(np.uint8).reshape(-1).copy()).cuda()
+        k = int(rec.block_k[0])
+        if not (rec.block_k == k).all():
+            raise ValueError('windowed recomputation: one block length')
+        cfg = rec.launch_cfg(k, order, None, plain=False)
+        rec._run_groups(dev.data_ptr(), (b - a) * G, cfg, stream.cuda_stream)
+        ev = torch.cuda.Event()
+        ev.record(stream)
+        self._tables.append(dev)   # alive until the backward synchronises
+        return ev
+
+    def _reverse_windows(self, lam, deta, dGn):
+        """Windows last first: each window recomputed in one launch (side
+        stream; the last window at the end of forward when eager_recompute),
+        then tvbg_adjoint_mpr_groups over the whole window in one launch,
+        reading the window's traces in place.  The recomputation of window
+        w + 1 overlaps the reverse kernel of window w; events order each
+        recomputation after the reverse kernel that last read its buffer."""
         from .engine import DeviceStatus
         torch = self.torch
         lib = nat.load()
-        recs = self._rec_sets
-        S = len(rev)
-        segs = [(t0, n) for (t0, n, _, _) in rev]
-        plans = [None] * S
-        for j in range(2):
-            ks = list(range(j, S, 2))
-            if ks:
-                for k, pl in zip(ks, recs[j].prepare_segments([segs[k] for k in ks])):
-                    plans[k] = pl
         I, N, T, K = self.I, self.N, self.T, self.adj_k
         Gn = (I + 7) // 8
         R = (1 << self.lognh_g) + K
@@ -418,18 +508,23 @@ class FCFit:
         else:
             self._adj_ring.zero_()
         ring = self._adj_ring
-        threads, cluster = self.adjoint_shape
+        threads, cluster, pipe = self.adjoint_shape
+        if pipe and self.dmin < 2 * K:
+            raise ValueError('pipelined reverse kernel: every delay >= 2 K')
+        W, wins, bufs, _ = self._windows()
+        nw = len(wins)
         g = np.arange(Gn, dtype=np.int64)[None, :]           # [1, Gn]
-        t0s = np.array([r[0] for r in rev], np.int64)[:, None]
-        lens = np.array([r[1] for r in rev], np.int64)[:, None]
+        t0s = np.array([wins[w][0] * self.C for w in range(nw)], np.int64)[:, None]
+        lens = np.array([sum(self.ckpt[k][1] for k in range(*wins[w])) for w in range(nw)],
+                        np.int64)[:, None]
+        tr0 = np.array([bufs[w % len(bufs)][0].data_ptr() for w in range(nw)], np.int64)[:, None]
         Gl = np.zeros(Gn * 8, np.float32)
         Gl[:I] = self.G
-        tab = np.zeros((len(rev), Gn), dtype=nat.ADJOINT_GROUP_DTYPE)
+        tab = np.zeros((nw, Gn), dtype=nat.ADJOINT_GROUP_DTYPE)
         tab['edges_t'] = self.edges_tg.data_ptr()
         tab['row_t'] = self.row_t.data_ptr()
         tab['nodes'] = self.nodes_t.data_ptr()
-        seg0 = np.array([recs[k % 2].gtrace.data_ptr() for k in range(S)], np.int64)[:, None]
-        tab['seg'] = seg0 + 4 * g * self.C * N * 3 * 8
+        tab['seg'] = tr0 + 4 * g * W * self.C * N * 3 * 8
         tab['dr'] = self.dr.data_ptr() + 4 * (8 * g * (T + 1) * N + t0s * N)
         tab['lam'] = lam.data_ptr() + 4 * 8 * g * N * 2
         tab['ring'] = ring.data_ptr() + 4 * g * N * R * 8
@@ -442,6 +537,7 @@ class FCFit:
         tab['lognh'] = self.lognh_g
         tab['lanes'] = np.minimum(8, I - 8 * g)
         tab['dmin'] = self.dmin
+        tab['flush_every'] = self.C      # partial sums grouped per segment
         tab['dt'] = np.float32(self.dt)
         tab['G'] = Gl.reshape(1, Gn, 8)
         tab['consts'] = self.consts[:4]
@@ -450,27 +546,26 @@ class FCFit:
         status = DeviceStatus()
         main, side = torch.cuda.current_stream(), self._side
         side.wait_stream(main)
-        done = []
-        for k, ((t0, n, st, rg), pl) in enumerate(zip(rev, plans)):
-            rec = recs[k % 2]
-            if k >= 2:
-                side.wait_event(done[k - 2])
-            with torch.cuda.stream(side):
-                rec.gstate.copy_(st)
-                rec.ring.copy_(rg)
-            rec.launch(pl, stream=side)
-            ready = torch.cuda.Event()
-            ready.record(side)
-            main.wait_event(ready)
-            nat.check(lib.tvbg_adjoint_mpr_groups(dev.data_ptr() + k * row_bytes, Gn, threads,
-                                                  cluster, K, status.t.data_ptr(),
+        ready = [None] * nw
+        done = [None] * nw
+        ready[0], self._eager = self._eager, None
+        if ready[0] is None:
+            ready[0] = self._recompute_window(0, side)
+        for w in range(nw):
+            if w + 1 < nw:
+                if w >= 1:
+                    side.wait_event(done[w - 1])       # buffer (w + 1) % 2 last read by window w - 1
+                ready[w + 1] = self._recompute_window(w + 1, side)
+            main.wait_event(ready[w])
+            nat.check(lib.tvbg_adjoint_mpr_groups(dev.data_ptr() + w * row_bytes, Gn, threads,
+                                                  cluster, K, pipe, status.t.data_ptr(),
                                                   main.cuda_stream))
-            done.append(torch.cuda.Event())
-            done[-1].record(main)
+            done[w] = torch.cuda.Event()
+            done[w].record(main)
         main.wait_stream(side)
         torch.cuda.synchronize()
-        for rec in recs:
-            rec.status.check()
+        self._tables = []
+        self._rec_gs.status.check()
         status.check()
         return dGn.sum(1), deta
 
