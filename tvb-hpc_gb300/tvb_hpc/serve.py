@@ -101,14 +101,19 @@ def footprint(req):
     return base
 
 
-def adjoint_bytes(I, N, T, nh, checkpoint_every=100):
+def adjoint_bytes(I, N, T, nh, checkpoint_every=100, trace_budget=2 << 30):
     """Device bytes of adjoint.FCFit for I instances, N nodes, T steps:
-    the rate series (FP32 trace), dL/dr (FP32), the loss scratch (FC and A), one state + ring checkpoint per chunk of
-    checkpoint_every steps, the recomputation trace and the adjoint ring."""
+    the rate series (FP32 trace), dL/dr (FP32), the loss scratch (FC and A),
+    one state + ring checkpoint per chunk of checkpoint_every steps, the
+    recomputation (windows of segments: r, V, S traces and working copies of
+    their checkpoints, at most trace_budget) and the adjoint ring."""
+    C = int(checkpoint_every)
+    S = -(-T // C)
     series = I * T * N * (4 + 4)               # r trace and dL/dr (FP32)
-    ckpt = -(-T // checkpoint_every) * I * N * (nh + 2) * 4
-    chunk = I * checkpoint_every * N * 3 * 4 + I * N * nh * 4
-    return series + ckpt + chunk + I * N * N * (8 * 2 + 4) + I * N * 8 * 3
+    ckpt = S * I * N * (nh + 8 + 2) * 4
+    per_seg = I * C * N * 3 * 4 + I * N * (nh + 8 + 2) * 4
+    recompute = max(per_seg, min(S * per_seg, int(trace_budget)))
+    return series + ckpt + recompute + I * N * N * (8 * 2 + 4) + I * N * 8 * 3
 
 
 class Server:
