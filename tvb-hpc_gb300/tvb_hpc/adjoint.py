@@ -161,6 +161,7 @@ class FCFit:
         self._win = None
         self._eager = None
         self._tables = []
+        self._deferred = []      # status words of earlier calls, copied to the host
         # the recomputation on the grouped layout runs in windows of segments,
         # one launch per window, their traces (r, V, S) and working copies of
         # the checkpoints within trace_budget bytes; the last window is
@@ -222,6 +223,28 @@ class FCFit:
         assert shape[3] == PIPELINED
         gs.set_shape(*shape)
         return gs
+
+    def _defer(self, *statuses):
+        """Copy device status words to pinned host memory without waiting
+        (checked by check() or at the end of the next call, once that call's
+        work is queued: the device never waits for the host)."""
+        torch = self.torch
+        for st in statuses:
+            h = torch.empty(1, dtype=torch.int32, pin_memory=True)
+            h.copy_(st.t, non_blocking=True)
+            ev = torch.cuda.Event()
+            ev.record()
+            self._deferred.append((h, ev))
+
+    def check(self, upto=None):
+        """Raise if a kernel of an earlier forward/backward reported a
+        device-side error (waits for those kernels)."""
+        pend = self._deferred if upto is None else self._deferred[:upto]
+        self._deferred = [] if upto is None else self._deferred[upto:]
+        for h, ev in pend:
+            ev.synchronize()
+            if int(h[0]) != 0:
+                raise nat.TvbgError(int(h[0]), 'device-side check failed in the adjoint')
 
     def forward(self, G, eta):
         "Loss [I] (FP64); keeps checkpoints and the rate series for backward."
@@ -292,7 +315,11 @@ class FCFit:
             self._eager = self._recompute_window(0, side)
         loss = self._loss(fw.gtrace.data_ptr() + 4 * N * L, T * N * L, fw.gstate.data_ptr(),
                           N * 2 * L, 2 * L, L)
-        fw.status.check()   # waits for this stream only
+        # this call's status copied without waiting; the earlier calls' checked
+        # now that this call's work is queued behind theirs
+        n_prev = len(self._deferred)
+        self._defer(fw.status)
+        self.check(n_prev)
         return loss
 
     def _loss(self, x, xs, last, ls, lns, lanes):
@@ -563,11 +590,11 @@ class FCFit:
             done[w] = torch.cuda.Event()
             done[w].record(main)
         main.wait_stream(side)
-        torch.cuda.synchronize()
-        self._tables = []
-        self._rec_gs.status.check()
-        status.check()
-        return dGn.sum(1), deta
+        dG = dGn.sum(1)
+        n_prev = len(self._deferred)
+        self._defer(self._rec_gs.status, status)
+        self.check(n_prev)
+        return dG, deta
 
 
 class FCFitLoss:

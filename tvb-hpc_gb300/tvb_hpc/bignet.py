@@ -80,10 +80,10 @@ class SingleNetwork:
         self.ring = torch.zeros(N * self.R, dtype=torch.float32, device=dev)
         st = (np.zeros((N, self.ns), np.float32) if state0 is None
               else np.broadcast_to(np.asarray(state0, np.float32), (N, self.ns)))
-        self.state = torch.from_numpy(np.ascontiguousarray(st)).to(dev)
+        self.state = torch.from_numpy(np.array(st, np.float32)).to(dev)   # a writable copy
         npm = (model.node_params(N) if nparam is None
                else np.broadcast_to(np.asarray(nparam, np.float32).reshape(N, -1), (N, self.npar)))
-        self.nparam = torch.from_numpy(np.ascontiguousarray(npm, np.float32)).to(dev)
+        self.nparam = torch.from_numpy(np.array(npm, np.float32)).to(dev)
         fl = 0
         if getattr(scheme, 'noise', False) and np.any(self.sigma != 0):
             fl |= nat.F_NOISE
