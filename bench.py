@@ -1348,6 +1348,7 @@ def adjoint_finish(args, wl, gs, torch, world, rank, barrier_fn=None):
     barrier()
     clocks.hold(gs.run)
     clk = clocks.stop()
+    gs.prob.check()   # the status words of every timed call's kernels
     total_ms = timer.ms()
     t = torch.tensor([total_ms], device='cuda')
     if world > 1:
@@ -1364,6 +1365,7 @@ def adjoint_finish(args, wl, gs, torch, world, rank, barrier_fn=None):
         out = (loss.cpu(), dG.cpu(), deta.cpu())
     barrier()
     e2e_s = time.perf_counter() - t0
+    gs.prob.check()
     h2d = wl['couplings'].nbytes + wl['eta'].nbytes
     d2h = sum(o.numel() * o.element_size() for o in out)
     err = gs.grad_error()

@@ -311,6 +311,7 @@ class Server:
             prob = FCFit(req.conn, req.dt, float(req.speeds[0]), req.x0, req.target, req.nsteps)
             prob.forward(req.couplings, np.asarray(req.nparam).reshape(req.couplings.size, -1))
             out = tuple(t.cpu().numpy() for t in prob.backward())
+            prob.check()   # the status words of its kernels
         del prob
         torch.cuda.empty_cache()   # give the adjoint's memory back for admission
         return out
