@@ -653,9 +653,9 @@ int tvbg_rmap_from_avg(int32_t nroi, int32_t nvar, int32_t nnode, const int32_t 
  * ---- serving pool ---------------------------------------------------------
  * Continuous batching of sweep requests in native code: requests are copied
  * in (tvbg_serve_admit), admitted to the device when their footprint fits
- * the pool's HBM budget, advanced together one chunk of steps per
- * tvbg_serve_tick (each request's lane-interleaved groups on its own
- * stream, joined into the pool's), retired when done (final state copied
+ * the pool's HBM budget, advanced chunk by chunk from tvbg_serve_tick (each
+ * request's lane-interleaved groups on its own stream, at its own pace),
+ * retired when done (final state copied
  * out, device memory freed), and polled or cancelled by id.  The pool is
  * the one object that allocates device memory behind its calls: it is
  * created and destroyed explicitly.  The reference has no serving layer;
@@ -698,20 +698,29 @@ typedef struct tvbg_serve_request {
 #define TVBG_SERVE_DONE 2
 #define TVBG_SERVE_CANCELLED 3
 
-/* A pool with `hbm_budget` bytes for admitted requests, advancing every
- * active request by up to `chunk` steps per tick on `stream` (NULL: its own
- * stream, created at the first tick).  Creating a pool and admitting
- * requests (host planning only) touch no device. */
+/* A pool with `hbm_budget` bytes for admitted requests, advancing each
+ * active request by up to `chunk` steps per chunk, every request on a
+ * stream of its own (`stream` is reserved: pass NULL).  Creating a pool and
+ * admitting requests (host planning only) touch no device. */
 int tvbg_serve_create(int64_t hbm_budget, int32_t chunk, void *stream, tvbg_serve **out);
 int tvbg_serve_destroy(tvbg_serve *pool);
 /* Copy a request in and queue it; *id identifies it.  Rejects requests whose
  * delays are shorter than the group kernel's blocks (d_min < 3) or whose
  * footprint exceeds the whole budget. */
 int tvbg_serve_admit(tvbg_serve *pool, const tvbg_serve_request *req, int64_t *id);
-/* Admit queued requests that fit, advance every active one by one chunk,
- * retire the finished; waits for this tick's device work.  *n_active and
- * *n_queued (either may be NULL) count what is left. */
+/* Admit queued requests that fit and start a chunk for every active request
+ * with none running; then, once some chunk is done (waiting at most 20 ms
+ * when none is yet), take every finished chunk (status word, progress,
+ * retirement of the finished requests: final state copied out, device
+ * memory given back) and start the next chunk of its request at once.
+ * Requests advance at their own pace, none waits for the others' chunks;
+ * device memory is stream-ordered (cudaMallocAsync / cudaFreeAsync), so
+ * admission and retirement do not wait for the device either.  *n_active
+ * and *n_queued (either may be NULL) count what is left. */
 int tvbg_serve_tick(tvbg_serve *pool, int32_t *n_active, int32_t *n_queued);
+/* Ids of the requests retired since the last call, oldest first: up to cap
+ * of them into ids, *n = how many. */
+int tvbg_serve_finished(tvbg_serve *pool, int64_t *ids, int32_t cap, int32_t *n);
 /* *status = TVBG_SERVE_*; once done, the final state is copied to
  * state_out (host [n_inst][N][nsvar]) when it is not NULL. */
 int tvbg_serve_poll(tvbg_serve *pool, int64_t id, int32_t *status, float *state_out);

@@ -20,10 +20,13 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
+#include <condition_variable>
 #include <cstring>
 #include <deque>
 #include <map>
+#include <mutex>
 #include <new>
 #include <vector>
 
@@ -33,8 +36,65 @@
 using namespace tvbg;
 
 namespace {
+struct Request;
+}
+
+struct tvbg_serve {
+    int64_t cap = 0;               // budget at creation: a request larger never fits
+    int64_t budget = 0, used = 0;  // current admission budget (tvbg_serve_set_budget)
+    int32_t chunk = 0;
+    int64_t cta_cap = 0;           // admission stops at this many resident CTAs (0: no cap,
+                                   // -1: 3 x SMs)
+    int64_t active_ctas = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int64_t next_id = 1;
+    std::deque<Request*> queue;
+    std::vector<Request*> active;
+    std::map<int64_t, Request*> all;
+    std::vector<int64_t> finished;                 // retired ids not yet fetched
+    std::map<size_t, std::vector<void*>> pinned;   // free pinned staging blocks by size
+    // chunk completions, counted by a host function after each chunk; a
+    // tick with nothing completed waits on cv for the next one
+    std::mutex mu;
+    std::condition_variable cv;
+    uint64_t completions = 0;
+};
+
+namespace {
 
 constexpr int L = TVBG_GROUP_LANES;
+
+// Pinned host staging, recycled through the pool (cudaFreeHost would wait
+// for the device): blocks of a power of two >= 256 bytes.
+size_t pinned_class(size_t n) {
+    size_t c = 256;
+    while (c < n) c <<= 1;
+    return c;
+}
+void* pinned_get(tvbg_serve& p, size_t bytes) {
+    std::vector<void*>& v = p.pinned[bytes];
+    if (!v.empty()) {
+        void* h = v.back();
+        v.pop_back();
+        return h;
+    }
+    void* h = nullptr;
+    return cudaMallocHost(&h, bytes) == cudaSuccess ? h : nullptr;
+}
+void pinned_put(tvbg_serve& p, void* h, size_t bytes) {
+    if (h) p.pinned[bytes].push_back(h);
+}
+
+// Host function enqueued after each chunk: counts it and wakes a waiting tick.
+void CUDART_CB chunk_done(void* arg) {
+    tvbg_serve* p = static_cast<tvbg_serve*>(arg);
+    {
+        std::lock_guard<std::mutex> lk(p->mu);
+        ++p->completions;
+    }
+    p->cv.notify_all();
+}
 
 // (state variables, per-node parameters, observables) of each model id
 struct ModelShape {
@@ -93,7 +153,9 @@ struct Request {
     cudaEvent_t done_ev = nullptr;
     std::vector<tvbg_group> records;
     tvbg_group* h_records = nullptr;  // pinned staging of records (asynchronous uploads)
-    int32_t* h_status = nullptr;      // pinned copy of the status word, read after each tick
+    size_t h_records_bytes = 0;       // its block size (pool cache class)
+    int32_t* h_status = nullptr;      // pinned copy of the status word, read once its chunk is done
+    int64_t inflight = 0;             // steps of the chunk running now (0: none)
     int64_t ctas = 0;                 // CTAs of one chunk: groups x cluster
     std::vector<float> result;        // [n_inst][N][ns] once done
 };
@@ -284,24 +346,25 @@ bool pipelined_fits(const Request& r) {
     return true;
 }
 
-int materialise(Request& r) {
+// Device memory is stream-ordered (cudaMallocAsync / cudaFreeAsync on the
+// request's stream): admitting or retiring a request never waits for the
+// other requests' chunks, as cudaFree would.
+int materialise(tvbg_serve& p, Request& r) {
     if (r.tpn == TVBG_GROUP_PIPELINED && !pipelined_fits(r)) plain_shape(r);
-    cudaError_t e = cudaMalloc(&r.dev, r.bytes);
-    if (e != cudaSuccess) {
-        r.dev = nullptr;
-        return set_cuda_error(e, "tvbg_serve: cudaMalloc");
-    }
-    e = cudaStreamCreateWithFlags(&r.stream, cudaStreamNonBlocking);
+    cudaError_t e = cudaStreamCreateWithFlags(&r.stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&r.done_ev, cudaEventDisableTiming);
     if (e != cudaSuccess) return set_cuda_error(e, "tvbg_serve: stream");
-    const int N = r.N, ns = r.shape.ns, np = r.npar, G = static_cast<int>(r.members.size());
-    e = cudaMallocHost(&r.h_records, static_cast<size_t>(std::max(1, G)) * sizeof(tvbg_group));
-    if (e == cudaSuccess) e = cudaMallocHost(&r.h_status, sizeof(int32_t));
+    e = cudaMallocAsync(reinterpret_cast<void**>(&r.dev), r.bytes, r.stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(r.stream);  // usable from any stream
     if (e != cudaSuccess) {
-        r.h_records = nullptr;
-        r.h_status = nullptr;
-        return set_cuda_error(e, "tvbg_serve: pinned staging");
+        r.dev = nullptr;
+        return set_cuda_error(e, "tvbg_serve: cudaMallocAsync");
     }
+    const int N = r.N, ns = r.shape.ns, np = r.npar, G = static_cast<int>(r.members.size());
+    r.h_records_bytes = pinned_class(static_cast<size_t>(std::max(1, G)) * sizeof(tvbg_group));
+    r.h_records = static_cast<tvbg_group*>(pinned_get(p, r.h_records_bytes));
+    r.h_status = static_cast<int32_t*>(pinned_get(p, 256));
+    if (!r.h_records || !r.h_status) return set_error(TVBG_ECUDA, "tvbg_serve: pinned staging");
     *r.h_status = 0;
     r.ctas = static_cast<int64_t>(G) * r.cluster;
     // lane-interleaved state and parameters [G][N][*][L]
@@ -389,11 +452,11 @@ int materialise(Request& r) {
     return TVBG_OK;
 }
 
-void release(Request& r) {
-    if (r.stream) cudaStreamSynchronize(r.stream);
-    if (r.dev) cudaFree(r.dev);
-    if (r.h_records) cudaFreeHost(r.h_records);
-    if (r.h_status) cudaFreeHost(r.h_status);
+void release(tvbg_serve& p, Request& r) {
+    if (r.stream) cudaStreamSynchronize(r.stream);   // this request's chunk only
+    if (r.dev) cudaFreeAsync(r.dev, r.stream);
+    pinned_put(p, r.h_records, r.h_records_bytes);
+    pinned_put(p, r.h_status, 256);
     r.h_records = nullptr;
     r.h_status = nullptr;
     if (r.done_ev) cudaEventDestroy(r.done_ev);
@@ -401,12 +464,14 @@ void release(Request& r) {
     r.dev = nullptr;
     r.stream = nullptr;
     r.done_ev = nullptr;
+    r.inflight = 0;
     r.records.clear();
     r.records.shrink_to_fit();
 }
 
-// Enqueue the next `steps` steps of every group of r on r.stream.
-int launch_chunk(Request& r, int64_t steps) {
+// Enqueue the next `steps` steps of every group of r on r.stream, then the
+// status word's copy, the chunk's event and its completion count.
+int launch_chunk(tvbg_serve& p, Request& r, int64_t steps) {
     const int G = static_cast<int>(r.records.size());
     for (int g = 0; g < G; ++g) {
         tvbg_group& rec = r.records[g];
@@ -414,8 +479,8 @@ int launch_chunk(Request& r, int64_t steps) {
         rec.nsteps = static_cast<int32_t>(steps);
         for (size_t l = 0; l < r.members[g].size(); ++l) rec.lanes[l].nsteps = static_cast<int32_t>(steps);
     }
-    // refilling the pinned staging is safe: every tick ends with the pool
-    // stream synchronised, which waited for this request's previous upload
+    // refilling the pinned staging is safe: a request's next chunk is
+    // launched only once its previous chunk's event (after that upload) is done
     std::memcpy(r.h_records, r.records.data(), G * sizeof(tvbg_group));
     cudaError_t e = cudaMemcpyAsync(r.dev + r.off_groups, r.h_records, G * sizeof(tvbg_group),
                                     cudaMemcpyHostToDevice, r.stream);
@@ -446,7 +511,9 @@ int launch_chunk(Request& r, int64_t steps) {
                         r.stream);
     if (e != cudaSuccess) return set_cuda_error(e, "tvbg_serve: status copy");
     e = cudaEventRecord(r.done_ev, r.stream);
+    if (e == cudaSuccess) e = cudaLaunchHostFunc(r.stream, chunk_done, &p);
     if (e != cudaSuccess) return set_cuda_error(e, "tvbg_serve: event");
+    r.inflight = steps;
     return TVBG_OK;
 }
 
@@ -469,22 +536,17 @@ int collect(Request& r) {
     return TVBG_OK;
 }
 
-}  // namespace
+// Launch the next chunk of every active request with none running.
+int launch_idle(tvbg_serve& p) {
+    for (Request* r : p.active) {
+        if (r->inflight || r->done >= r->nsteps) continue;
+        int rc = launch_chunk(p, *r, std::min<int64_t>(p.chunk, r->nsteps - r->done));
+        if (rc) return rc;
+    }
+    return TVBG_OK;
+}
 
-struct tvbg_serve {
-    int64_t cap = 0;               // budget at creation: a request larger never fits
-    int64_t budget = 0, used = 0;  // current admission budget (tvbg_serve_set_budget)
-    int32_t chunk = 0;
-    int64_t cta_cap = 0;           // admission stops at this many resident CTAs (0: no cap,
-                                   // -1: 3 x SMs)
-    int64_t active_ctas = 0;
-    cudaStream_t stream = nullptr;
-    bool own_stream = false;
-    int64_t next_id = 1;
-    std::deque<Request*> queue;
-    std::vector<Request*> active;
-    std::map<int64_t, Request*> all;
-};
+}  // namespace
 
 extern "C" {
 
@@ -502,10 +564,12 @@ int tvbg_serve_create(int64_t hbm_budget, int32_t chunk, void* stream, tvbg_serv
 
 int tvbg_serve_destroy(tvbg_serve* p) {
     if (!p) return TVBG_OK;
-    for (auto& kv : p->all) {
-        release(*kv.second);
+    for (auto& kv : p->all) {   // each waits for its request's chunk (and callback)
+        release(*p, *kv.second);
         delete kv.second;
     }
+    for (auto& kv : p->pinned)
+        for (void* h : kv.second) cudaFreeHost(h);
     if (p->own_stream && p->stream) cudaStreamDestroy(p->stream);
     delete p;
     return TVBG_OK;
@@ -562,16 +626,13 @@ int tvbg_serve_admit(tvbg_serve* p, const tvbg_serve_request* q, int64_t* id) {
     return TVBG_OK;
 }
 
+// A rolling tick: admit what fits, launch a chunk for every active request
+// with none running, wait (at most 20 ms) until some chunk is done when none
+// is yet, then take every finished chunk -- status word, clock, retirement
+// -- and relaunch its request at once.  Requests advance at their own pace:
+// no request waits for the slowest chunk of the others.
 int tvbg_serve_tick(tvbg_serve* p, int32_t* n_active, int32_t* n_queued) {
     if (!p) return set_error(TVBG_EINVAL, "tvbg_serve_tick: null");
-    if (!p->stream) {
-        cudaError_t e = cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking);
-        if (e != cudaSuccess) {
-            p->stream = nullptr;
-            return set_cuda_error(e, "tvbg_serve_tick: stream");
-        }
-        p->own_stream = true;
-    }
     if (p->cta_cap < 0) {  // -1: about three waves of CTAs resident at once
         int dev = 0, sms = 0;
         cudaError_t e = cudaGetDevice(&dev);
@@ -589,9 +650,9 @@ int tvbg_serve_tick(tvbg_serve* p, int32_t* n_active, int32_t* n_queued) {
         if (p->used + static_cast<int64_t>(r->bytes) > p->budget || r->bytes > free_b) break;
         const int64_t ctas = static_cast<int64_t>(r->members.size()) * r->cluster;
         if (p->cta_cap > 0 && !p->active.empty() && p->active_ctas + ctas > p->cta_cap) break;
-        int rc = materialise(*r);
+        int rc = materialise(*p, *r);
         if (rc) {
-            release(*r);
+            release(*p, *r);
             return rc;
         }
         p->queue.pop_front();
@@ -600,53 +661,65 @@ int tvbg_serve_tick(tvbg_serve* p, int32_t* n_active, int32_t* n_queued) {
         r->status = TVBG_SERVE_ACTIVE;
         p->active.push_back(r);
     }
-    // one chunk for every active request, each on its stream, joined into the pool's
-    cudaEvent_t start;
-    cudaError_t e = cudaEventCreateWithFlags(&start, cudaEventDisableTiming);
-    if (e != cudaSuccess) return set_cuda_error(e, "tvbg_serve_tick: event");
-    e = cudaEventRecord(start, p->stream);
-    std::vector<int64_t> steps(p->active.size());
-    int rc = e == cudaSuccess ? TVBG_OK : set_cuda_error(e, "tvbg_serve_tick: event");
-    for (size_t i = 0; i < p->active.size() && rc == TVBG_OK; ++i) {
-        Request& r = *p->active[i];
-        steps[i] = std::min<int64_t>(p->chunk, r.nsteps - r.done);
-        e = cudaStreamWaitEvent(r.stream, start, 0);
-        if (e != cudaSuccess) {
-            rc = set_cuda_error(e, "tvbg_serve_tick: wait");
-            break;
-        }
-        if (steps[i] > 0) rc = launch_chunk(r, steps[i]);
-        else if (cudaEventRecord(r.done_ev, r.stream) != cudaSuccess)
-            rc = set_error(TVBG_ECUDA, "tvbg_serve_tick: event");
-        if (rc == TVBG_OK) {
-            e = cudaStreamWaitEvent(p->stream, r.done_ev, 0);
-            if (e != cudaSuccess) rc = set_cuda_error(e, "tvbg_serve_tick: join");
-        }
+    uint64_t mark;
+    {
+        std::lock_guard<std::mutex> lk(p->mu);
+        mark = p->completions;
     }
-    cudaEventDestroy(start);
+    int rc = launch_idle(*p);
     if (rc) return rc;
-    e = cudaStreamSynchronize(p->stream);
-    if (e != cudaSuccess) return set_cuda_error(e, "tvbg_serve_tick: synchronize");
-    // status words first (copied back with each chunk): an error here leaves
-    // every request as it was
-    for (size_t i = 0; i < p->active.size(); ++i) {
-        if (*p->active[i]->h_status != 0)
-            return set_error(TVBG_EDEVICE, "tvbg_serve_tick: a group kernel reported an error");
+    // finished chunks (a chunk counted after `mark` wakes the wait below;
+    // one counted before it is already seen by its event)
+    auto finished = [&](Request& r, bool* done) -> int {
+        *done = false;
+        if (!r.inflight) {
+            *done = r.done >= r.nsteps;  // zero steps: retire without a chunk
+            return TVBG_OK;
+        }
+        const cudaError_t q = cudaEventQuery(r.done_ev);
+        if (q == cudaErrorNotReady) return TVBG_OK;
+        if (q != cudaSuccess) return set_cuda_error(q, "tvbg_serve_tick: event");
+        *done = true;
+        return TVBG_OK;
+    };
+    bool any = false;
+    for (Request* r : p->active) {
+        bool d = false;
+        if ((rc = finished(*r, &d))) return rc;
+        any = any || d;
     }
-    // clocks and retirement; the active list is rebuilt before any return, so
-    // a retired (released) request never stays in it, and a request whose
-    // result could not be collected stays active and is collected next tick
+    if (!any) {
+        bool running = false;
+        for (const Request* r : p->active) running = running || r->inflight > 0;
+        if (running) {
+            std::unique_lock<std::mutex> lk(p->mu);
+            p->cv.wait_for(lk, std::chrono::milliseconds(20), [&] { return p->completions != mark; });
+        }
+    }
+    // take the finished chunks: status words first (an error leaves the
+    // request as it was), then clocks and retirement; the active list is
+    // rebuilt before any return, so a released request never stays in it
     std::vector<Request*> keep;
     for (size_t i = 0; i < p->active.size(); ++i) {
         Request& r = *p->active[i];
-        r.done += steps[i];
-        if (rc == TVBG_OK && r.done >= r.nsteps) {
+        bool d = false;
+        if (rc == TVBG_OK) rc = finished(r, &d);
+        if (rc == TVBG_OK && d && r.inflight) {
+            if (*r.h_status != 0) {
+                rc = set_error(TVBG_EDEVICE, "tvbg_serve_tick: a group kernel reported an error");
+            } else {
+                r.done += r.inflight;
+                r.inflight = 0;
+            }
+        }
+        if (rc == TVBG_OK && d && r.done >= r.nsteps) {
             rc = collect(r);
             if (rc == TVBG_OK) {
-                release(r);
+                release(*p, r);
                 p->used -= static_cast<int64_t>(r.bytes);
                 p->active_ctas -= r.ctas;
                 r.status = TVBG_SERVE_DONE;
+                p->finished.push_back(r.id);
                 continue;
             }
         }
@@ -654,8 +727,19 @@ int tvbg_serve_tick(tvbg_serve* p, int32_t* n_active, int32_t* n_queued) {
     }
     p->active.swap(keep);
     if (rc) return rc;
+    rc = launch_idle(*p);  // the finished chunks' requests run on at once
+    if (rc) return rc;
     if (n_active) *n_active = static_cast<int32_t>(p->active.size());
     if (n_queued) *n_queued = static_cast<int32_t>(p->queue.size());
+    return TVBG_OK;
+}
+
+int tvbg_serve_finished(tvbg_serve* p, int64_t* ids, int32_t cap, int32_t* n) {
+    if (!p || !n || cap < 0 || (cap > 0 && !ids)) return set_error(TVBG_EINVAL, "tvbg_serve_finished: bad arguments");
+    const size_t k = std::min<size_t>(static_cast<size_t>(cap), p->finished.size());
+    std::copy(p->finished.begin(), p->finished.begin() + k, ids);
+    p->finished.erase(p->finished.begin(), p->finished.begin() + k);
+    *n = static_cast<int32_t>(k);
     return TVBG_OK;
 }
 
@@ -679,7 +763,7 @@ int tvbg_serve_cancel(tvbg_serve* p, int64_t id) {
         p->queue.erase(std::find(p->queue.begin(), p->queue.end(), r));
     } else if (r->status == TVBG_SERVE_ACTIVE) {
         p->active.erase(std::find(p->active.begin(), p->active.end(), r));
-        release(*r);
+        release(*p, *r);
         p->used -= static_cast<int64_t>(r->bytes);
         p->active_ctas -= r->ctas;
     } else {

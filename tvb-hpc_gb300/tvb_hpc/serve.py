@@ -377,6 +377,12 @@ class Server:
         self.phase_s['admit'] += t_s - t_d
         if self.native is not None:
             self._native_tick()
+            # the pool's requests go on at their own pace while this tick's
+            # Python-path chunk runs
+            while not done.query():
+                self._native_tick()
+                if not self.native_busy:
+                    time.sleep(0.0005)
         # wait for this tick's launches and the admissions' copies only (a
         # gradient job may be running on its own stream)
         done.synchronize()
@@ -445,8 +451,9 @@ class NativeServer:
     """
     The serving pool in native code (tvbg_serve_*): the same continuous
     batching as Server for requests without gradients, run by the C++ pool
-    -- requests copied in, admitted by the HBM budget, advanced one chunk
-    per tick on per-request streams, retired, polled and cancelled by id.
+    -- requests copied in, admitted by the HBM budget, advanced chunk by
+    chunk on per-request streams (each at its own pace), retired,
+    polled and cancelled by id.
     Each request's result equals lane-interleaved groups of the same inputs
     (GroupSet), alone or in any mix.
     """
@@ -463,8 +470,10 @@ class NativeServer:
         if max_ctas is not None:    # admission cap in resident CTAs (0: none; -1: the default)
             nat.check(self.lib.tvbg_serve_set_concurrency(h, int(max_ctas)))
         self.reqs = {}          # rid -> (Request, native id, kept host arrays)
+        self.by_nid = {}        # native id -> rid
         self.done = []
         self.ticks = 0
+        self._fin = np.zeros(4096, np.int64)
 
     def close(self):
         if self.h is not None:
@@ -522,23 +531,32 @@ class NativeServer:
         nid = ctypes.c_int64()
         nat.check(self.lib.tvbg_serve_admit(self.h, ctypes.byref(q), ctypes.byref(nid)))
         self.reqs[req.rid] = (req, nid.value, m.nsvar)
+        self.by_nid[nid.value] = req.rid
         return nid.value
 
     def tick(self):
-        "Admit what fits, advance every active request one chunk, retire; (active, queued)."
+        """One pool tick (admit, start idle requests' chunks, take finished
+        chunks as they end); the requests retired in it are fetched by id.
+        Returns (active, queued)."""
         import ctypes
         a, q = ctypes.c_int32(), ctypes.c_int32()
         self.nat.check(self.lib.tvbg_serve_tick(self.h, ctypes.byref(a), ctypes.byref(q)))
         self.ticks += 1
         now = self.clock()
-        for rid, (req, nid, ns) in self.reqs.items():
-            if req.finished is None and self.poll(rid) == 'done':
+        n = ctypes.c_int32()
+        while True:
+            self.nat.check(self.lib.tvbg_serve_finished(self.h, self._fin.ctypes.data,
+                                                        self._fin.size, ctypes.byref(n)))
+            for nid in self._fin[:n.value].tolist():
+                req, _, ns = self.reqs[self.by_nid[nid]]
                 req.finished = now
                 out = np.zeros((req.couplings.size, req.conn.nnode, ns), np.float32)
                 st = ctypes.c_int32()
                 self.nat.check(self.lib.tvbg_serve_poll(self.h, nid, ctypes.byref(st), out.ctypes.data))
                 req.state = out
                 self.done.append(req)
+            if n.value < self._fin.size:
+                break
         return a.value, q.value
 
     def poll(self, rid):
