@@ -1513,7 +1513,8 @@ def serve_window(rate, seconds, max_inst, chunk, conns, seed=7, drain_s=60.0, sa
     180 GB budget; ticks until every request is done or `drain_s` after the
     window, then cancels what is left.  Sampled every `sample_s`: the
     requests in the system (arrived, not finished) and the work backlog
-    (node-steps arrived minus node-steps taken, finished or not).  The queue
+    (node-steps arrived minus node-steps handed to the device: taken, or in
+    a chunk running now).  The queue
     kept up when the backlog does not grow over the second half of the
     window (least-squares slope below 5 % of the offered node-steps/s) and
     no request was left at the cut-off; served node-steps/s count every
@@ -1536,7 +1537,11 @@ def serve_window(rate, seconds, max_inst, chunk, conns, seed=7, drain_s=60.0, sa
         if now - t_start >= next_s:
             arr = [r for r in reqs if r.arrival <= now]
             finished = sum(1 for r in arr if r.finished is not None)
-            backlog = sum(r.node_steps for r in arr if r.error is None) - srv.work_done(arr)
+            # work not yet handed to the device: the pool's running chunks
+            # count as taken (they are on the GPU; completed-only counts would
+            # show the running chunks of a rolling pool as a growing backlog)
+            backlog = (sum(r.node_steps for r in arr if r.error is None)
+                       - srv.work_done(arr, issued=True))
             samples.append((round(now - t_start, 2), len(arr) - finished, float('%.4g' % backlog)))
             next_s += sample_s
     t_cut = time.perf_counter() - t_start
@@ -1608,6 +1613,11 @@ def serve_arm(args):
         res.pop('samples_t_insystem_backlog')
         sweep.append(res)
     kept = [x['rate_per_s'] for x in sweep if x['queue_kept_up']]
+    # a second reading of the same runs: the requests in the system do not
+    # grow over the second half of the window (slope below 5 % of the arrival
+    # rate) and none is left at the cut-off
+    kept_req = [x['rate_per_s'] for x in sweep
+                if x['left_at_cutoff'] == 0 and x['in_system_slope_per_s'] < 0.05 * x['rate_per_s']]
     if args.serve_no_plain:
         plain_groups = plain = {'value': None}
     else:
@@ -1628,6 +1638,7 @@ def serve_arm(args):
             'serve': main,
             'rate_sweep': sweep,
             'largest_rate_kept_up': max(kept) if kept else None,
+            'largest_rate_kept_up_by_requests': max(kept_req) if kept_req else None,
             'plain_groups': plain_groups,
             'plain': plain,
             'served_vs_plain_groups': (round(served / plain_groups['value'], 3)

@@ -737,6 +737,9 @@ int tvbg_serve_usage(tvbg_serve *pool, int64_t id, int64_t *used, int64_t *footp
 int tvbg_serve_set_concurrency(tvbg_serve *pool, int64_t max_ctas);
 /* Steps request id has taken so far (every instance takes the same). */
 int tvbg_serve_progress(tvbg_serve *pool, int64_t id, int64_t *steps_done);
+/* Steps handed to the device for request id: those taken plus the chunk
+ * running now. */
+int tvbg_serve_issued(tvbg_serve *pool, int64_t id, int64_t *steps);
 /* Admission budget of the following ticks, at most the creation budget: a
  * caller that holds device memory of its own under the same budget (the
  * Python serving path beside the pool) passes what it leaves free, so the

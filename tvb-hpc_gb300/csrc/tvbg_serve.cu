@@ -781,6 +781,14 @@ int tvbg_serve_progress(tvbg_serve* p, int64_t id, int64_t* steps_done) {
     return TVBG_OK;
 }
 
+int tvbg_serve_issued(tvbg_serve* p, int64_t id, int64_t* steps) {
+    if (!p || !steps) return set_error(TVBG_EINVAL, "tvbg_serve_issued: null");
+    auto it = p->all.find(id);
+    if (it == p->all.end()) return set_error(TVBG_EINVAL, "tvbg_serve_issued: unknown id");
+    *steps = it->second->done + it->second->inflight;
+    return TVBG_OK;
+}
+
 int tvbg_serve_set_concurrency(tvbg_serve* p, int64_t max_ctas) {
     if (!p) return set_error(TVBG_EINVAL, "tvbg_serve_set_concurrency: null");
     p->cta_cap = max_ctas < 0 ? -1 : max_ctas;

@@ -278,6 +278,7 @@ SIGNATURES = {
                                         ctypes.POINTER(_i64)]),
     'tvbg_serve_tick': (ctypes.c_int, [_vp, _ip, _ip]),
     'tvbg_serve_finished': (ctypes.c_int, [_vp, _vp, _i32, _vp]),
+    'tvbg_serve_issued': (ctypes.c_int, [_vp, _i64, _vp]),
     'tvbg_serve_poll': (ctypes.c_int, [_vp, _i64, _ip, _vp]),
     'tvbg_serve_cancel': (ctypes.c_int, [_vp, _i64]),
     'tvbg_serve_usage': (ctypes.c_int, [_vp, _i64, ctypes.POINTER(_i64), ctypes.POINTER(_i64)]),

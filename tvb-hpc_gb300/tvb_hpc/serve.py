@@ -422,9 +422,10 @@ class Server:
                 break
         return self.done
 
-    def work_done(self, reqs):
+    def work_done(self, reqs, issued=False):
         """Node-steps taken so far by `reqs` (submitted to this server),
-        finished or not."""
+        finished or not; with `issued`, the pool's running chunks count too
+        (the work handed to the device)."""
         total = 0.0
         for r in reqs:
             if r.error is not None:
@@ -432,7 +433,8 @@ class Server:
             if r.finished is not None and r.state is not None:
                 steps = r.nsteps
             elif self.native is not None and r.rid in self.native.reqs:
-                steps = self.native.steps_done(r.rid)
+                steps = (self.native.steps_issued(r.rid) if issued
+                         else self.native.steps_done(r.rid))
             else:
                 steps = r.steps_done
             total += float(r.couplings.size) * r.conn.nnode * steps
@@ -588,6 +590,13 @@ class NativeServer:
         import ctypes
         d = ctypes.c_int64()
         self.nat.check(self.lib.tvbg_serve_progress(self.h, self.reqs[rid][1], ctypes.byref(d)))
+        return int(d.value)
+
+    def steps_issued(self, rid):
+        "Steps of request rid handed to the device: taken plus the chunk running now."
+        import ctypes
+        d = ctypes.c_int64()
+        self.nat.check(self.lib.tvbg_serve_issued(self.h, self.reqs[rid][1], ctypes.byref(d)))
         return int(d.value)
 
     def set_budget(self, nbytes):
