@@ -150,6 +150,10 @@ def test_native_pool_budget_cancel(cuda):
         pool.submit(r)
     a, q = pool.tick()
     assert a >= 1 and a + q == len(reqs) and pool.used() <= 1.5 * max(fp)
+    # issued steps: those taken plus the chunk running now (<= one chunk ahead)
+    for r in reqs:
+        d, i = pool.steps_done(r.rid), pool.steps_issued(r.rid)
+        assert d <= i <= min(r.nsteps, d + 500)
     assert pool.cancel(reqs[-1].rid) and pool.poll(reqs[-1].rid) == 'cancelled'
     assert not pool.cancel(reqs[-1].rid)
     rest = pool.run()
