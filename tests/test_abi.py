@@ -51,6 +51,25 @@ def test_struct_layouts_match():
             == nat.ADJOINT_GROUP_DTYPE.itemsize == 168)
 
 
+def test_adjoint_recompute_windows_plan():
+    """plan_windows: windows of at most W segments, last first, covering
+    every segment once; one buffer for one window, two otherwise."""
+    from tvb_hpc.adjoint import plan_windows
+    for S in (1, 7, 20):
+        for per, budget, win in ((10, 1000, None), (10, 60, None), (10, 15, None), (10, 1000, 3)):
+            W, wins, nbuf = plan_windows(S, per, budget, win)
+            covered = [k for a, b in wins for k in range(a, b)]
+            assert sorted(covered) == list(range(S))
+            assert all(0 < b - a <= W for a, b in wins)
+            assert [a for a, _ in wins] == sorted([a for a, _ in wins], reverse=True)
+            assert nbuf == (1 if len(wins) == 1 else 2)
+            if win is None:
+                assert nbuf * W * per <= max(budget, nbuf * per)
+    assert plan_windows(20, 71, 2000) == (20, [(0, 20)], 1)
+    # 15 segments fit the budget, not all 20: two buffers of 7
+    assert plan_windows(20, 100, 1500) == (7, [(13, 20), (6, 13), (0, 6)], 2)
+
+
 def test_adjoint_group_edges_and_shapes():
     """Group packing of the transposed CSR: same out-edge order as the
     per-instance packing, pk = (i << 16) | d; launch shapes hold N."""

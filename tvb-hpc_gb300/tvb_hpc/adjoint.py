@@ -81,6 +81,26 @@ def transpose_edges_group(row, col, w, delays):
     return row_t, out
 
 
+def plan_windows(S, per_segment, budget, window=None):
+    """Windows of the recomputation over S checkpoint segments, last
+    first: (W, [(a, b), ...], buffers).  W segments per window, as many as
+    `budget` bytes hold at `per_segment` bytes each (one buffer for a single
+    window, two when the recomputation of the next window overlaps the
+    reverse kernel of this one), or `window` when given."""
+    S = int(S)
+    W = max(1, min(S, int(budget) // int(per_segment)))
+    if W < S:
+        W = max(1, int(budget) // (2 * int(per_segment)))
+    if window:
+        W = max(1, min(S, int(window)))
+    wins = []
+    b = S
+    while b > 0:
+        wins.append((max(0, b - W), b))
+        b -= W
+    return W, wins, 1 if len(wins) == 1 else 2
+
+
 def adjoint_group_shape(N, pipelined=False, slots=16, max_threads=512, max_cluster=16):
     """(threads, cluster, pipelined) of tvbg_adjoint_mpr_groups for N
     nodes: about `slots` node slots per CTA (measured at N = 84, 256
@@ -452,23 +472,14 @@ class FCFit:
         buffers when there is more than one window); the buffers, allocated
         once: traces [G][W C][N][3][8] and working copies of W checkpoints."""
         torch = self.torch
-        if self._win is not None:
-            return self._win
         rec = self._rec_gs
         S = len(self.ckpt)
         G, N, C = rec.n_groups, self.N, self.C
         per = 4 * (G * C * N * 3 * 8 + rec.gstate.numel() + rec.ring.numel())
-        W = max(1, min(S, self.trace_budget // per))
-        if W < S:
-            W = max(1, self.trace_budget // (2 * per))
-        if self.recompute_window:
-            W = max(1, min(S, int(self.recompute_window)))
-        wins = []
-        b = S
-        while b > 0:
-            wins.append((max(0, b - W), b))
-            b -= W
-        nbuf = 1 if len(wins) == 1 else 2
+        W, wins, nbuf = plan_windows(S, per, self.trace_budget, self.recompute_window)
+        if self._win is not None and self._win[0] == W and len(self._win[2]) == nbuf \
+                and self._win[1] == wins:
+            return self._win
         bufs = [(torch.empty((G, W * C, N, 3, 8), dtype=torch.float32, device='cuda'),
                  torch.empty((W, ) + tuple(rec.gstate.shape), dtype=torch.float32, device='cuda'),
                  torch.empty((W, rec.ring.numel()), dtype=torch.float32, device='cuda'))
