@@ -46,8 +46,6 @@ struct tvbg_serve {
     int64_t cta_cap = 0;           // admission stops at this many resident CTAs (0: no cap,
                                    // -1: 3 x SMs)
     int64_t active_ctas = 0;
-    cudaStream_t stream = nullptr;
-    bool own_stream = false;
     int64_t next_id = 1;
     std::deque<Request*> queue;
     std::vector<Request*> active;
@@ -557,7 +555,7 @@ int tvbg_serve_create(int64_t hbm_budget, int32_t chunk, void* stream, tvbg_serv
     p->budget = hbm_budget;
     p->cap = hbm_budget;
     p->chunk = chunk;
-    p->stream = static_cast<cudaStream_t>(stream);  // NULL: the pool's own, made at the first tick
+    (void)stream;  // reserved: every request runs on a stream of its own
     *out = p;
     return TVBG_OK;
 }
@@ -570,7 +568,6 @@ int tvbg_serve_destroy(tvbg_serve* p) {
     }
     for (auto& kv : p->pinned)
         for (void* h : kv.second) cudaFreeHost(h);
-    if (p->own_stream && p->stream) cudaStreamDestroy(p->stream);
     delete p;
     return TVBG_OK;
 }
