@@ -85,12 +85,14 @@ extern "C" int tvbg_fcfit_zgrad(const float* d_z, const float* d_a, float* d_out
 // X_b [T][N] (rows 0..T-2 from x, row T-1 from `last` when given), its
 // Pearson FC in FP64, the loss mean_{i<j} (FC_ij - F*_ij)^2 and
 // dL/dX = (Z A - Z diag(FC A)) / nrm, Z = (X - mean) / nrm, A = 2 (FC - F*) / P
-// with a zero diagonal (P = N (N - 1) / 2).  The FC is a symmetric FP64
-// Gram (one DFMA per product, upper-triangle tiles only); diag(FC A) is the
-// time reduction sum_t Z_ti (Z A)_ti of the chain rule, taken from FC in
-// FP64; Z, Z A and the epilogue are FP32 (Z A is a sum over N nodes per
-// sample), the precision of the backward.  (The Pearson FC restates refs/covar.c:70-109 / metric.py:111-139
-// as an exact two-pass FP64 sum.)
+// with a zero diagonal (P = N (N - 1) / 2).  Kernels: FP64 means; the
+// centred Gram, upper triangle only (FP32 error-free transformations for
+// N <= 192, FP64 tiles above); per instance the norms from the Gram's
+// diagonal, FC, loss, A and diag(FC A) (the chain rule's time reduction
+// sum_t Z_ti (Z A)_ti, taken from FC in FP64); dL/dX in FP32 (Z A is a sum
+// over N nodes per sample, the precision of the backward).  The Pearson FC
+// restates refs/covar.c:70-109 / metric.py:111-139 as a two-pass sum
+// (centred Gram of the centred series) accurate to FP64 level.
 // ---------------------------------------------------------------------------
 
 namespace {
