@@ -621,14 +621,17 @@ int tvbg_fcfit_zgrad(const float *d_z, const float *d_a, float *d_out, int32_t n
  * l = b % lanes (lanes = 1: per-instance arrays; 8: lane-interleaved
  * groups): row s < T - 1 at d_x + g * x_inst_stride + l + (s * N + i) *
  * lanes, row T - 1 at d_last + g * last_inst_stride + l + i *
- * last_node_stride (or from d_x too when d_last is NULL).  Computes the Pearson FC in FP64
- * (two-pass means and norms, a symmetric Gram with FP64 products and sums;
- * into d_fc [n_inst][N][N] when not NULL), d_loss[b] = mean_{i<j}
+ * last_node_stride (or from d_x too when d_last is NULL).  Computes the
+ * Pearson FC to FP64 accuracy (two-pass: FP64 means, then the centred Gram,
+ * upper triangle only, in FP32 error-free arithmetic for N <= 192 -- every
+ * product exact, sums carried in two FP32 words, error below 4e-12 of
+ * ||c_i|| ||c_j|| -- and in FP64 above; norms from its diagonal; into
+ * d_fc [n_inst][N][N] when not NULL), d_loss[b] = mean_{i<j}
  * (FC_ij - target_ij)^2 (FP64) and, when d_dx is not NULL, dL/dX (FP32) at
  * d_dx + b * dx_inst_stride + s * N + i.  target [N][N] FP64; d_scratch of
  * tvbg_fcfit_scratch_bytes().  Restates the Pearson FC of refs/covar.c:70-109
- * (metric.py:111-139) as an exact two-pass sum; the loss and its gradient
- * have no counterpart in the reference.
+ * (metric.py:111-139) as a two-pass sum; the loss and its gradient have no
+ * counterpart in the reference.
  */
 int tvbg_fcfit_scratch_bytes(int32_t n_inst, int32_t N, int64_t *bytes);
 int tvbg_fcfit_loss(const float *d_x, int64_t x_inst_stride, const float *d_last,
