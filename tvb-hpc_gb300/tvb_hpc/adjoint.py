@@ -11,18 +11,25 @@ Problem (one connectome, I instances, T steps, deterministic):
 on the pipelined lane-interleaved group kernel where the delays allow
 (every delay >= 2 K - 1), else on the per-instance step kernel -- keeping
 the state and the history ring at every chunk start (checkpoints) and the
-rate series for the FC; tvbg_fcfit_loss then takes
-the FC (a symmetric FP64 Gram), the loss and dL/dr on the device in one
-call, no library GEMM.  ``FCFit.backward`` walks the chunks backwards:
-each chunk is recomputed from its checkpoint on the same kernel
-(bit-identical to the forward) with the state and coupling sums traced
-(the group kernel's TVBG_F_TRACE_CSUM column, read in place by the
-adjoint), and the reverse-time recursion runs over it, carrying the adjoint
-state and an adjoint ring of mu_V between chunks: on lane-interleaved
-groups of 8 instances, time-blocked (tvbg_adjoint_mpr_groups), where every
-delay is at least 4 steps and N <= 1024, else per instance
-(tvbg_adjoint_mpr, through tvbg_adjoint.seg_lanes on a group trace);
-dL/dG and dL/deta accumulate in FP64.
+rate series for the FC; tvbg_fcfit_loss then takes the FC (FP64 means, a
+centred upper-triangle Gram in FP32 error-free arithmetic), the loss and
+dL/dr on the device in one call, no library GEMM.
+
+``FCFit.backward`` walks the chunks backwards.  On the grouped layout the
+chunks are recomputed in windows (as many as `trace_budget` holds, one
+launch per window: every chunk from a working copy of its checkpoint, on
+the forward's kernel, so bit-identical), the last window already at the end
+of forward on a side stream; the recomputation traces the state and the
+coupling sums (the group kernel's TVBG_F_TRACE_CSUM column).  The
+reverse-time recursion then runs over each window in one launch, on
+lane-interleaved groups of 8 instances, time-blocked, with two thread teams
+where every delay is >= 2 K (tvbg_adjoint_mpr_groups), carrying the adjoint
+state and an adjoint ring of mu_V between windows.  Elsewhere (delays under
+4 steps, N > 1024, the per-instance layout) chunk by chunk per instance
+(tvbg_adjoint_mpr; through tvbg_adjoint.seg_lanes on a group trace).
+dL/dG and dL/deta accumulate in FP64, their partial sums grouped per chunk
+in every form, so every form gives the same bits.  Neither call waits for
+the device: status words are checked at the next call (or by check()).
 
 ``FCFitLoss`` wraps it as a torch.autograd.Function of (G [I], eta [I, N]).
 The reference builds only symbolic partials (tvb_hpc/model.py:61-65) and an
