@@ -28,8 +28,10 @@ state and an adjoint ring of mu_V between windows.  Elsewhere (delays under
 4 steps, N > 1024, the per-instance layout) chunk by chunk per instance
 (tvbg_adjoint_mpr; through tvbg_adjoint.seg_lanes on a group trace).
 dL/dG and dL/deta accumulate in FP64, their partial sums grouped per chunk
-in every form, so every form gives the same bits.  Neither call waits for
-the device: status words are checked at the next call (or by check()).
+in every form, so on the same traces the reverse kernels (per instance or
+on groups, one team or two, any window) give the same bits.  Neither call
+waits for the device: status words are checked at the next call (or by
+check()).
 
 ``FCFitLoss`` wraps it as a torch.autograd.Function of (G [I], eta [I, N]).
 The reference builds only symbolic partials (tvb_hpc/model.py:61-65) and an
