@@ -112,3 +112,18 @@ def test_set_budget():
         nat.check(lib.tvbg_serve_set_budget(h, 1 << 40))   # clamped to the creation budget
     finally:
         lib.tvbg_serve_destroy(h)
+
+
+def test_adjoint_footprint_counts_recompute_windows():
+    """A gradient request's adjoint memory counts the recomputation windows:
+    all segments when trace_budget holds them, else trace_budget, and at
+    least one segment (traces r, V, S and a working copy of its checkpoint)."""
+    from tvb_hpc import serve
+    I, N, T, nh = 256, 84, 2000, 512
+    per_seg = I * 100 * N * 3 * 4 + I * N * (nh + 8 + 2) * 4
+    full = serve.adjoint_bytes(I, N, T, nh)                      # 2 GiB: all 20 segments
+    small = serve.adjoint_bytes(I, N, T, nh, trace_budget=1 << 28)
+    tiny = serve.adjoint_bytes(I, N, T, nh, trace_budget=1)
+    assert 20 * per_seg < (2 << 30)
+    assert full - small == 20 * per_seg - (1 << 28)
+    assert small - tiny == (1 << 28) - per_seg
