@@ -309,3 +309,20 @@ def test_oracle_flag_values_match_the_abi():
     for name in ('NOISE', 'BOLD', 'TRACE', 'WRAP_FMOD', 'NO_WRAP', 'TRACKA'):
         m = re.search(r'#define ORC_F_%s (\d+)u' % name, src)
         assert int(m.group(1)) == getattr(nat, 'F_' + name)
+
+
+def test_pipelined_shape_min_ctas():
+    """pipelined_shape: the smallest cluster holding one node per slot, or,
+    with min_ctas, the smallest that also gives the set that many CTAs
+    (the adjoint's 32 groups of N = 84 on 152 SMs: 256 threads x 6)."""
+    from types import SimpleNamespace
+    from tvb_hpc import groups
+    gs = SimpleNamespace(can_pipeline=True, N=84, n_groups=32)
+    assert groups.pipelined_shape(gs) == (704, 2, 0, groups.PIPELINED)
+    assert groups.pipelined_shape(gs, min_ctas=152) == (256, 6, 0, groups.PIPELINED)
+    assert groups.pipelined_shape(gs, min_ctas=10 ** 6)[1] == 16      # the largest cluster
+    for t, c, _, tpn in [groups.pipelined_shape(SimpleNamespace(can_pipeline=True, N=n, n_groups=g),
+                                                min_ctas=152) for n in (17, 68, 400, 998) for g in (1, 32)]:
+        assert t % 64 == 0 and t <= 1024 and tpn == groups.PIPELINED
+    # no pipelining: the plain default shape
+    assert groups.pipelined_shape(SimpleNamespace(can_pipeline=False, N=84, n_groups=32))[3] == 1
